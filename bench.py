@@ -1,0 +1,389 @@
+"""Benchmark of the GB300 PBF step: particle-solver-iterations per second.
+
+Workload (one line of JSON on rank 0): the voxel-solid dam break -- 262,144
+fluid particles (64^3 jittered lattice) and ~50k static solid particles from
+a seeded 64 x 64 heightmap in a 128 x 64 x 128 box, h = 1, 4 solver
+iterations, dt = 1/60, PBF step (poly6 / spiky, s_corr, box and solid
+collision, XSPH).  A "step" is one full step (prediction, counting sort,
+neighbour lists, 4 x (lambda, delta-p), XSPH and commit).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+value     sum over ranks of fluid particles x iterations / device time per
+          step (CUDA events on the library's stream, max over ranks); L2 is
+          flushed (a 256 MiB write) before every timed step.
+e2e       the same metric through the C ABI with the state in page-locked
+          host memory: every step uploads x and v, steps, downloads x and v.
+roofline  the step's dominant kernel, from a live per-stage CUDA-event
+          profile: algorithmic bytes per launch / average launch time.
+cpu_baseline  the oracle's restatement of the reference step (one solver
+          iteration, single thread) on the same scene, on this host.
+Multi-GPU: every rank steps its own replica (the scene does not shard; no
+collective on the data path), scaling "weak".
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "PBF particle-solver-iters/s"
+UNIT = "particle-iters/s"
+WORKLOAD = "config1_voxel_solids_262k"
+
+# Algorithmic bytes per particle per launch of each stage: compulsory fp32
+# state traffic (positions 12 B, lambda 4 B; neighbour gathers counted as
+# cache hits).
+STAGE_BYTES = {"lambda": 12 + 4, "delta": 12 + 4 + 12}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-extras", action="store_true")
+    ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU baseline work")
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------ helpers --
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self, gpu_index=0):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.f.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9 or not parts[0].isdigit() or int(parts[0]) != gpu_index:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "nccl" if args.impl == "ours" else "gloo"
+        if args.impl == "ours":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    return world, rank, local
+
+
+def dist_max(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+# --------------------------------------------------------------- CPU legs --
+
+def cpu_reference_rate(scene, budget_s, min_steps=3):
+    """The reference step restated by the oracle (one solver iteration, single
+    thread): median time of steps each restored from the same snapshot."""
+    from oracle import oracle as O
+    O.build()
+    p = O.reference_params(*scene.domain)
+    p.rest_density, p.mass, p.relaxation_epsilon = 1.0, 1.0, 10.0
+    p.gravity[1] = -9.81
+    p.s_corr_dq, p.s_corr_k, p.s_corr_n = 0.2, 0.1, 4.0
+    p.clamp_cells = 1
+    v0 = np.zeros_like(scene.x)
+    times = []
+    t_start = time.perf_counter()
+    while len(times) < min_steps or (time.perf_counter() - t_start < budget_s and len(times) < 50):
+        t0 = time.perf_counter()
+        O.compat_step(p, scene.dt, scene.x, v0, solid=scene.solid if scene.ns else None)
+        times.append(time.perf_counter() - t0)
+        if time.perf_counter() - t_start > 3 * budget_s:
+            break
+    t = statistics.median(times)
+    return scene.n / t, len(times), t
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    from lustrine_gb300 import scenes
+    sc = scenes.config1()
+    rates = []
+    for _ in range(args.warmup):
+        cpu_reference_rate(sc, 0.0, min_steps=1)
+    for _ in range(args.steps):
+        r, _, _ = cpu_reference_rate(sc, 0.0, min_steps=1)
+        rates.append(r)
+    value = statistics.median(rates)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": sc.n / value * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded jittered lattice + seeded heightmap solids)",
+        "config": {"workload": WORKLOAD, "fluid_particles": sc.n, "solid_particles": sc.ns,
+                   "solver_iterations": 1, "semantics": "reference simulate_fluid, one pass"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port",
+                         "sample": f"{args.steps} single steps of the full scene from one snapshot"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# -------------------------------------------------------------- GPU legs --
+
+def time_steps(sim, dt, steps, flush, ext):
+    import torch
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    torch.cuda.synchronize()
+    for k in range(steps):
+        with torch.cuda.stream(ext):
+            flush.zero_()
+            starts[k].record(ext)
+        sim.step(dt)
+        with torch.cuda.stream(ext):
+            ends[k].record(ext)
+    torch.cuda.synchronize()
+    return [s.elapsed_time(e) for s, e in zip(starts, ends)]
+
+
+def profile_stages(sim, dt, reps=3):
+    acc = {}
+    for _ in range(reps):
+        for k, (ms, cnt) in sim.profile_step(dt).items():
+            a = acc.setdefault(k, [0.0, 0])
+            a[0] += ms / reps
+            a[1] = cnt
+    return acc
+
+
+def run_scene(sc, params, steps, warmup, flush):
+    import torch
+    from lustrine_gb300 import PbfSim
+    sim = PbfSim(params, sc.n, sc.ns)
+    sim.upload(sc.x, None, sc.solid if sc.ns else None)
+    sim.step(sc.dt, warmup)
+    sim.synchronize()
+    ext = torch.cuda.ExternalStream(sim.stream())
+    ms = time_steps(sim, sc.dt, steps, flush, ext)
+    st = sim.status()
+    return sim, ext, ms, st
+
+
+def run_ours(args, world, rank, local):
+    import torch
+    from lustrine_gb300 import PRECISION_MIXED, pbf_params, scenes
+    torch.cuda.set_device(local)
+    sc = scenes.config1()
+    params = pbf_params(*sc.domain, iterations=sc.iterations, c_xsph=sc.c_xsph)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    clocks = ClockSampler()
+
+    sim, ext, _, _ = run_scene(sc, params, 1, args.warmup, flush)  # warm-up, graph capture
+    barrier(world)
+    clocks.start()
+    ms = time_steps(sim, sc.dt, args.steps, flush, ext)
+    clk = clocks.stop(local)
+    status = sim.status()
+    barrier(world)
+    ms_step = dist_max(sum(ms) / len(ms), world)
+    iters = params.iterations
+    value = world * sc.n * iters / (ms_step * 1e-3)
+    launches = sim.launches_per_step() * args.steps
+
+    # live per-stage profile (CUDA events on the library stream)
+    prof = profile_stages(sim, sc.dt)
+    peak, peak_kind = measured_peaks()
+    cand = {k: v for k, v in prof.items() if k in STAGE_BYTES}
+    dom = max(cand, key=lambda k: cand[k][0])
+    ms_launch = cand[dom][0] / max(cand[dom][1], 1)
+    bytes_launch = STAGE_BYTES[dom] * sc.n
+    achieved = bytes_launch / (ms_launch * 1e-3) / 1e9
+    traffic = read_traffic(dom)
+    # whole-step algorithmic bytes per particle-iteration (state traffic model)
+    cells = (sc.domain[0] + 1) * (sc.domain[1] + 1) * (sc.domain[2] + 1)
+    bpi = 44 + (192 + 8 * cells / sc.n + 12 * sc.ns / sc.n) / iters
+    step_achieved = value / world * bpi / 1e9
+
+    # end to end through the C ABI with page-locked host buffers
+    e2e = run_e2e(sim, sc, args, ext)
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "impl": "ours",
+        "data": "synthetic (seeded jittered lattice + seeded heightmap solids)",
+        "config": {"workload": WORKLOAD, "fluid_particles": sc.n, "solid_particles": sc.ns,
+                   "box": list(sc.domain), "h": 1.0, "solver_iterations": iters, "dt": sc.dt,
+                   "precision": "fp32", "l2": "flushed (256 MiB write) before every timed step",
+                   "parallelism": f"replicas x{world}"},
+        "gpu_launches": launches,
+        "status": status,
+        "e2e": e2e,
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+                     "traffic": traffic, "bytes_per_launch": bytes_launch,
+                     "ms_per_launch": ms_launch},
+        "step_roofline": {"bytes_per_particle_iter": bpi, "achieved": step_achieved,
+                          "frac": step_achieved / peak, "unit": "GB/s"},
+        "stage_ms": {k: round(v[0], 5) for k, v in prof.items()},
+    }
+    if clk:
+        line["clocks"] = clk
+    if rank == 0:
+        rate, nsteps, t = cpu_reference_rate(sc, args.cpu_budget)
+        line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": 1, "kind": "port",
+                                "sample": f"median of {nsteps} single reference-semantics steps "
+                                          f"(1 solver iteration) of the full scene from one "
+                                          f"snapshot, {t * 1e3:.1f} ms each",
+                                "nproc": os.cpu_count()}
+    if not args.no_extras and rank == 0:
+        line["variants"] = run_variants(args, flush)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def run_e2e(sim, sc, args, ext):
+    import torch
+    n = sc.n
+    x = torch.from_numpy(sim.positions()).pin_memory()
+    v = torch.from_numpy(sim.velocities()).pin_memory()
+    steps = max(3, args.steps // 2)
+    for _ in range(2):
+        sim.upload_state_async(x.data_ptr(), v.data_ptr())
+        sim.step(sc.dt)
+        sim.download_state_async(x.data_ptr(), v.data_ptr())
+    sim.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        sim.upload_state_async(x.data_ptr(), v.data_ptr())
+        sim.step(sc.dt)
+        sim.download_state_async(x.data_ptr(), v.data_ptr())
+        sim.synchronize()  # the host reads the step's result
+    dt_wall = (time.perf_counter() - t0) / steps
+    return {"value": n * sim.params.iterations / dt_wall, "unit": UNIT,
+            "h2d_bytes_per_step": 2 * 12 * n, "d2h_bytes_per_step": 2 * 12 * n,
+            "ms_per_step": dt_wall * 1e3,
+            "path": "lustrine_pbf_upload_state_async + lustrine_pbf_step + "
+                    "lustrine_pbf_download_state_async (page-locked host buffers)"}
+
+
+def run_variants(args, flush):
+    """Other configurations of the same step (not the headline)."""
+    from lustrine_gb300 import PRECISION_MIXED, pbf_params, scenes
+    out = {}
+    k = max(3, min(args.steps, 10))
+    sc = scenes.config1()
+    p = pbf_params(*sc.domain, iterations=sc.iterations, c_xsph=sc.c_xsph, precision=PRECISION_MIXED)
+    sim, _, ms, st = run_scene(sc, p, k, 3, flush)
+    out["config1_mixed"] = {"value": sc.n * p.iterations / (np.mean(ms) * 1e-3),
+                            "ms_per_step": float(np.mean(ms)), "status": st}
+    sim.close()
+    sc = scenes.config2()
+    p = pbf_params(*sc.domain, iterations=sc.iterations, c_xsph=sc.c_xsph)
+    sim, _, ms, st = run_scene(sc, p, k, 3, flush)
+    prof = profile_stages(sim, sc.dt, reps=2)
+    out["config2_plain_2M"] = {"value": sc.n * p.iterations / (np.mean(ms) * 1e-3),
+                               "ms_per_step": float(np.mean(ms)), "status": st,
+                               "stage_ms": {a: round(b[0], 4) for a, b in prof.items()}}
+    sim.close()
+    return out
+
+
+def read_traffic(kernel):
+    """DRAM bytes per launch of the dominant kernel from the committed ncu
+    summary (profiles/), or None."""
+    path = os.path.join(ROOT, "profiles", f"ncu_{kernel}_{WORKLOAD}.txt")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.startswith("traffic_bytes_per_launch:"):
+            return float(line.split(":", 1)[1])
+    return None
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_ours(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

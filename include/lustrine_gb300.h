@@ -1,0 +1,250 @@
+/*
+ * lustrine_gb300.h -- C ABI of the GB300 position-based-fluid step.
+ *
+ * Two layers, both plain C (pointers and sizes; no CUDA or C++ types):
+ *
+ * 1. The reference's C entry points for the fluid path, same names, argument
+ *    layouts and void returns as Lustrine::Wrapper (src/LustrineWrapper.hpp),
+ *    over a process-global simulation, so a game binding that loads the
+ *    reference's LustrineWrapper library can load this one instead.  Each
+ *    records its outcome for lustrine_last_status().
+ *
+ * 2. lustrine_pbf_*: a context API with explicit state (arrays in, arrays
+ *    out, status codes), used by layer 1 and by callers that hold their own
+ *    particle arrays -- the C++ Simulation adapter in lustrine_gb300_sim.hpp,
+ *    the tests and the benchmark.
+ *
+ * Threading: one context is driven from one host thread at a time; steps are
+ * asynchronous on the context's CUDA stream and every download synchronises.
+ */
+#ifndef LUSTRINE_GB300_H
+#define LUSTRINE_GB300_H
+
+#include <stdbool.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define LUSTRINE_API __attribute__((visibility("default")))
+#else
+#define LUSTRINE_API
+#endif
+
+/* ------------------------------------------------------------------ status */
+enum {
+    LUSTRINE_OK = 0,
+    LUSTRINE_ERR_ARGS = 1,           /* invalid argument */
+    LUSTRINE_ERR_CUDA = 2,           /* a CUDA runtime call failed */
+    LUSTRINE_ERR_NOMEM = 3,          /* device or host allocation failed */
+    LUSTRINE_ERR_NBR_OVERFLOW = 4,   /* a neighbour list exceeded max_neighbors */
+    LUSTRINE_ERR_CELL_RANGE = 5,     /* reference mode: a particle left the grid (clamped) */
+    LUSTRINE_ERR_UNSUPPORTED = 6,    /* option not provided by this build */
+    LUSTRINE_ERR_NO_SIMULATION = 7,  /* wrapper call before init_simulation */
+    LUSTRINE_ERR_TIMEOUT = 8,        /* a bounded device wait gave up */
+    LUSTRINE_ERR_BAD_VALUE = 9       /* non-finite particle state */
+};
+
+enum {
+    LUSTRINE_MODE_REFERENCE = 0, /* simulate_fluid semantics (Simulate.cpp:27-115), Jacobi update */
+    LUSTRINE_MODE_PBF = 1        /* PBF: iterations, poly6/spiky, s_corr, solids, box, XSPH */
+};
+
+enum {
+    LUSTRINE_PRECISION_FP32 = 0,  /* absolute fp32 positions */
+    LUSTRINE_PRECISION_MIXED = 1  /* int cell index + fp32 offset, Kahan density (PBF mode) */
+};
+
+/* ------------------------------------------------- layer 1: reference ABI */
+/* Layouts of Lustrine::SimulationParameters (src/Simulation.hpp:83-92) and
+ * Lustrine::Wrapper::{SimulationData, Color, Vec3, GridWrapper}
+ * (src/LustrineWrapper.hpp:30-74). */
+typedef struct SimulationParameters {
+    int X, Y, Z;
+    float particleRadius;
+    float particleDiameter;
+} SimulationParameters;
+
+typedef struct SimulationData {
+    int num_sand_particles;
+    int num_solid_particles;
+    int start_sand_index;
+    int end_sand_index;
+    int start_solid_index;
+    int end_solid_index;
+} SimulationData;
+
+typedef struct Color {
+    float r, g, b, a;
+} Color;
+
+typedef struct Vec3 {
+    float x, y, z;
+} Vec3;
+
+typedef struct GridWrapper {
+    int* cells;
+    Color* colors;
+    Color color;
+    Vec3 position;
+    bool has_one_color_per_cell;
+    int X;
+    int Y;
+    int Z;
+    int num_grid_cells;
+    int num_occupied_grid_cells;
+    int type; /* 0 solid, 1 sand (Simulation.hpp:28-32) */
+} GridWrapper;
+
+/* LustrineWrapper.hpp:86-94 / LustrineWrapper.cpp:165-221.  Builds the scene
+ * with the reference's init_simulation layout (kernel radius 3.1 r, solid
+ * cells whose value is 1 masked out, Lustrine.cpp:188,253) and selects the
+ * GPU fluid step in reference mode. */
+LUSTRINE_API void init_simulation(const SimulationParameters* parameters, SimulationData* data,
+                                  GridWrapper* sand_grids, int num_sand_grids,
+                                  GridWrapper* solid_grids, int num_solid_grids, int subdivision);
+/* LustrineWrapper.hpp:97-107 / LustrineWrapper.cpp:223-282 (kernel radius =
+ * kernel_radius_scale * r, Lustrine.cpp:545).  with_credits is not supported
+ * (the credits text is a sand-solver feature) and records LUSTRINE_ERR_UNSUPPORTED. */
+LUSTRINE_API void init_simulation_extra_parameters(const SimulationParameters* parameters,
+                                                   SimulationData* data, GridWrapper* sand_grids,
+                                                   int num_sand_grids, GridWrapper* solid_grids,
+                                                   int num_solid_grids, int subdivision,
+                                                   float kernel_radius_scale, int with_credits);
+/* LustrineWrapper.cpp:343-351: one step of the selected fluid step.  The
+ * attract/blow flags drive the sand solver only and are ignored. */
+LUSTRINE_API void simulate(float dt, bool attract_flag, bool blow_flag);
+LUSTRINE_API void simulate_no_flags(float dt);
+/* LustrineWrapper.cpp:377-379: copies 3 * num_sand_particles floats (particle
+ * positions in the order init_simulation created them).  Synchronises. */
+LUSTRINE_API void simulation_bind_positions_copy(float* position_ptr);
+/* LustrineWrapper.cpp:353-375 */
+LUSTRINE_API void cleanup_simulation(void);
+/* LustrineWrapper.cpp:336-341 + Lustrine.cpp:618-639: fills grid with an
+ * X * Y * Z block; allocates grid->cells with new[] like the reference (the
+ * caller owns it; free with lustrine_free_grid). */
+LUSTRINE_API void init_grid_box(const SimulationParameters* parameters, GridWrapper* grid, int X,
+                                int Y, int Z, Vec3 position, Color color, int type);
+/* LustrineWrapper.cpp:142-144 */
+LUSTRINE_API int get_num_sand_particles(void);
+/* LustrineWrapper.cpp:705-707 (returns the float cell size converted to int) */
+LUSTRINE_API int get_grid_cell_size(void);
+/* LustrineWrapper.cpp:666-677.  0 and 1 select the reference's sand solvers,
+ * which this library does not provide (LUSTRINE_ERR_UNSUPPORTED, step
+ * unchanged); 2 selects the fluid step with reference semantics; 3 the PBF
+ * step. */
+LUSTRINE_API void set_simulate_function(int index);
+
+/* Outcome of the last layer-1 call (LUSTRINE_OK or an error code). */
+LUSTRINE_API int lustrine_last_status(void);
+/* The context behind the layer-1 simulation (NULL before init_simulation). */
+struct lustrine_pbf;
+LUSTRINE_API struct lustrine_pbf* lustrine_global_context(void);
+/* Frees what init_grid_box allocated in grid. */
+LUSTRINE_API void lustrine_free_grid(GridWrapper* grid);
+
+/* --------------------------------------------------- layer 2: context API */
+typedef struct lustrine_pbf_params {
+    int mode;                 /* LUSTRINE_MODE_* */
+    int precision;            /* LUSTRINE_PRECISION_* */
+    int domain[3];            /* box X, Y, Z (Simulation::domainX/Y/Z) */
+    float particle_radius;
+    float kernel_radius;      /* h */
+    float kernel_factor;      /* reference cubic kernel scale, 0.5 */
+    float cell_size;          /* grid cell; the reference uses h */
+    float rest_density;
+    float mass;
+    float gravity[3];
+    float relaxation_epsilon;
+    float s_corr_dq;          /* s_corr distance (absolute) */
+    float s_corr_k;
+    float s_corr_n;
+    float c_xsph;             /* PBF mode */
+    float solid_contact;      /* PBF mode: push-out distance to solid particles */
+    int iterations;           /* PBF mode: solver iterations per step */
+    int max_neighbors;        /* neighbour list capacity per particle */
+    int clamp_cells;          /* reference mode: clamp cell coordinates to the grid */
+    int use_graph;            /* replay each step from a captured CUDA graph */
+} lustrine_pbf_params;
+
+typedef struct lustrine_pbf lustrine_pbf;
+
+/* Parameters of init_simulation_extra_parameters (Lustrine.cpp:543-555) with
+ * the reference's physical defaults (Simulation.hpp:147-171). */
+LUSTRINE_API void lustrine_pbf_params_reference(lustrine_pbf_params* p, int X, int Y, int Z,
+                                                float particle_radius, float kernel_radius_scale);
+
+LUSTRINE_API int lustrine_pbf_create(const lustrine_pbf_params* p, int n_fluid, int n_solid,
+                                     lustrine_pbf** out);
+LUSTRINE_API int lustrine_pbf_destroy(lustrine_pbf* s);
+/* Change parameters (same mode/precision/domain/max_neighbors as at create). */
+LUSTRINE_API int lustrine_pbf_set_params(lustrine_pbf* s, const lustrine_pbf_params* p);
+LUSTRINE_API int lustrine_pbf_get_params(const lustrine_pbf* s, lustrine_pbf_params* p);
+LUSTRINE_API int lustrine_pbf_counts(const lustrine_pbf* s, int* n_fluid, int* n_solid);
+
+/* State in: x, v as 3 * n_fluid floats (v may be NULL: zero), solid as
+ * 3 * n_solid floats in the reference's storage order (solid id n_fluid + k).
+ * _device: the pointers are device memory.  Both copy; the caller keeps
+ * ownership. */
+LUSTRINE_API int lustrine_pbf_upload(lustrine_pbf* s, const float* x, const float* v,
+                                     const float* solid);
+LUSTRINE_API int lustrine_pbf_upload_device(lustrine_pbf* s, const float* x, const float* v,
+                                            const float* solid);
+/* Fluid state only (x, v), host memory, asynchronous when the buffers are
+ * page-locked. */
+LUSTRINE_API int lustrine_pbf_upload_state_async(lustrine_pbf* s, const float* x, const float* v);
+
+/* Advance by dt (asynchronous on the context stream). */
+LUSTRINE_API int lustrine_pbf_step(lustrine_pbf* s, float dt);
+LUSTRINE_API int lustrine_pbf_steps(lustrine_pbf* s, float dt, int count);
+LUSTRINE_API int lustrine_pbf_synchronize(lustrine_pbf* s);
+
+/* State out, in the caller's particle order (host pointers, any may be NULL;
+ * synchronises): x, v 3 * n_fluid floats; lambdas, density n_fluid floats
+ * (last lambda pass). */
+LUSTRINE_API int lustrine_pbf_download(lustrine_pbf* s, float* x, float* v, float* lambdas,
+                                       float* density);
+/* Asynchronous x, v download into host buffers (page-locked for overlap). */
+LUSTRINE_API int lustrine_pbf_download_state_async(lustrine_pbf* s, float* x, float* v);
+/* Positions in double (exact for the mixed representation), host, synchronises. */
+LUSTRINE_API int lustrine_pbf_download_positions_f64(lustrine_pbf* s, double* x);
+/* Neighbour lists of the last step in the caller's ids (solids n_fluid + k):
+ * count[n_fluid], idx[n_fluid * cap] row-major.  Synchronises. */
+LUSTRINE_API int lustrine_pbf_neighbors(lustrine_pbf* s, int* count, int* idx, int cap);
+/* FP64 reductions on the device: [0] mass, [1..3] momentum, [4] kinetic
+ * energy, [5..7] centre of mass, [8] max |rho / rho0 - 1| of the last lambda
+ * pass.  Synchronises. */
+LUSTRINE_API int lustrine_pbf_reduce(lustrine_pbf* s, double out[9]);
+/* Device-side error bits since the last call, as a status code (synchronises). */
+LUSTRINE_API int lustrine_pbf_status(lustrine_pbf* s);
+/* The context's cudaStream_t, as void*. */
+LUSTRINE_API int lustrine_pbf_stream(lustrine_pbf* s, void** stream);
+/* One step with direct launches and a CUDA event after each stage, on the
+ * context stream; stage_ms[k] receives the milliseconds of stage k (summed
+ * over the solver iterations) and stage_launches[k] its event count.
+ * Synchronises. */
+enum {
+    LUSTRINE_STAGE_PREDICT = 0, /* prediction + cell key + histogram */
+    LUSTRINE_STAGE_SCAN = 1,    /* prefix scan over cells */
+    LUSTRINE_STAGE_SORT = 2,    /* index scatter, stabilisation, reorder */
+    LUSTRINE_STAGE_LISTS = 3,   /* neighbour lists */
+    LUSTRINE_STAGE_LAMBDA = 4,  /* density constraint pass(es) */
+    LUSTRINE_STAGE_DELTA = 5,   /* position correction pass(es) */
+    LUSTRINE_STAGE_XSPH = 6,    /* XSPH + commit */
+    LUSTRINE_NUM_STAGES = 7
+};
+LUSTRINE_API int lustrine_pbf_profile_step(lustrine_pbf* s, float dt, double* stage_ms,
+                                           int* stage_launches, int num_stages);
+/* Kernel launches one step issues (for launch accounting). */
+LUSTRINE_API int lustrine_pbf_launches_per_step(const lustrine_pbf* s);
+
+LUSTRINE_API const char* lustrine_error_string(int code);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LUSTRINE_GB300_H */

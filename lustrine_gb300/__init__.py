@@ -1,0 +1,11 @@
+"""GB300-native (sm_103a) position-based-fluid step of Lustrine.
+
+The compute path is liblustrine_gb300.so (hand-written CUDA kernels behind a
+C ABI, include/lustrine_gb300.h); this package is its Python host side.
+"""
+from ._lib import LustrineError, load
+from .pbf import (MODE_PBF, MODE_REFERENCE, PRECISION_FP32, PRECISION_MIXED, PbfParams, PbfSim,
+                  pbf_params, reference_params)
+
+__all__ = ["LustrineError", "load", "PbfSim", "PbfParams", "pbf_params", "reference_params",
+           "MODE_PBF", "MODE_REFERENCE", "PRECISION_FP32", "PRECISION_MIXED"]

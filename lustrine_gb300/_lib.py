@@ -1,0 +1,155 @@
+"""ctypes binding of liblustrine_gb300.so (the C ABI in include/lustrine_gb300.h).
+
+The library is the product: every call below goes to CUDA kernels.  There is
+no CPU fallback -- if the library is missing and cannot be built, importing
+the binding raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from . import build as _build
+
+LUSTRINE_OK = 0
+ERRORS = {
+    1: "LUSTRINE_ERR_ARGS",
+    2: "LUSTRINE_ERR_CUDA",
+    3: "LUSTRINE_ERR_NOMEM",
+    4: "LUSTRINE_ERR_NBR_OVERFLOW",
+    5: "LUSTRINE_ERR_CELL_RANGE",
+    6: "LUSTRINE_ERR_UNSUPPORTED",
+    7: "LUSTRINE_ERR_NO_SIMULATION",
+    8: "LUSTRINE_ERR_TIMEOUT",
+    9: "LUSTRINE_ERR_BAD_VALUE",
+}
+MODE_REFERENCE, MODE_PBF = 0, 1
+PRECISION_FP32, PRECISION_MIXED = 0, 1
+
+
+class LustrineError(RuntimeError):
+    def __init__(self, code: int, what: str = ""):
+        self.code = code
+        super().__init__(f"{what}: {ERRORS.get(code, code)}" if what else ERRORS.get(code, str(code)))
+
+
+# ------------------------------------------------------------ C structures --
+
+class SimulationParameters(C.Structure):
+    _fields_ = [("X", C.c_int), ("Y", C.c_int), ("Z", C.c_int),
+                ("particleRadius", C.c_float), ("particleDiameter", C.c_float)]
+
+
+class SimulationData(C.Structure):
+    _fields_ = [("num_sand_particles", C.c_int), ("num_solid_particles", C.c_int),
+                ("start_sand_index", C.c_int), ("end_sand_index", C.c_int),
+                ("start_solid_index", C.c_int), ("end_solid_index", C.c_int)]
+
+
+class Color(C.Structure):
+    _fields_ = [("r", C.c_float), ("g", C.c_float), ("b", C.c_float), ("a", C.c_float)]
+
+
+class Vec3(C.Structure):
+    _fields_ = [("x", C.c_float), ("y", C.c_float), ("z", C.c_float)]
+
+
+class GridWrapper(C.Structure):
+    _fields_ = [("cells", C.POINTER(C.c_int)), ("colors", C.POINTER(Color)), ("color", Color),
+                ("position", Vec3), ("has_one_color_per_cell", C.c_bool), ("X", C.c_int),
+                ("Y", C.c_int), ("Z", C.c_int), ("num_grid_cells", C.c_int),
+                ("num_occupied_grid_cells", C.c_int), ("type", C.c_int)]
+
+
+class PbfParams(C.Structure):
+    _fields_ = [("mode", C.c_int), ("precision", C.c_int), ("domain", C.c_int * 3),
+                ("particle_radius", C.c_float), ("kernel_radius", C.c_float),
+                ("kernel_factor", C.c_float), ("cell_size", C.c_float),
+                ("rest_density", C.c_float), ("mass", C.c_float), ("gravity", C.c_float * 3),
+                ("relaxation_epsilon", C.c_float), ("s_corr_dq", C.c_float),
+                ("s_corr_k", C.c_float), ("s_corr_n", C.c_float), ("c_xsph", C.c_float),
+                ("solid_contact", C.c_float), ("iterations", C.c_int),
+                ("max_neighbors", C.c_int), ("clamp_cells", C.c_int), ("use_graph", C.c_int)]
+
+
+# Every symbol include/lustrine_gb300.h declares, with its ctypes signature.
+_P = C.c_void_p
+_FP = C.POINTER(C.c_float)
+_IP = C.POINTER(C.c_int)
+_DP = C.POINTER(C.c_double)
+SIGNATURES = {
+    # layer 1: the reference's wrapper entry points
+    "init_simulation": (None, [C.POINTER(SimulationParameters), C.POINTER(SimulationData),
+                               C.POINTER(GridWrapper), C.c_int, C.POINTER(GridWrapper), C.c_int,
+                               C.c_int]),
+    "init_simulation_extra_parameters": (None, [C.POINTER(SimulationParameters),
+                                                C.POINTER(SimulationData), C.POINTER(GridWrapper),
+                                                C.c_int, C.POINTER(GridWrapper), C.c_int, C.c_int,
+                                                C.c_float, C.c_int]),
+    "simulate": (None, [C.c_float, C.c_bool, C.c_bool]),
+    "simulate_no_flags": (None, [C.c_float]),
+    "simulation_bind_positions_copy": (None, [_FP]),
+    "cleanup_simulation": (None, []),
+    "init_grid_box": (None, [C.POINTER(SimulationParameters), C.POINTER(GridWrapper), C.c_int,
+                             C.c_int, C.c_int, Vec3, Color, C.c_int]),
+    "get_num_sand_particles": (C.c_int, []),
+    "get_grid_cell_size": (C.c_int, []),
+    "set_simulate_function": (None, [C.c_int]),
+    "lustrine_last_status": (C.c_int, []),
+    "lustrine_global_context": (_P, []),
+    "lustrine_free_grid": (None, [C.POINTER(GridWrapper)]),
+    # layer 2: context API
+    "lustrine_pbf_params_reference": (None, [C.POINTER(PbfParams), C.c_int, C.c_int, C.c_int,
+                                             C.c_float, C.c_float]),
+    "lustrine_pbf_create": (C.c_int, [C.POINTER(PbfParams), C.c_int, C.c_int, C.POINTER(_P)]),
+    "lustrine_pbf_destroy": (C.c_int, [_P]),
+    "lustrine_pbf_set_params": (C.c_int, [_P, C.POINTER(PbfParams)]),
+    "lustrine_pbf_get_params": (C.c_int, [_P, C.POINTER(PbfParams)]),
+    "lustrine_pbf_counts": (C.c_int, [_P, _IP, _IP]),
+    "lustrine_pbf_upload": (C.c_int, [_P, _P, _P, _P]),
+    "lustrine_pbf_upload_device": (C.c_int, [_P, _P, _P, _P]),
+    "lustrine_pbf_upload_state_async": (C.c_int, [_P, _P, _P]),
+    "lustrine_pbf_step": (C.c_int, [_P, C.c_float]),
+    "lustrine_pbf_steps": (C.c_int, [_P, C.c_float, C.c_int]),
+    "lustrine_pbf_synchronize": (C.c_int, [_P]),
+    "lustrine_pbf_download": (C.c_int, [_P, _P, _P, _P, _P]),
+    "lustrine_pbf_download_state_async": (C.c_int, [_P, _P, _P]),
+    "lustrine_pbf_download_positions_f64": (C.c_int, [_P, _P]),
+    "lustrine_pbf_neighbors": (C.c_int, [_P, _P, _P, C.c_int]),
+    "lustrine_pbf_reduce": (C.c_int, [_P, _DP]),
+    "lustrine_pbf_status": (C.c_int, [_P]),
+    "lustrine_pbf_stream": (C.c_int, [_P, C.POINTER(_P)]),
+    "lustrine_pbf_launches_per_step": (C.c_int, [_P]),
+    "lustrine_pbf_profile_step": (C.c_int, [_P, C.c_float, _DP, _IP, C.c_int]),
+    "lustrine_error_string": (C.c_char_p, [C.c_int]),
+}
+
+_lib = None
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True) -> C.CDLL:
+    """Load the CUDA library (building it with nvcc if it is missing or stale)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if build_if_missing and not _build.up_to_date():
+        _build.build()
+    path = _build.LIB
+    if not os.path.exists(path):
+        raise RuntimeError(f"liblustrine_gb300.so not found at {path}; run lustrine_gb300.build")
+    lib = C.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(code: int, what: str = "") -> None:
+    if code != LUSTRINE_OK:
+        raise LustrineError(code, what)

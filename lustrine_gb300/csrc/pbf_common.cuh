@@ -1,0 +1,81 @@
+// pbf_common.cuh -- device-side types shared by the PBF kernels.
+//
+// Data layout in HBM (one scene, n fluid particles, ns static solids):
+//   fluid state, structure of arrays in cell order (rebuilt every step):
+//     x    float4[n]   committed positions  (w: packed cell in mixed precision)
+//     xs   float4[n]   predicted positions, two copies for the Jacobi solve
+//     v    float4[n]   velocities
+//     id   int[n]      caller's particle id of each slot
+//   cell table: count[C], start[C + 1] (exclusive scan of count)
+//   solids: float4[ns] sorted by cell once at upload, sstart[C + 1]
+//   neighbour lists: nbr[max_nbrs * n], column-major (entry k of slot i at
+//     k * n + i) so a warp's loads of entry k are one coalesced line;
+//     fluid neighbours are slot numbers >= 0, solids are -1 - solid slot.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace lgb {
+
+// Device status bits, OR-ed into a status word instead of trapping.
+enum : int {
+    ST_NBR_OVERFLOW = 1,  // a neighbour list hit max_nbrs (list truncated)
+    ST_CELL_RANGE = 2,    // compat mode: a cell id left the grid (clamped)
+    ST_TIMEOUT = 4,       // a bounded wait gave up
+    ST_BAD_VALUE = 8,     // a non-finite position was met
+};
+
+// Everything a step kernel reads, passed by value (constant bank).
+struct StepParams {
+    int n, ns;            // fluid, solid particle counts
+    int gx, gy, gz;       // grid dims
+    int num_cells;
+    int max_nbrs;
+    int clamp_cells;      // compat mode: clamp cell coords per axis
+    float cell, inv_cell;
+    float h, h2;
+    // reference (compat) cubic kernel, Kernels.cpp:6-41
+    float kfac, cubic_k, cubic_l;
+    // PBF kernels: poly6 K6 (h^2 - r^2)^3, spiky gradient -Ks (h - r)^2 d / r
+    float k6, ks, inv_w_dq;
+    float mass, rho0, eps;
+    float dq, sk, sn;     // s_corr distance, k and exponent
+    int sn_int;           // exponent as an integer in [0, 32], or -1
+    float c_xsph, contact;
+    float gxv, gyv, gzv;  // gravity
+    float lox, loy, loz, hix, hiy, hiz;  // box bounds for the position clamp
+    float dt;
+};
+
+// Mixed precision: a cell's integer coordinates packed into 32 bits,
+// x in the low bits, then y, then z.
+struct CellPack {
+    unsigned mx, my, mz;  // per-axis masks
+    int by_shift, bz_shift;
+};
+
+__device__ __forceinline__ float dot3(float ax, float ay, float az) {
+    return ax * ax + ay * ay + az * az;
+}
+
+__device__ __forceinline__ void set_status(int* status, int bit) {
+    if ((*(volatile int*)status & bit) == 0) atomicOr(status, bit);
+}
+
+// x^n for an integer n >= 0 evaluated in double and rounded once to float:
+// the exact power of a float has at most 24 n significant bits, so for the
+// small n used here the double product is within a few 2^-53 of it and the
+// final rounding is the correctly rounded float (checked against a 113-bit
+// evaluation over all floats in (1e-8, 1] for n = 3, 4).
+__device__ __forceinline__ float ipow_rn(float x, int n) {
+    double r = 1.0, b = (double)x;
+    while (n) {
+        if (n & 1) r *= b;
+        b *= b;
+        n >>= 1;
+    }
+    return (float)r;
+}
+
+}  // namespace lgb

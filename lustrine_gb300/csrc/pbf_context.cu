@@ -1,0 +1,688 @@
+// pbf_context.cu -- lustrine_pbf_* context API: device state, one step as a
+// fixed sequence of kernel launches on the context stream, optionally
+// replayed from a captured CUDA graph (one graph per state buffer parity).
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include "lustrine_gb300.h"
+#include "pbf_context.h"
+#include "pbf_kernels.h"
+
+using namespace lgb;
+
+namespace {
+
+constexpr double kPi = 3.14159265358979323846;  // Lustrine.cpp:16
+
+template <class T>
+int dalloc(T** p, size_t count) {
+    *p = nullptr;
+    if (count == 0) count = 1;
+    return cudaMalloc((void**)p, count * sizeof(T)) == cudaSuccess ? LUSTRINE_OK : LUSTRINE_ERR_NOMEM;
+}
+
+int bits_for(int values) {
+    int b = 0;
+    while ((1 << b) < values) b++;
+    return b;
+}
+
+}  // namespace
+
+#define CK(call)                                                     \
+    do {                                                             \
+        cudaError_t e_ = (call);                                     \
+        if (e_ != cudaSuccess) return lgb_cuda_status(e_, #call);    \
+    } while (0)
+
+int lgb_cuda_status(cudaError_t e, const char* what) {
+    if (getenv("LUSTRINE_DEBUG")) fprintf(stderr, "lustrine: %s: %s\n", what, cudaGetErrorString(e));
+    return e == cudaErrorMemoryAllocation ? LUSTRINE_ERR_NOMEM : LUSTRINE_ERR_CUDA;
+}
+
+extern "C" void lustrine_pbf_params_reference(lustrine_pbf_params* p, int X, int Y, int Z,
+                                              float particle_radius, float kernel_radius_scale) {
+    std::memset(p, 0, sizeof(*p));
+    p->mode = LUSTRINE_MODE_REFERENCE;
+    p->precision = LUSTRINE_PRECISION_FP32;
+    p->domain[0] = X;
+    p->domain[1] = Y;
+    p->domain[2] = Z;
+    p->particle_radius = particle_radius;
+    p->kernel_radius = kernel_radius_scale * particle_radius;  // Lustrine.cpp:545
+    p->kernel_factor = 0.5f;                                   // Simulation.hpp:147
+    p->cell_size = 1.0f * p->kernel_radius;                    // Lustrine.cpp:546
+    p->rest_density = 24.0f;                                   // Simulation.hpp:157-171
+    p->mass = 5.0f;
+    p->gravity[0] = 0.0f;
+    p->gravity[1] = -10.0f;
+    p->gravity[2] = 0.0f;
+    p->relaxation_epsilon = 10.0f;
+    p->s_corr_dq = 0.5f;
+    p->s_corr_k = 1.0f;
+    p->s_corr_n = 4.0f;
+    p->c_xsph = 0.1f;
+    p->solid_contact = 2.0f * particle_radius;
+    p->iterations = 1;
+    p->max_neighbors = 96;
+    p->clamp_cells = 1;
+    p->use_graph = 1;
+}
+
+// Derived per-scene constants.  Reference-mode constants are computed with
+// the reference's float/double mix (Lustrine.cpp:549-555).
+static int derive(const lustrine_pbf_params& q, int n, int ns, StepParams* sp, CellPack* cp) {
+    if (q.domain[0] <= 0 || q.domain[1] <= 0 || q.domain[2] <= 0) return LUSTRINE_ERR_ARGS;
+    if (!(q.kernel_radius > 0.0f) || !(q.cell_size > 0.0f) || !(q.rest_density > 0.0f))
+        return LUSTRINE_ERR_ARGS;
+    if (q.max_neighbors <= 0 || q.iterations < 1 || q.iterations > 1000) return LUSTRINE_ERR_ARGS;
+    if (q.mode != LUSTRINE_MODE_REFERENCE && q.mode != LUSTRINE_MODE_PBF) return LUSTRINE_ERR_ARGS;
+    if (q.precision == LUSTRINE_PRECISION_MIXED && q.mode != LUSTRINE_MODE_PBF)
+        return LUSTRINE_ERR_UNSUPPORTED;
+    StepParams p;
+    std::memset(&p, 0, sizeof(p));
+    p.n = n;
+    p.ns = ns;
+    const float dX = (float)q.domain[0], dY = (float)q.domain[1], dZ = (float)q.domain[2];
+    p.gx = (int)(dX / q.cell_size) + 1;
+    p.gy = (int)(dY / q.cell_size) + 1;
+    p.gz = (int)(dZ / q.cell_size) + 1;
+    const long long C = (long long)p.gx * p.gy * p.gz;
+    if (C > (1LL << 31) - 2) return LUSTRINE_ERR_UNSUPPORTED;
+    p.num_cells = (int)C;
+    p.max_nbrs = q.max_neighbors;
+    p.clamp_cells = q.clamp_cells;
+    p.cell = q.cell_size;
+    p.inv_cell = 1.0f / q.cell_size;
+    p.h = q.kernel_radius;
+    p.h2 = q.kernel_radius * q.kernel_radius;
+    p.kfac = q.kernel_factor;
+    {
+        float h3 = (float)std::pow((double)q.kernel_radius, 3);
+        p.cubic_k = (float)(8.0 / (kPi * (double)h3));
+        p.cubic_l = (float)(48.0 / (kPi * (double)h3));
+    }
+    const double h = (double)q.kernel_radius;
+    p.k6 = (float)(315.0 / (64.0 * kPi * std::pow(h, 9)));
+    p.ks = (float)(45.0 / (kPi * std::pow(h, 6)));
+    {
+        double d = h * h - (double)q.s_corr_dq * (double)q.s_corr_dq;
+        double wdq = q.s_corr_dq <= q.kernel_radius ? 315.0 / (64.0 * kPi * std::pow(h, 9)) * d * d * d : 0.0;
+        p.inv_w_dq = wdq > 0.0 ? (float)(1.0 / wdq) : 0.0f;
+    }
+    p.mass = q.mass;
+    p.rho0 = q.rest_density;
+    p.eps = q.relaxation_epsilon;
+    p.dq = q.s_corr_dq;
+    p.sk = q.s_corr_k;
+    p.sn = q.s_corr_n;
+    p.sn_int = (q.s_corr_n >= 0.0f && q.s_corr_n <= 32.0f && std::floor(q.s_corr_n) == q.s_corr_n)
+                   ? (int)q.s_corr_n
+                   : -1;
+    p.c_xsph = q.c_xsph;
+    p.contact = q.solid_contact;
+    p.gxv = q.gravity[0];
+    p.gyv = q.gravity[1];
+    p.gzv = q.gravity[2];
+    const float r = q.particle_radius;
+    if (q.mode == LUSTRINE_MODE_REFERENCE) {
+        // Simulate.cpp:35-37,106-108: bounds [r, (int)domain - r]
+        p.lox = p.loy = p.loz = r;
+        p.hix = (float)q.domain[0] - r;
+        p.hiy = (float)q.domain[1] - r;
+        p.hiz = (float)q.domain[2] - r;
+    } else {
+        p.lox = p.loy = p.loz = r;
+        p.hix = dX - r;
+        p.hiy = dY - r;
+        p.hiz = dZ - r;
+    }
+    CellPack c;
+    std::memset(&c, 0, sizeof(c));
+    if (q.precision == LUSTRINE_PRECISION_MIXED) {
+        // cells a clamped position can occupy: 0 .. floor(hi / cell)
+        int vx = (int)std::floor(p.hix / p.cell) + 1, vy = (int)std::floor(p.hiy / p.cell) + 1,
+            vz = (int)std::floor(p.hiz / p.cell) + 1;
+        int bx = bits_for(vx), by = bits_for(vy), bz = bits_for(vz);
+        if (bx + by + bz > 32) return LUSTRINE_ERR_UNSUPPORTED;
+        c.mx = bx ? (unsigned)((1ull << bx) - 1) : 0u;
+        c.my = by ? (unsigned)((1ull << by) - 1) : 0u;
+        c.mz = bz ? (unsigned)((1ull << bz) - 1) : 0u;
+        c.by_shift = bx;
+        c.bz_shift = bx + by;
+    }
+    *sp = p;
+    *cp = c;
+    return LUSTRINE_OK;
+}
+
+lustrine_pbf::~lustrine_pbf() {
+    for (int k = 0; k < 2; k++)
+        if (graph_exec[k]) cudaGraphExecDestroy(graph_exec[k]);
+    void* ptrs[] = {x[0], x[1], xs[0], xs[1], v[0], v[1], id[0], id[1], xs_alt, vtmp, key, key_sorted,
+                    rank, tmp, perm, count, start, block_sums, solid, solid_raw, sstart, nbr, cnt, lam,
+                    lam_by_id, rho, status, red, out3, out3d, iota, solid_id};
+    for (void* q : ptrs)
+        if (q) cudaFree(q);
+    if (stream) cudaStreamDestroy(stream);
+}
+
+static int ctx_alloc(lustrine_pbf* s) {
+    const int n = s->n, ns = s->ns, C = s->sp.num_cells, m = n > ns ? n : ns;
+    int rc = LUSTRINE_OK;
+    for (int k = 0; k < 2 && !rc; k++) {
+        rc = rc ? rc : dalloc(&s->x[k], n);
+        rc = rc ? rc : dalloc(&s->xs[k], n);
+        rc = rc ? rc : dalloc(&s->v[k], n);
+        rc = rc ? rc : dalloc(&s->id[k], n);
+    }
+    rc = rc ? rc : dalloc(&s->xs_alt, n);
+    rc = rc ? rc : dalloc(&s->vtmp, n);
+    rc = rc ? rc : dalloc(&s->key, m);
+    rc = rc ? rc : dalloc(&s->key_sorted, n);
+    rc = rc ? rc : dalloc(&s->rank, m);
+    rc = rc ? rc : dalloc(&s->tmp, m);
+    rc = rc ? rc : dalloc(&s->perm, m);
+    rc = rc ? rc : dalloc(&s->count, C);
+    rc = rc ? rc : dalloc(&s->start, (size_t)C + 1);
+    rc = rc ? rc : dalloc(&s->block_sums, scan_block_sums_size(C));
+    rc = rc ? rc : dalloc(&s->solid, ns);
+    rc = rc ? rc : dalloc(&s->solid_raw, ns);
+    rc = rc ? rc : dalloc(&s->sstart, (size_t)C + 1);
+    rc = rc ? rc : dalloc(&s->nbr, (size_t)s->sp.max_nbrs * (size_t)n);
+    rc = rc ? rc : dalloc(&s->cnt, n);
+    rc = rc ? rc : dalloc(&s->lam, n);
+    s->lam_by_id_len = (size_t)(n + ns > s->sp.max_nbrs ? n + ns : s->sp.max_nbrs) + 1;
+    rc = rc ? rc : dalloc(&s->lam_by_id, s->lam_by_id_len);
+    rc = rc ? rc : dalloc(&s->rho, n);
+    rc = rc ? rc : dalloc(&s->status, 4);
+    rc = rc ? rc : dalloc(&s->red, 9);
+    rc = rc ? rc : dalloc(&s->out3, (size_t)3 * m);
+    rc = rc ? rc : dalloc(&s->out3d, (size_t)3 * n);
+    rc = rc ? rc : dalloc(&s->iota, n);
+    rc = rc ? rc : dalloc(&s->solid_id, ns);
+    if (rc) return rc;
+    if (n) {
+        std::vector<int> ids((size_t)n);
+        for (int i = 0; i < n; i++) ids[(size_t)i] = i;
+        CK(cudaMemcpy(s->iota, ids.data(), (size_t)n * sizeof(int), cudaMemcpyHostToDevice));
+    }
+    CK(cudaMemsetAsync(s->lam_by_id, 0, s->lam_by_id_len * sizeof(float), s->stream));
+    CK(cudaMemsetAsync(s->lam, 0, (size_t)(n ? n : 1) * sizeof(float), s->stream));
+    CK(cudaMemsetAsync(s->rho, 0, (size_t)(n ? n : 1) * sizeof(float), s->stream));
+    CK(cudaMemsetAsync(s->cnt, 0, (size_t)(n ? n : 1) * sizeof(int), s->stream));
+    CK(cudaMemsetAsync(s->status, 0, 4 * sizeof(int), s->stream));
+    CK(cudaMemsetAsync(s->sstart, 0, ((size_t)C + 1) * sizeof(int), s->stream));
+    return LUSTRINE_OK;
+}
+
+extern "C" int lustrine_pbf_create(const lustrine_pbf_params* p, int n_fluid, int n_solid,
+                                   lustrine_pbf** out) {
+    if (!p || !out || n_fluid < 0 || n_solid < 0) return LUSTRINE_ERR_ARGS;
+    *out = nullptr;
+    lustrine_pbf* s = new (std::nothrow) lustrine_pbf();
+    if (!s) return LUSTRINE_ERR_NOMEM;
+    s->prm = *p;
+    s->n = n_fluid;
+    s->ns = n_solid;
+    int rc = derive(*p, n_fluid, n_solid, &s->sp, &s->cp);
+    if (rc) {
+        delete s;
+        return rc;
+    }
+    if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete s;
+        return LUSTRINE_ERR_CUDA;
+    }
+    rc = ctx_alloc(s);
+    if (rc) {
+        delete s;
+        return rc;
+    }
+    *out = s;
+    return LUSTRINE_OK;
+}
+
+extern "C" int lustrine_pbf_destroy(lustrine_pbf* s) {
+    if (!s) return LUSTRINE_ERR_ARGS;
+    cudaStreamSynchronize(s->stream);
+    delete s;
+    return LUSTRINE_OK;
+}
+
+extern "C" int lustrine_pbf_set_params(lustrine_pbf* s, const lustrine_pbf_params* p) {
+    if (!s || !p) return LUSTRINE_ERR_ARGS;
+    if (p->precision != s->prm.precision ||
+        p->domain[0] != s->prm.domain[0] || p->domain[1] != s->prm.domain[1] ||
+        p->domain[2] != s->prm.domain[2] || p->max_neighbors != s->prm.max_neighbors ||
+        p->cell_size != s->prm.cell_size)
+        return LUSTRINE_ERR_ARGS;
+    StepParams sp;
+    CellPack cp;
+    int rc = derive(*p, s->n, s->ns, &sp, &cp);
+    if (rc) return rc;
+    s->prm = *p;
+    s->sp = sp;
+    s->cp = cp;
+    s->invalidate_graphs();
+    return LUSTRINE_OK;
+}
+
+extern "C" int lustrine_pbf_get_params(const lustrine_pbf* s, lustrine_pbf_params* p) {
+    if (!s || !p) return LUSTRINE_ERR_ARGS;
+    *p = s->prm;
+    return LUSTRINE_OK;
+}
+
+extern "C" int lustrine_pbf_counts(const lustrine_pbf* s, int* n_fluid, int* n_solid) {
+    if (!s) return LUSTRINE_ERR_ARGS;
+    if (n_fluid) *n_fluid = s->n;
+    if (n_solid) *n_solid = s->ns;
+    return LUSTRINE_OK;
+}
+
+void lustrine_pbf::invalidate_graphs() {
+    for (int k = 0; k < 2; k++) {
+        if (graph_exec[k]) cudaGraphExecDestroy(graph_exec[k]);
+        graph_exec[k] = nullptr;
+    }
+}
+
+bool lustrine_pbf::mixed() const { return prm.precision == LUSTRINE_PRECISION_MIXED; }
+
+// Sort the static solids by cell once (ascending id within a cell).
+static int setup_solids(lustrine_pbf* s) {
+    const int ns = s->ns, C = s->sp.num_cells;
+    StepParams p = s->sp;
+    CK(cudaMemsetAsync(s->count, 0, (size_t)C * sizeof(int), s->stream));
+    if (ns > 0) {
+        if (s->prm.mode == LUSTRINE_MODE_REFERENCE)
+            launch_key_ref(p, s->solid_raw, ns, s->key, s->rank, s->count, s->status, s->stream);
+        else
+            launch_key(s->mixed(), p, s->cp, s->solid_raw, ns, s->key, s->rank, s->count, s->stream);
+    }
+    launch_scan(s->count, C, s->block_sums, s->sstart, s->stream);
+    launch_sort_tail(s->key, s->rank, s->sstart, nullptr, ns, s->tmp, s->perm, s->stream);
+    launch_gather_solid(s->perm, ns, s->solid_raw, s->solid, s->stream);
+    CK(cudaGetLastError());
+    return LUSTRINE_OK;
+}
+
+// Pack caller arrays (device memory, 3 floats per particle, caller order)
+// into the state representation; slot k holds particle k.
+static int pack_fluid(lustrine_pbf* s, const float* dx, const float* dv) {
+    const int n = s->n, c = s->cur;
+    if (!n) return LUSTRINE_OK;
+    launch_pack_pos(s->mixed(), s->sp, s->cp, dx, n, s->x[c], s->stream);
+    if (dv)
+        launch_pack_pos(false, s->sp, s->cp, dv, n, s->v[c], s->stream);
+    else
+        CK(cudaMemsetAsync(s->v[c], 0, (size_t)n * sizeof(float4), s->stream));
+    CK(cudaMemcpyAsync(s->id[c], s->iota, (size_t)n * sizeof(int), cudaMemcpyDeviceToDevice, s->stream));
+    CK(cudaGetLastError());
+    return LUSTRINE_OK;
+}
+
+static int pack_solids(lustrine_pbf* s, const float* dsolid) {
+    if (s->ns > 0) launch_pack_pos(s->mixed(), s->sp, s->cp, dsolid, s->ns, s->solid_raw, s->stream);
+    CK(cudaGetLastError());
+    int rc = setup_solids(s);
+    if (rc) return rc;
+    if (s->ns > 0)
+        CK(cudaMemcpyAsync(s->solid_id, s->perm, (size_t)s->ns * sizeof(int), cudaMemcpyDeviceToDevice, s->stream));
+    return LUSTRINE_OK;
+}
+
+extern "C" int lustrine_pbf_upload(lustrine_pbf* s, const float* x, const float* v, const float* solid) {
+    if (!s || (!x && s->n > 0) || (s->ns > 0 && !solid)) return LUSTRINE_ERR_ARGS;
+    const int n = s->n, ns = s->ns;
+    s->cur = 0;
+    s->invalidate_graphs();
+    // staging: positions in out3d (6n floats), velocities and then solids in out3
+    float* sx = (float*)s->out3d;
+    if (n) CK(cudaMemcpyAsync(sx, x, (size_t)n * 3 * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+    if (v && n) CK(cudaMemcpyAsync(s->out3, v, (size_t)n * 3 * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+    int rc = pack_fluid(s, sx, v ? s->out3 : nullptr);
+    if (rc) return rc;
+    if (ns) CK(cudaMemcpyAsync(s->out3, solid, (size_t)ns * 3 * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+    rc = pack_solids(s, s->out3);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(s->stream));
+    s->have_state = true;
+    s->lists_valid = false;
+    return LUSTRINE_OK;
+}
+
+extern "C" int lustrine_pbf_upload_device(lustrine_pbf* s, const float* x, const float* v,
+                                          const float* solid) {
+    if (!s || (!x && s->n > 0) || (s->ns > 0 && !solid)) return LUSTRINE_ERR_ARGS;
+    s->cur = 0;
+    s->invalidate_graphs();
+    int rc = pack_fluid(s, x, v);
+    if (rc) return rc;
+    rc = pack_solids(s, solid);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(s->stream));
+    s->have_state = true;
+    s->lists_valid = false;
+    return LUSTRINE_OK;
+}
+
+extern "C" int lustrine_pbf_upload_state_async(lustrine_pbf* s, const float* x, const float* v) {
+    if (!s || !s->have_state || (!x && s->n > 0)) return LUSTRINE_ERR_ARGS;
+    const int n = s->n;
+    if (!n) return LUSTRINE_OK;
+    // Written in caller order into the current side; the next step re-sorts.
+    float* sx = (float*)s->out3d;
+    CK(cudaMemcpyAsync(sx, x, (size_t)n * 3 * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+    if (v) CK(cudaMemcpyAsync(s->out3, v, (size_t)n * 3 * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+    return pack_fluid(s, sx, v ? s->out3 : nullptr);
+}
+
+// Optional per-stage event marks for lustrine_pbf_profile_step.
+struct StageMarks {
+    cudaEvent_t ev[64];
+    int stage[64];
+    int count = 0;
+    void mark(int stg, cudaStream_t st) {
+        if (count < 64) {
+            cudaEventRecord(ev[count], st);
+            stage[count++] = stg;
+        }
+    }
+};
+
+// One step's launches.  Returns the number of kernels launched.
+static int enqueue_step(lustrine_pbf* s, cudaStream_t st, StageMarks* mk = nullptr) {
+    const int c = s->cur, o = 1 - c, n = s->n, C = s->sp.num_cells;
+    const StepParams& p = s->sp;
+    const bool mixed = s->mixed();
+    int k = 0;
+    if (mk) mk->mark(-1, st);
+    cudaMemsetAsync(s->count, 0, (size_t)C * sizeof(int), st);
+    if (s->prm.mode == LUSTRINE_MODE_REFERENCE)
+        launch_predict_ref(p, s->x[c], s->v[c], s->xs[c], s->key, s->rank, s->count, s->status, st);
+    else
+        launch_predict(mixed, p, s->cp, s->x[c], s->v[c], s->xs[c], s->key, s->rank, s->count, st);
+    k += 1;
+    if (mk) mk->mark(LUSTRINE_STAGE_PREDICT, st);
+    launch_scan(s->count, C, s->block_sums, s->start, st);
+    k += 3;
+    if (mk) mk->mark(LUSTRINE_STAGE_SCAN, st);
+    const int* tie = s->prm.mode == LUSTRINE_MODE_REFERENCE ? s->id[c] : nullptr;
+    launch_sort_tail(s->key, s->rank, s->start, tie, n, s->tmp, s->perm, st);
+    launch_gather_state(s->perm, n, s->key, s->x[c], s->xs[c], s->v[c], s->id[c], s->key_sorted,
+                        s->x[o], s->xs[o], s->v[o], s->id[o], st);
+    k += 3;
+    if (mk) mk->mark(LUSTRINE_STAGE_SORT, st);
+    if (s->prm.mode == LUSTRINE_MODE_REFERENCE) {
+        launch_lists_ref(p, s->xs[o], s->key_sorted, s->start, s->solid, s->sstart, s->nbr, s->cnt,
+                         s->status, st);
+        if (mk) mk->mark(LUSTRINE_STAGE_LISTS, st);
+        launch_lambda_ref(p, s->xs[o], s->id[o], s->nbr, s->cnt, s->solid, s->lam_by_id, s->rho, st);
+        if (mk) mk->mark(LUSTRINE_STAGE_LAMBDA, st);
+        launch_delta_ref(p, s->xs[o], s->xs_alt, s->x[o], s->v[o], s->id[o], s->nbr, s->cnt, s->solid,
+                         s->lam_by_id, st);
+        if (mk) mk->mark(LUSTRINE_STAGE_DELTA, st);
+        k += 3;
+    } else {
+        launch_lists(mixed, p, s->cp, s->xs[o], s->start, s->solid, s->sstart, s->nbr, s->cnt,
+                     s->status, st);
+        k += 1;
+        if (mk) mk->mark(LUSTRINE_STAGE_LISTS, st);
+        float4* a = s->xs[o];
+        float4* b = s->xs_alt;
+        const int iters = s->prm.iterations;
+        for (int it = 0; it < iters; it++) {
+            launch_lambda(mixed, p, s->cp, a, s->nbr, s->cnt, s->solid, s->lam, s->rho, st);
+            if (mk) mk->mark(LUSTRINE_STAGE_LAMBDA, st);
+            launch_delta(mixed, p, s->cp, a, b, s->nbr, s->cnt, s->solid, s->lam, s->x[o],
+                         it == iters - 1 ? s->vtmp : nullptr, st);
+            if (mk) mk->mark(LUSTRINE_STAGE_DELTA, st);
+            float4* t = a;
+            a = b;
+            b = t;
+            k += 2;
+        }
+        launch_xsph(mixed, p, s->cp, a, s->vtmp, s->nbr, s->cnt, s->x[o], s->v[o], st);
+        k += 1;
+        if (mk) mk->mark(LUSTRINE_STAGE_XSPH, st);
+    }
+    return k;
+}
+
+extern "C" int lustrine_pbf_step(lustrine_pbf* s, float dt) {
+    if (!s || !s->have_state) return LUSTRINE_ERR_ARGS;
+    if (!(dt > 0.0f) || !std::isfinite(dt)) return LUSTRINE_ERR_ARGS;
+    if (s->prm.mode == LUSTRINE_MODE_REFERENCE) {
+        // Simulate.cpp:31: dt = glm::clamp(dt, 0.001f, 0.01f)
+        dt = dt < 0.001f ? 0.001f : dt;
+        dt = dt > 0.01f ? 0.01f : dt;
+    }
+    if (s->sp.dt != dt) {
+        s->sp.dt = dt;
+        s->invalidate_graphs();
+    }
+    const int c = s->cur;
+    if (s->prm.use_graph) {
+        if (!s->graph_exec[c]) {
+            cudaGraph_t g = nullptr;
+            CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+            s->launches = enqueue_step(s, s->stream);
+            cudaError_t e = cudaStreamEndCapture(s->stream, &g);
+            if (e != cudaSuccess) return lgb_cuda_status(e, "cudaStreamEndCapture");
+            e = cudaGraphInstantiate(&s->graph_exec[c], g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) return lgb_cuda_status(e, "cudaGraphInstantiate");
+        }
+        CK(cudaGraphLaunch(s->graph_exec[c], s->stream));
+    } else {
+        s->launches = enqueue_step(s, s->stream);
+        CK(cudaGetLastError());
+    }
+    s->cur = 1 - c;
+    s->lists_valid = true;
+    s->steps_done++;
+    return LUSTRINE_OK;
+}
+
+extern "C" int lustrine_pbf_steps(lustrine_pbf* s, float dt, int count) {
+    if (count < 0) return LUSTRINE_ERR_ARGS;
+    for (int k = 0; k < count; k++) {
+        int rc = lustrine_pbf_step(s, dt);
+        if (rc) return rc;
+    }
+    return LUSTRINE_OK;
+}
+
+extern "C" int lustrine_pbf_profile_step(lustrine_pbf* s, float dt, double* stage_ms,
+                                         int* stage_launches, int num_stages) {
+    if (!s || !s->have_state || !stage_ms || num_stages <= 0) return LUSTRINE_ERR_ARGS;
+    if (!(dt > 0.0f) || !std::isfinite(dt)) return LUSTRINE_ERR_ARGS;
+    if (s->prm.mode == LUSTRINE_MODE_REFERENCE) {
+        dt = dt < 0.001f ? 0.001f : dt;
+        dt = dt > 0.01f ? 0.01f : dt;
+    }
+    if (s->sp.dt != dt) {
+        s->sp.dt = dt;
+        s->invalidate_graphs();
+    }
+    StageMarks mk;
+    for (int e = 0; e < 64; e++) CK(cudaEventCreate(&mk.ev[e]));
+    s->launches = enqueue_step(s, s->stream, &mk);
+    cudaError_t err = cudaGetLastError();
+    if (err == cudaSuccess) err = cudaStreamSynchronize(s->stream);
+    for (int k = 0; k < num_stages; k++) {
+        stage_ms[k] = 0.0;
+        if (stage_launches) stage_launches[k] = 0;
+    }
+    if (err == cudaSuccess)
+        for (int e = 1; e < mk.count; e++) {
+            float ms = 0.0f;
+            cudaEventElapsedTime(&ms, mk.ev[e - 1], mk.ev[e]);
+            const int stg = mk.stage[e];
+            if (stg >= 0 && stg < num_stages) {
+                stage_ms[stg] += ms;
+                if (stage_launches) stage_launches[stg] += 1;
+            }
+        }
+    for (int e = 0; e < 64; e++) cudaEventDestroy(mk.ev[e]);
+    if (err != cudaSuccess) return lgb_cuda_status(err, "profile_step");
+    s->cur = 1 - s->cur;
+    s->lists_valid = true;
+    s->steps_done++;
+    return LUSTRINE_OK;
+}
+
+extern "C" int lustrine_pbf_synchronize(lustrine_pbf* s) {
+    if (!s) return LUSTRINE_ERR_ARGS;
+    CK(cudaStreamSynchronize(s->stream));
+    return LUSTRINE_OK;
+}
+
+// Device-side unpermute of the current state into out3 (positions) /
+// out3d (velocities) in caller order.
+static void unpermute_state(lustrine_pbf* s, bool pos, bool vel) {
+    const int c = s->cur;
+    if (pos) launch_unpermute_pos(s->mixed(), s->sp, s->cp, s->x[c], s->id[c], s->n, s->out3, s->stream);
+    if (vel)
+        launch_unpermute_pos(false, s->sp, s->cp, s->v[c], s->id[c], s->n, (float*)s->out3d, s->stream);
+}
+
+extern "C" int lustrine_pbf_download(lustrine_pbf* s, float* x, float* v, float* lambdas, float* density) {
+    if (!s || !s->have_state) return LUSTRINE_ERR_ARGS;
+    const int n = s->n;
+    if (!n) return LUSTRINE_OK;
+    const size_t b3 = (size_t)n * 3 * sizeof(float);
+    unpermute_state(s, x != nullptr, v != nullptr);
+    if (x) CK(cudaMemcpyAsync(x, s->out3, b3, cudaMemcpyDeviceToHost, s->stream));
+    if (v) CK(cudaMemcpyAsync(v, s->out3d, b3, cudaMemcpyDeviceToHost, s->stream));
+    if (lambdas || density) {
+        std::vector<int> ids((size_t)n);
+        CK(cudaMemcpyAsync(ids.data(), s->id[s->cur], (size_t)n * sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+        std::vector<float> lam((size_t)n), rho((size_t)n);
+        const bool ref = s->prm.mode == LUSTRINE_MODE_REFERENCE;
+        if (lambdas) {
+            if (ref)
+                CK(cudaMemcpyAsync(lambdas, s->lam_by_id, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+            else
+                CK(cudaMemcpyAsync(lam.data(), s->lam, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+        }
+        if (density) CK(cudaMemcpyAsync(rho.data(), s->rho, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+        for (int k = 0; k < n; k++) {
+            const int i = ids[(size_t)k];
+            if (lambdas && !ref) lambdas[i] = lam[(size_t)k];
+            if (density) density[i] = rho[(size_t)k];
+        }
+    }
+    CK(cudaStreamSynchronize(s->stream));
+    return LUSTRINE_OK;
+}
+
+extern "C" int lustrine_pbf_download_state_async(lustrine_pbf* s, float* x, float* v) {
+    if (!s || !s->have_state) return LUSTRINE_ERR_ARGS;
+    const int n = s->n;
+    if (!n) return LUSTRINE_OK;
+    const size_t b3 = (size_t)n * 3 * sizeof(float);
+    unpermute_state(s, x != nullptr, v != nullptr);
+    if (x) CK(cudaMemcpyAsync(x, s->out3, b3, cudaMemcpyDeviceToHost, s->stream));
+    if (v) CK(cudaMemcpyAsync(v, s->out3d, b3, cudaMemcpyDeviceToHost, s->stream));
+    return LUSTRINE_OK;
+}
+
+extern "C" int lustrine_pbf_download_positions_f64(lustrine_pbf* s, double* x) {
+    if (!s || !s->have_state || !x) return LUSTRINE_ERR_ARGS;
+    const int n = s->n;
+    if (!n) return LUSTRINE_OK;
+    launch_unpermute_pos_d(s->mixed(), s->sp, s->cp, s->x[s->cur], s->id[s->cur], n, s->out3d, s->stream);
+    CK(cudaMemcpyAsync(x, s->out3d, (size_t)n * 3 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return LUSTRINE_OK;
+}
+
+extern "C" int lustrine_pbf_neighbors(lustrine_pbf* s, int* count, int* idx, int cap) {
+    if (!s || !count || (idx && cap <= 0)) return LUSTRINE_ERR_ARGS;
+    if (!s->lists_valid) return LUSTRINE_ERR_ARGS;
+    const int n = s->n, maxn = s->sp.max_nbrs;
+    if (!n) return LUSTRINE_OK;
+    std::vector<int> cnt((size_t)n), ids((size_t)n), nbr((size_t)maxn * n), sid((size_t)s->ns);
+    // Lists refer to the sorted slots of the state the step started from:
+    // the committed side's id array maps fluid slots; solid slots map back
+    // through the solid sort permutation.
+    CK(cudaMemcpyAsync(cnt.data(), s->cnt, (size_t)n * sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaMemcpyAsync(ids.data(), s->id[s->cur], (size_t)n * sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaMemcpyAsync(nbr.data(), s->nbr, (size_t)maxn * n * sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+    if (s->ns) CK(cudaMemcpyAsync(sid.data(), s->solid_id, (size_t)s->ns * sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    int rc = LUSTRINE_OK;
+    for (int k = 0; k < n; k++) {
+        const int i = ids[(size_t)k];
+        const int c = cnt[(size_t)k];
+        count[i] = c;
+        if (!idx) continue;
+        if (c > cap) rc = LUSTRINE_ERR_NBR_OVERFLOW;
+        for (int e = 0; e < c && e < cap; e++) {
+            int j = nbr[(size_t)e * n + k];
+            idx[(size_t)i * cap + e] = j >= 0 ? ids[(size_t)j] : n + sid[(size_t)(-1 - j)];
+        }
+    }
+    return rc;
+}
+
+extern "C" int lustrine_pbf_reduce(lustrine_pbf* s, double out[9]) {
+    if (!s || !s->have_state || !out) return LUSTRINE_ERR_ARGS;
+    const int c = s->cur;
+    launch_reduce(s->mixed(), s->sp, s->cp, s->x[c], s->v[c], s->steps_done ? s->rho : nullptr, s->red,
+                  s->stream);
+    CK(cudaMemcpyAsync(out, s->red, 9 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    if (out[0] > 0.0)
+        for (int k = 5; k < 8; k++) out[k] /= out[0];
+    return LUSTRINE_OK;
+}
+
+extern "C" int lustrine_pbf_status(lustrine_pbf* s) {
+    if (!s) return LUSTRINE_ERR_ARGS;
+    int st[4] = {0, 0, 0, 0};
+    CK(cudaMemcpyAsync(st, s->status, sizeof(st), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    CK(cudaMemsetAsync(s->status, 0, sizeof(st), s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    if (st[0] & ST_TIMEOUT) return LUSTRINE_ERR_TIMEOUT;
+    if (st[0] & ST_NBR_OVERFLOW) return LUSTRINE_ERR_NBR_OVERFLOW;
+    if (st[0] & ST_CELL_RANGE) return LUSTRINE_ERR_CELL_RANGE;
+    if (st[0] & ST_BAD_VALUE) return LUSTRINE_ERR_BAD_VALUE;
+    return LUSTRINE_OK;
+}
+
+extern "C" int lustrine_pbf_stream(lustrine_pbf* s, void** stream) {
+    if (!s || !stream) return LUSTRINE_ERR_ARGS;
+    *stream = (void*)s->stream;
+    return LUSTRINE_OK;
+}
+
+extern "C" int lustrine_pbf_launches_per_step(const lustrine_pbf* s) {
+    if (!s) return -1;
+    int iters = s->prm.mode == LUSTRINE_MODE_REFERENCE ? 0 : s->prm.iterations;
+    return s->prm.mode == LUSTRINE_MODE_REFERENCE ? 10 : 9 + 2 * iters;
+}
+
+extern "C" const char* lustrine_error_string(int code) {
+    switch (code) {
+    case LUSTRINE_OK: return "ok";
+    case LUSTRINE_ERR_ARGS: return "invalid argument";
+    case LUSTRINE_ERR_CUDA: return "CUDA runtime error";
+    case LUSTRINE_ERR_NOMEM: return "out of memory";
+    case LUSTRINE_ERR_NBR_OVERFLOW: return "neighbour list capacity exceeded";
+    case LUSTRINE_ERR_CELL_RANGE: return "particle left the grid (cell clamped)";
+    case LUSTRINE_ERR_UNSUPPORTED: return "unsupported option";
+    case LUSTRINE_ERR_NO_SIMULATION: return "no simulation initialised";
+    case LUSTRINE_ERR_TIMEOUT: return "device wait timed out";
+    case LUSTRINE_ERR_BAD_VALUE: return "non-finite particle state";
+    default: return "unknown status";
+    }
+}

@@ -1,0 +1,66 @@
+// pbf_context.h -- the context behind lustrine_pbf_* (host-side definition).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "lustrine_gb300.h"
+#include "pbf_common.cuh"
+
+int lgb_cuda_status(cudaError_t e, const char* what);
+
+struct lustrine_pbf {
+    lustrine_pbf_params prm{};
+    lgb::StepParams sp{};
+    lgb::CellPack cp{};
+    int n = 0, ns = 0;
+    cudaStream_t stream = nullptr;
+
+    // fluid state, two sides: the committed state is on side `cur`; a step
+    // sorts it into side 1 - cur and solves there.
+    float4* x[2] = {nullptr, nullptr};
+    float4* xs[2] = {nullptr, nullptr};
+    float4* v[2] = {nullptr, nullptr};
+    int* id[2] = {nullptr, nullptr};
+    int cur = 0;
+    float4* xs_alt = nullptr;  // Jacobi ping-pong partner of xs
+    float4* vtmp = nullptr;    // velocities before XSPH
+    int* iota = nullptr;       // 0..n-1
+
+    // counting sort
+    int* key = nullptr;
+    int* key_sorted = nullptr;
+    int* rank = nullptr;
+    int* tmp = nullptr;
+    int* perm = nullptr;
+    int* count = nullptr;
+    int* start = nullptr;
+    int* block_sums = nullptr;
+
+    // static solids, sorted by cell
+    float4* solid = nullptr;
+    float4* solid_raw = nullptr;
+    int* solid_id = nullptr;   // caller's solid index of each sorted slot
+    int* sstart = nullptr;
+
+    // neighbour lists and per-particle outputs
+    int* nbr = nullptr;
+    int* cnt = nullptr;
+    float* lam = nullptr;
+    float* lam_by_id = nullptr;
+    size_t lam_by_id_len = 0;
+    float* rho = nullptr;
+    int* status = nullptr;
+    double* red = nullptr;
+    float* out3 = nullptr;    // 3 * max(n, ns) floats of staging
+    double* out3d = nullptr;  // 3 * n doubles of staging
+
+    cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};
+    int launches = 0;
+    long long steps_done = 0;
+    bool have_state = false;
+    bool lists_valid = false;
+
+    ~lustrine_pbf();
+    void invalidate_graphs();
+    bool mixed() const;
+};

@@ -1,0 +1,61 @@
+// pbf_kernels.h -- host-side launchers of the PBF kernels (one scene).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "pbf_common.cuh"
+
+namespace lgb {
+
+// pbf_sort.cu
+void launch_scan(const int* count, int C, int* block_sums, int* start, cudaStream_t st);
+int scan_block_sums_size(int C);
+void launch_sort_tail(const int* key, const int* rank, const int* start, const int* tie, int n,
+                      int* tmp, int* perm, cudaStream_t st);
+void launch_gather_state(const int* perm, int n, const int* key, const float4* x, const float4* xs,
+                         const float4* v, const int* id, int* key_out, float4* x_out,
+                         float4* xs_out, float4* v_out, int* id_out, cudaStream_t st);
+void launch_gather_solid(const int* perm, int n, const float4* src, float4* dst, cudaStream_t st);
+
+// pbf_compat.cu (reference semantics, no FMA contraction)
+void launch_predict_ref(const StepParams& p, const float4* x, float4* v, float4* xs, int* key,
+                        int* rank, int* count, int* status, cudaStream_t st);
+void launch_key_ref(const StepParams& p, const float4* pos, int m, int* key, int* rank, int* count,
+                    int* status, cudaStream_t st);
+void launch_lists_ref(const StepParams& p, const float4* xs, const int* key, const int* fstart,
+                      const float4* solid, const int* sstart, int* nbr, int* cnt, int* status,
+                      cudaStream_t st);
+void launch_lambda_ref(const StepParams& p, const float4* xs, const int* id, const int* nbr,
+                       const int* cnt, const float4* solid, float* lam_by_id, float* rho,
+                       cudaStream_t st);
+void launch_delta_ref(const StepParams& p, const float4* xs, float4* xs_out, float4* x, float4* v,
+                      const int* id, const int* nbr, const int* cnt, const float4* solid,
+                      const float* lam_by_id, cudaStream_t st);
+
+// pbf_solver.cu (PBF; mixed = cell index + offset representation)
+void launch_predict(bool mixed, const StepParams& p, const CellPack& cp, const float4* x, float4* v,
+                    float4* xs, int* key, int* rank, int* count, cudaStream_t st);
+void launch_key(bool mixed, const StepParams& p, const CellPack& cp, const float4* pos, int m,
+                int* key, int* rank, int* count, cudaStream_t st);
+void launch_lists(bool mixed, const StepParams& p, const CellPack& cp, const float4* xs,
+                  const int* fstart, const float4* solid, const int* sstart, int* nbr, int* cnt,
+                  int* status, cudaStream_t st);
+void launch_lambda(bool mixed, const StepParams& p, const CellPack& cp, const float4* xs,
+                   const int* nbr, const int* cnt, const float4* solid, float* lam, float* rho,
+                   cudaStream_t st);
+void launch_delta(bool mixed, const StepParams& p, const CellPack& cp, const float4* xs,
+                  float4* xs_out, const int* nbr, const int* cnt, const float4* solid,
+                  const float* lam, const float4* x, float4* v_out, cudaStream_t st);
+void launch_xsph(bool mixed, const StepParams& p, const CellPack& cp, const float4* xs,
+                 const float4* v_in, const int* nbr, const int* cnt, float4* x_out, float4* v_out,
+                 cudaStream_t st);
+void launch_unpermute_pos(bool mixed, const StepParams& p, const CellPack& cp, const float4* a,
+                          const int* id, int n, float* out, cudaStream_t st);
+void launch_unpermute_pos_d(bool mixed, const StepParams& p, const CellPack& cp, const float4* a,
+                            const int* id, int n, double* out, cudaStream_t st);
+void launch_pack_pos(bool mixed, const StepParams& p, const CellPack& cp, const float* in, int n,
+                     float4* out, cudaStream_t st);
+void launch_reduce(bool mixed, const StepParams& p, const CellPack& cp, const float4* x,
+                   const float4* v, const float* rho, double* out, cudaStream_t st);
+
+}  // namespace lgb

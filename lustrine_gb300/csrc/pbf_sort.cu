@@ -1,0 +1,181 @@
+// pbf_sort.cu -- cell counting sort of particles, rebuilt every step.
+//
+// The reference bins particles into a vector per cell (Neighbors.cpp:370-384);
+// its counting sort (Sorting.cpp:12-34) is histogram -> prefix scan -> stable
+// scatter.  The GPU form:
+//   1. histogram: the prediction kernel does atomicAdd(count[key]) and keeps
+//      the returned value as the particle's provisional rank in its cell;
+//   2. exclusive scan of count over all cells (reduce, scan block sums,
+//      down-sweep; no inter-block waits);
+//   3. scatter of particle indices to start[key] + rank;
+//   4. stabilisation: atomic arrival order is arbitrary, so each slot counts
+//      the members of its cell with a smaller tie key (previous slot, or the
+//      caller's id in compat mode) and moves to that rank -- the result is
+//      the stable order of the reference's counting sort;
+//   5. one gather of the particle state into the new order.
+#include "pbf_common.cuh"
+#include "pbf_kernels.h"
+
+namespace lgb {
+
+constexpr int SCAN_THREADS = 256;
+constexpr int SCAN_ITEMS = 8;
+constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+
+__device__ __forceinline__ int warp_inclusive_scan(int v) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += t;
+    }
+    return v;
+}
+
+// Exclusive scan of one value per thread across the block; returns the
+// exclusive prefix and writes the block total to *total.
+__device__ __forceinline__ int block_exclusive_scan(int v, int* total) {
+    __shared__ int warp_sums[SCAN_THREADS / 32 + 1];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int inc = warp_inclusive_scan(v);
+    if (lane == 31) warp_sums[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+        int w = lane < SCAN_THREADS / 32 ? warp_sums[lane] : 0;
+        int wi = warp_inclusive_scan(w);
+        if (lane < SCAN_THREADS / 32) warp_sums[lane] = wi - w;
+        if (lane == SCAN_THREADS / 32 - 1) warp_sums[SCAN_THREADS / 32] = wi;
+    }
+    __syncthreads();
+    int res = inc - v + warp_sums[warp];
+    *total = warp_sums[SCAN_THREADS / 32];
+    __syncthreads();
+    return res;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(const int* __restrict__ count, int C,
+                                                              int* __restrict__ block_sums) {
+    const int base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_ITEMS;
+    int s = 0;
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; k++)
+        if (base + k < C) s += count[base + k];
+    int total;
+    block_exclusive_scan(s, &total);
+    if (threadIdx.x == 0) block_sums[blockIdx.x] = total;
+}
+
+// One block: exclusive scan of the per-tile sums, in place.
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_sums(int* __restrict__ block_sums, int nb) {
+    int carry = 0;
+    for (int base = 0; base < nb; base += SCAN_THREADS) {
+        int i = base + threadIdx.x;
+        int v = i < nb ? block_sums[i] : 0;
+        int total;
+        int ex = block_exclusive_scan(v, &total);
+        if (i < nb) block_sums[i] = ex + carry;
+        carry += total;
+    }
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_down(const int* __restrict__ count, int C,
+                                                            const int* __restrict__ block_sums,
+                                                            int* __restrict__ start) {
+    const int base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_ITEMS;
+    int vals[SCAN_ITEMS];
+    int s = 0;
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; k++) {
+        vals[k] = base + k < C ? count[base + k] : 0;
+        s += vals[k];
+    }
+    int total;
+    int ex = block_exclusive_scan(s, &total) + block_sums[blockIdx.x];
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; k++) {
+        if (base + k < C) start[base + k] = ex;
+        ex += vals[k];
+    }
+    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == SCAN_THREADS - 1) start[C] = ex;
+}
+
+__global__ void k_scatter_index(const int* __restrict__ key, const int* __restrict__ rank,
+                                const int* __restrict__ start, int n, int* __restrict__ tmp) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) tmp[start[key[i]] + rank[i]] = i;
+}
+
+__global__ void k_stabilize(const int* __restrict__ tmp, const int* __restrict__ key,
+                            const int* __restrict__ start, const int* __restrict__ tie, int n,
+                            int* __restrict__ perm) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const int i = tmp[s];
+    const int c = key[i];
+    const int a = start[c], b = start[c + 1];
+    const int mine = tie ? tie[i] : i;
+    int r = 0;
+    for (int t = a; t < b; t++) {
+        int o = tmp[t];
+        int ot = tie ? tie[o] : o;
+        r += ot < mine;
+    }
+    perm[a + r] = i;
+}
+
+__global__ void k_gather_state(const int* __restrict__ perm, int n, const int* __restrict__ key,
+                               const float4* __restrict__ x, const float4* __restrict__ xs,
+                               const float4* __restrict__ v, const int* __restrict__ id,
+                               int* __restrict__ key_out, float4* __restrict__ x_out,
+                               float4* __restrict__ xs_out, float4* __restrict__ v_out,
+                               int* __restrict__ id_out) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const int i = perm[s];
+    key_out[s] = key[i];
+    x_out[s] = x[i];
+    xs_out[s] = xs[i];
+    v_out[s] = v[i];
+    id_out[s] = id[i];
+}
+
+__global__ void k_gather_solid(const int* __restrict__ perm, int n, const float4* __restrict__ src,
+                               float4* __restrict__ dst) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < n) dst[s] = src[perm[s]];
+}
+
+// ------------------------------------------------------------------ launch --
+
+static inline int blocks_for(int n, int t) { return (n + t - 1) / t; }
+
+void launch_scan(const int* count, int C, int* block_sums, int* start, cudaStream_t st) {
+    int nb = blocks_for(C, SCAN_TILE);
+    k_scan_reduce<<<nb, SCAN_THREADS, 0, st>>>(count, C, block_sums);
+    k_scan_sums<<<1, SCAN_THREADS, 0, st>>>(block_sums, nb);
+    k_scan_down<<<nb, SCAN_THREADS, 0, st>>>(count, C, block_sums, start);
+}
+
+int scan_block_sums_size(int C) { return blocks_for(C, SCAN_TILE) + 1; }
+
+void launch_sort_tail(const int* key, const int* rank, const int* start, const int* tie, int n,
+                      int* tmp, int* perm, cudaStream_t st) {
+    if (n <= 0) return;
+    k_scatter_index<<<blocks_for(n, 256), 256, 0, st>>>(key, rank, start, n, tmp);
+    k_stabilize<<<blocks_for(n, 256), 256, 0, st>>>(tmp, key, start, tie, n, perm);
+}
+
+void launch_gather_state(const int* perm, int n, const int* key, const float4* x, const float4* xs,
+                         const float4* v, const int* id, int* key_out, float4* x_out,
+                         float4* xs_out, float4* v_out, int* id_out, cudaStream_t st) {
+    if (n <= 0) return;
+    k_gather_state<<<blocks_for(n, 256), 256, 0, st>>>(perm, n, key, x, xs, v, id, key_out, x_out,
+                                                       xs_out, v_out, id_out);
+}
+
+void launch_gather_solid(const int* perm, int n, const float4* src, float4* dst, cudaStream_t st) {
+    if (n <= 0) return;
+    k_gather_solid<<<blocks_for(n, 256), 256, 0, st>>>(perm, n, src, dst);
+}
+
+}  // namespace lgb

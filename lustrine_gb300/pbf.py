@@ -1,0 +1,199 @@
+"""Python host side of the GB300 PBF step: a thin object over the lustrine_pbf_*
+context API of liblustrine_gb300.so.
+
+    sim = PbfSim(params, n_fluid, n_solid)
+    sim.upload(x, v, solid)          # numpy (n, 3) float32 arrays, caller order
+    sim.step(dt)                     # CUDA kernels, asynchronous
+    x, v = sim.positions(), sim.velocities()
+
+Particle ids: fluid 0..n-1 in the caller's order; solids n..n+ns-1 in the
+order given to upload (the reference's storage order of solids).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import (MODE_PBF, MODE_REFERENCE, PRECISION_FP32, PRECISION_MIXED, LustrineError,
+                   PbfParams, check)
+
+__all__ = ["PbfSim", "PbfParams", "reference_params", "pbf_params", "MODE_PBF", "MODE_REFERENCE",
+           "PRECISION_FP32", "PRECISION_MIXED", "LustrineError"]
+
+
+def reference_params(X, Y, Z, radius=0.5, kernel_radius_scale=2.0) -> PbfParams:
+    """Parameters as init_simulation_extra_parameters sets them
+    (Lustrine.cpp:543-555) with the reference's physical defaults
+    (Simulation.hpp:147-171), in reference mode."""
+    p = PbfParams()
+    _lib.load().lustrine_pbf_params_reference(C.byref(p), X, Y, Z, radius, kernel_radius_scale)
+    return p
+
+
+def pbf_params(X, Y, Z, *, radius=0.5, h=1.0, rest_density=1.0, mass=1.0, gravity=-9.81,
+               iterations=4, s_corr_k=0.1, s_corr_n=4.0, s_corr_dq_frac=0.2, c_xsph=0.01,
+               epsilon=10.0, precision=PRECISION_FP32, max_neighbors=64, use_graph=True) -> PbfParams:
+    """PBF-mode parameters of the benchmark scenes (dam breaks at unit spacing)."""
+    p = reference_params(X, Y, Z, radius, h / radius)
+    p.mode = MODE_PBF
+    p.precision = precision
+    p.rest_density = rest_density
+    p.mass = mass
+    p.gravity[0], p.gravity[1], p.gravity[2] = 0.0, gravity, 0.0
+    p.relaxation_epsilon = epsilon
+    p.iterations = iterations
+    p.s_corr_k = s_corr_k
+    p.s_corr_n = s_corr_n
+    p.s_corr_dq = s_corr_dq_frac * h
+    p.c_xsph = c_xsph
+    p.solid_contact = 2.0 * radius
+    p.max_neighbors = max_neighbors
+    p.use_graph = 1 if use_graph else 0
+    return p
+
+
+def _f32(a, n):
+    a = np.ascontiguousarray(a, dtype=np.float32).reshape(-1)
+    if a.size != 3 * n:
+        raise ValueError(f"expected {3 * n} floats, got {a.size}")
+    return a
+
+
+def _ptr(a):
+    return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+class PbfSim:
+    """One scene on the GPU (a lustrine_pbf context)."""
+
+    def __init__(self, params: PbfParams, n_fluid: int, n_solid: int = 0):
+        self.lib = _lib.load()
+        self.params = params
+        self.n = int(n_fluid)
+        self.ns = int(n_solid)
+        h = C.c_void_p()
+        check(self.lib.lustrine_pbf_create(C.byref(params), self.n, self.ns, C.byref(h)),
+              "lustrine_pbf_create")
+        self.h = h
+
+    # lifecycle -------------------------------------------------------------
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            self.lib.lustrine_pbf_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # state in --------------------------------------------------------------
+    def upload(self, x, v=None, solid=None):
+        x = _f32(x, self.n)
+        v = None if v is None else _f32(v, self.n)
+        s = None if (solid is None or self.ns == 0) else _f32(solid, self.ns)
+        check(self.lib.lustrine_pbf_upload(self.h, _ptr(x), _ptr(v), _ptr(s)), "upload")
+
+    def upload_device(self, x_ptr: int, v_ptr: int | None, solid_ptr: int | None):
+        """Device pointers (e.g. torch tensors' data_ptr()) of 3 floats per particle."""
+        check(self.lib.lustrine_pbf_upload_device(self.h, C.c_void_p(x_ptr),
+                                                  C.c_void_p(v_ptr) if v_ptr else None,
+                                                  C.c_void_p(solid_ptr) if solid_ptr else None),
+              "upload_device")
+
+    def upload_state_async(self, x_ptr: int, v_ptr: int | None):
+        """Host pointers (page-locked for asynchrony) of x and v, 3 floats each."""
+        check(self.lib.lustrine_pbf_upload_state_async(self.h, C.c_void_p(x_ptr),
+                                                       C.c_void_p(v_ptr) if v_ptr else None),
+              "upload_state_async")
+
+    def set_params(self, params: PbfParams):
+        check(self.lib.lustrine_pbf_set_params(self.h, C.byref(params)), "set_params")
+        self.params = params
+
+    # stepping --------------------------------------------------------------
+    def step(self, dt: float, count: int = 1):
+        check(self.lib.lustrine_pbf_steps(self.h, float(dt), int(count)), "step")
+
+    def synchronize(self):
+        check(self.lib.lustrine_pbf_synchronize(self.h), "synchronize")
+
+    def stream(self) -> int:
+        s = C.c_void_p()
+        check(self.lib.lustrine_pbf_stream(self.h, C.byref(s)), "stream")
+        return s.value or 0
+
+    def launches_per_step(self) -> int:
+        return int(self.lib.lustrine_pbf_launches_per_step(self.h))
+
+    # state out -------------------------------------------------------------
+    def download(self, x=True, v=True, lambdas=False, density=False):
+        n = self.n
+        ax = np.empty((n, 3), np.float32) if x else None
+        av = np.empty((n, 3), np.float32) if v else None
+        al = np.empty(n, np.float32) if lambdas else None
+        ad = np.empty(n, np.float32) if density else None
+        check(self.lib.lustrine_pbf_download(self.h, _ptr(ax), _ptr(av), _ptr(al), _ptr(ad)),
+              "download")
+        return ax, av, al, ad
+
+    def download_state_async(self, x_ptr: int, v_ptr: int | None):
+        check(self.lib.lustrine_pbf_download_state_async(self.h, C.c_void_p(x_ptr),
+                                                         C.c_void_p(v_ptr) if v_ptr else None),
+              "download_state_async")
+
+    def positions(self):
+        return self.download(x=True, v=False)[0]
+
+    def velocities(self):
+        return self.download(x=False, v=True)[1]
+
+    def lambdas(self):
+        return self.download(x=False, v=False, lambdas=True)[2]
+
+    def density(self):
+        return self.download(x=False, v=False, density=True)[3]
+
+    def positions_f64(self):
+        out = np.empty((self.n, 3), np.float64)
+        check(self.lib.lustrine_pbf_download_positions_f64(self.h, _ptr(out)), "positions_f64")
+        return out
+
+    def neighbors(self, cap: int | None = None):
+        """(count[n], idx[n, cap]) of the last step, in particle ids."""
+        cap = cap or self.params.max_neighbors
+        cnt = np.zeros(self.n, np.int32)
+        idx = np.full((self.n, cap), -1, np.int32)
+        check(self.lib.lustrine_pbf_neighbors(self.h, _ptr(cnt), _ptr(idx), cap), "neighbors")
+        return cnt, idx
+
+    def reduce(self):
+        """FP64 device reductions: mass, momentum[3], kinetic energy,
+        centre of mass[3], max |rho/rho0 - 1|."""
+        out = (C.c_double * 9)()
+        check(self.lib.lustrine_pbf_reduce(self.h, out), "reduce")
+        r = list(out)
+        return dict(mass=r[0], momentum=r[1:4], kinetic=r[4], com=r[5:8], max_density_error=r[8])
+
+    STAGES = ("predict", "scan", "sort", "lists", "lambda", "delta", "xsph")
+
+    def profile_step(self, dt: float) -> dict:
+        """One step with a CUDA event after each stage (direct launches):
+        {stage: (milliseconds, events)}."""
+        ms = (C.c_double * len(self.STAGES))()
+        cnt = (C.c_int * len(self.STAGES))()
+        check(self.lib.lustrine_pbf_profile_step(self.h, float(dt), ms, cnt, len(self.STAGES)),
+              "profile_step")
+        return {k: (ms[i], cnt[i]) for i, k in enumerate(self.STAGES)}
+
+    def status(self) -> int:
+        return int(self.lib.lustrine_pbf_status(self.h))

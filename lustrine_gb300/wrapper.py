@@ -1,0 +1,129 @@
+"""Python mirror of the reference's C entry points (Lustrine::Wrapper,
+src/LustrineWrapper.hpp:86-171) as exported by liblustrine_gb300.so.
+
+The calls keep the reference's names and argument meaning; unlike the
+reference, each one's outcome is available from last_status().
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import Color, GridWrapper, SimulationData, SimulationParameters, Vec3
+
+__all__ = ["SimulationParameters", "SimulationData", "GridWrapper", "Vec3", "Color",
+           "init_grid_box", "init_simulation", "init_simulation_extra_parameters", "simulate",
+           "simulate_no_flags", "simulation_bind_positions_copy", "cleanup_simulation",
+           "get_num_sand_particles", "get_grid_cell_size", "set_simulate_function",
+           "last_status", "free_grid"]
+
+
+def _lib_():
+    return _lib.load()
+
+
+def init_grid_box(params: SimulationParameters, X, Y, Z, position, color=(1, 0, 0, 1), type_=1):
+    g = GridWrapper()
+    _lib_().init_grid_box(C.byref(params), C.byref(g), X, Y, Z, Vec3(*position), Color(*color), type_)
+    return g
+
+
+def grid_from_cells(cells: np.ndarray, position, type_=0, color=(1, 1, 1, 1)):
+    """A GridWrapper over an occupancy array indexed [x, y, z] (the reference's
+    grid index x * Y * Z + y * Z + z).  Keep the returned array alive."""
+    cells = np.ascontiguousarray(cells, np.int32)
+    X, Y, Z = cells.shape
+    g = GridWrapper()
+    g.cells = cells.ctypes.data_as(C.POINTER(C.c_int))
+    g.colors = C.POINTER(Color)()
+    g.color = Color(*color)
+    g.position = Vec3(*position)
+    g.has_one_color_per_cell = False
+    g.X, g.Y, g.Z = X, Y, Z
+    g.num_grid_cells = X * Y * Z
+    g.num_occupied_grid_cells = int((cells != 0).sum())
+    g.type = type_
+    return g, cells
+
+
+def free_grid(g: GridWrapper):
+    _lib_().lustrine_free_grid(C.byref(g))
+
+
+def _grid_array(grids):
+    arr = (GridWrapper * max(len(grids), 1))(*grids)
+    return arr
+
+
+def init_simulation(params, sand, solid=(), subdivision=1):
+    data = SimulationData()
+    sa, so = _grid_array(sand), _grid_array(solid)
+    _lib_().init_simulation(C.byref(params), C.byref(data), sa, len(sand), so, len(solid), subdivision)
+    return data
+
+
+def init_simulation_extra_parameters(params, sand, solid=(), subdivision=1, kernel_radius_scale=2.0,
+                                     with_credits=0):
+    data = SimulationData()
+    sa, so = _grid_array(sand), _grid_array(solid)
+    _lib_().init_simulation_extra_parameters(C.byref(params), C.byref(data), sa, len(sand), so,
+                                             len(solid), subdivision, kernel_radius_scale,
+                                             with_credits)
+    return data
+
+
+def simulate(dt, attract=False, blow=False):
+    _lib_().simulate(dt, attract, blow)
+
+
+def simulate_no_flags(dt):
+    _lib_().simulate_no_flags(dt)
+
+
+def simulation_bind_positions_copy(out: np.ndarray | None = None) -> np.ndarray:
+    n = get_num_sand_particles()
+    if out is None:
+        out = np.empty((n, 3), np.float32)
+    _lib_().simulation_bind_positions_copy(out.ctypes.data_as(C.POINTER(C.c_float)))
+    return out
+
+
+def cleanup_simulation():
+    _lib_().cleanup_simulation()
+
+
+def get_num_sand_particles() -> int:
+    return int(_lib_().get_num_sand_particles())
+
+
+def get_grid_cell_size() -> int:
+    return int(_lib_().get_grid_cell_size())
+
+
+def set_simulate_function(index: int):
+    _lib_().set_simulate_function(index)
+
+
+def last_status() -> int:
+    return int(_lib_().lustrine_last_status())
+
+
+def global_context():
+    """The lustrine_pbf context behind the wrapper simulation (a PbfSim view)."""
+    from .pbf import PbfSim
+    h = _lib_().lustrine_global_context()
+    if not h:
+        return None
+    sim = PbfSim.__new__(PbfSim)
+    sim.lib = _lib_()
+    sim.h = C.c_void_p(h)
+    n, ns = C.c_int(), C.c_int()
+    _lib_().lustrine_pbf_counts(sim.h, C.byref(n), C.byref(ns))
+    sim.n, sim.ns = n.value, ns.value
+    p = _lib.PbfParams()
+    _lib_().lustrine_pbf_get_params(sim.h, C.byref(p))
+    sim.params = p
+    sim.close = lambda: None  # owned by the wrapper singleton
+    return sim

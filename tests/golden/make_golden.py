@@ -1,0 +1,136 @@
+"""Write the golden fixtures under tests/golden/ by running the reference's own
+code, compiled from the reference tree by `make -C oracle ref`.
+
+    python tests/golden/make_golden.py [--ref /root/reference]
+
+Fixtures (all from the reference binary, never from the restatement):
+  counting_sort.npz   Sorting::counting_sort on the unit test's input
+                      (experiments/unit_tests/main.cpp:46-89: 20,000 keys
+                      rand() % 1987 from glibc's default seed).
+  ref_c0_step.npz     one Lustrine::simulate step with simulate_fluid
+                      (Simulate.cpp:27-115) of the 10,000-particle dam break
+                      (20 x 25 x 20 block from (10, 0, 10), 40^3 box, r = 0.5,
+                      h = 1.0, rho0 = 1, m = 1, g = -9.81, s_corr 0.1 / 4 /
+                      0.2, jitter seed 0, dt = 1/60): input state, neighbour
+                      lists (CSR, reference order), lambdas, x* and x, v.
+  ref_solids_2step.npz  two steps of an 800-particle block (from (7, 3, 7),
+                      resting on the solid tops) over a seeded
+                      24 x 4 x 24 voxel heightmap (1,168 solids) in a
+                      24 x 16 x 24 box, same parameters.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import oracle as O  # noqa: E402
+from lustrine_gb300 import scenes  # noqa: E402
+
+PHYS = dict(rest_density=1.0, mass=1.0, gravity=(0.0, -9.81, 0.0), eps=10.0, dq=0.2, k=0.1, n=4.0)
+
+
+def csr(cnt, idx):
+    off = np.zeros(len(cnt) + 1, np.int64)
+    off[1:] = np.cumsum(cnt)
+    flat = np.concatenate([idx[i, : cnt[i]] for i in range(len(cnt))]) if len(cnt) else np.zeros(0)
+    return off.astype(np.int32), flat.astype(np.int32)
+
+
+def glibc_rand_keys(num, mod):
+    libc = ctypes.CDLL("libc.so.6")
+    libc.srand(1)
+    return np.array([libc.rand() % mod for _ in range(num)], np.int32)
+
+
+def make_counting_sort(R):
+    keys = glibc_rand_keys(20000, 1987)
+    perm = R.counting_sort(keys, 1987)
+    np.savez_compressed(os.path.join(HERE, "counting_sort.npz"), keys=keys, num_cells=1987,
+                        perm=perm)
+
+
+def set_phys(R):
+    R.set_params(PHYS["rest_density"], PHYS["mass"], PHYS["gravity"], PHYS["eps"], PHYS["dq"],
+                 PHYS["k"], PHYS["n"])
+
+
+def make_c0(R):
+    sc = scenes.config0(seed=0)
+    n = R.init(40, 40, 40, (20, 25, 20), (10, 0, 10))
+    assert n == sc.n
+    x0_ref, _, _, _ = R.state()
+    assert np.array_equal(x0_ref, scenes.lattice((20, 25, 20), (10, 0, 10)))
+    set_phys(R)
+    v0 = np.zeros_like(sc.x)
+    R.set_state(sc.x, v0)
+    dt = np.float32(1.0 / 60.0)
+    R.step(dt)
+    x, xs, v, lam = R.state()
+    cnt, idx = R.neighbors(cap=256)
+    off, flat = csr(cnt, idx)
+    np.savez_compressed(os.path.join(HERE, "ref_c0_step.npz"), domain=np.array([40, 40, 40]),
+                        x0=sc.x, v0=v0, dt=dt, x=x, xs=xs, v=v, lam=lam, nbr_off=off, nbr=flat,
+                        grid=np.array([R.info(7), R.info(8), R.info(9)]), floats=R.floats(),
+                        ptrs=np.array([R.info(k) for k in range(5)]))
+
+
+def solid_grid(seed=7):
+    rng = np.random.default_rng(seed)
+    GX, GY, GZ = 24, 4, 24
+    H = rng.integers(1, 4, size=(GX, GZ))
+    cells = np.zeros((GX, GY, GZ), np.int32)
+    for xx in range(GX):
+        for zz in range(GZ):
+            cells[xx, : H[xx, zz], zz] = 1
+    return cells, rng
+
+
+def make_solids(R):
+    cells, rng = solid_grid()
+    n = R.init(24, 16, 24, (10, 8, 10), (7, 3, 7), solids=[(cells.shape, (0, 0, 0), cells)])
+    set_phys(R)
+    x0_ref, _, _, _ = R.state()
+    x0 = (x0_ref + rng.uniform(-0.05, 0.05, x0_ref.shape)).astype(np.float32)
+    v0 = np.zeros_like(x0)
+    R.set_state(x0, v0)
+    solid = R.solids()
+    dt = np.float32(1.0 / 60.0)
+    out = dict(domain=np.array([24, 16, 24]), x0=x0, v0=v0, solid=solid, dt=dt, cells=cells,
+               ptrs=np.array([R.info(k) for k in range(5)]))
+    for s in (1, 2):
+        R.step(dt)
+        x, xs, v, lam = R.state()
+        cnt, idx = R.neighbors(cap=256)
+        off, flat = csr(cnt, idx)
+        out.update({f"x{s}": x, f"v{s}": v, f"lam{s}": lam, f"nbr_off{s}": off, f"nbr{s}": flat})
+    np.savez_compressed(os.path.join(HERE, "ref_solids_2step.npz"), **out)
+    return n
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    a = ap.parse_args()
+    path = O.build_ref(a.ref)
+    if not path:
+        raise SystemExit("the reference tree is not available; fixtures are committed")
+    R = O.Reference(path)
+    make_counting_sort(R)
+    make_c0(R)
+    make_solids(R)
+    R.L.ref_free()
+    for f in sorted(os.listdir(HERE)):
+        if f.endswith(".npz"):
+            print(f, os.path.getsize(os.path.join(HERE, f)))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,192 @@
+"""GPU PBF step against the CPU oracle (the FP64 restatement of the same
+step).  Tolerances: one step -- positions within 2e-5 of the box size,
+lambdas within 1e-4 of max |lambda|, densities within 1e-5 relative; the
+mixed-precision representation keeps the density within 1e-4 relative of the
+FP64 oracle evaluated at the GPU's own positions."""
+import numpy as np
+import pytest
+
+from conftest import rows_sets
+
+pytestmark = pytest.mark.gpu
+
+
+def _params(sc, **kw):
+    from lustrine_gb300 import pbf_params
+    p = pbf_params(*sc.domain, iterations=sc.iterations, c_xsph=sc.c_xsph)
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+def _oracle_params(orc, p):
+    q = orc.reference_params(p.domain[0], p.domain[1], p.domain[2], p.particle_radius,
+                             p.kernel_radius / p.particle_radius)
+    for f in ("rest_density", "mass", "relaxation_epsilon", "s_corr_dq", "s_corr_k", "s_corr_n",
+              "c_xsph", "solid_contact", "iterations"):
+        setattr(q, f, getattr(p, f))
+    for a in range(3):
+        q.gravity[a] = p.gravity[a]
+    return q
+
+
+def _small_solid_scene():
+    from lustrine_gb300 import scenes
+    rng = np.random.default_rng(5)
+    x = scenes.jitter(scenes.lattice((12, 10, 12), (6, 4, 6)), 0.05, rng)
+    solid, _ = scenes.heightmap_solids(24, 1500, origin=(0, 0, 0), rng=rng, max_height=5)
+    return scenes.Scene("small_solids", (24, 20, 24), x, solid, dt=1 / 60, iterations=4)
+
+
+@pytest.mark.parametrize("which", ["c0", "solids"])
+def test_pbf_one_step_matches_fp64_oracle(orc, which):
+    from lustrine_gb300 import PbfSim, scenes
+    sc = scenes.config0(seed=21) if which == "c0" else _small_solid_scene()
+    p = _params(sc)
+    sim = PbfSim(p, sc.n, sc.ns)
+    sim.upload(sc.x, None, sc.solid if sc.ns else None)
+    sim.step(sc.dt)
+    assert sim.status() == 0
+    x, v, lam, rho = sim.download(lambdas=True, density=True)
+    q = _oracle_params(orc, p)
+    o = orc.pbf_step(q, sc.dt, sc.x, np.zeros_like(sc.x), solid=sc.solid if sc.ns else None)
+    L = max(sc.domain)
+    assert np.abs(x - o["x"]).max() <= 2e-5 * L
+    assert np.abs(v - o["v"]).max() <= 2e-5 * L / sc.dt
+    assert np.abs(lam - o["lambdas"]).max() <= 1e-4 * np.abs(o["lambdas"]).max()
+    assert np.abs(rho - o["density"]).max() <= 1e-5 * np.abs(o["density"]).max()
+    cnt, _ = sim.neighbors()
+    # neighbour counts agree except for pairs at r = h within rounding
+    assert np.mean(cnt == o["nbr_count"]) > 0.999
+    sim.close()
+
+
+def test_pbf_neighbour_sets_exact_at_same_positions(orc):
+    """With iterations = 1, no gravity and dt tiny, x* = x: the neighbour sets
+    of the PBF lists equal the oracle's set of particles within h."""
+    from lustrine_gb300 import PbfSim, scenes
+    sc = _small_solid_scene()
+    p = _params(sc, iterations=1)
+    p.gravity[1] = 0.0
+    sim = PbfSim(p, sc.n, sc.ns)
+    sim.upload(sc.x, None, sc.solid)
+    sim.step(1e-6)
+    cnt, idx = sim.neighbors()
+    q = orc.reference_params(*sc.domain)
+    ocnt, oidx = orc.compat_neighbors(q, sc.x, sc.solid)
+    for a, b in zip(rows_sets(cnt, idx), rows_sets(ocnt, oidx)):
+        assert np.array_equal(a, b)
+    sim.close()
+
+
+def test_mixed_precision_density_error_vs_fp64(orc):
+    from lustrine_gb300 import PRECISION_MIXED, PbfSim, scenes
+    sc = scenes.config0(seed=22)
+    p = _params(sc, precision=PRECISION_MIXED)
+    sim = PbfSim(p, sc.n)
+    sim.upload(sc.x)
+    for _ in range(3):
+        sim.step(sc.dt)
+    assert sim.status() == 0
+    # density of the last lambda pass vs FP64 at the same predicted positions is
+    # checked through the committed state: recompute both at x
+    xd = sim.positions_f64()
+    q = _oracle_params(orc, p)
+    rho64 = orc.pbf_density(q, xd)
+    sim2 = PbfSim(_params(sc, precision=PRECISION_MIXED, iterations=1), sc.n)
+    sim2.upload(xd.astype(np.float32))
+    sim2.step(1e-7)  # a lambda pass at (almost) the committed positions
+    rho = sim2.density()
+    x2 = sim2.positions_f64()
+    rho64b = orc.pbf_density(q, x2)
+    assert np.abs(rho - rho64b).max() / np.abs(rho64b).max() <= 1e-4
+    assert np.isfinite(rho64).all()
+    sim.close()
+    sim2.close()
+
+
+def test_mixed_and_plain_agree_near_origin(orc):
+    from lustrine_gb300 import PRECISION_MIXED, PbfSim, scenes
+    sc = scenes.config0(seed=23)
+    out = []
+    for prec in (0, PRECISION_MIXED):
+        sim = PbfSim(_params(sc, precision=prec), sc.n)
+        sim.upload(sc.x)
+        sim.step(sc.dt, 2)
+        out.append(sim.positions())
+        sim.close()
+    assert np.abs(out[0] - out[1]).max() < 1e-3
+
+
+def test_graph_and_direct_launches_are_identical():
+    from lustrine_gb300 import PbfSim, scenes
+    sc = scenes.config0(seed=24)
+    res = []
+    for g in (True, False):
+        sim = PbfSim(_params(sc, use_graph=1 if g else 0), sc.n)
+        sim.upload(sc.x)
+        sim.step(sc.dt, 5)
+        res.append(sim.download())
+        sim.close()
+    assert np.array_equal(res[0][0], res[1][0]) and np.array_equal(res[0][1], res[1][1])
+
+
+def test_rollout_statistics_vs_fp64_oracle(orc):
+    """40 steps of the 10k dam break: kinetic energy, centre of mass and max
+    density error track the FP64 oracle run from the same state."""
+    from lustrine_gb300 import PbfSim, scenes
+    sc = scenes.config0(seed=25)
+    p = _params(sc)
+    q = _oracle_params(orc, p)
+    sim = PbfSim(p, sc.n)
+    sim.upload(sc.x)
+    x, v = sc.x.astype(np.float64), np.zeros((sc.n, 3))
+    for s in range(40):
+        sim.step(sc.dt)
+        o = orc.pbf_step(q, sc.dt, x, v)
+        x, v = o["x"], o["v"]
+        if s % 10 == 9:
+            r = sim.reduce()
+            ke64 = 0.5 * q.mass * (v ** 2).sum()
+            com64 = x.mean(0)
+            assert abs(r["mass"] - sc.n * q.mass) < 1e-6
+            assert abs(r["kinetic"] - ke64) <= 0.02 * ke64 + 1e-6
+            assert np.abs(np.array(r["com"]) - com64).max() <= 0.02
+            err64 = np.abs(o["density"] / q.rest_density - 1).max()
+            assert abs(r["max_density_error"] - err64) <= 0.02 * err64
+    xg = sim.positions()
+    assert (xg >= 0.5 - 1e-5).all() and (xg <= 39.5 + 1e-5).all()
+    sim.close()
+
+
+def test_neighbour_overflow_is_reported_not_faulted():
+    from lustrine_gb300 import PbfSim, scenes
+    sc = scenes.config0(seed=26)
+    sim = PbfSim(_params(sc, max_neighbors=2), sc.n)
+    sim.upload(sc.x)
+    sim.step(sc.dt)
+    assert sim.status() == 4  # LUSTRINE_ERR_NBR_OVERFLOW
+    assert sim.status() == 0  # cleared
+    sim.close()
+
+
+def test_edge_cases_empty_single_and_no_solids():
+    from lustrine_gb300 import LustrineError, PbfSim, pbf_params
+    p = pbf_params(8, 8, 8)
+    sim = PbfSim(p, 0, 0)
+    sim.upload(np.zeros((0, 3), np.float32))
+    sim.step(1 / 60)
+    assert sim.positions().shape == (0, 3)
+    sim.close()
+    sim = PbfSim(p, 1, 0)
+    sim.upload(np.array([[4.0, 4.0, 4.0]], np.float32))
+    sim.step(1 / 60, 10)
+    x = sim.positions()
+    assert x[0, 1] < 4.0 and np.isfinite(x).all()
+    sim.close()
+    with pytest.raises(LustrineError):
+        PbfSim(p, -1, 0)
+    bad = pbf_params(8, 8, 8)
+    bad.iterations = 0
+    with pytest.raises(LustrineError):
+        PbfSim(bad, 10, 0)

@@ -1,0 +1,140 @@
+"""GPU reference-mode step against the reference (golden vectors written by the
+reference's own code) and the oracle.  Contract: neighbour sets bit-exact as
+sets; lambdas, positions and velocities within 1e-5 relative error, with
+positions and velocities compared against the Jacobi form of the reference
+step (the GPU's update; the reference's in-place Gauss-Seidel sweep is
+sequential)."""
+import numpy as np
+import pytest
+
+from conftest import csr_sets, golden, phys_params, rows_sets
+
+pytestmark = pytest.mark.gpu
+
+REL = 1e-5
+
+
+def normwise_rel(a, b):
+    """Per-particle |a - b| / max(|b|, 1e-3 rms|b|)."""
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    nb = np.linalg.norm(b.reshape(len(b), -1), axis=1)
+    floor = 1e-3 * np.sqrt(np.mean(nb ** 2)) if nb.size else 1.0
+    return np.linalg.norm((a - b).reshape(len(b), -1), axis=1) / np.maximum(nb, floor)
+
+
+def _sim(domain, n, ns=0, **kw):
+    from lustrine_gb300 import PbfSim, reference_params
+    p = phys_params(reference_params(*domain))
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return PbfSim(p, n, ns)
+
+
+def test_reference_mode_c0_matches_reference(orc):
+    g = golden("ref_c0_step.npz")
+    n = len(g["x0"])
+    sim = _sim(tuple(int(a) for a in g["domain"]), n)
+    sim.upload(g["x0"], g["v0"])
+    sim.step(float(g["dt"]))
+    assert sim.status() == 0
+    cnt, idx = sim.neighbors(cap=256)
+    ref_sets = csr_sets(g["nbr_off"], g["nbr"])
+    gpu_sets = rows_sets(cnt, idx)
+    assert all(np.array_equal(a, b) for a, b in zip(gpu_sets, ref_sets))
+    # the GPU also reproduces the reference's list order
+    flat = np.concatenate([idx[i, :cnt[i]] for i in range(n)])
+    assert np.array_equal(flat, g["nbr"])
+    lam = sim.lambdas()
+    scale = np.abs(g["lam"]).max()
+    assert np.all(np.abs(lam - g["lam"]) <= REL * np.maximum(np.abs(g["lam"]), 1e-3 * scale))
+    # positions and velocities against the Jacobi form (oracle pinned to the reference)
+    p = phys_params(orc.reference_params(40, 40, 40))
+    p.jacobi = 1
+    o = orc.compat_step(p, float(g["dt"]), g["x0"], g["v0"])
+    x, v, _, _ = sim.download()
+    assert normwise_rel(x, o["x"]).max() <= REL
+    assert normwise_rel(v, o["v"]).max() <= REL
+    # and bitwise equality is the expected outcome (same operations, no FMA)
+    assert np.array_equal(lam, g["lam"])
+    assert np.array_equal(x, o["x"]) and np.array_equal(v, o["v"])
+    sim.close()
+
+
+def test_reference_mode_solids_two_steps(orc):
+    g = golden("ref_solids_2step.npz")
+    n, ns = len(g["x0"]), len(g["solid"])
+    domain = tuple(int(a) for a in g["domain"])
+    sim = _sim(domain, n, ns)
+    sim.upload(g["x0"], g["v0"], g["solid"])
+    p = phys_params(orc.reference_params(*domain))
+    p.jacobi = 1
+    o = dict(x=g["x0"], v=g["v0"], lambdas=None)
+    for s in (1, 2):
+        sim.step(float(g["dt"]))
+        o = orc.compat_step(p, float(g["dt"]), o["x"], o["v"], solid=g["solid"], lambdas=o["lambdas"])
+        cnt, idx = sim.neighbors(cap=256)
+        if s == 1:  # step 1 starts from the reference's own state
+            ref_sets = csr_sets(g["nbr_off1"], g["nbr1"])
+            assert all(np.array_equal(a, b) for a, b in zip(rows_sets(cnt, idx), ref_sets))
+            assert (g["nbr1"] >= n).any()
+            lam = sim.lambdas()
+            assert np.abs(lam - g["lam1"]).max() <= REL * np.abs(g["lam1"]).max()
+        assert all(np.array_equal(a, b) for a, b in
+                   zip(rows_sets(cnt, idx), rows_sets(o["nbr_count"], o["nbr_idx"])))
+        x, v, lam, _ = sim.download(lambdas=True)
+        assert normwise_rel(x, o["x"]).max() <= REL
+        assert normwise_rel(v, o["v"]).max() <= REL
+        assert np.abs(lam - o["lambdas"][:n]).max() <= REL * np.abs(o["lambdas"][:n]).max()
+    assert sim.status() == 0
+    sim.close()
+
+
+def test_reference_mode_rollout_matches_oracle(orc):
+    """20 steps (cell clamp on both sides, as the reference overflows its cell
+    table once particles leave the grid)."""
+    from lustrine_gb300 import scenes
+    sc = scenes.config0(seed=11)
+    sim = _sim(sc.domain, sc.n)
+    sim.upload(sc.x, None)
+    p = phys_params(orc.reference_params(*sc.domain))
+    p.jacobi = 1
+    p.clamp_cells = 1
+    o = dict(x=sc.x, v=np.zeros_like(sc.x), lambdas=None)
+    for _ in range(20):
+        sim.step(sc.dt)
+        o = orc.compat_step(p, sc.dt, o["x"], o["v"], lambdas=o["lambdas"])
+    x, v, _, _ = sim.download()
+    assert np.array_equal(x, o["x"]) and np.array_equal(v, o["v"])
+    sim.close()
+
+
+def test_wrapper_entry_points_drive_reference_mode(orc):
+    from lustrine_gb300 import wrapper as W
+    prm = W.SimulationParameters(24, 16, 24, 0.5, 1.0)
+    sand = W.init_grid_box(prm, 6, 5, 6, (8, 2, 8), type_=1)
+    data = W.init_simulation_extra_parameters(prm, [sand], [], 1, 2.0, 0)
+    assert W.last_status() == 0
+    assert data.num_sand_particles == 180 and data.end_sand_index == 180
+    assert data.start_solid_index == data.end_solid_index == 24 * 16 * 24 - 1
+    assert W.get_num_sand_particles() == 180 and W.get_grid_cell_size() == 1
+    W.set_simulate_function(0)
+    assert W.last_status() == 6  # sand solver not provided
+    W.set_simulate_function(2)
+    assert W.last_status() == 0
+    for _ in range(3):
+        W.simulate(1 / 60, False, False)
+    x = W.simulation_bind_positions_copy()
+    # the same scene through the oracle: reference defaults (rho0 24, m 5, g -10, ...)
+    from lustrine_gb300 import scenes
+    x0 = scenes.lattice((6, 5, 6), (8, 2, 8))
+    p = orc.reference_params(24, 16, 24)
+    p.jacobi = 1
+    p.clamp_cells = 1
+    o = dict(x=x0, v=np.zeros_like(x0), lambdas=None)
+    for _ in range(3):
+        o = orc.compat_step(p, 1 / 60, o["x"], o["v"], lambdas=o["lambdas"])
+    assert np.array_equal(x, o["x"])
+    W.cleanup_simulation()
+    W.free_grid(sand)
+    W.simulate(0.01)
+    assert W.last_status() == 7  # no simulation

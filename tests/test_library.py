@@ -1,0 +1,64 @@
+"""The C-ABI library without a GPU: it builds for sm_103a, loads, exports
+every symbol include/lustrine_gb300.h declares, and its structs have the
+reference's layouts.  No compute call is made here."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+
+from conftest import ROOT
+
+
+def _declared_symbols():
+    text = open(os.path.join(ROOT, "include", "lustrine_gb300.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"LUSTRINE_API\s+[\w\s\*]+?\b(\w+)\s*\(", text)))
+
+
+def test_library_builds_and_exports_every_declared_symbol():
+    from lustrine_gb300 import _lib
+    lib = _lib.load()
+    declared = _declared_symbols()
+    assert len(declared) >= 30
+    missing = [s for s in declared if not hasattr(lib, s)]
+    assert not missing, missing
+    # the Python binding covers the same set
+    assert set(declared) <= set(_lib.SIGNATURES), set(declared) - set(_lib.SIGNATURES)
+
+
+def test_struct_layouts_match_reference_abi():
+    from lustrine_gb300._lib import (Color, GridWrapper, PbfParams, SimulationData,
+                                     SimulationParameters, Vec3)
+    assert C.sizeof(SimulationParameters) == 20   # 3 ints + 2 floats (Simulation.hpp:83-92)
+    assert C.sizeof(SimulationData) == 24         # 6 ints (LustrineWrapper.hpp:30-41)
+    assert C.sizeof(Color) == 16 and C.sizeof(Vec3) == 12
+    # GridWrapper (LustrineWrapper.hpp:62-74) on LP64: 2 pointers, Color, Vec3, bool, 6 ints
+    assert GridWrapper.color.offset == 16 and GridWrapper.position.offset == 32
+    assert GridWrapper.has_one_color_per_cell.offset == 44 and GridWrapper.X.offset == 48
+    assert GridWrapper.type.offset == 68 and C.sizeof(GridWrapper) == 72
+    assert C.sizeof(PbfParams) == 4 * 24  # 24 four-byte fields
+
+
+def test_error_strings_and_reference_params_need_no_gpu():
+    from lustrine_gb300 import _lib, reference_params
+    lib = _lib.load()
+    assert lib.lustrine_error_string(4) == b"neighbour list capacity exceeded"
+    p = reference_params(40, 40, 40)
+    # Lustrine.cpp:545-546 with kernel_radius_scale 2 and Simulation.hpp defaults
+    assert p.kernel_radius == 1.0 and p.cell_size == 1.0 and p.kernel_factor == 0.5
+    assert p.rest_density == 24.0 and p.mass == 5.0 and p.gravity[1] == -10.0
+
+
+def test_scenes_match_config_shapes():
+    from lustrine_gb300 import scenes
+    c0 = scenes.config0()
+    assert c0.n == 10_000 and c0.domain == (40, 40, 40)
+    assert np.abs(c0.x - scenes.lattice((20, 25, 20), (10, 0, 10))).max() <= 0.05 + 1e-6
+    c1 = scenes.config1()
+    assert c1.n == 262_144 and 47_500 <= c1.ns <= 52_500
+    assert (c1.solid.min(0) >= 0).all() and (c1.solid.max(0) <= np.array(c1.domain)).all()
+    counts = scenes.batched_counts()
+    assert len(counts) == 512 and counts.min() >= 1024 and counts.max() <= 65536
+    s = scenes.batched_scene(1500, np.random.default_rng(0))
+    assert s.n == 1500 and (s.x.max(0) < np.array(s.domain)).all()
