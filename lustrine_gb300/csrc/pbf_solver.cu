@@ -369,6 +369,11 @@ __global__ void k_pack_pos(StepParams p, CellPack cp, const float* __restrict__ 
         out[i] = make_float4(x, y, z, 0.0f);
         return;
     }
+    // Positions are clamped into the box first, so the cell coordinates stay
+    // within the packed field widths (floor(hi / cell) per axis).
+    x = clampf(x, p.lox, p.hix);
+    y = clampf(y, p.loy, p.hiy);
+    z = clampf(z, p.loz, p.hiz);
     int cx = min(max((int)floorf(x * p.inv_cell), 0), p.gx - 1);
     int cy = min(max((int)floorf(y * p.inv_cell), 0), p.gy - 1);
     int cz = min(max((int)floorf(z * p.inv_cell), 0), p.gz - 1);
