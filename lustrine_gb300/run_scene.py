@@ -1,0 +1,45 @@
+"""Step one of the benchmark scenes on the GPU and print timing and FP64
+statistics.
+
+    python -m lustrine_gb300.run_scene --config config2 --steps 5 [--mixed] [--no-graph]
+
+Used for profiling captures of a single configuration (a fixed, short
+sequence of launches) and as a quick end-to-end check of an installation.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import time
+
+from . import PRECISION_FP32, PRECISION_MIXED, PbfSim, pbf_params, scenes
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--config", default="config1", choices=["config0", "config1", "config2"])
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--mixed", action="store_true")
+    ap.add_argument("--no-graph", action="store_true")
+    ap.add_argument("--max-neighbors", type=int, default=64)
+    a = ap.parse_args(argv)
+    sc = getattr(scenes, a.config)()
+    p = pbf_params(*sc.domain, iterations=sc.iterations, c_xsph=sc.c_xsph,
+                   precision=PRECISION_MIXED if a.mixed else PRECISION_FP32,
+                   max_neighbors=a.max_neighbors, use_graph=not a.no_graph)
+    with PbfSim(p, sc.n, sc.ns) as sim:
+        sim.upload(sc.x, None, sc.solid if sc.ns else None)
+        t0 = time.perf_counter()
+        sim.step(sc.dt, a.steps)
+        sim.synchronize()
+        wall = time.perf_counter() - t0
+        r = sim.reduce()
+        out = {"config": sc.name, "n": sc.n, "ns": sc.ns, "steps": a.steps,
+               "wall_ms_per_step": wall / max(a.steps, 1) * 1e3, "status": sim.status(),
+               "kinetic": r["kinetic"], "com": r["com"], "max_density_error": r["max_density_error"]}
+    print(json.dumps(out))
+    return 0 if out["status"] == 0 else 1
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())
