@@ -369,14 +369,13 @@ __global__ void k_pack_pos(StepParams p, CellPack cp, const float* __restrict__ 
         out[i] = make_float4(x, y, z, 0.0f);
         return;
     }
-    // Positions are clamped into the box first, so the cell coordinates stay
-    // within the packed field widths (floor(hi / cell) per axis).
-    x = clampf(x, p.lox, p.hix);
-    y = clampf(y, p.loy, p.hiy);
-    z = clampf(z, p.loz, p.hiz);
-    int cx = min(max((int)floorf(x * p.inv_cell), 0), p.gx - 1);
-    int cy = min(max((int)floorf(y * p.inv_cell), 0), p.gy - 1);
-    int cz = min(max((int)floorf(z * p.inv_cell), 0), p.gz - 1);
+    // The cell is clamped to the cells a clamped position can occupy (the
+    // packed field widths); the offset keeps the exact position, so a caller
+    // position outside the box stays where it is (it may then lie outside
+    // [0, cell)) and the next prediction clamps it like the plain form does.
+    int cx = min(max((int)floorf(x * p.inv_cell), 0), (int)floorf(p.hix * p.inv_cell));
+    int cy = min(max((int)floorf(y * p.inv_cell), 0), (int)floorf(p.hiy * p.inv_cell));
+    int cz = min(max((int)floorf(z * p.inv_cell), 0), (int)floorf(p.hiz * p.inv_cell));
     out[i] = make_float4(x - (float)cx * p.cell, y - (float)cy * p.cell, z - (float)cz * p.cell,
                          pack_cell(cp, cx, cy, cz));
 }
