@@ -92,6 +92,8 @@ static int derive(const lustrine_pbf_params& q, int n, int ns, StepParams* sp, C
     p.gz = (int)(dZ / q.cell_size) + 1;
     const long long C = (long long)p.gx * p.gy * p.gz;
     if (C > (1LL << 31) - 2) return LUSTRINE_ERR_UNSUPPORTED;
+    // PBF neighbour entries hold a 26-bit slot
+    if (q.mode == LUSTRINE_MODE_PBF && (n >= (1 << 26) || ns >= (1 << 26))) return LUSTRINE_ERR_UNSUPPORTED;
     p.num_cells = (int)C;
     p.max_nbrs = q.max_neighbors;
     p.clamp_cells = q.clamp_cells;
@@ -412,11 +414,12 @@ static int enqueue_step(lustrine_pbf* s, cudaStream_t st, StageMarks* mk = nullp
     launch_scan(s->count, C, s->block_sums, s->start, st);
     k += 3;
     if (mk) mk->mark(LUSTRINE_STAGE_SCAN, st);
+    // stable within a cell: by the caller's id in reference mode (the
+    // reference's list order), by the previous slot otherwise
     const int* tie = s->prm.mode == LUSTRINE_MODE_REFERENCE ? s->id[c] : nullptr;
-    launch_sort_tail(s->key, s->rank, s->start, tie, n, s->tmp, s->perm, st);
-    launch_gather_state(s->perm, n, s->key, s->x[c], s->xs[c], s->v[c], s->id[c], s->key_sorted,
-                        s->x[o], s->xs[o], s->v[o], s->id[o], st);
-    k += 3;
+    launch_sort_state(s->key, s->rank, s->start, tie, n, s->tmp, s->x[c], s->xs[c], s->v[c], s->id[c],
+                      s->key_sorted, s->x[o], s->xs[o], s->v[o], s->id[o], st);
+    k += 2;
     if (mk) mk->mark(LUSTRINE_STAGE_SORT, st);
     if (s->prm.mode == LUSTRINE_MODE_REFERENCE) {
         launch_lists_ref(p, s->xs[o], s->key_sorted, s->start, s->solid, s->sstart, s->nbr, s->cnt,
@@ -429,17 +432,20 @@ static int enqueue_step(lustrine_pbf* s, cudaStream_t st, StageMarks* mk = nullp
         if (mk) mk->mark(LUSTRINE_STAGE_DELTA, st);
         k += 3;
     } else {
-        launch_lists(mixed, p, s->cp, s->xs[o], s->start, s->solid, s->sstart, s->nbr, s->cnt,
-                     s->status, st);
-        k += 1;
-        if (mk) mk->mark(LUSTRINE_STAGE_LISTS, st);
+        // iteration 0's lambda pass builds the neighbour lists as it goes
         float4* a = s->xs[o];
         float4* b = s->xs_alt;
         const int iters = s->prm.iterations;
         for (int it = 0; it < iters; it++) {
-            launch_lambda(mixed, p, s->cp, a, s->nbr, s->cnt, s->solid, s->lam, s->rho, st);
-            if (mk) mk->mark(LUSTRINE_STAGE_LAMBDA, st);
-            launch_delta(mixed, p, s->cp, a, b, s->nbr, s->cnt, s->solid, s->lam, s->x[o],
+            if (it == 0) {
+                launch_lists_lambda(mixed, p, a, s->key_sorted, s->start, s->solid, s->sstart, s->nbr,
+                                    s->cnt, s->rho, s->status, st);
+                if (mk) mk->mark(LUSTRINE_STAGE_LISTS, st);
+            } else {
+                launch_lambda(mixed, p, a, s->nbr, s->cnt, s->solid, s->rho, st);
+                if (mk) mk->mark(LUSTRINE_STAGE_LAMBDA, st);
+            }
+            launch_delta(mixed, p, s->cp, a, b, s->nbr, s->cnt, s->solid, s->key_sorted, s->x[o],
                          it == iters - 1 ? s->vtmp : nullptr, st);
             if (mk) mk->mark(LUSTRINE_STAGE_DELTA, st);
             float4* t = a;
@@ -447,11 +453,21 @@ static int enqueue_step(lustrine_pbf* s, cudaStream_t st, StageMarks* mk = nullp
             b = t;
             k += 2;
         }
-        launch_xsph(mixed, p, s->cp, a, s->vtmp, s->nbr, s->cnt, s->x[o], s->v[o], st);
+        launch_xsph(mixed, p, s->cp, a, s->vtmp, s->nbr, s->cnt, s->key_sorted, s->x[o], s->v[o], st);
         k += 1;
         if (mk) mk->mark(LUSTRINE_STAGE_XSPH, st);
     }
     return k;
+}
+
+// Host bookkeeping after the launches of a step that started on side c.
+static void finish_step(lustrine_pbf* s, int c) {
+    s->cur = 1 - c;
+    s->lists_valid = true;
+    s->steps_done++;
+    // PBF: iteration k's lambdas are written into xs[1 - c] for even k and
+    // into xs_alt for odd k (the Jacobi ping-pong)
+    s->lam_src = (s->prm.iterations % 2 == 1) ? s->xs[1 - c] : s->xs_alt;
 }
 
 extern "C" int lustrine_pbf_step(lustrine_pbf* s, float dt) {
@@ -483,9 +499,7 @@ extern "C" int lustrine_pbf_step(lustrine_pbf* s, float dt) {
         s->launches = enqueue_step(s, s->stream);
         CK(cudaGetLastError());
     }
-    s->cur = 1 - c;
-    s->lists_valid = true;
-    s->steps_done++;
+    finish_step(s, c);
     return LUSTRINE_OK;
 }
 
@@ -531,9 +545,7 @@ extern "C" int lustrine_pbf_profile_step(lustrine_pbf* s, float dt, double* stag
         }
     for (int e = 0; e < 64; e++) cudaEventDestroy(mk.ev[e]);
     if (err != cudaSuccess) return lgb_cuda_status(err, "profile_step");
-    s->cur = 1 - s->cur;
-    s->lists_valid = true;
-    s->steps_done++;
+    finish_step(s, s->cur);
     return LUSTRINE_OK;
 }
 
@@ -568,8 +580,11 @@ extern "C" int lustrine_pbf_download(lustrine_pbf* s, float* x, float* v, float*
         if (lambdas) {
             if (ref)
                 CK(cudaMemcpyAsync(lambdas, s->lam_by_id, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
-            else
-                CK(cudaMemcpyAsync(lam.data(), s->lam, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+            else if (s->lam_src)  // PBF: lambdas are the w of the last pass's positions
+                CK(cudaMemcpy2DAsync(lam.data(), sizeof(float),
+                                     reinterpret_cast<const char*>(s->lam_src) + 3 * sizeof(float),
+                                     sizeof(float4), sizeof(float), (size_t)n, cudaMemcpyDeviceToHost,
+                                     s->stream));
         }
         if (density) CK(cudaMemcpyAsync(rho.data(), s->rho, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
         CK(cudaStreamSynchronize(s->stream));
@@ -627,7 +642,10 @@ extern "C" int lustrine_pbf_neighbors(lustrine_pbf* s, int* count, int* idx, int
         if (c > cap) rc = LUSTRINE_ERR_NBR_OVERFLOW;
         for (int e = 0; e < c && e < cap; e++) {
             int j = nbr[(size_t)e * n + k];
-            idx[(size_t)i * cap + e] = j >= 0 ? ids[(size_t)j] : n + sid[(size_t)(-1 - j)];
+            if (s->prm.mode == LUSTRINE_MODE_REFERENCE)
+                idx[(size_t)i * cap + e] = j >= 0 ? ids[(size_t)j] : n + sid[(size_t)(-1 - j)];
+            else  // PBF entry: slot in bits 0-25, solid flag in bit 31
+                idx[(size_t)i * cap + e] = j >= 0 ? ids[(size_t)(j & 0x3FFFFFF)] : n + sid[(size_t)(j & 0x3FFFFFF)];
         }
     }
     return rc;
@@ -668,7 +686,7 @@ extern "C" int lustrine_pbf_stream(lustrine_pbf* s, void** stream) {
 extern "C" int lustrine_pbf_launches_per_step(const lustrine_pbf* s) {
     if (!s) return -1;
     int iters = s->prm.mode == LUSTRINE_MODE_REFERENCE ? 0 : s->prm.iterations;
-    return s->prm.mode == LUSTRINE_MODE_REFERENCE ? 10 : 9 + 2 * iters;
+    return s->prm.mode == LUSTRINE_MODE_REFERENCE ? 9 : 7 + 2 * iters;
 }
 
 extern "C" const char* lustrine_error_string(int code) {

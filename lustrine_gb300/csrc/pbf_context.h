@@ -46,6 +46,7 @@ struct lustrine_pbf {
     int* nbr = nullptr;
     int* cnt = nullptr;
     float* lam = nullptr;
+    float4* lam_src = nullptr;  // PBF: the buffer whose w holds the last lambdas
     float* lam_by_id = nullptr;
     size_t lam_by_id_len = 0;
     float* rho = nullptr;

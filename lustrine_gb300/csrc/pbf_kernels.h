@@ -16,6 +16,11 @@ void launch_gather_state(const int* perm, int n, const int* key, const float4* x
                          const float4* v, const int* id, int* key_out, float4* x_out,
                          float4* xs_out, float4* v_out, int* id_out, cudaStream_t st);
 void launch_gather_solid(const int* perm, int n, const float4* src, float4* dst, cudaStream_t st);
+// index scatter + stabilisation fused with the reorder of the particle state
+void launch_sort_state(const int* key, const int* rank, const int* start, const int* tie, int n,
+                       int* tmp, const float4* x, const float4* xs, const float4* v, const int* id,
+                       int* key_out, float4* x_out, float4* xs_out, float4* v_out, int* id_out,
+                       cudaStream_t st);
 
 // pbf_compat.cu (reference semantics, no FMA contraction)
 void launch_predict_ref(const StepParams& p, const float4* x, float4* v, float4* xs, int* key,
@@ -37,18 +42,18 @@ void launch_predict(bool mixed, const StepParams& p, const CellPack& cp, const f
                     float4* xs, int* key, int* rank, int* count, cudaStream_t st);
 void launch_key(bool mixed, const StepParams& p, const CellPack& cp, const float4* pos, int m,
                 int* key, int* rank, int* count, cudaStream_t st);
-void launch_lists(bool mixed, const StepParams& p, const CellPack& cp, const float4* xs,
-                  const int* fstart, const float4* solid, const int* sstart, int* nbr, int* cnt,
-                  int* status, cudaStream_t st);
-void launch_lambda(bool mixed, const StepParams& p, const CellPack& cp, const float4* xs,
-                   const int* nbr, const int* cnt, const float4* solid, float* lam, float* rho,
-                   cudaStream_t st);
+// neighbour lists + first lambda pass (lambda stored in xs.w)
+void launch_lists_lambda(bool mixed, const StepParams& p, float4* xs, const int* key_sorted,
+                         const int* fstart, const float4* solid, const int* sstart, int* nbr,
+                         int* cnt, float* rho, int* status, cudaStream_t st);
+void launch_lambda(bool mixed, const StepParams& p, float4* xs, const int* nbr, const int* cnt,
+                   const float4* solid, float* rho, cudaStream_t st);
 void launch_delta(bool mixed, const StepParams& p, const CellPack& cp, const float4* xs,
                   float4* xs_out, const int* nbr, const int* cnt, const float4* solid,
-                  const float* lam, const float4* x, float4* v_out, cudaStream_t st);
+                  const int* key_sorted, const float4* x, float4* v_out, cudaStream_t st);
 void launch_xsph(bool mixed, const StepParams& p, const CellPack& cp, const float4* xs,
-                 const float4* v_in, const int* nbr, const int* cnt, float4* x_out, float4* v_out,
-                 cudaStream_t st);
+                 const float4* v_in, const int* nbr, const int* cnt, const int* key_sorted,
+                 float4* x_out, float4* v_out, cudaStream_t st);
 void launch_unpermute_pos(bool mixed, const StepParams& p, const CellPack& cp, const float4* a,
                           const int* id, int n, float* out, cudaStream_t st);
 void launch_unpermute_pos_d(bool mixed, const StepParams& p, const CellPack& cp, const float4* a,

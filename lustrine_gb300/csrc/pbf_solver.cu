@@ -4,18 +4,39 @@
 // Kernels.cpp:43-67, with N Jacobi solver iterations over neighbour lists
 // built once per step.
 //
-// Two position representations (template parameter MIXED):
+// Position representations (template parameter MIXED):
 //   plain  float4 xyz = absolute position;
-//   mixed  float4 xyz = offset inside the particle's cell, in [0, cell),
-//          w = the cell's integer coordinates packed in 32 bits (bit-cast).
-//          Neighbour offsets are (o_i - o_j) + (c_i - c_j) * cell with
-//          c_i - c_j in {-1, 0, 1}, so their precision does not depend on
-//          how far the particles are from the origin; density sums use
+//   mixed  xyz = offset from the particle's cell corner, the cell being the
+//          sorted key of the step (fixed during the step's iterations, so an
+//          offset may leave [0, cell) until the next prediction renormalises
+//          it); the committed state keeps the cell packed in w.  Neighbour
+//          offsets are (o_i - o_j) + (c_i - c_j) * cell with the cell
+//          difference cached in the neighbour list entry, so their precision
+//          does not depend on the distance to the origin; density sums use
 //          compensated (Kahan) accumulation.
+// During the iterations w of the predicted positions holds the particle's
+// lambda, written in place by the lambda pass, so the position pass gathers
+// one float4 per neighbour.
+//
+// Neighbour list entry (int32): bits 0-25 slot, bits 26-30 the neighbour's
+// cell offset code (dx + 1) + 3 (dz + 1) + 9 (dy + 1), bit 31 set for solids.
 #include "pbf_common.cuh"
 #include "pbf_kernels.h"
 
 namespace lgb {
+
+constexpr int SLOT_BITS = 26;
+constexpr int SLOT_MASK = (1 << SLOT_BITS) - 1;
+constexpr int UNROLL = 4;
+
+__device__ __forceinline__ int entry(int slot, int code, bool solid) {
+    return slot | (code << SLOT_BITS) | (solid ? (int)0x80000000u : 0);
+}
+__device__ __forceinline__ int entry_slot(int e) { return e & SLOT_MASK; }
+__device__ __forceinline__ bool entry_solid(int e) { return e < 0; }
+__device__ __forceinline__ int entry_code(int e) { return (e >> SLOT_BITS) & 31; }
+// the particle itself: a fluid entry of its own slot (any cell code)
+__device__ __forceinline__ bool entry_is(int e, int s) { return (e & (SLOT_MASK | (int)0x80000000u)) == s; }
 
 // ---------------------------------------------------------------- helpers --
 
@@ -30,64 +51,43 @@ __device__ __forceinline__ float pack_cell(const CellPack& cp, int cx, int cy, i
     return __uint_as_float(u);
 }
 
-// a - b as a float3
-template <bool MIXED>
-__device__ __forceinline__ float3 rel(const StepParams& p, const CellPack& cp, float4 a, float4 b) {
-    if (!MIXED) return make_float3(a.x - b.x, a.y - b.y, a.z - b.z);
-    int3 ca = unpack_cell(cp, a.w), cb = unpack_cell(cp, b.w);
-    return make_float3((a.x - b.x) + (float)(ca.x - cb.x) * p.cell,
-                       (a.y - b.y) + (float)(ca.y - cb.y) * p.cell,
-                       (a.z - b.z) + (float)(ca.z - cb.z) * p.cell);
-}
-
-// cell coordinates of a position (clamped into the grid)
-template <bool MIXED>
-__device__ __forceinline__ int3 cell_of(const StepParams& p, const CellPack& cp, float4 a) {
-    if (MIXED) return unpack_cell(cp, a.w);
-    int cx = (int)floorf(a.x * p.inv_cell), cy = (int)floorf(a.y * p.inv_cell),
-        cz = (int)floorf(a.z * p.inv_cell);
-    return make_int3(min(max(cx, 0), p.gx - 1), min(max(cy, 0), p.gy - 1),
-                     min(max(cz, 0), p.gz - 1));
-}
-
 __device__ __forceinline__ int linear_cell(const StepParams& p, int3 c) {
     return c.y * p.gx * p.gz + c.x * p.gz + c.z;
 }
 
-// One axis of an absolute position clamped to [lo, hi].
+__device__ __forceinline__ int3 decode_cell(const StepParams& p, int key) {
+    const int slab = p.gx * p.gz;
+    const int y = key / slab;
+    const int r = key - y * slab;
+    const int x = r / p.gz;
+    return make_int3(x, y, r - x * p.gz);
+}
+
 __device__ __forceinline__ float clampf(float v, float lo, float hi) { return fminf(fmaxf(v, lo), hi); }
 
-// Mixed: move an (offset, cell) pair by delta, renormalise the offset into
-// [0, cell) and clamp the absolute position to [lo, hi].
-__device__ __forceinline__ void mixed_axis(const StepParams& p, float& o, int& c, float lo, float hi) {
-    float k = floorf(o * p.inv_cell);
-    if (k != 0.0f) {
-        c += (int)k;
-        o -= k * p.cell;
-        if (o >= p.cell) { o -= p.cell; c += 1; }
-        if (o < 0.0f) { o += p.cell; c -= 1; }
-    }
-    float a = (float)c * p.cell + o;
-    if (a < lo || a > hi) {
-        float t = clampf(a, lo, hi);
-        int tc = (int)floorf(t * p.inv_cell);
-        c = tc;
-        o = t - (float)tc * p.cell;
-    }
+__device__ __forceinline__ int3 plain_cell(const StepParams& p, float x, float y, float z) {
+    int cx = (int)floorf(x * p.inv_cell), cy = (int)floorf(y * p.inv_cell),
+        cz = (int)floorf(z * p.inv_cell);
+    return make_int3(min(max(cx, 0), p.gx - 1), min(max(cy, 0), p.gy - 1), min(max(cz, 0), p.gz - 1));
+}
+
+// Offset of the neighbour's cell from the particle's: code -> -(c_j - c_i) * cell
+// as the vector to add to (o_i - o_j).
+__device__ __forceinline__ float3 code_shift(const StepParams& p, int code) {
+    const int dx = code % 3 - 1, dz = (code / 3) % 3 - 1, dy = code / 9 - 1;
+    return make_float3(-(float)dx * p.cell, -(float)dy * p.cell, -(float)dz * p.cell);
 }
 
 template <bool MIXED>
-__device__ __forceinline__ float4 advance(const StepParams& p, const CellPack& cp, float4 a, float dx,
-                                          float dy, float dz) {
-    if (!MIXED)
-        return make_float4(clampf(a.x + dx, p.lox, p.hix), clampf(a.y + dy, p.loy, p.hiy),
-                           clampf(a.z + dz, p.loz, p.hiz), 0.0f);
-    int3 c = unpack_cell(cp, a.w);
-    float ox = a.x + dx, oy = a.y + dy, oz = a.z + dz;
-    mixed_axis(p, ox, c.x, p.lox, p.hix);
-    mixed_axis(p, oy, c.y, p.loy, p.hiy);
-    mixed_axis(p, oz, c.z, p.loz, p.hiz);
-    return make_float4(ox, oy, oz, pack_cell(cp, c.x, c.y, c.z));
+__device__ __forceinline__ float3 rel_e(const StepParams& p, float4 a, float4 b, int e) {
+    float3 d = make_float3(a.x - b.x, a.y - b.y, a.z - b.z);
+    if (MIXED) {
+        float3 s = code_shift(p, entry_code(e));
+        d.x += s.x;
+        d.y += s.y;
+        d.z += s.z;
+    }
+    return d;
 }
 
 __device__ __forceinline__ float poly6(const StepParams& p, float r2) {
@@ -95,7 +95,7 @@ __device__ __forceinline__ float poly6(const StepParams& p, float r2) {
     return r2 <= p.h2 ? p.k6 * d * d * d : 0.0f;
 }
 
-// spiky gradient magnitude factor: dW(d) = f * d
+// spiky gradient as a factor on the offset: dW(d) = f * d
 __device__ __forceinline__ float spiky_factor(const StepParams& p, float r) {
     float f = p.h - r;
     return (r > 0.0f && r <= p.h) ? -p.ks * f * f / r : 0.0f;
@@ -116,14 +116,42 @@ __device__ __forceinline__ float scorr(const StepParams& p, float r2) {
     return -p.sk * pw;
 }
 
-__device__ __forceinline__ float4 load_nbr(int j, const float4* __restrict__ xs,
-                                           const float4* __restrict__ solid) {
-    return j >= 0 ? xs[j] : solid[-1 - j];
+__device__ __forceinline__ float4 load_entry(int e, const float4* __restrict__ xs,
+                                             const float4* __restrict__ solid) {
+    return entry_solid(e) ? __ldg(&solid[entry_slot(e)]) : xs[entry_slot(e)];
+}
+
+// Mixed: one axis of an (offset, cell) pair renormalised into [0, cell) and
+// clamped to the box [lo, hi].
+__device__ __forceinline__ void renorm_axis(const StepParams& p, float& o, int& c, float lo, float hi) {
+    float k = floorf(o * p.inv_cell);
+    if (k != 0.0f) {
+        c += (int)k;
+        o -= k * p.cell;
+        if (o >= p.cell) { o -= p.cell; c += 1; }
+        if (o < 0.0f) { o += p.cell; c -= 1; }
+    }
+    float a = (float)c * p.cell + o;
+    if (a < lo || a > hi) {
+        float t = clampf(a, lo, hi);
+        int tc = (int)floorf(t * p.inv_cell);
+        c = tc;
+        o = t - (float)tc * p.cell;
+    }
+}
+
+// Mixed: clamp an offset in a fixed cell so the absolute position is in [lo, hi].
+__device__ __forceinline__ float clamp_offset(const StepParams& p, float o, int c, float lo, float hi) {
+    float base = (float)c * p.cell;
+    float a = base + o;
+    if (a < lo) return lo - base;
+    if (a > hi) return hi - base;
+    return o;
 }
 
 // ---------------------------------------------------------------- kernels --
 
-// Prediction, box clamp, cell key and histogram.
+// Prediction with the box clamp, cell key and histogram.
 template <bool MIXED>
 __global__ void k_predict(StepParams p, CellPack cp, const float4* __restrict__ x,
                           float4* __restrict__ v, float4* __restrict__ xs, int* __restrict__ key,
@@ -135,9 +163,23 @@ __global__ void k_predict(StepParams p, CellPack cp, const float4* __restrict__ 
     vi.y += p.gyv * p.dt;
     vi.z += p.gzv * p.dt;
     v[i] = vi;
-    float4 s = advance<MIXED>(p, cp, x[i], vi.x * p.dt, vi.y * p.dt, vi.z * p.dt);
+    const float4 xi = x[i];
+    int3 c;
+    float4 s;
+    if (!MIXED) {
+        s = make_float4(clampf(xi.x + vi.x * p.dt, p.lox, p.hix), clampf(xi.y + vi.y * p.dt, p.loy, p.hiy),
+                        clampf(xi.z + vi.z * p.dt, p.loz, p.hiz), 0.0f);
+        c = plain_cell(p, s.x, s.y, s.z);
+    } else {
+        c = unpack_cell(cp, xi.w);
+        float ox = xi.x + vi.x * p.dt, oy = xi.y + vi.y * p.dt, oz = xi.z + vi.z * p.dt;
+        renorm_axis(p, ox, c.x, p.lox, p.hix);
+        renorm_axis(p, oy, c.y, p.loy, p.hiy);
+        renorm_axis(p, oz, c.z, p.loz, p.hiz);
+        s = make_float4(ox, oy, oz, 0.0f);
+    }
     xs[i] = s;
-    int k = linear_cell(p, cell_of<MIXED>(p, cp, s));
+    const int k = linear_cell(p, c);
     key[i] = k;
     rank[i] = atomicAdd(&count[k], 1);
 }
@@ -147,45 +189,95 @@ __global__ void k_key(StepParams p, CellPack cp, const float4* __restrict__ pos,
                       int* __restrict__ key, int* __restrict__ rank, int* __restrict__ count) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m) return;
-    int k = linear_cell(p, cell_of<MIXED>(p, cp, pos[i]));
+    float4 q = pos[i];
+    int3 c = MIXED ? unpack_cell(cp, q.w) : plain_cell(p, q.x, q.y, q.z);
+    int k = linear_cell(p, c);
     key[i] = k;
     rank[i] = atomicAdd(&count[k], 1);
 }
 
-// Neighbour lists: the 3 x 3 rows of cells around the particle's cell; the
-// three cells of a row are consecutive ids, hence one contiguous slot range.
+// Neighbour search fused with the first lambda pass: walks the 27 cells
+// around the particle's cell, writes the list and accumulates the density
+// constraint over the accepted neighbours.
+struct LambdaAcc {
+    float density, comp, S, gx, gy, gz;
+};
+
 template <bool MIXED>
-__global__ void __launch_bounds__(128) k_lists(StepParams p, CellPack cp, const float4* __restrict__ xs,
-                                               const int* __restrict__ fstart,
-                                               const float4* __restrict__ solid,
-                                               const int* __restrict__ sstart, int* __restrict__ nbr,
-                                               int* __restrict__ cnt, int* status) {
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void lambda_accumulate(const StepParams& p, LambdaAcc& a, float3 d,
+                                                  bool self, bool solid) {
+    const float r2 = dot3(d.x, d.y, d.z);
+    const float w = p.mass * poly6(p, r2);
+    if (MIXED) {
+        float y = w - a.comp;
+        float t = a.density + y;
+        a.comp = (t - a.density) - y;
+        a.density = t;
+    } else {
+        a.density += w;
+    }
+    if (self) return;
+    const float f = spiky_factor(p, sqrtf(r2)) * (p.mass / p.rho0);
+    const float ax = f * d.x, ay = f * d.y, az = f * d.z;
+    if (!solid) a.S += dot3(ax, ay, az);
+    a.gx += ax;
+    a.gy += ay;
+    a.gz += az;
+}
+
+__device__ __forceinline__ float lambda_of(const StepParams& p, const LambdaAcc& a) {
+    const float S = a.S + dot3(a.gx, a.gy, a.gz);
+    return -(a.density / p.rho0 - 1.0f) / (S + p.eps);
+}
+
+template <bool MIXED>
+__global__ void __launch_bounds__(128) k_lists_lambda(StepParams p, float4* __restrict__ xs,
+                                                      const int* __restrict__ key_sorted,
+                                                      const int* __restrict__ fstart,
+                                                      const float4* __restrict__ solid,
+                                                      const int* __restrict__ sstart,
+                                                      int* __restrict__ nbr, int* __restrict__ cnt,
+                                                      float* __restrict__ rho, int* status) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= p.n) return;
     const float4 self = xs[s];
-    const int3 c = cell_of<MIXED>(p, cp, self);
-    const int z0 = max(c.z - 1, 0), z1 = min(c.z + 1, p.gz - 1);
+    const int3 c = decode_cell(p, key_sorted[s]);
+    LambdaAcc a = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
     int c_n = 0;
+    const int slab = p.gx * p.gz;
     for (int dy = -1; dy <= 1; dy++) {
         const int y = c.y + dy;
         if (y < 0 || y >= p.gy) continue;
         for (int dx = -1; dx <= 1; dx++) {
-            const int x = c.x + dx;
-            if (x < 0 || x >= p.gx) continue;
-            const int row = y * p.gx * p.gz + x * p.gz;
-            for (int t = fstart[row + z0], e = fstart[row + z1 + 1]; t < e; t++) {
-                float3 d = rel<MIXED>(p, cp, self, xs[t]);
-                if (dot3(d.x, d.y, d.z) <= p.h2) {
-                    if (c_n < p.max_nbrs) nbr[(size_t)c_n * p.n + s] = t;
-                    c_n++;
-                }
-            }
-            if (p.ns > 0) {
-                for (int t = sstart[row + z0], e = sstart[row + z1 + 1]; t < e; t++) {
-                    float3 d = rel<MIXED>(p, cp, self, solid[t]);
+            const int xx = c.x + dx;
+            if (xx < 0 || xx >= p.gx) continue;
+            const int row = y * slab + xx * p.gz;
+            for (int dz = -1; dz <= 1; dz++) {
+                const int z = c.z + dz;
+                if (z < 0 || z >= p.gz) continue;
+                const int code = (dx + 1) + 3 * (dz + 1) + 9 * (dy + 1);
+                const float sx = -(float)dx * p.cell, sy = -(float)dy * p.cell,
+                            sz = -(float)dz * p.cell;
+                for (int t = fstart[row + z], e = fstart[row + z + 1]; t < e; t++) {
+                    const float4 q = xs[t];
+                    float3 d = make_float3(self.x - q.x, self.y - q.y, self.z - q.z);
+                    if (MIXED) { d.x += sx; d.y += sy; d.z += sz; }
                     if (dot3(d.x, d.y, d.z) <= p.h2) {
-                        if (c_n < p.max_nbrs) nbr[(size_t)c_n * p.n + s] = -1 - t;
+                        if (c_n < p.max_nbrs) nbr[(size_t)c_n * p.n + s] = entry(t, code, false);
                         c_n++;
+                        lambda_accumulate<MIXED>(p, a, d, t == s, false);
+                    }
+                }
+                if (p.ns > 0) {
+                    for (int t = sstart[row + z], e = sstart[row + z + 1]; t < e; t++) {
+                        const float4 q = __ldg(&solid[t]);
+                        float3 d = make_float3(self.x - q.x, self.y - q.y, self.z - q.z);
+                        if (MIXED) { d.x += sx; d.y += sy; d.z += sz; }
+                        if (dot3(d.x, d.y, d.z) <= p.h2) {
+                            if (c_n < p.max_nbrs) nbr[(size_t)c_n * p.n + s] = entry(t, code, true);
+                            c_n++;
+                            lambda_accumulate<MIXED>(p, a, d, false, true);
+                        }
                     }
                 }
             }
@@ -196,45 +288,38 @@ __global__ void __launch_bounds__(128) k_lists(StepParams p, CellPack cp, const 
         c_n = p.max_nbrs;
     }
     cnt[s] = c_n;
+    // lambda into w in place: neighbours read only xyz of this element here
+    reinterpret_cast<float*>(xs)[4 * (size_t)s + 3] = lambda_of(p, a);
+    if (rho) rho[s] = a.density;
 }
 
-// Density constraint and its multiplier (Macklin & Mueller eq. 1, 8, 11).
+// Lambda pass over the lists (iterations after the first).
 template <bool MIXED>
-__global__ void __launch_bounds__(128) k_lambda(StepParams p, CellPack cp, const float4* __restrict__ xs,
+__global__ void __launch_bounds__(128) k_lambda(StepParams p, float4* __restrict__ xs,
                                                 const int* __restrict__ nbr, const int* __restrict__ cnt,
                                                 const float4* __restrict__ solid,
-                                                float* __restrict__ lam, float* __restrict__ rho) {
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
+                                                float* __restrict__ rho) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= p.n) return;
     const float4 self = xs[s];
     const int c = cnt[s];
-    const float mr = p.mass / p.rho0;
-    float density = 0.0f, comp = 0.0f, S = 0.0f;
-    float gx = 0.0f, gy = 0.0f, gz = 0.0f;
-    for (int k = 0; k < c; k++) {
-        const int j = nbr[(size_t)k * p.n + s];
-        float3 d = rel<MIXED>(p, cp, self, load_nbr(j, xs, solid));
-        float r2 = dot3(d.x, d.y, d.z);
-        float w = p.mass * poly6(p, r2);
-        if (MIXED) {
-            float y = w - comp;
-            float t = density + y;
-            comp = (t - density) - y;
-            density = t;
-        } else {
-            density += w;
+    LambdaAcc a = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    for (int k = 0; k < c; k += UNROLL) {
+        int e[UNROLL];
+        float4 q[UNROLL];
+#pragma unroll
+        for (int u = 0; u < UNROLL; u++) e[u] = k + u < c ? __ldg(&nbr[(size_t)(k + u) * p.n + s]) : s;
+#pragma unroll
+        for (int u = 0; u < UNROLL; u++) q[u] = load_entry(e[u], xs, solid);
+#pragma unroll
+        for (int u = 0; u < UNROLL; u++) {
+            if (k + u >= c) break;
+            float3 d = rel_e<MIXED>(p, self, q[u], e[u]);
+            lambda_accumulate<MIXED>(p, a, d, entry_is(e[u], s), entry_solid(e[u]));
         }
-        if (j == s) continue;
-        float f = spiky_factor(p, sqrtf(r2)) * mr;
-        float ax = f * d.x, ay = f * d.y, az = f * d.z;
-        if (j >= 0) S += dot3(ax, ay, az);
-        gx += ax;
-        gy += ay;
-        gz += az;
     }
-    S += dot3(gx, gy, gz);
-    lam[s] = -(density / p.rho0 - 1.0f) / (S + p.eps);
-    if (rho) rho[s] = density;
+    reinterpret_cast<float*>(xs)[4 * (size_t)s + 3] = lambda_of(p, a);
+    if (rho) rho[s] = a.density;
 }
 
 // Position correction with s_corr, solid push-out and box clamp (Jacobi).
@@ -244,48 +329,75 @@ __global__ void __launch_bounds__(128) k_delta(StepParams p, CellPack cp, const 
                                                float4* __restrict__ xs_out, const int* __restrict__ nbr,
                                                const int* __restrict__ cnt,
                                                const float4* __restrict__ solid,
-                                               const float* __restrict__ lam,
+                                               const int* __restrict__ key_sorted,
                                                const float4* __restrict__ x, float4* __restrict__ v_out) {
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= p.n) return;
     const float4 self = xs[s];
-    const float li = lam[s];
+    const float li = self.w;
     const int c = cnt[s];
     float px = 0.0f, py = 0.0f, pz = 0.0f;
     float cx = 0.0f, cy = 0.0f, cz = 0.0f;
     int nct = 0;
-    for (int k = 0; k < c; k++) {
-        const int j = nbr[(size_t)k * p.n + s];
-        if (j == s) continue;
-        float3 d = rel<MIXED>(p, cp, self, load_nbr(j, xs, solid));
-        float r2 = dot3(d.x, d.y, d.z);
-        float r = sqrtf(r2);
-        float lj = j >= 0 ? lam[j] : li;
-        float w = (li + lj + scorr(p, r2)) * spiky_factor(p, r);
-        px += w * d.x;
-        py += w * d.y;
-        pz += w * d.z;
-        if (j < 0 && r < p.contact && r > 0.0f) {
-            float q = (p.contact - r) / r;
-            cx += q * d.x;
-            cy += q * d.y;
-            cz += q * d.z;
-            nct++;
+    for (int k = 0; k < c; k += UNROLL) {
+        int e[UNROLL];
+        float4 q[UNROLL];
+#pragma unroll
+        for (int u = 0; u < UNROLL; u++) e[u] = k + u < c ? __ldg(&nbr[(size_t)(k + u) * p.n + s]) : s;
+#pragma unroll
+        for (int u = 0; u < UNROLL; u++) q[u] = load_entry(e[u], xs, solid);
+#pragma unroll
+        for (int u = 0; u < UNROLL; u++) {
+            if (k + u >= c) break;
+            if (entry_is(e[u], s)) continue;
+            const bool sol = entry_solid(e[u]);
+            float3 d = rel_e<MIXED>(p, self, q[u], e[u]);
+            const float r2 = dot3(d.x, d.y, d.z);
+            const float r = sqrtf(r2);
+            const float lj = sol ? li : q[u].w;
+            const float w = (li + lj + scorr(p, r2)) * spiky_factor(p, r);
+            px += w * d.x;
+            py += w * d.y;
+            pz += w * d.z;
+            if (sol && r < p.contact && r > 0.0f) {
+                const float t = (p.contact - r) / r;
+                cx += t * d.x;
+                cy += t * d.y;
+                cz += t * d.z;
+                nct++;
+            }
         }
     }
     const float mr = p.mass / p.rho0;
     float dx = px * mr, dy = py * mr, dz = pz * mr;
     if (nct) {
-        float inv = 1.0f / (float)nct;
+        const float inv = 1.0f / (float)nct;
         dx += cx * inv;
         dy += cy * inv;
         dz += cz * inv;
     }
-    float4 out = advance<MIXED>(p, cp, self, dx, dy, dz);
+    float4 out;
+    int3 cs = make_int3(0, 0, 0);
+    if (!MIXED) {
+        out = make_float4(clampf(self.x + dx, p.lox, p.hix), clampf(self.y + dy, p.loy, p.hiy),
+                          clampf(self.z + dz, p.loz, p.hiz), 0.0f);
+    } else {
+        cs = decode_cell(p, key_sorted[s]);
+        out = make_float4(clamp_offset(p, self.x + dx, cs.x, p.lox, p.hix),
+                          clamp_offset(p, self.y + dy, cs.y, p.loy, p.hiy),
+                          clamp_offset(p, self.z + dz, cs.z, p.loz, p.hiz), 0.0f);
+    }
     xs_out[s] = out;
     if (v_out) {
-        float3 d = rel<MIXED>(p, cp, out, x[s]);
-        float inv_dt = 1.0f / p.dt;
+        const float4 xo = x[s];
+        float3 d = make_float3(out.x - xo.x, out.y - xo.y, out.z - xo.z);
+        if (MIXED) {
+            int3 co = unpack_cell(cp, xo.w);
+            d.x += (float)(cs.x - co.x) * p.cell;
+            d.y += (float)(cs.y - co.y) * p.cell;
+            d.z += (float)(cs.z - co.z) * p.cell;
+        }
+        const float inv_dt = 1.0f / p.dt;
         v_out[s] = make_float4(d.x * inv_dt, d.y * inv_dt, d.z * inv_dt, 0.0f);
     }
 }
@@ -295,27 +407,47 @@ template <bool MIXED>
 __global__ void __launch_bounds__(128) k_xsph(StepParams p, CellPack cp, const float4* __restrict__ xs,
                                               const float4* __restrict__ v_in,
                                               const int* __restrict__ nbr, const int* __restrict__ cnt,
+                                              const int* __restrict__ key_sorted,
                                               float4* __restrict__ x_out, float4* __restrict__ v_out) {
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= p.n) return;
     const float4 self = xs[s];
     const float4 vi = v_in[s];
     const int c = cnt[s];
     float ax = 0.0f, ay = 0.0f, az = 0.0f;
     if (p.c_xsph != 0.0f) {
-        for (int k = 0; k < c; k++) {
-            const int j = nbr[(size_t)k * p.n + s];
-            if (j == s || j < 0) continue;
-            float3 d = rel<MIXED>(p, cp, self, xs[j]);
-            float w = poly6(p, dot3(d.x, d.y, d.z));
-            float4 vj = v_in[j];
-            ax += (vj.x - vi.x) * w;
-            ay += (vj.y - vi.y) * w;
-            az += (vj.z - vi.z) * w;
+        for (int k = 0; k < c; k += UNROLL) {
+            int e[UNROLL];
+            float4 q[UNROLL], vj[UNROLL];
+#pragma unroll
+            for (int u = 0; u < UNROLL; u++) {
+                int t = k + u < c ? __ldg(&nbr[(size_t)(k + u) * p.n + s]) : s;
+                e[u] = entry_solid(t) ? s : t;  // solids take no part
+            }
+#pragma unroll
+            for (int u = 0; u < UNROLL; u++) {
+                q[u] = xs[entry_slot(e[u])];
+                vj[u] = v_in[entry_slot(e[u])];
+            }
+#pragma unroll
+            for (int u = 0; u < UNROLL; u++) {
+                if (k + u >= c) break;
+                if (entry_is(e[u], s)) continue;
+                float3 d = rel_e<MIXED>(p, self, q[u], e[u]);
+                const float w = poly6(p, dot3(d.x, d.y, d.z));
+                ax += (vj[u].x - vi.x) * w;
+                ay += (vj[u].y - vi.y) * w;
+                az += (vj[u].z - vi.z) * w;
+            }
         }
     }
     v_out[s] = make_float4(vi.x + p.c_xsph * ax, vi.y + p.c_xsph * ay, vi.z + p.c_xsph * az, 0.0f);
-    x_out[s] = self;
+    if (!MIXED) {
+        x_out[s] = make_float4(self.x, self.y, self.z, 0.0f);
+    } else {
+        int3 cs = decode_cell(p, key_sorted[s]);
+        x_out[s] = make_float4(self.x, self.y, self.z, pack_cell(cp, cs.x, cs.y, cs.z));
+    }
 }
 
 // Absolute positions (float3 triples) in the caller's id order.
@@ -460,34 +592,34 @@ void launch_key(bool mixed, const StepParams& p, const CellPack& cp, const float
     LGB_DISPATCH(mixed, k_key, blocks_for(m, 256), 256, st, p, cp, pos, m, key, rank, count);
 }
 
-void launch_lists(bool mixed, const StepParams& p, const CellPack& cp, const float4* xs,
-                  const int* fstart, const float4* solid, const int* sstart, int* nbr, int* cnt,
-                  int* status, cudaStream_t st) {
+void launch_lists_lambda(bool mixed, const StepParams& p, float4* xs, const int* key_sorted,
+                         const int* fstart, const float4* solid, const int* sstart, int* nbr,
+                         int* cnt, float* rho, int* status, cudaStream_t st) {
     if (p.n <= 0) return;
-    LGB_DISPATCH(mixed, k_lists, blocks_for(p.n, 128), 128, st, p, cp, xs, fstart, solid, sstart, nbr,
-                 cnt, status);
+    LGB_DISPATCH(mixed, k_lists_lambda, blocks_for(p.n, 128), 128, st, p, xs, key_sorted, fstart, solid,
+                 sstart, nbr, cnt, rho, status);
 }
 
-void launch_lambda(bool mixed, const StepParams& p, const CellPack& cp, const float4* xs,
-                   const int* nbr, const int* cnt, const float4* solid, float* lam, float* rho,
-                   cudaStream_t st) {
+void launch_lambda(bool mixed, const StepParams& p, float4* xs, const int* nbr, const int* cnt,
+                   const float4* solid, float* rho, cudaStream_t st) {
     if (p.n <= 0) return;
-    LGB_DISPATCH(mixed, k_lambda, blocks_for(p.n, 128), 128, st, p, cp, xs, nbr, cnt, solid, lam, rho);
+    LGB_DISPATCH(mixed, k_lambda, blocks_for(p.n, 128), 128, st, p, xs, nbr, cnt, solid, rho);
 }
 
 void launch_delta(bool mixed, const StepParams& p, const CellPack& cp, const float4* xs,
                   float4* xs_out, const int* nbr, const int* cnt, const float4* solid,
-                  const float* lam, const float4* x, float4* v_out, cudaStream_t st) {
+                  const int* key_sorted, const float4* x, float4* v_out, cudaStream_t st) {
     if (p.n <= 0) return;
-    LGB_DISPATCH(mixed, k_delta, blocks_for(p.n, 128), 128, st, p, cp, xs, xs_out, nbr, cnt, solid, lam,
-                 x, v_out);
+    LGB_DISPATCH(mixed, k_delta, blocks_for(p.n, 128), 128, st, p, cp, xs, xs_out, nbr, cnt, solid,
+                 key_sorted, x, v_out);
 }
 
 void launch_xsph(bool mixed, const StepParams& p, const CellPack& cp, const float4* xs,
-                 const float4* v_in, const int* nbr, const int* cnt, float4* x_out, float4* v_out,
-                 cudaStream_t st) {
+                 const float4* v_in, const int* nbr, const int* cnt, const int* key_sorted,
+                 float4* x_out, float4* v_out, cudaStream_t st) {
     if (p.n <= 0) return;
-    LGB_DISPATCH(mixed, k_xsph, blocks_for(p.n, 128), 128, st, p, cp, xs, v_in, nbr, cnt, x_out, v_out);
+    LGB_DISPATCH(mixed, k_xsph, blocks_for(p.n, 128), 128, st, p, cp, xs, v_in, nbr, cnt, key_sorted,
+                 x_out, v_out);
 }
 
 void launch_unpermute_pos(bool mixed, const StepParams& p, const CellPack& cp, const float4* a,

@@ -123,6 +123,35 @@ __global__ void k_stabilize(const int* __restrict__ tmp, const int* __restrict__
     perm[a + r] = i;
 }
 
+// Stabilisation fused with the reorder: the slot found for particle i
+// receives its state directly (no permutation array round trip).
+__global__ void k_stabilize_gather(const int* __restrict__ tmp, const int* __restrict__ key,
+                                   const int* __restrict__ start, const int* __restrict__ tie, int n,
+                                   const float4* __restrict__ x, const float4* __restrict__ xs,
+                                   const float4* __restrict__ v, const int* __restrict__ id,
+                                   int* __restrict__ key_out, float4* __restrict__ x_out,
+                                   float4* __restrict__ xs_out, float4* __restrict__ v_out,
+                                   int* __restrict__ id_out) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const int i = tmp[s];
+    const int c = key[i];
+    const int a = start[c], b = start[c + 1];
+    const int mine = tie ? tie[i] : i;
+    int r = 0;
+    for (int t = a; t < b; t++) {
+        int o = tmp[t];
+        int ot = tie ? tie[o] : o;
+        r += ot < mine;
+    }
+    const int f = a + r;
+    key_out[f] = c;
+    x_out[f] = x[i];
+    xs_out[f] = xs[i];
+    v_out[f] = v[i];
+    id_out[f] = id[i];
+}
+
 __global__ void k_gather_state(const int* __restrict__ perm, int n, const int* __restrict__ key,
                                const float4* __restrict__ x, const float4* __restrict__ xs,
                                const float4* __restrict__ v, const int* __restrict__ id,
@@ -171,6 +200,16 @@ void launch_gather_state(const int* perm, int n, const int* key, const float4* x
     if (n <= 0) return;
     k_gather_state<<<blocks_for(n, 256), 256, 0, st>>>(perm, n, key, x, xs, v, id, key_out, x_out,
                                                        xs_out, v_out, id_out);
+}
+
+void launch_sort_state(const int* key, const int* rank, const int* start, const int* tie, int n,
+                       int* tmp, const float4* x, const float4* xs, const float4* v, const int* id,
+                       int* key_out, float4* x_out, float4* xs_out, float4* v_out, int* id_out,
+                       cudaStream_t st) {
+    if (n <= 0) return;
+    k_scatter_index<<<blocks_for(n, 256), 256, 0, st>>>(key, rank, start, n, tmp);
+    k_stabilize_gather<<<blocks_for(n, 256), 256, 0, st>>>(tmp, key, start, tie, n, x, xs, v, id, key_out,
+                                                           x_out, xs_out, v_out, id_out);
 }
 
 void launch_gather_solid(const int* perm, int n, const float4* src, float4* dst, cudaStream_t st) {

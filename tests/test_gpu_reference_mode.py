@@ -132,7 +132,7 @@ def test_reference_mode_rollout_statistics(orc):
     state perturbed by one ulp in 1% of the particles."""
     from lustrine_gb300 import scenes
     sc = scenes.config0(seed=12)
-    sim = _sim(sc.domain, sc.n)
+    sim = _sim(sc.domain, sc.n, max_neighbors=512)  # clustering reaches ~100 neighbours
     sim.upload(sc.x, None)
     p = phys_params(orc.reference_params(*sc.domain))
     p.jacobi = 1
