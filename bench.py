@@ -230,11 +230,13 @@ def profile_stages(sim, dt, reps=3):
 
 def run_scene(sc, params, steps, warmup, flush):
     import torch
-    from lustrine_gb300 import PbfSim
+    from lustrine_gb300 import PbfSim, tuning
     sim = PbfSim(params, sc.n, sc.ns)
     sim.upload(sc.x, None, sc.solid if sc.ns else None)
     sim.step(sc.dt, warmup)
     sim.synchronize()
+    # launch shape chosen by the autotuner on this GPU (timed from this state)
+    sim.tuned = tuning.tune(sim, sc.dt, steps=3, cache=None)
     ext = torch.cuda.ExternalStream(sim.stream())
     ms = time_steps(sim, sc.dt, steps, flush, ext)
     st = sim.status()
@@ -287,7 +289,7 @@ def run_ours(args, world, rank, local):
         "config": {"workload": WORKLOAD, "fluid_particles": sc.n, "solid_particles": sc.ns,
                    "box": list(sc.domain), "h": 1.0, "solver_iterations": iters, "dt": sc.dt,
                    "precision": "fp32", "l2": "flushed (256 MiB write) before every timed step",
-                   "parallelism": f"replicas x{world}"},
+                   "parallelism": f"replicas x{world}", "launch_shape": sim.tuned["tuning"]},
         "gpu_launches": launches,
         "status": status,
         "e2e": e2e,
@@ -348,7 +350,8 @@ def run_variants(args, flush):
     p = pbf_params(*sc.domain, iterations=sc.iterations, c_xsph=sc.c_xsph, precision=PRECISION_MIXED)
     sim, _, ms, st = run_scene(sc, p, k, 3, flush)
     out["config1_mixed"] = {"value": sc.n * p.iterations / (np.mean(ms) * 1e-3),
-                            "ms_per_step": float(np.mean(ms)), "status": st}
+                            "ms_per_step": float(np.mean(ms)), "status": st,
+                            "launch_shape": sim.tuned["tuning"]}
     sim.close()
     sc = scenes.config2()
     p = pbf_params(*sc.domain, iterations=sc.iterations, c_xsph=sc.c_xsph)
@@ -356,6 +359,7 @@ def run_variants(args, flush):
     prof = profile_stages(sim, sc.dt, reps=2)
     out["config2_plain_2M"] = {"value": sc.n * p.iterations / (np.mean(ms) * 1e-3),
                                "ms_per_step": float(np.mean(ms)), "status": st,
+                               "launch_shape": sim.tuned["tuning"],
                                "stage_ms": {a: round(b[0], 4) for a, b in prof.items()}}
     sim.close()
     return out

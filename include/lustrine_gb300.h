@@ -238,6 +238,22 @@ enum {
 };
 LUSTRINE_API int lustrine_pbf_profile_step(lustrine_pbf* s, float dt, double* stage_ms,
                                            int* stage_launches, int num_stages);
+/* Launch shape of the PBF iteration kernels (lambda, delta-p, XSPH) and of
+ * the neighbour-list build.  block and list_block: 64, 128 or 256 threads;
+ * unroll: neighbour gathers in flight per thread, 1, 2 or 4. */
+typedef struct lustrine_pbf_tuning {
+    int block;
+    int unroll;
+    int list_block;
+} lustrine_pbf_tuning;
+LUSTRINE_API int lustrine_pbf_set_tuning(lustrine_pbf* s, const lustrine_pbf_tuning* t);
+LUSTRINE_API int lustrine_pbf_get_tuning(const lustrine_pbf* s, lustrine_pbf_tuning* t);
+/* Autotuner: times `steps` graph-replayed steps of every launch shape from
+ * the current state (restored before each candidate and at the end), keeps
+ * the fastest and returns it with its milliseconds per step.  The state is
+ * unchanged on return.  Reference mode has a single shape (returned as is). */
+LUSTRINE_API int lustrine_pbf_autotune(lustrine_pbf* s, float dt, int steps, lustrine_pbf_tuning* best,
+                                       float* best_ms);
 /* Kernel launches one step issues (for launch accounting). */
 LUSTRINE_API int lustrine_pbf_launches_per_step(const lustrine_pbf* s);
 

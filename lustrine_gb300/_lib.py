@@ -72,6 +72,10 @@ class PbfParams(C.Structure):
                 ("max_neighbors", C.c_int), ("clamp_cells", C.c_int), ("use_graph", C.c_int)]
 
 
+class PbfTuning(C.Structure):
+    _fields_ = [("block", C.c_int), ("unroll", C.c_int), ("list_block", C.c_int)]
+
+
 # Every symbol include/lustrine_gb300.h declares, with its ctypes signature.
 _P = C.c_void_p
 _FP = C.POINTER(C.c_float)
@@ -121,6 +125,9 @@ SIGNATURES = {
     "lustrine_pbf_stream": (C.c_int, [_P, C.POINTER(_P)]),
     "lustrine_pbf_launches_per_step": (C.c_int, [_P]),
     "lustrine_pbf_profile_step": (C.c_int, [_P, C.c_float, _DP, _IP, C.c_int]),
+    "lustrine_pbf_set_tuning": (C.c_int, [_P, C.POINTER(PbfTuning)]),
+    "lustrine_pbf_get_tuning": (C.c_int, [_P, C.POINTER(PbfTuning)]),
+    "lustrine_pbf_autotune": (C.c_int, [_P, C.c_float, C.c_int, C.POINTER(PbfTuning), _FP]),
     "lustrine_error_string": (C.c_char_p, [C.c_int]),
 }
 

@@ -48,6 +48,13 @@ struct StepParams {
     float dt;
 };
 
+// Launch shape of the PBF iteration kernels, chosen per scene by the autotuner.
+struct Tuning {
+    int block;       // threads per block of the lambda, delta and XSPH passes (64, 128, 256)
+    int unroll;      // neighbour gathers in flight per thread (1, 2, 4)
+    int list_block;  // threads per block of the list build (64, 128, 256)
+};
+
 // Mixed precision: a cell's integer coordinates packed into 32 bits,
 // x in the low bits, then y, then z.
 struct CellPack {

@@ -436,16 +436,18 @@ static int enqueue_step(lustrine_pbf* s, cudaStream_t st, StageMarks* mk = nullp
         float4* a = s->xs[o];
         float4* b = s->xs_alt;
         const int iters = s->prm.iterations;
+        const Tuning& tu = s->tune;
         for (int it = 0; it < iters; it++) {
+            float* rho = it == iters - 1 ? s->rho : nullptr;  // densities of the last pass only
             if (it == 0) {
-                launch_lists_lambda(mixed, p, a, s->key_sorted, s->start, s->solid, s->sstart, s->nbr,
-                                    s->cnt, s->rho, s->status, st);
+                launch_lists_lambda(mixed, tu, p, a, s->key_sorted, s->start, s->solid, s->sstart,
+                                    s->nbr, s->cnt, rho, s->status, st);
                 if (mk) mk->mark(LUSTRINE_STAGE_LISTS, st);
             } else {
-                launch_lambda(mixed, p, a, s->nbr, s->cnt, s->solid, s->rho, st);
+                launch_lambda(mixed, tu, p, a, s->nbr, s->cnt, s->solid, rho, st);
                 if (mk) mk->mark(LUSTRINE_STAGE_LAMBDA, st);
             }
-            launch_delta(mixed, p, s->cp, a, b, s->nbr, s->cnt, s->solid, s->key_sorted, s->x[o],
+            launch_delta(mixed, tu, p, s->cp, a, b, s->nbr, s->cnt, s->solid, s->key_sorted, s->x[o],
                          it == iters - 1 ? s->vtmp : nullptr, st);
             if (mk) mk->mark(LUSTRINE_STAGE_DELTA, st);
             float4* t = a;
@@ -453,7 +455,7 @@ static int enqueue_step(lustrine_pbf* s, cudaStream_t st, StageMarks* mk = nullp
             b = t;
             k += 2;
         }
-        launch_xsph(mixed, p, s->cp, a, s->vtmp, s->nbr, s->cnt, s->key_sorted, s->x[o], s->v[o], st);
+        launch_xsph(mixed, tu, p, s->cp, a, s->vtmp, s->nbr, s->cnt, s->key_sorted, s->x[o], s->v[o], st);
         k += 1;
         if (mk) mk->mark(LUSTRINE_STAGE_XSPH, st);
     }
@@ -547,6 +549,132 @@ extern "C" int lustrine_pbf_profile_step(lustrine_pbf* s, float dt, double* stag
     if (err != cudaSuccess) return lgb_cuda_status(err, "profile_step");
     finish_step(s, s->cur);
     return LUSTRINE_OK;
+}
+
+extern "C" int lustrine_pbf_set_tuning(lustrine_pbf* s, const lustrine_pbf_tuning* t) {
+    if (!s || !t) return LUSTRINE_ERR_ARGS;
+    auto ok = [](int b) { return b == 64 || b == 128 || b == 256; };
+    if (!ok(t->block) || !ok(t->list_block) || (t->unroll != 1 && t->unroll != 2 && t->unroll != 4))
+        return LUSTRINE_ERR_ARGS;
+    s->tune = Tuning{t->block, t->unroll, t->list_block};
+    s->invalidate_graphs();
+    return LUSTRINE_OK;
+}
+
+extern "C" int lustrine_pbf_get_tuning(const lustrine_pbf* s, lustrine_pbf_tuning* t) {
+    if (!s || !t) return LUSTRINE_ERR_ARGS;
+    t->block = s->tune.block;
+    t->unroll = s->tune.unroll;
+    t->list_block = s->tune.list_block;
+    return LUSTRINE_OK;
+}
+
+// Copies of the committed state, so every candidate starts from it.
+struct Snapshot {
+    float4 *x = nullptr, *v = nullptr;
+    int* id = nullptr;
+    ~Snapshot() {
+        cudaFree(x);
+        cudaFree(v);
+        cudaFree(id);
+    }
+};
+
+static int snapshot_take(lustrine_pbf* s, Snapshot& sn) {
+    const size_t n = (size_t)(s->n ? s->n : 1);
+    CK(cudaMalloc((void**)&sn.x, n * sizeof(float4)));
+    CK(cudaMalloc((void**)&sn.v, n * sizeof(float4)));
+    CK(cudaMalloc((void**)&sn.id, n * sizeof(int)));
+    const int c = s->cur;
+    CK(cudaMemcpyAsync(sn.x, s->x[c], (size_t)s->n * sizeof(float4), cudaMemcpyDeviceToDevice, s->stream));
+    CK(cudaMemcpyAsync(sn.v, s->v[c], (size_t)s->n * sizeof(float4), cudaMemcpyDeviceToDevice, s->stream));
+    CK(cudaMemcpyAsync(sn.id, s->id[c], (size_t)s->n * sizeof(int), cudaMemcpyDeviceToDevice, s->stream));
+    return LUSTRINE_OK;
+}
+
+static int snapshot_restore(lustrine_pbf* s, const Snapshot& sn, int side) {
+    s->cur = side;
+    CK(cudaMemcpyAsync(s->x[side], sn.x, (size_t)s->n * sizeof(float4), cudaMemcpyDeviceToDevice, s->stream));
+    CK(cudaMemcpyAsync(s->v[side], sn.v, (size_t)s->n * sizeof(float4), cudaMemcpyDeviceToDevice, s->stream));
+    CK(cudaMemcpyAsync(s->id[side], sn.id, (size_t)s->n * sizeof(int), cudaMemcpyDeviceToDevice, s->stream));
+    return LUSTRINE_OK;
+}
+
+// Milliseconds per step of `steps` graph-replayed steps from the snapshot
+// with the current tuning (two untimed steps capture both parities' graphs).
+static int time_candidate(lustrine_pbf* s, const Snapshot& sn, int side, float dt, int steps, float* ms) {
+    int rc = snapshot_restore(s, sn, side);
+    if (rc) return rc;
+    for (int k = 0; k < 2; k++)
+        if ((rc = lustrine_pbf_step(s, dt))) return rc;
+    if ((rc = snapshot_restore(s, sn, side))) return rc;
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    cudaEventRecord(e0, s->stream);
+    for (int k = 0; k < steps && !rc; k++) rc = lustrine_pbf_step(s, dt);
+    cudaEventRecord(e1, s->stream);
+    cudaError_t e = cudaEventSynchronize(e1);
+    float t = 0.0f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    if (e != cudaSuccess) return lgb_cuda_status(e, "autotune timing");
+    *ms = t / (float)steps;
+    return LUSTRINE_OK;
+}
+
+extern "C" int lustrine_pbf_autotune(lustrine_pbf* s, float dt, int steps, lustrine_pbf_tuning* best,
+                                     float* best_ms) {
+    if (!s || !s->have_state || steps < 1 || !(dt > 0.0f)) return LUSTRINE_ERR_ARGS;
+    if (s->prm.mode != LUSTRINE_MODE_PBF || s->n == 0) {
+        // the reference-semantics kernels have a single launch shape
+        if (best) lustrine_pbf_get_tuning(s, best);
+        if (best_ms) *best_ms = 0.0f;
+        return LUSTRINE_OK;
+    }
+    const int use_graph = s->prm.use_graph;
+    s->prm.use_graph = 1;
+    Snapshot sn;
+    int rc = snapshot_take(s, sn);
+    const int side = s->cur;
+    Tuning keep = s->tune, top = s->tune;
+    float top_ms = 3.4e38f;
+    static const int blocks[3] = {64, 128, 256};
+    static const int unrolls[3] = {1, 2, 4};
+    // the iteration kernels' shape first, then the list build's block size
+    for (int bi = 0; bi < 3 && !rc; bi++)
+        for (int ui = 0; ui < 3 && !rc; ui++) {
+            s->tune = Tuning{blocks[bi], unrolls[ui], keep.list_block};
+            s->invalidate_graphs();
+            float ms = 0.0f;
+            rc = time_candidate(s, sn, side, dt, steps, &ms);
+            if (!rc && ms < top_ms) {
+                top_ms = ms;
+                top = s->tune;
+            }
+        }
+    for (int bi = 0; bi < 3 && !rc; bi++) {
+        s->tune = Tuning{top.block, top.unroll, blocks[bi]};
+        s->invalidate_graphs();
+        float ms = 0.0f;
+        rc = time_candidate(s, sn, side, dt, steps, &ms);
+        if (!rc && ms < top_ms) {
+            top_ms = ms;
+            top = s->tune;
+        }
+    }
+    s->tune = rc ? keep : top;
+    s->invalidate_graphs();
+    s->prm.use_graph = use_graph;
+    int rc2 = snapshot_restore(s, sn, side);
+    if (!rc) rc = rc2;
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    if (!rc && e != cudaSuccess) rc = lgb_cuda_status(e, "autotune");
+    if (best) lustrine_pbf_get_tuning(s, best);
+    if (best_ms) *best_ms = top_ms;
+    return rc;
 }
 
 extern "C" int lustrine_pbf_synchronize(lustrine_pbf* s) {

@@ -12,6 +12,7 @@ struct lustrine_pbf {
     lustrine_pbf_params prm{};
     lgb::StepParams sp{};
     lgb::CellPack cp{};
+    lgb::Tuning tune{128, 4, 128};
     int n = 0, ns = 0;
     cudaStream_t stream = nullptr;
 

@@ -43,17 +43,19 @@ void launch_predict(bool mixed, const StepParams& p, const CellPack& cp, const f
 void launch_key(bool mixed, const StepParams& p, const CellPack& cp, const float4* pos, int m,
                 int* key, int* rank, int* count, cudaStream_t st);
 // neighbour lists + first lambda pass (lambda stored in xs.w)
-void launch_lists_lambda(bool mixed, const StepParams& p, float4* xs, const int* key_sorted,
-                         const int* fstart, const float4* solid, const int* sstart, int* nbr,
-                         int* cnt, float* rho, int* status, cudaStream_t st);
-void launch_lambda(bool mixed, const StepParams& p, float4* xs, const int* nbr, const int* cnt,
-                   const float4* solid, float* rho, cudaStream_t st);
-void launch_delta(bool mixed, const StepParams& p, const CellPack& cp, const float4* xs,
-                  float4* xs_out, const int* nbr, const int* cnt, const float4* solid,
-                  const int* key_sorted, const float4* x, float4* v_out, cudaStream_t st);
-void launch_xsph(bool mixed, const StepParams& p, const CellPack& cp, const float4* xs,
-                 const float4* v_in, const int* nbr, const int* cnt, const int* key_sorted,
-                 float4* x_out, float4* v_out, cudaStream_t st);
+void launch_lists_lambda(bool mixed, const Tuning& tu, const StepParams& p, float4* xs,
+                         const int* key_sorted, const int* fstart, const float4* solid,
+                         const int* sstart, int* nbr, int* cnt, float* rho, int* status,
+                         cudaStream_t st);
+void launch_lambda(bool mixed, const Tuning& tu, const StepParams& p, float4* xs, const int* nbr,
+                   const int* cnt, const float4* solid, float* rho, cudaStream_t st);
+void launch_delta(bool mixed, const Tuning& tu, const StepParams& p, const CellPack& cp,
+                  const float4* xs, float4* xs_out, const int* nbr, const int* cnt,
+                  const float4* solid, const int* key_sorted, const float4* x, float4* v_out,
+                  cudaStream_t st);
+void launch_xsph(bool mixed, const Tuning& tu, const StepParams& p, const CellPack& cp,
+                 const float4* xs, const float4* v_in, const int* nbr, const int* cnt,
+                 const int* key_sorted, float4* x_out, float4* v_out, cudaStream_t st);
 void launch_unpermute_pos(bool mixed, const StepParams& p, const CellPack& cp, const float4* a,
                           const int* id, int n, float* out, cudaStream_t st);
 void launch_unpermute_pos_d(bool mixed, const StepParams& p, const CellPack& cp, const float4* a,

@@ -27,7 +27,6 @@ namespace lgb {
 
 constexpr int SLOT_BITS = 26;
 constexpr int SLOT_MASK = (1 << SLOT_BITS) - 1;
-constexpr int UNROLL = 4;
 
 __device__ __forceinline__ int entry(int slot, int code, bool solid) {
     return slot | (code << SLOT_BITS) | (solid ? (int)0x80000000u : 0);
@@ -230,14 +229,51 @@ __device__ __forceinline__ float lambda_of(const StepParams& p, const LambdaAcc&
     return -(a.density / p.rho0 - 1.0f) / (S + p.eps);
 }
 
-template <bool MIXED>
-__global__ void __launch_bounds__(128) k_lists_lambda(StepParams p, float4* __restrict__ xs,
-                                                      const int* __restrict__ key_sorted,
-                                                      const int* __restrict__ fstart,
-                                                      const float4* __restrict__ solid,
-                                                      const int* __restrict__ sstart,
-                                                      int* __restrict__ nbr, int* __restrict__ cnt,
-                                                      float* __restrict__ rho, int* status) {
+// One row (dy, dx) of the stencil: the cells z0..z1 of a row are consecutive
+// ids, so their particles form one slot range; the cell bounds are loaded
+// once per row and give each candidate's dz.
+template <bool MIXED, bool SOLID>
+__device__ __forceinline__ void walk_row(const StepParams& p, const float4& self, int s,
+                                         const float4* __restrict__ pos, const int* __restrict__ start,
+                                         int row, int zc, int dx, int dy, LambdaAcc& a, int& c_n,
+                                         int* __restrict__ nbr) {
+    const int z0 = max(zc - 1, 0), z1 = min(zc + 1, p.gz - 1);
+    int b[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) b[k] = (z0 + k <= z1 + 1) ? start[row + z0 + k] : 0;
+    const float sx = -(float)dx * p.cell, sy = -(float)dy * p.cell;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const int z = z0 + k;
+        if (z > z1) break;
+        const int dz = z - zc;
+        const int code = (dx + 1) + 3 * (dz + 1) + 9 * (dy + 1);
+        const float sz = -(float)dz * p.cell;
+        for (int t = b[k]; t < b[k + 1]; t++) {
+            const float4 q = SOLID ? __ldg(&pos[t]) : pos[t];
+            float3 d = make_float3(self.x - q.x, self.y - q.y, self.z - q.z);
+            if (MIXED) {
+                d.x += sx;
+                d.y += sy;
+                d.z += sz;
+            }
+            if (dot3(d.x, d.y, d.z) <= p.h2) {
+                if (c_n < p.max_nbrs) nbr[(size_t)c_n * p.n + s] = entry(t, code, SOLID);
+                c_n++;
+                lambda_accumulate<MIXED>(p, a, d, !SOLID && t == s, SOLID);
+            }
+        }
+    }
+}
+
+template <bool MIXED, int B>
+__global__ void __launch_bounds__(B) k_lists_lambda(StepParams p, float4* __restrict__ xs,
+                                                    const int* __restrict__ key_sorted,
+                                                    const int* __restrict__ fstart,
+                                                    const float4* __restrict__ solid,
+                                                    const int* __restrict__ sstart,
+                                                    int* __restrict__ nbr, int* __restrict__ cnt,
+                                                    float* __restrict__ rho, int* status) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= p.n) return;
     const float4 self = xs[s];
@@ -252,35 +288,8 @@ __global__ void __launch_bounds__(128) k_lists_lambda(StepParams p, float4* __re
             const int xx = c.x + dx;
             if (xx < 0 || xx >= p.gx) continue;
             const int row = y * slab + xx * p.gz;
-            for (int dz = -1; dz <= 1; dz++) {
-                const int z = c.z + dz;
-                if (z < 0 || z >= p.gz) continue;
-                const int code = (dx + 1) + 3 * (dz + 1) + 9 * (dy + 1);
-                const float sx = -(float)dx * p.cell, sy = -(float)dy * p.cell,
-                            sz = -(float)dz * p.cell;
-                for (int t = fstart[row + z], e = fstart[row + z + 1]; t < e; t++) {
-                    const float4 q = xs[t];
-                    float3 d = make_float3(self.x - q.x, self.y - q.y, self.z - q.z);
-                    if (MIXED) { d.x += sx; d.y += sy; d.z += sz; }
-                    if (dot3(d.x, d.y, d.z) <= p.h2) {
-                        if (c_n < p.max_nbrs) nbr[(size_t)c_n * p.n + s] = entry(t, code, false);
-                        c_n++;
-                        lambda_accumulate<MIXED>(p, a, d, t == s, false);
-                    }
-                }
-                if (p.ns > 0) {
-                    for (int t = sstart[row + z], e = sstart[row + z + 1]; t < e; t++) {
-                        const float4 q = __ldg(&solid[t]);
-                        float3 d = make_float3(self.x - q.x, self.y - q.y, self.z - q.z);
-                        if (MIXED) { d.x += sx; d.y += sy; d.z += sz; }
-                        if (dot3(d.x, d.y, d.z) <= p.h2) {
-                            if (c_n < p.max_nbrs) nbr[(size_t)c_n * p.n + s] = entry(t, code, true);
-                            c_n++;
-                            lambda_accumulate<MIXED>(p, a, d, false, true);
-                        }
-                    }
-                }
-            }
+            walk_row<MIXED, false>(p, self, s, xs, fstart, row, c.z, dx, dy, a, c_n, nbr);
+            if (p.ns > 0) walk_row<MIXED, true>(p, self, s, solid, sstart, row, c.z, dx, dy, a, c_n, nbr);
         }
     }
     if (c_n > p.max_nbrs) {
@@ -293,26 +302,27 @@ __global__ void __launch_bounds__(128) k_lists_lambda(StepParams p, float4* __re
     if (rho) rho[s] = a.density;
 }
 
-// Lambda pass over the lists (iterations after the first).
-template <bool MIXED>
-__global__ void __launch_bounds__(128) k_lambda(StepParams p, float4* __restrict__ xs,
-                                                const int* __restrict__ nbr, const int* __restrict__ cnt,
-                                                const float4* __restrict__ solid,
-                                                float* __restrict__ rho) {
+// Lambda pass over the lists (iterations after the first); U neighbour
+// gathers in flight per thread.
+template <bool MIXED, int U, int B>
+__global__ void __launch_bounds__(B) k_lambda(StepParams p, float4* __restrict__ xs,
+                                              const int* __restrict__ nbr, const int* __restrict__ cnt,
+                                              const float4* __restrict__ solid,
+                                              float* __restrict__ rho) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= p.n) return;
     const float4 self = xs[s];
     const int c = cnt[s];
     LambdaAcc a = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
-    for (int k = 0; k < c; k += UNROLL) {
-        int e[UNROLL];
-        float4 q[UNROLL];
+    for (int k = 0; k < c; k += U) {
+        int e[U];
+        float4 q[U];
 #pragma unroll
-        for (int u = 0; u < UNROLL; u++) e[u] = k + u < c ? __ldg(&nbr[(size_t)(k + u) * p.n + s]) : s;
+        for (int u = 0; u < U; u++) e[u] = k + u < c ? __ldg(&nbr[(size_t)(k + u) * p.n + s]) : s;
 #pragma unroll
-        for (int u = 0; u < UNROLL; u++) q[u] = load_entry(e[u], xs, solid);
+        for (int u = 0; u < U; u++) q[u] = load_entry(e[u], xs, solid);
 #pragma unroll
-        for (int u = 0; u < UNROLL; u++) {
+        for (int u = 0; u < U; u++) {
             if (k + u >= c) break;
             float3 d = rel_e<MIXED>(p, self, q[u], e[u]);
             lambda_accumulate<MIXED>(p, a, d, entry_is(e[u], s), entry_solid(e[u]));
@@ -324,8 +334,8 @@ __global__ void __launch_bounds__(128) k_lambda(StepParams p, float4* __restrict
 
 // Position correction with s_corr, solid push-out and box clamp (Jacobi).
 // The last iteration also writes v = (x* - x) / dt.
-template <bool MIXED>
-__global__ void __launch_bounds__(128) k_delta(StepParams p, CellPack cp, const float4* __restrict__ xs,
+template <bool MIXED, int U, int B>
+__global__ void __launch_bounds__(B) k_delta(StepParams p, CellPack cp, const float4* __restrict__ xs,
                                                float4* __restrict__ xs_out, const int* __restrict__ nbr,
                                                const int* __restrict__ cnt,
                                                const float4* __restrict__ solid,
@@ -339,15 +349,15 @@ __global__ void __launch_bounds__(128) k_delta(StepParams p, CellPack cp, const 
     float px = 0.0f, py = 0.0f, pz = 0.0f;
     float cx = 0.0f, cy = 0.0f, cz = 0.0f;
     int nct = 0;
-    for (int k = 0; k < c; k += UNROLL) {
-        int e[UNROLL];
-        float4 q[UNROLL];
+    for (int k = 0; k < c; k += U) {
+        int e[U];
+        float4 q[U];
 #pragma unroll
-        for (int u = 0; u < UNROLL; u++) e[u] = k + u < c ? __ldg(&nbr[(size_t)(k + u) * p.n + s]) : s;
+        for (int u = 0; u < U; u++) e[u] = k + u < c ? __ldg(&nbr[(size_t)(k + u) * p.n + s]) : s;
 #pragma unroll
-        for (int u = 0; u < UNROLL; u++) q[u] = load_entry(e[u], xs, solid);
+        for (int u = 0; u < U; u++) q[u] = load_entry(e[u], xs, solid);
 #pragma unroll
-        for (int u = 0; u < UNROLL; u++) {
+        for (int u = 0; u < U; u++) {
             if (k + u >= c) break;
             if (entry_is(e[u], s)) continue;
             const bool sol = entry_solid(e[u]);
@@ -403,12 +413,12 @@ __global__ void __launch_bounds__(128) k_delta(StepParams p, CellPack cp, const 
 }
 
 // XSPH viscosity (Macklin & Mueller eq. 17) and commit x = x*.
-template <bool MIXED>
-__global__ void __launch_bounds__(128) k_xsph(StepParams p, CellPack cp, const float4* __restrict__ xs,
-                                              const float4* __restrict__ v_in,
-                                              const int* __restrict__ nbr, const int* __restrict__ cnt,
-                                              const int* __restrict__ key_sorted,
-                                              float4* __restrict__ x_out, float4* __restrict__ v_out) {
+template <bool MIXED, int U, int B>
+__global__ void __launch_bounds__(B) k_xsph(StepParams p, CellPack cp, const float4* __restrict__ xs,
+                                            const float4* __restrict__ v_in,
+                                            const int* __restrict__ nbr, const int* __restrict__ cnt,
+                                            const int* __restrict__ key_sorted,
+                                            float4* __restrict__ x_out, float4* __restrict__ v_out) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= p.n) return;
     const float4 self = xs[s];
@@ -416,21 +426,21 @@ __global__ void __launch_bounds__(128) k_xsph(StepParams p, CellPack cp, const f
     const int c = cnt[s];
     float ax = 0.0f, ay = 0.0f, az = 0.0f;
     if (p.c_xsph != 0.0f) {
-        for (int k = 0; k < c; k += UNROLL) {
-            int e[UNROLL];
-            float4 q[UNROLL], vj[UNROLL];
+        for (int k = 0; k < c; k += U) {
+            int e[U];
+            float4 q[U], vj[U];
 #pragma unroll
-            for (int u = 0; u < UNROLL; u++) {
+            for (int u = 0; u < U; u++) {
                 int t = k + u < c ? __ldg(&nbr[(size_t)(k + u) * p.n + s]) : s;
                 e[u] = entry_solid(t) ? s : t;  // solids take no part
             }
 #pragma unroll
-            for (int u = 0; u < UNROLL; u++) {
+            for (int u = 0; u < U; u++) {
                 q[u] = xs[entry_slot(e[u])];
                 vj[u] = v_in[entry_slot(e[u])];
             }
 #pragma unroll
-            for (int u = 0; u < UNROLL; u++) {
+            for (int u = 0; u < U; u++) {
                 if (k + u >= c) break;
                 if (entry_is(e[u], s)) continue;
                 float3 d = rel_e<MIXED>(p, self, q[u], e[u]);
@@ -592,34 +602,72 @@ void launch_key(bool mixed, const StepParams& p, const CellPack& cp, const float
     LGB_DISPATCH(mixed, k_key, blocks_for(m, 256), 256, st, p, cp, pos, m, key, rank, count);
 }
 
-void launch_lists_lambda(bool mixed, const StepParams& p, float4* xs, const int* key_sorted,
-                         const int* fstart, const float4* solid, const int* sstart, int* nbr,
-                         int* cnt, float* rho, int* status, cudaStream_t st) {
+// Kernels templated on (MIXED, U, B) are instantiated for U in {1, 2, 4} and
+// B in {64, 128, 256}; the tuning picks one (TUNE_CASE expands the switch).
+#define TUNE_LAUNCH(KERNEL, MIX, U_, B_, N, ST, ...)                                            \
+    KERNEL<MIX, U_, B_><<<blocks_for(N, B_), B_, 0, ST>>>(__VA_ARGS__)
+#define TUNE_BLOCKS(KERNEL, MIX, U_, tu, N, ST, ...)                                            \
+    do {                                                                                        \
+        if (tu.block <= 64)                                                                     \
+            TUNE_LAUNCH(KERNEL, MIX, U_, 64, N, ST, __VA_ARGS__);                               \
+        else if (tu.block <= 128)                                                               \
+            TUNE_LAUNCH(KERNEL, MIX, U_, 128, N, ST, __VA_ARGS__);                              \
+        else                                                                                    \
+            TUNE_LAUNCH(KERNEL, MIX, U_, 256, N, ST, __VA_ARGS__);                              \
+    } while (0)
+#define TUNE_CASE(KERNEL, MIX, tu, N, ST, ...)                                                  \
+    do {                                                                                        \
+        if (tu.unroll <= 1)                                                                     \
+            TUNE_BLOCKS(KERNEL, MIX, 1, tu, N, ST, __VA_ARGS__);                                \
+        else if (tu.unroll == 2)                                                                \
+            TUNE_BLOCKS(KERNEL, MIX, 2, tu, N, ST, __VA_ARGS__);                                \
+        else                                                                                    \
+            TUNE_BLOCKS(KERNEL, MIX, 4, tu, N, ST, __VA_ARGS__);                                \
+    } while (0)
+#define TUNE_DISPATCH(KERNEL, mixed, tu, N, ST, ...)                                            \
+    do {                                                                                        \
+        if (mixed)                                                                              \
+            TUNE_CASE(KERNEL, true, tu, N, ST, __VA_ARGS__);                                    \
+        else                                                                                    \
+            TUNE_CASE(KERNEL, false, tu, N, ST, __VA_ARGS__);                                   \
+    } while (0)
+
+void launch_lists_lambda(bool mixed, const Tuning& tu, const StepParams& p, float4* xs,
+                         const int* key_sorted, const int* fstart, const float4* solid,
+                         const int* sstart, int* nbr, int* cnt, float* rho, int* status,
+                         cudaStream_t st) {
     if (p.n <= 0) return;
-    LGB_DISPATCH(mixed, k_lists_lambda, blocks_for(p.n, 128), 128, st, p, xs, key_sorted, fstart, solid,
-                 sstart, nbr, cnt, rho, status);
+    const int B = tu.list_block <= 64 ? 64 : (tu.list_block <= 128 ? 128 : 256);
+    if (mixed) {
+        if (B == 64) k_lists_lambda<true, 64><<<blocks_for(p.n, 64), 64, 0, st>>>(p, xs, key_sorted, fstart, solid, sstart, nbr, cnt, rho, status);
+        else if (B == 128) k_lists_lambda<true, 128><<<blocks_for(p.n, 128), 128, 0, st>>>(p, xs, key_sorted, fstart, solid, sstart, nbr, cnt, rho, status);
+        else k_lists_lambda<true, 256><<<blocks_for(p.n, 256), 256, 0, st>>>(p, xs, key_sorted, fstart, solid, sstart, nbr, cnt, rho, status);
+    } else {
+        if (B == 64) k_lists_lambda<false, 64><<<blocks_for(p.n, 64), 64, 0, st>>>(p, xs, key_sorted, fstart, solid, sstart, nbr, cnt, rho, status);
+        else if (B == 128) k_lists_lambda<false, 128><<<blocks_for(p.n, 128), 128, 0, st>>>(p, xs, key_sorted, fstart, solid, sstart, nbr, cnt, rho, status);
+        else k_lists_lambda<false, 256><<<blocks_for(p.n, 256), 256, 0, st>>>(p, xs, key_sorted, fstart, solid, sstart, nbr, cnt, rho, status);
+    }
 }
 
-void launch_lambda(bool mixed, const StepParams& p, float4* xs, const int* nbr, const int* cnt,
-                   const float4* solid, float* rho, cudaStream_t st) {
+void launch_lambda(bool mixed, const Tuning& tu, const StepParams& p, float4* xs, const int* nbr,
+                   const int* cnt, const float4* solid, float* rho, cudaStream_t st) {
     if (p.n <= 0) return;
-    LGB_DISPATCH(mixed, k_lambda, blocks_for(p.n, 128), 128, st, p, xs, nbr, cnt, solid, rho);
+    TUNE_DISPATCH(k_lambda, mixed, tu, p.n, st, p, xs, nbr, cnt, solid, rho);
 }
 
-void launch_delta(bool mixed, const StepParams& p, const CellPack& cp, const float4* xs,
-                  float4* xs_out, const int* nbr, const int* cnt, const float4* solid,
-                  const int* key_sorted, const float4* x, float4* v_out, cudaStream_t st) {
+void launch_delta(bool mixed, const Tuning& tu, const StepParams& p, const CellPack& cp,
+                  const float4* xs, float4* xs_out, const int* nbr, const int* cnt,
+                  const float4* solid, const int* key_sorted, const float4* x, float4* v_out,
+                  cudaStream_t st) {
     if (p.n <= 0) return;
-    LGB_DISPATCH(mixed, k_delta, blocks_for(p.n, 128), 128, st, p, cp, xs, xs_out, nbr, cnt, solid,
-                 key_sorted, x, v_out);
+    TUNE_DISPATCH(k_delta, mixed, tu, p.n, st, p, cp, xs, xs_out, nbr, cnt, solid, key_sorted, x, v_out);
 }
 
-void launch_xsph(bool mixed, const StepParams& p, const CellPack& cp, const float4* xs,
-                 const float4* v_in, const int* nbr, const int* cnt, const int* key_sorted,
-                 float4* x_out, float4* v_out, cudaStream_t st) {
+void launch_xsph(bool mixed, const Tuning& tu, const StepParams& p, const CellPack& cp,
+                 const float4* xs, const float4* v_in, const int* nbr, const int* cnt,
+                 const int* key_sorted, float4* x_out, float4* v_out, cudaStream_t st) {
     if (p.n <= 0) return;
-    LGB_DISPATCH(mixed, k_xsph, blocks_for(p.n, 128), 128, st, p, cp, xs, v_in, nbr, cnt, key_sorted,
-                 x_out, v_out);
+    TUNE_DISPATCH(k_xsph, mixed, tu, p.n, st, p, cp, xs, v_in, nbr, cnt, key_sorted, x_out, v_out);
 }
 
 void launch_unpermute_pos(bool mixed, const StepParams& p, const CellPack& cp, const float4* a,

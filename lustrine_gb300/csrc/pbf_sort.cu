@@ -32,23 +32,25 @@ __device__ __forceinline__ int warp_inclusive_scan(int v) {
     return v;
 }
 
-// Exclusive scan of one value per thread across the block; returns the
-// exclusive prefix and writes the block total to *total.
+// Exclusive scan of one value per thread across a block of THREADS threads;
+// returns the exclusive prefix and writes the block total to *total.
+template <int THREADS>
 __device__ __forceinline__ int block_exclusive_scan(int v, int* total) {
-    __shared__ int warp_sums[SCAN_THREADS / 32 + 1];
+    constexpr int W = THREADS / 32;
+    __shared__ int warp_sums[W + 1];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     int inc = warp_inclusive_scan(v);
     if (lane == 31) warp_sums[warp] = inc;
     __syncthreads();
     if (warp == 0) {
-        int w = lane < SCAN_THREADS / 32 ? warp_sums[lane] : 0;
+        int w = lane < W ? warp_sums[lane] : 0;
         int wi = warp_inclusive_scan(w);
-        if (lane < SCAN_THREADS / 32) warp_sums[lane] = wi - w;
-        if (lane == SCAN_THREADS / 32 - 1) warp_sums[SCAN_THREADS / 32] = wi;
+        if (lane < W) warp_sums[lane] = wi - w;
+        if (lane == W - 1) warp_sums[W] = wi;
     }
     __syncthreads();
     int res = inc - v + warp_sums[warp];
-    *total = warp_sums[SCAN_THREADS / 32];
+    *total = warp_sums[W];
     __syncthreads();
     return res;
 }
@@ -61,19 +63,32 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(const int* __restr
     for (int k = 0; k < SCAN_ITEMS; k++)
         if (base + k < C) s += count[base + k];
     int total;
-    block_exclusive_scan(s, &total);
+    block_exclusive_scan<SCAN_THREADS>(s, &total);
     if (threadIdx.x == 0) block_sums[blockIdx.x] = total;
 }
 
-// One block: exclusive scan of the per-tile sums, in place.
-__global__ void __launch_bounds__(SCAN_THREADS) k_scan_sums(int* __restrict__ block_sums, int nb) {
+// One block: exclusive scan of the per-tile sums, in place; 8 sums per
+// thread, so up to 8192 tiles (33.5 M cells) take one pass.
+constexpr int SUMS_THREADS = 1024;
+constexpr int SUMS_ITEMS = 8;
+__global__ void __launch_bounds__(SUMS_THREADS) k_scan_sums(int* __restrict__ block_sums, int nb) {
     int carry = 0;
-    for (int base = 0; base < nb; base += SCAN_THREADS) {
-        int i = base + threadIdx.x;
-        int v = i < nb ? block_sums[i] : 0;
+    for (int base = 0; base < nb; base += SUMS_THREADS * SUMS_ITEMS) {
+        const int first = base + threadIdx.x * SUMS_ITEMS;
+        int vals[SUMS_ITEMS];
+        int s = 0;
+#pragma unroll
+        for (int k = 0; k < SUMS_ITEMS; k++) {
+            vals[k] = first + k < nb ? block_sums[first + k] : 0;
+            s += vals[k];
+        }
         int total;
-        int ex = block_exclusive_scan(v, &total);
-        if (i < nb) block_sums[i] = ex + carry;
+        int ex = block_exclusive_scan<SUMS_THREADS>(s, &total) + carry;
+#pragma unroll
+        for (int k = 0; k < SUMS_ITEMS; k++) {
+            if (first + k < nb) block_sums[first + k] = ex;
+            ex += vals[k];
+        }
         carry += total;
     }
 }
@@ -90,7 +105,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_down(const int* __restric
         s += vals[k];
     }
     int total;
-    int ex = block_exclusive_scan(s, &total) + block_sums[blockIdx.x];
+    int ex = block_exclusive_scan<SCAN_THREADS>(s, &total) + block_sums[blockIdx.x];
 #pragma unroll
     for (int k = 0; k < SCAN_ITEMS; k++) {
         if (base + k < C) start[base + k] = ex;
@@ -181,7 +196,7 @@ static inline int blocks_for(int n, int t) { return (n + t - 1) / t; }
 void launch_scan(const int* count, int C, int* block_sums, int* start, cudaStream_t st) {
     int nb = blocks_for(C, SCAN_TILE);
     k_scan_reduce<<<nb, SCAN_THREADS, 0, st>>>(count, C, block_sums);
-    k_scan_sums<<<1, SCAN_THREADS, 0, st>>>(block_sums, nb);
+    k_scan_sums<<<1, SUMS_THREADS, 0, st>>>(block_sums, nb);
     k_scan_down<<<nb, SCAN_THREADS, 0, st>>>(count, C, block_sums, start);
 }
 

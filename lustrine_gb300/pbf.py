@@ -184,6 +184,25 @@ class PbfSim:
         r = list(out)
         return dict(mass=r[0], momentum=r[1:4], kinetic=r[4], com=r[5:8], max_density_error=r[8])
 
+    # launch shape -----------------------------------------------------------
+    def get_tuning(self) -> dict:
+        t = _lib.PbfTuning()
+        check(self.lib.lustrine_pbf_get_tuning(self.h, C.byref(t)), "get_tuning")
+        return {"block": t.block, "unroll": t.unroll, "list_block": t.list_block}
+
+    def set_tuning(self, block: int, unroll: int, list_block: int):
+        t = _lib.PbfTuning(block, unroll, list_block)
+        check(self.lib.lustrine_pbf_set_tuning(self.h, C.byref(t)), "set_tuning")
+
+    def autotune(self, dt: float, steps: int = 3) -> tuple[dict, float]:
+        """Time every launch shape from the current state (state unchanged);
+        keeps and returns the fastest with its ms per step."""
+        t = _lib.PbfTuning()
+        ms = C.c_float()
+        check(self.lib.lustrine_pbf_autotune(self.h, float(dt), int(steps), C.byref(t), C.byref(ms)),
+              "autotune")
+        return {"block": t.block, "unroll": t.unroll, "list_block": t.list_block}, float(ms.value)
+
     STAGES = ("predict", "scan", "sort", "lists", "lambda", "delta", "xsph")
 
     def profile_step(self, dt: float) -> dict:

@@ -150,6 +150,31 @@ def test_mixed_and_plain_agree_near_origin(orc):
     assert err.max() < 1e-3, (err.max(), i, out[0][i], out[1][i], sc.x[i])
 
 
+def test_autotune_keeps_state_and_all_shapes_agree():
+    from lustrine_gb300 import PbfSim, scenes
+    sc = scenes.config0(seed=27)
+    sim = PbfSim(_params(sc), sc.n)
+    sim.upload(sc.x)
+    sim.step(sc.dt, 2)
+    before = sim.download()
+    best, ms = sim.autotune(sc.dt, steps=2)
+    after = sim.download()
+    assert np.array_equal(before[0], after[0]) and np.array_equal(before[1], after[1])
+    assert best["block"] in (64, 128, 256) and best["unroll"] in (1, 2, 4) and ms > 0
+    assert sim.get_tuning() == best
+    # every launch shape computes the same step (same summation order)
+    ref = None
+    for blk, unr in ((64, 1), (128, 2), (256, 4)):
+        sim.upload(before[0], before[1])
+        sim.set_tuning(blk, unr, blk)
+        sim.step(sc.dt)
+        x = sim.positions()
+        if ref is None:
+            ref = x
+        assert np.abs(x - ref).max() <= 1e-5
+    sim.close()
+
+
 def test_graph_and_direct_launches_are_identical():
     from lustrine_gb300 import PbfSim, scenes
     sc = scenes.config0(seed=24)
