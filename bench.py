@@ -353,6 +353,14 @@ def run_variants(args, flush):
                             "ms_per_step": float(np.mean(ms)), "status": st,
                             "launch_shape": sim.tuned["tuning"]}
     sim.close()
+    # the same step without programmatic dependent launch between kernels
+    os.environ["LUSTRINE_NO_PDL"] = "1"
+    p = pbf_params(*sc.domain, iterations=sc.iterations, c_xsph=sc.c_xsph)
+    sim, _, ms, st = run_scene(sc, p, k, 3, flush)
+    del os.environ["LUSTRINE_NO_PDL"]
+    out["config1_no_pdl"] = {"value": sc.n * p.iterations / (np.mean(ms) * 1e-3),
+                             "ms_per_step": float(np.mean(ms)), "status": st}
+    sim.close()
     sc = scenes.config2()
     p = pbf_params(*sc.domain, iterations=sc.iterations, c_xsph=sc.c_xsph)
     sim, _, ms, st = run_scene(sc, p, k, 3, flush)

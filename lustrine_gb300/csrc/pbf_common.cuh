@@ -16,6 +16,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <utility>
+
 namespace lgb {
 
 // Device status bits, OR-ed into a status word instead of trapping.
@@ -40,6 +42,9 @@ struct StepParams {
     // PBF kernels: poly6 K6 (h^2 - r^2)^3, spiky gradient -Ks (h - r)^2 d / r
     float k6, ks, inv_w_dq;
     float mass, rho0, eps;
+    float mr;             // mass / rho0
+    float self_density;   // m W(0) = m K6 h^6 (the particle's own density term)
+    float inv_dt;
     float dq, sk, sn;     // s_corr distance, k and exponent
     int sn_int;           // exponent as an integer in [0, 32], or -1
     float c_xsph, contact;
@@ -65,6 +70,39 @@ struct CellPack {
 __device__ __forceinline__ float dot3(float ax, float ay, float az) {
     return ax * ax + ay * ay + az * az;
 }
+
+// Programmatic dependent launch: a step kernel launched with programmatic
+// stream serialisation may start while its predecessor drains; it waits
+// here, before reading anything the predecessor wrote, until that grid has
+// completed and its writes are visible.  Without the launch attribute this
+// returns at once.
+__device__ __forceinline__ void pdl_wait() {
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 900
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+#endif
+}
+
+// Launch with programmatic stream serialisation allowed (when pdl is set).
+template <typename... KArgs, typename... Args>
+inline void launch_k(void (*kernel)(KArgs...), int grid, int block, cudaStream_t st, bool pdl,
+                     Args&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = pdl ? 1 : 0;
+    cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+
+// Whether the launchers of the calling thread use programmatic dependent
+// launch (set by the context around a step's launches).
+void set_pdl(bool on);
+bool pdl_enabled();
 
 __device__ __forceinline__ void set_status(int* status, int bit) {
     if ((*(volatile int*)status & bit) == 0) atomicOr(status, bit);

@@ -109,6 +109,7 @@ static int derive(const lustrine_pbf_params& q, int n, int ns, StepParams* sp, C
     }
     const double h = (double)q.kernel_radius;
     p.k6 = (float)(315.0 / (64.0 * kPi * std::pow(h, 9)));
+    p.self_density = (float)((double)q.mass * 315.0 / (64.0 * kPi * std::pow(h, 9)) * std::pow(h, 6));
     p.ks = (float)(45.0 / (kPi * std::pow(h, 6)));
     {
         double d = h * h - (double)q.s_corr_dq * (double)q.s_corr_dq;
@@ -117,6 +118,7 @@ static int derive(const lustrine_pbf_params& q, int n, int ns, StepParams* sp, C
     }
     p.mass = q.mass;
     p.rho0 = q.rest_density;
+    p.mr = q.mass / q.rest_density;
     p.eps = q.relaxation_epsilon;
     p.dq = q.s_corr_dq;
     p.sk = q.s_corr_k;
@@ -218,6 +220,8 @@ static int ctx_alloc(lustrine_pbf* s) {
     CK(cudaMemsetAsync(s->cnt, 0, (size_t)(n ? n : 1) * sizeof(int), s->stream));
     CK(cudaMemsetAsync(s->status, 0, 4 * sizeof(int), s->stream));
     CK(cudaMemsetAsync(s->sstart, 0, ((size_t)C + 1) * sizeof(int), s->stream));
+    CK(cudaMemsetAsync(s->count, 0, (size_t)C * sizeof(int), s->stream));
+    s->use_pdl = getenv("LUSTRINE_NO_PDL") == nullptr;
     return LUSTRINE_OK;
 }
 
@@ -404,7 +408,9 @@ static int enqueue_step(lustrine_pbf* s, cudaStream_t st, StageMarks* mk = nullp
     const bool mixed = s->mixed();
     int k = 0;
     if (mk) mk->mark(-1, st);
-    cudaMemsetAsync(s->count, 0, (size_t)C * sizeof(int), st);
+    // count[] is all zero here: zeroed at allocation and by every scan's
+    // down-sweep.  Step kernels use programmatic dependent launch.
+    set_pdl(s->use_pdl);
     if (s->prm.mode == LUSTRINE_MODE_REFERENCE)
         launch_predict_ref(p, s->x[c], s->v[c], s->xs[c], s->key, s->rank, s->count, s->status, st);
     else
@@ -459,6 +465,7 @@ static int enqueue_step(lustrine_pbf* s, cudaStream_t st, StageMarks* mk = nullp
         k += 1;
         if (mk) mk->mark(LUSTRINE_STAGE_XSPH, st);
     }
+    set_pdl(false);
     return k;
 }
 
@@ -482,6 +489,7 @@ extern "C" int lustrine_pbf_step(lustrine_pbf* s, float dt) {
     }
     if (s->sp.dt != dt) {
         s->sp.dt = dt;
+        s->sp.inv_dt = 1.0f / dt;
         s->invalidate_graphs();
     }
     const int c = s->cur;
@@ -524,6 +532,7 @@ extern "C" int lustrine_pbf_profile_step(lustrine_pbf* s, float dt, double* stag
     }
     if (s->sp.dt != dt) {
         s->sp.dt = dt;
+        s->sp.inv_dt = 1.0f / dt;
         s->invalidate_graphs();
     }
     StageMarks mk;
@@ -762,18 +771,22 @@ extern "C" int lustrine_pbf_neighbors(lustrine_pbf* s, int* count, int* idx, int
     if (s->ns) CK(cudaMemcpyAsync(sid.data(), s->solid_id, (size_t)s->ns * sizeof(int), cudaMemcpyDeviceToHost, s->stream));
     CK(cudaStreamSynchronize(s->stream));
     int rc = LUSTRINE_OK;
+    const bool ref = s->prm.mode == LUSTRINE_MODE_REFERENCE;
     for (int k = 0; k < n; k++) {
         const int i = ids[(size_t)k];
         const int c = cnt[(size_t)k];
-        count[i] = c;
+        // PBF lists leave the particle itself out; it is reported first
+        const int self = ref ? 0 : 1;
+        count[i] = c + self;
         if (!idx) continue;
-        if (c > cap) rc = LUSTRINE_ERR_NBR_OVERFLOW;
-        for (int e = 0; e < c && e < cap; e++) {
+        if (c + self > cap) rc = LUSTRINE_ERR_NBR_OVERFLOW;
+        if (self) idx[(size_t)i * cap] = i;
+        for (int e = 0; e < c && e + self < cap; e++) {
             int j = nbr[(size_t)e * n + k];
-            if (s->prm.mode == LUSTRINE_MODE_REFERENCE)
+            if (ref)
                 idx[(size_t)i * cap + e] = j >= 0 ? ids[(size_t)j] : n + sid[(size_t)(-1 - j)];
             else  // PBF entry: slot in bits 0-25, solid flag in bit 31
-                idx[(size_t)i * cap + e] = j >= 0 ? ids[(size_t)(j & 0x3FFFFFF)] : n + sid[(size_t)(j & 0x3FFFFFF)];
+                idx[(size_t)i * cap + e + 1] = j >= 0 ? ids[(size_t)(j & 0x3FFFFFF)] : n + sid[(size_t)(j & 0x3FFFFFF)];
         }
     }
     return rc;

@@ -60,6 +60,7 @@ struct lustrine_pbf {
     int launches = 0;
     long long steps_done = 0;
     bool have_state = false;
+    bool use_pdl = true;  // programmatic dependent launch between step kernels
     bool lists_valid = false;
 
     ~lustrine_pbf();

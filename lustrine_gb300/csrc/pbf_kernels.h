@@ -8,7 +8,8 @@
 namespace lgb {
 
 // pbf_sort.cu
-void launch_scan(const int* count, int C, int* block_sums, int* start, cudaStream_t st);
+// exclusive scan count -> start (C + 1 entries); zeroes count behind it
+void launch_scan(int* count, int C, int* block_sums, int* start, cudaStream_t st);
 int scan_block_sums_size(int C);
 void launch_sort_tail(const int* key, const int* rank, const int* start, const int* tie, int n,
                       int* tmp, int* perm, cudaStream_t st);

@@ -94,10 +94,21 @@ __device__ __forceinline__ float poly6(const StepParams& p, float r2) {
     return r2 <= p.h2 ? p.k6 * d * d * d : 0.0f;
 }
 
+// Distance terms of a pair from r^2: r and 1/r from one reciprocal square
+// root (the PBF kernels are issue-bound; an IEEE sqrt and divide per pair
+// cost more than the rest of the pair's arithmetic).
+struct PairR {
+    float r, inv_r;
+};
+__device__ __forceinline__ PairR pair_r(float r2) {
+    const float inv_r = r2 > 0.0f ? rsqrtf(r2) : 0.0f;
+    return PairR{r2 * inv_r, inv_r};
+}
+
 // spiky gradient as a factor on the offset: dW(d) = f * d
-__device__ __forceinline__ float spiky_factor(const StepParams& p, float r) {
-    float f = p.h - r;
-    return (r > 0.0f && r <= p.h) ? -p.ks * f * f / r : 0.0f;
+__device__ __forceinline__ float spiky_factor(const StepParams& p, PairR q) {
+    const float f = p.h - q.r;
+    return (q.inv_r > 0.0f && q.r <= p.h) ? -p.ks * f * f * q.inv_r : 0.0f;
 }
 
 __device__ __forceinline__ float scorr(const StepParams& p, float r2) {
@@ -155,6 +166,7 @@ template <bool MIXED>
 __global__ void k_predict(StepParams p, CellPack cp, const float4* __restrict__ x,
                           float4* __restrict__ v, float4* __restrict__ xs, int* __restrict__ key,
                           int* __restrict__ rank, int* __restrict__ count) {
+    pdl_wait();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
     float4 vi = v[i];
@@ -197,14 +209,19 @@ __global__ void k_key(StepParams p, CellPack cp, const float4* __restrict__ pos,
 
 // Neighbour search fused with the first lambda pass: walks the 27 cells
 // around the particle's cell, writes the list and accumulates the density
-// constraint over the accepted neighbours.
+// constraint over the accepted neighbours.  The particle itself is not in
+// its list: its density term m W(0) starts the sum and it has no gradient.
 struct LambdaAcc {
     float density, comp, S, gx, gy, gz;
 };
 
+__device__ __forceinline__ LambdaAcc lambda_init(const StepParams& p) {
+    return LambdaAcc{p.self_density, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+}
+
 template <bool MIXED>
 __device__ __forceinline__ void lambda_accumulate(const StepParams& p, LambdaAcc& a, float3 d,
-                                                  bool self, bool solid) {
+                                                  bool solid) {
     const float r2 = dot3(d.x, d.y, d.z);
     const float w = p.mass * poly6(p, r2);
     if (MIXED) {
@@ -215,8 +232,7 @@ __device__ __forceinline__ void lambda_accumulate(const StepParams& p, LambdaAcc
     } else {
         a.density += w;
     }
-    if (self) return;
-    const float f = spiky_factor(p, sqrtf(r2)) * (p.mass / p.rho0);
+    const float f = spiky_factor(p, pair_r(r2)) * p.mr;
     const float ax = f * d.x, ay = f * d.y, az = f * d.z;
     if (!solid) a.S += dot3(ax, ay, az);
     a.gx += ax;
@@ -250,6 +266,7 @@ __device__ __forceinline__ void walk_row(const StepParams& p, const float4& self
         const int code = (dx + 1) + 3 * (dz + 1) + 9 * (dy + 1);
         const float sz = -(float)dz * p.cell;
         for (int t = b[k]; t < b[k + 1]; t++) {
+            if (!SOLID && t == s) continue;
             const float4 q = SOLID ? __ldg(&pos[t]) : pos[t];
             float3 d = make_float3(self.x - q.x, self.y - q.y, self.z - q.z);
             if (MIXED) {
@@ -260,7 +277,7 @@ __device__ __forceinline__ void walk_row(const StepParams& p, const float4& self
             if (dot3(d.x, d.y, d.z) <= p.h2) {
                 if (c_n < p.max_nbrs) nbr[(size_t)c_n * p.n + s] = entry(t, code, SOLID);
                 c_n++;
-                lambda_accumulate<MIXED>(p, a, d, !SOLID && t == s, SOLID);
+                lambda_accumulate<MIXED>(p, a, d, SOLID);
             }
         }
     }
@@ -274,11 +291,12 @@ __global__ void __launch_bounds__(B) k_lists_lambda(StepParams p, float4* __rest
                                                     const int* __restrict__ sstart,
                                                     int* __restrict__ nbr, int* __restrict__ cnt,
                                                     float* __restrict__ rho, int* status) {
+    pdl_wait();
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= p.n) return;
     const float4 self = xs[s];
     const int3 c = decode_cell(p, key_sorted[s]);
-    LambdaAcc a = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    LambdaAcc a = lambda_init(p);
     int c_n = 0;
     const int slab = p.gx * p.gz;
     for (int dy = -1; dy <= 1; dy++) {
@@ -309,23 +327,25 @@ __global__ void __launch_bounds__(B) k_lambda(StepParams p, float4* __restrict__
                                               const int* __restrict__ nbr, const int* __restrict__ cnt,
                                               const float4* __restrict__ solid,
                                               float* __restrict__ rho) {
+    pdl_wait();
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= p.n) return;
     const float4 self = xs[s];
     const int c = cnt[s];
-    LambdaAcc a = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    const int* __restrict__ col = nbr + s;
+    LambdaAcc a = lambda_init(p);
     for (int k = 0; k < c; k += U) {
         int e[U];
         float4 q[U];
 #pragma unroll
-        for (int u = 0; u < U; u++) e[u] = k + u < c ? __ldg(&nbr[(size_t)(k + u) * p.n + s]) : s;
+        for (int u = 0; u < U; u++) e[u] = k + u < c ? __ldg(&col[(size_t)(k + u) * p.n]) : s;
 #pragma unroll
         for (int u = 0; u < U; u++) q[u] = load_entry(e[u], xs, solid);
 #pragma unroll
         for (int u = 0; u < U; u++) {
             if (k + u >= c) break;
             float3 d = rel_e<MIXED>(p, self, q[u], e[u]);
-            lambda_accumulate<MIXED>(p, a, d, entry_is(e[u], s), entry_solid(e[u]));
+            lambda_accumulate<MIXED>(p, a, d, entry_solid(e[u]));
         }
     }
     reinterpret_cast<float*>(xs)[4 * (size_t)s + 3] = lambda_of(p, a);
@@ -341,11 +361,13 @@ __global__ void __launch_bounds__(B) k_delta(StepParams p, CellPack cp, const fl
                                                const float4* __restrict__ solid,
                                                const int* __restrict__ key_sorted,
                                                const float4* __restrict__ x, float4* __restrict__ v_out) {
+    pdl_wait();
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= p.n) return;
     const float4 self = xs[s];
     const float li = self.w;
     const int c = cnt[s];
+    const int* __restrict__ col = nbr + s;
     float px = 0.0f, py = 0.0f, pz = 0.0f;
     float cx = 0.0f, cy = 0.0f, cz = 0.0f;
     int nct = 0;
@@ -353,24 +375,23 @@ __global__ void __launch_bounds__(B) k_delta(StepParams p, CellPack cp, const fl
         int e[U];
         float4 q[U];
 #pragma unroll
-        for (int u = 0; u < U; u++) e[u] = k + u < c ? __ldg(&nbr[(size_t)(k + u) * p.n + s]) : s;
+        for (int u = 0; u < U; u++) e[u] = k + u < c ? __ldg(&col[(size_t)(k + u) * p.n]) : s;
 #pragma unroll
         for (int u = 0; u < U; u++) q[u] = load_entry(e[u], xs, solid);
 #pragma unroll
         for (int u = 0; u < U; u++) {
             if (k + u >= c) break;
-            if (entry_is(e[u], s)) continue;
             const bool sol = entry_solid(e[u]);
             float3 d = rel_e<MIXED>(p, self, q[u], e[u]);
             const float r2 = dot3(d.x, d.y, d.z);
-            const float r = sqrtf(r2);
+            const PairR pr = pair_r(r2);
             const float lj = sol ? li : q[u].w;
-            const float w = (li + lj + scorr(p, r2)) * spiky_factor(p, r);
+            const float w = (li + lj + scorr(p, r2)) * spiky_factor(p, pr);
             px += w * d.x;
             py += w * d.y;
             pz += w * d.z;
-            if (sol && r < p.contact && r > 0.0f) {
-                const float t = (p.contact - r) / r;
+            if (sol && pr.r < p.contact && pr.inv_r > 0.0f) {
+                const float t = (p.contact - pr.r) * pr.inv_r;
                 cx += t * d.x;
                 cy += t * d.y;
                 cz += t * d.z;
@@ -378,10 +399,9 @@ __global__ void __launch_bounds__(B) k_delta(StepParams p, CellPack cp, const fl
             }
         }
     }
-    const float mr = p.mass / p.rho0;
-    float dx = px * mr, dy = py * mr, dz = pz * mr;
+    float dx = px * p.mr, dy = py * p.mr, dz = pz * p.mr;
     if (nct) {
-        const float inv = 1.0f / (float)nct;
+        const float inv = __frcp_rn((float)nct);
         dx += cx * inv;
         dy += cy * inv;
         dz += cz * inv;
@@ -407,8 +427,7 @@ __global__ void __launch_bounds__(B) k_delta(StepParams p, CellPack cp, const fl
             d.y += (float)(cs.y - co.y) * p.cell;
             d.z += (float)(cs.z - co.z) * p.cell;
         }
-        const float inv_dt = 1.0f / p.dt;
-        v_out[s] = make_float4(d.x * inv_dt, d.y * inv_dt, d.z * inv_dt, 0.0f);
+        v_out[s] = make_float4(d.x * p.inv_dt, d.y * p.inv_dt, d.z * p.inv_dt, 0.0f);
     }
 }
 
@@ -419,11 +438,13 @@ __global__ void __launch_bounds__(B) k_xsph(StepParams p, CellPack cp, const flo
                                             const int* __restrict__ nbr, const int* __restrict__ cnt,
                                             const int* __restrict__ key_sorted,
                                             float4* __restrict__ x_out, float4* __restrict__ v_out) {
+    pdl_wait();
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= p.n) return;
     const float4 self = xs[s];
     const float4 vi = v_in[s];
     const int c = cnt[s];
+    const int* __restrict__ col = nbr + s;
     float ax = 0.0f, ay = 0.0f, az = 0.0f;
     if (p.c_xsph != 0.0f) {
         for (int k = 0; k < c; k += U) {
@@ -431,8 +452,8 @@ __global__ void __launch_bounds__(B) k_xsph(StepParams p, CellPack cp, const flo
             float4 q[U], vj[U];
 #pragma unroll
             for (int u = 0; u < U; u++) {
-                int t = k + u < c ? __ldg(&nbr[(size_t)(k + u) * p.n + s]) : s;
-                e[u] = entry_solid(t) ? s : t;  // solids take no part
+                int t = k + u < c ? __ldg(&col[(size_t)(k + u) * p.n]) : s;
+                e[u] = entry_solid(t) ? s : t;  // solids take no part (skipped as s)
             }
 #pragma unroll
             for (int u = 0; u < U; u++) {
@@ -582,12 +603,14 @@ __global__ void __launch_bounds__(256) k_reduce(StepParams p, CellPack cp, const
 
 static inline int blocks_for(int n, int t) { return (n + t - 1) / t; }
 
+// Step kernels go through launch_k (programmatic dependent launch when the
+// calling context enables it); the others are launched plainly.
 #define LGB_DISPATCH(MIXED_FLAG, KERNEL, GRID, BLOCK, ST, ...)                        \
     do {                                                                              \
         if (MIXED_FLAG)                                                               \
-            KERNEL<true><<<GRID, BLOCK, 0, ST>>>(__VA_ARGS__);                        \
+            launch_k(KERNEL<true>, GRID, BLOCK, ST, pdl_enabled(), __VA_ARGS__);      \
         else                                                                          \
-            KERNEL<false><<<GRID, BLOCK, 0, ST>>>(__VA_ARGS__);                       \
+            launch_k(KERNEL<false>, GRID, BLOCK, ST, pdl_enabled(), __VA_ARGS__);     \
     } while (0)
 
 void launch_predict(bool mixed, const StepParams& p, const CellPack& cp, const float4* x, float4* v,
@@ -605,7 +628,7 @@ void launch_key(bool mixed, const StepParams& p, const CellPack& cp, const float
 // Kernels templated on (MIXED, U, B) are instantiated for U in {1, 2, 4} and
 // B in {64, 128, 256}; the tuning picks one (TUNE_CASE expands the switch).
 #define TUNE_LAUNCH(KERNEL, MIX, U_, B_, N, ST, ...)                                            \
-    KERNEL<MIX, U_, B_><<<blocks_for(N, B_), B_, 0, ST>>>(__VA_ARGS__)
+    launch_k(KERNEL<MIX, U_, B_>, blocks_for(N, B_), B_, ST, pdl_enabled(), __VA_ARGS__)
 #define TUNE_BLOCKS(KERNEL, MIX, U_, tu, N, ST, ...)                                            \
     do {                                                                                        \
         if (tu.block <= 64)                                                                     \
@@ -638,15 +661,20 @@ void launch_lists_lambda(bool mixed, const Tuning& tu, const StepParams& p, floa
                          cudaStream_t st) {
     if (p.n <= 0) return;
     const int B = tu.list_block <= 64 ? 64 : (tu.list_block <= 128 ? 128 : 256);
+    const bool pdl = pdl_enabled();
+#define LGB_LISTS(MIX, BB)                                                                      \
+    launch_k(k_lists_lambda<MIX, BB>, blocks_for(p.n, BB), BB, st, pdl, p, xs, key_sorted, fstart, \
+             solid, sstart, nbr, cnt, rho, status)
     if (mixed) {
-        if (B == 64) k_lists_lambda<true, 64><<<blocks_for(p.n, 64), 64, 0, st>>>(p, xs, key_sorted, fstart, solid, sstart, nbr, cnt, rho, status);
-        else if (B == 128) k_lists_lambda<true, 128><<<blocks_for(p.n, 128), 128, 0, st>>>(p, xs, key_sorted, fstart, solid, sstart, nbr, cnt, rho, status);
-        else k_lists_lambda<true, 256><<<blocks_for(p.n, 256), 256, 0, st>>>(p, xs, key_sorted, fstart, solid, sstart, nbr, cnt, rho, status);
+        if (B == 64) LGB_LISTS(true, 64);
+        else if (B == 128) LGB_LISTS(true, 128);
+        else LGB_LISTS(true, 256);
     } else {
-        if (B == 64) k_lists_lambda<false, 64><<<blocks_for(p.n, 64), 64, 0, st>>>(p, xs, key_sorted, fstart, solid, sstart, nbr, cnt, rho, status);
-        else if (B == 128) k_lists_lambda<false, 128><<<blocks_for(p.n, 128), 128, 0, st>>>(p, xs, key_sorted, fstart, solid, sstart, nbr, cnt, rho, status);
-        else k_lists_lambda<false, 256><<<blocks_for(p.n, 256), 256, 0, st>>>(p, xs, key_sorted, fstart, solid, sstart, nbr, cnt, rho, status);
+        if (B == 64) LGB_LISTS(false, 64);
+        else if (B == 128) LGB_LISTS(false, 128);
+        else LGB_LISTS(false, 256);
     }
+#undef LGB_LISTS
 }
 
 void launch_lambda(bool mixed, const Tuning& tu, const StepParams& p, float4* xs, const int* nbr,

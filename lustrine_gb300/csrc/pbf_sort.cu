@@ -5,18 +5,25 @@
 // scatter.  The GPU form:
 //   1. histogram: the prediction kernel does atomicAdd(count[key]) and keeps
 //      the returned value as the particle's provisional rank in its cell;
-//   2. exclusive scan of count over all cells (reduce, scan block sums,
-//      down-sweep; no inter-block waits);
+//   2. exclusive scan of count over all cells (reduce, scan of the tile
+//      sums, down-sweep; no inter-block waits); the down-sweep also zeroes
+//      count for the next step's histogram;
 //   3. scatter of particle indices to start[key] + rank;
 //   4. stabilisation: atomic arrival order is arbitrary, so each slot counts
 //      the members of its cell with a smaller tie key (previous slot, or the
 //      caller's id in compat mode) and moves to that rank -- the result is
-//      the stable order of the reference's counting sort;
-//   5. one gather of the particle state into the new order.
+//      the stable order of the reference's counting sort -- and the particle
+//      state is gathered into that slot in the same kernel.
 #include "pbf_common.cuh"
 #include "pbf_kernels.h"
 
 namespace lgb {
+
+namespace {
+thread_local bool t_pdl = false;
+}
+void set_pdl(bool on) { t_pdl = on; }
+bool pdl_enabled() { return t_pdl; }
 
 constexpr int SCAN_THREADS = 256;
 constexpr int SCAN_ITEMS = 8;
@@ -57,6 +64,7 @@ __device__ __forceinline__ int block_exclusive_scan(int v, int* total) {
 
 __global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(const int* __restrict__ count, int C,
                                                               int* __restrict__ block_sums) {
+    pdl_wait();
     const int base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_ITEMS;
     int s = 0;
 #pragma unroll
@@ -68,10 +76,11 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(const int* __restr
 }
 
 // One block: exclusive scan of the per-tile sums, in place; 8 sums per
-// thread, so up to 8192 tiles (33.5 M cells) take one pass.
+// thread, so up to 8192 tiles (16.7 M cells) take one pass.
 constexpr int SUMS_THREADS = 1024;
 constexpr int SUMS_ITEMS = 8;
 __global__ void __launch_bounds__(SUMS_THREADS) k_scan_sums(int* __restrict__ block_sums, int nb) {
+    pdl_wait();
     int carry = 0;
     for (int base = 0; base < nb; base += SUMS_THREADS * SUMS_ITEMS) {
         const int first = base + threadIdx.x * SUMS_ITEMS;
@@ -93,9 +102,12 @@ __global__ void __launch_bounds__(SUMS_THREADS) k_scan_sums(int* __restrict__ bl
     }
 }
 
-__global__ void __launch_bounds__(SCAN_THREADS) k_scan_down(const int* __restrict__ count, int C,
+// Down-sweep: start[c] = exclusive prefix of count; count is zeroed behind
+// it, ready for the next histogram.
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_down(int* __restrict__ count, int C,
                                                             const int* __restrict__ block_sums,
                                                             int* __restrict__ start) {
+    pdl_wait();
     const int base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_ITEMS;
     int vals[SCAN_ITEMS];
     int s = 0;
@@ -108,7 +120,10 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_down(const int* __restric
     int ex = block_exclusive_scan<SCAN_THREADS>(s, &total) + block_sums[blockIdx.x];
 #pragma unroll
     for (int k = 0; k < SCAN_ITEMS; k++) {
-        if (base + k < C) start[base + k] = ex;
+        if (base + k < C) {
+            start[base + k] = ex;
+            if (vals[k]) count[base + k] = 0;
+        }
         ex += vals[k];
     }
     if (blockIdx.x == gridDim.x - 1 && threadIdx.x == SCAN_THREADS - 1) start[C] = ex;
@@ -116,6 +131,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_down(const int* __restric
 
 __global__ void k_scatter_index(const int* __restrict__ key, const int* __restrict__ rank,
                                 const int* __restrict__ start, int n, int* __restrict__ tmp) {
+    pdl_wait();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) tmp[start[key[i]] + rank[i]] = i;
 }
@@ -147,6 +163,7 @@ __global__ void k_stabilize_gather(const int* __restrict__ tmp, const int* __res
                                    int* __restrict__ key_out, float4* __restrict__ x_out,
                                    float4* __restrict__ xs_out, float4* __restrict__ v_out,
                                    int* __restrict__ id_out) {
+    pdl_wait();
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
     const int i = tmp[s];
@@ -167,22 +184,6 @@ __global__ void k_stabilize_gather(const int* __restrict__ tmp, const int* __res
     id_out[f] = id[i];
 }
 
-__global__ void k_gather_state(const int* __restrict__ perm, int n, const int* __restrict__ key,
-                               const float4* __restrict__ x, const float4* __restrict__ xs,
-                               const float4* __restrict__ v, const int* __restrict__ id,
-                               int* __restrict__ key_out, float4* __restrict__ x_out,
-                               float4* __restrict__ xs_out, float4* __restrict__ v_out,
-                               int* __restrict__ id_out) {
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= n) return;
-    const int i = perm[s];
-    key_out[s] = key[i];
-    x_out[s] = x[i];
-    xs_out[s] = xs[i];
-    v_out[s] = v[i];
-    id_out[s] = id[i];
-}
-
 __global__ void k_gather_solid(const int* __restrict__ perm, int n, const float4* __restrict__ src,
                                float4* __restrict__ dst) {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -193,11 +194,12 @@ __global__ void k_gather_solid(const int* __restrict__ perm, int n, const float4
 
 static inline int blocks_for(int n, int t) { return (n + t - 1) / t; }
 
-void launch_scan(const int* count, int C, int* block_sums, int* start, cudaStream_t st) {
-    int nb = blocks_for(C, SCAN_TILE);
-    k_scan_reduce<<<nb, SCAN_THREADS, 0, st>>>(count, C, block_sums);
-    k_scan_sums<<<1, SUMS_THREADS, 0, st>>>(block_sums, nb);
-    k_scan_down<<<nb, SCAN_THREADS, 0, st>>>(count, C, block_sums, start);
+void launch_scan(int* count, int C, int* block_sums, int* start, cudaStream_t st) {
+    const int nb = blocks_for(C, SCAN_TILE);
+    const bool pdl = pdl_enabled();
+    launch_k(k_scan_reduce, nb, SCAN_THREADS, st, pdl, (const int*)count, C, block_sums);
+    launch_k(k_scan_sums, 1, SUMS_THREADS, st, pdl, block_sums, nb);
+    launch_k(k_scan_down, nb, SCAN_THREADS, st, pdl, count, C, (const int*)block_sums, start);
 }
 
 int scan_block_sums_size(int C) { return blocks_for(C, SCAN_TILE) + 1; }
@@ -209,22 +211,15 @@ void launch_sort_tail(const int* key, const int* rank, const int* start, const i
     k_stabilize<<<blocks_for(n, 256), 256, 0, st>>>(tmp, key, start, tie, n, perm);
 }
 
-void launch_gather_state(const int* perm, int n, const int* key, const float4* x, const float4* xs,
-                         const float4* v, const int* id, int* key_out, float4* x_out,
-                         float4* xs_out, float4* v_out, int* id_out, cudaStream_t st) {
-    if (n <= 0) return;
-    k_gather_state<<<blocks_for(n, 256), 256, 0, st>>>(perm, n, key, x, xs, v, id, key_out, x_out,
-                                                       xs_out, v_out, id_out);
-}
-
 void launch_sort_state(const int* key, const int* rank, const int* start, const int* tie, int n,
                        int* tmp, const float4* x, const float4* xs, const float4* v, const int* id,
                        int* key_out, float4* x_out, float4* xs_out, float4* v_out, int* id_out,
                        cudaStream_t st) {
     if (n <= 0) return;
-    k_scatter_index<<<blocks_for(n, 256), 256, 0, st>>>(key, rank, start, n, tmp);
-    k_stabilize_gather<<<blocks_for(n, 256), 256, 0, st>>>(tmp, key, start, tie, n, x, xs, v, id, key_out,
-                                                           x_out, xs_out, v_out, id_out);
+    const bool pdl = pdl_enabled();
+    launch_k(k_scatter_index, blocks_for(n, 256), 256, st, pdl, key, rank, start, n, tmp);
+    launch_k(k_stabilize_gather, blocks_for(n, 256), 256, st, pdl, (const int*)tmp, key, start, tie, n,
+             x, xs, v, id, key_out, x_out, xs_out, v_out, id_out);
 }
 
 void launch_gather_solid(const int* perm, int n, const float4* src, float4* dst, cudaStream_t st) {
