@@ -257,6 +257,18 @@ LUSTRINE_API int lustrine_pbf_autotune(lustrine_pbf* s, float dt, int steps, lus
 /* Kernel launches one step issues (for launch accounting). */
 LUSTRINE_API int lustrine_pbf_launches_per_step(const lustrine_pbf* s);
 
+/* Sorting::counting_sort (src/neighbors/Sorting.cpp:12-34, declared in
+ * src/neighbors/Sorting.hpp:12-18) on device arrays: a stable sort of
+ * keys[0..num_positions) in [0, num_cells).  sorted_indices receives the
+ * input index of the k-th smallest key (equal keys in input order) and
+ * counts (num_cells + 1 ints) the state the reference leaves in its counts
+ * array: the first output position of every key, then num_positions.  The
+ * extra scratch is taken with cudaMallocAsync on `stream` (a cudaStream_t,
+ * NULL for the default stream) and returned before the call ends; the call
+ * synchronises the stream.  LUSTRINE_ERR_ARGS if a key is out of range. */
+LUSTRINE_API int lustrine_counting_sort(int* counts, const int* keys, size_t num_positions,
+                                        size_t num_cells, int* sorted_indices, void* stream);
+
 LUSTRINE_API const char* lustrine_error_string(int code);
 
 #ifdef __cplusplus

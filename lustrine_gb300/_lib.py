@@ -128,6 +128,7 @@ SIGNATURES = {
     "lustrine_pbf_set_tuning": (C.c_int, [_P, C.POINTER(PbfTuning)]),
     "lustrine_pbf_get_tuning": (C.c_int, [_P, C.POINTER(PbfTuning)]),
     "lustrine_pbf_autotune": (C.c_int, [_P, C.c_float, C.c_int, C.POINTER(PbfTuning), _FP]),
+    "lustrine_counting_sort": (C.c_int, [_P, _P, C.c_size_t, C.c_size_t, _P, _P]),
     "lustrine_error_string": (C.c_char_p, [C.c_int]),
 }
 

@@ -28,6 +28,7 @@ UNITS = {
     "pbf_compat.cu": ["--fmad=false"],
     "pbf_solver.cu": [],
     "pbf_context.cu": [],
+    "pbf_sort_api.cu": [],
     "lustrine_wrapper.cpp": [],
 }
 

@@ -17,6 +17,22 @@ void launch_gather_state(const int* perm, int n, const int* key, const float4* x
                          const float4* v, const int* id, int* key_out, float4* x_out,
                          float4* xs_out, float4* v_out, int* id_out, cudaStream_t st);
 void launch_gather_solid(const int* perm, int n, const float4* src, float4* dst, cudaStream_t st);
+// Standalone stable counting sort of caller keys (Sorting::counting_sort,
+// src/neighbors/Sorting.cpp:12-34): scratch carved from one int buffer whose
+// count part must be zero on entry (the scan leaves it zero again).
+struct CountingSortScratch {
+    int* count;       // num_cells
+    int* block_sums;  // scan_block_sums_size(num_cells)
+    int* key;         // n (validated keys)
+    int* rank;        // n
+    int* tmp;         // n
+    int* status;      // 1
+};
+size_t counting_sort_scratch_ints(int n, int num_cells);
+CountingSortScratch counting_sort_scratch(int* base, int n, int num_cells);
+// start: num_cells + 1 exclusive offsets; sorted: n input indices in stable key order
+void launch_counting_sort(const int* keys, int n, int num_cells, CountingSortScratch w, int* start,
+                          int* sorted, cudaStream_t st);
 // index scatter + stabilisation fused with the reorder of the particle state
 void launch_sort_state(const int* key, const int* rank, const int* start, const int* tie, int n,
                        int* tmp, const float4* x, const float4* xs, const float4* v, const int* id,

@@ -190,6 +190,22 @@ __global__ void k_gather_solid(const int* __restrict__ perm, int n, const float4
     if (s < n) dst[s] = src[perm[s]];
 }
 
+// Histogram of caller keys (standalone counting sort).  A key outside
+// [0, num_cells) is recorded in *status and counted in cell 0 so that every
+// access stays in bounds.
+__global__ void k_key_hist(const int* __restrict__ keys, int n, int num_cells, int* __restrict__ key_out,
+                           int* __restrict__ rank, int* __restrict__ count, int* status) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int k = keys[i];
+    if (k < 0 || k >= num_cells) {
+        set_status(status, ST_BAD_VALUE);
+        k = 0;
+    }
+    key_out[i] = k;
+    rank[i] = atomicAdd(&count[k], 1);
+}
+
 // ------------------------------------------------------------------ launch --
 
 static inline int blocks_for(int n, int t) { return (n + t - 1) / t; }
@@ -225,6 +241,30 @@ void launch_sort_state(const int* key, const int* rank, const int* start, const 
 void launch_gather_solid(const int* perm, int n, const float4* src, float4* dst, cudaStream_t st) {
     if (n <= 0) return;
     k_gather_solid<<<blocks_for(n, 256), 256, 0, st>>>(perm, n, src, dst);
+}
+
+void launch_counting_sort(const int* keys, int n, int num_cells, CountingSortScratch w, int* start,
+                          int* sorted, cudaStream_t st) {
+    if (n > 0)
+        k_key_hist<<<blocks_for(n, 256), 256, 0, st>>>(keys, n, num_cells, w.key, w.rank, w.count, w.status);
+    launch_scan(w.count, num_cells, w.block_sums, start, st);
+    launch_sort_tail(w.key, w.rank, start, nullptr, n, w.tmp, sorted, st);
+}
+
+size_t counting_sort_scratch_ints(int n, int num_cells) {
+    // count[num_cells], block sums, key[n], rank[n], tmp[n], status
+    return (size_t)num_cells + (size_t)scan_block_sums_size(num_cells) + 3 * (size_t)n + 1;
+}
+
+CountingSortScratch counting_sort_scratch(int* base, int n, int num_cells) {
+    CountingSortScratch w;
+    w.count = base;
+    w.block_sums = w.count + num_cells;
+    w.key = w.block_sums + scan_block_sums_size(num_cells);
+    w.rank = w.key + n;
+    w.tmp = w.rank + n;
+    w.status = w.tmp + n;
+    return w;
 }
 
 }  // namespace lgb
