@@ -1,0 +1,150 @@
+// lustrine_gb300_sim.hpp -- the GB300 fluid step behind the reference's C++
+// step hook.
+//
+// The reference steps a Simulation through a function pointer,
+// Simulation::simulate_fun (src/Simulation.hpp:22,137), called by
+// Lustrine::simulate (src/Lustrine.cpp:803); its fluid step is
+// Lustrine::simulate_fluid(Simulation*, float) (src/Simulate.hpp:12).
+// lustrine_gb300::simulate_fluid<Simulation> has that signature:
+//
+//     #include "Lustrine.hpp"
+//     #include "lustrine_gb300_sim.hpp"
+//     sim.simulate_fun = lustrine_gb300::simulate_fluid<Lustrine::Simulation>;
+//     Lustrine::simulate(&sim, dt);      // now steps on the GPU
+//
+// It reads and writes the Simulation fields the reference step uses, with
+// the reference's layout (glm::vec3 arrays of 3 floats, sand in
+// [ptr_sand_start, ptr_sand_end), solids in [ptr_solid_start, ptr_solid_end),
+// Simulation.hpp:173-208) and its parameters (Simulation.hpp:144-171).  The
+// header needs only those field names, so it compiles against the
+// reference's Simulation or any struct with the same fields.
+//
+// Each call uploads positions and velocities of the sand range, runs one
+// reference-semantics step (Jacobi position update) on the GPU and writes
+// positions, positions_star, velocities and lambdas back.  The device
+// context of a Simulation is created on its first call (solids are uploaded
+// then: they are static in the fluid step) and kept until
+// lustrine_gb300::release(sim).  Errors are reported by last_status(), the
+// step itself returning void like the reference's.
+#pragma once
+
+#include <cstring>
+#include <mutex>
+#include <unordered_map>
+#include <vector>
+
+#include "lustrine_gb300.h"
+
+namespace lustrine_gb300 {
+
+namespace detail {
+struct Entry {
+    lustrine_pbf* ctx = nullptr;
+    int n = 0, ns = 0;
+};
+inline std::unordered_map<const void*, Entry>& table() {
+    static std::unordered_map<const void*, Entry> t;
+    return t;
+}
+inline std::mutex& table_mutex() {
+    static std::mutex m;
+    return m;
+}
+inline int& status() {
+    static thread_local int s = LUSTRINE_OK;
+    return s;
+}
+
+template <class Simulation>
+lustrine_pbf_params params_of(const Simulation* sim) {
+    lustrine_pbf_params p;
+    lustrine_pbf_params_reference(&p, (int)sim->domainX, (int)sim->domainY, (int)sim->domainZ,
+                                  sim->particleRadius, sim->kernelRadius / sim->particleRadius);
+    p.kernel_radius = sim->kernelRadius;
+    p.kernel_factor = sim->kernelFactor;
+    p.cell_size = sim->cell_size;
+    p.rest_density = sim->rest_density;
+    p.mass = sim->mass;
+    p.gravity[0] = sim->gravity.x;
+    p.gravity[1] = sim->gravity.y;
+    p.gravity[2] = sim->gravity.z;
+    p.relaxation_epsilon = sim->relaxation_epsilon;
+    p.s_corr_dq = sim->s_corr_dq;
+    p.s_corr_k = sim->s_corr_k;
+    p.s_corr_n = sim->s_corr_n;
+    p.mode = LUSTRINE_MODE_REFERENCE;
+    return p;
+}
+}  // namespace detail
+
+// Outcome of the last simulate_fluid call on this thread.
+inline int last_status() { return detail::status(); }
+
+// Free the device context of a Simulation (call before its arrays go away).
+template <class Simulation>
+void release(const Simulation* sim) {
+    std::lock_guard<std::mutex> lock(detail::table_mutex());
+    auto it = detail::table().find(sim);
+    if (it != detail::table().end()) {
+        lustrine_pbf_destroy(it->second.ctx);
+        detail::table().erase(it);
+    }
+}
+
+template <class Simulation>
+void simulate_fluid(Simulation* sim, float dt) {
+    const int start = sim->ptr_sand_start, end = sim->ptr_sand_end;
+    const int n = end > start ? end - start : 0;
+    const int ns = sim->ptr_solid_end > sim->ptr_solid_start ? sim->ptr_solid_end - sim->ptr_solid_start : 0;
+    detail::Entry e;
+    {
+        std::lock_guard<std::mutex> lock(detail::table_mutex());
+        e = detail::table()[sim];
+    }
+    const lustrine_pbf_params p = detail::params_of(sim);
+    int rc = LUSTRINE_OK;
+    if (e.ctx && (e.n != n || e.ns != ns)) {  // particles were added or removed
+        release(sim);
+        e = detail::Entry{};
+    }
+    float* x = reinterpret_cast<float*>(sim->positions) + 3 * (size_t)start;
+    float* v = reinterpret_cast<float*>(sim->velocities) + 3 * (size_t)start;
+    if (!e.ctx) {
+        rc = lustrine_pbf_create(&p, n, ns, &e.ctx);
+        const float* solid = ns ? reinterpret_cast<const float*>(sim->positions) + 3 * (size_t)sim->ptr_solid_start
+                                : nullptr;
+        if (!rc) rc = lustrine_pbf_upload(e.ctx, x, v, solid);
+        if (rc) {
+            if (e.ctx) lustrine_pbf_destroy(e.ctx);
+            detail::status() = rc;
+            return;
+        }
+        e.n = n;
+        e.ns = ns;
+        std::lock_guard<std::mutex> lock(detail::table_mutex());
+        detail::table()[sim] = e;
+    } else {
+        // the game may change parameters between steps (ImGui sliders do,
+        // experiments/fluid/fluid.cpp:176-189); unchanged ones keep the
+        // captured step graphs
+        lustrine_pbf_params cur;
+        lustrine_pbf_get_params(e.ctx, &cur);
+        cur.use_graph = p.use_graph;
+        cur.max_neighbors = p.max_neighbors;
+        if (std::memcmp(&cur, &p, sizeof(p)) != 0) rc = lustrine_pbf_set_params(e.ctx, &p);
+        if (!rc) rc = lustrine_pbf_upload_state_async(e.ctx, x, v);
+    }
+    if (!rc) rc = lustrine_pbf_step(e.ctx, dt);
+    std::vector<float> lam((size_t)n);
+    if (!rc) rc = lustrine_pbf_download(e.ctx, x, v, n ? lam.data() : nullptr, nullptr);
+    if (!rc) {
+        // Simulate.cpp:31-32,111: time_step holds the clamped dt; x* = x after the step
+        sim->time_step = dt < 0.001f ? 0.001f : (dt > 0.01f ? 0.01f : dt);
+        std::memcpy(reinterpret_cast<float*>(sim->positions_star) + 3 * (size_t)start, x,
+                    sizeof(float) * 3 * (size_t)n);
+        for (int i = 0; i < n && (size_t)(start + i) < sim->lambdas.size(); i++) sim->lambdas[start + i] = lam[i];
+    }
+    detail::status() = rc;
+}
+
+}  // namespace lustrine_gb300
