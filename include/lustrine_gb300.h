@@ -45,7 +45,8 @@ enum {
     LUSTRINE_ERR_UNSUPPORTED = 6,    /* option not provided by this build */
     LUSTRINE_ERR_NO_SIMULATION = 7,  /* wrapper call before init_simulation */
     LUSTRINE_ERR_TIMEOUT = 8,        /* a bounded device wait gave up */
-    LUSTRINE_ERR_BAD_VALUE = 9       /* non-finite particle state */
+    LUSTRINE_ERR_BAD_VALUE = 9,      /* non-finite particle state */
+    LUSTRINE_ERR_TOO_LARGE = 10      /* input larger than a fixed-scratch entry point's limit */
 };
 
 enum {
@@ -268,6 +269,25 @@ LUSTRINE_API int lustrine_pbf_launches_per_step(const lustrine_pbf* s);
  * synchronises the stream.  LUSTRINE_ERR_ARGS if a key is out of range. */
 LUSTRINE_API int lustrine_counting_sort(int* counts, const int* keys, size_t num_positions,
                                         size_t num_cells, int* sorted_indices, void* stream);
+
+/* No counterpart in the reference.  The same sort for callers that cannot
+ * allocate GPU memory while they run (an engine that budgets all device
+ * memory at level load and forbids allocation during a frame, where a
+ * cudaMalloc or cudaFree could synchronise the device; a host whose
+ * allocator policy rejects allocations outside its pool): it takes no memory
+ * and takes its scratch from a fixed array in the library's device image,
+ * LUSTRINE_NOALLOC_SCRATCH_BYTES on every GPU that loads the library, held
+ * until the process exits.  Limits: num_positions <= LUSTRINE_NOALLOC_MAX_KEYS
+ * and num_cells <= LUSTRINE_NOALLOC_MAX_CELLS, else LUSTRINE_ERR_TOO_LARGE.
+ * The first call on a device looks up the array's device address (make it
+ * before any stream capture).  All calls share the array: calls that overlap
+ * on the GPU race.  Same arguments, results and synchronisation as
+ * lustrine_counting_sort. */
+#define LUSTRINE_NOALLOC_MAX_KEYS (1 << 20)
+#define LUSTRINE_NOALLOC_MAX_CELLS (1 << 20)
+#define LUSTRINE_NOALLOC_SCRATCH_BYTES (17u << 20)
+LUSTRINE_API int lustrine_counting_sort_noalloc(int* counts, const int* keys, size_t num_positions,
+                                                size_t num_cells, int* sorted_indices, void* stream);
 
 LUSTRINE_API const char* lustrine_error_string(int code);
 

@@ -22,6 +22,7 @@ ERRORS = {
     7: "LUSTRINE_ERR_NO_SIMULATION",
     8: "LUSTRINE_ERR_TIMEOUT",
     9: "LUSTRINE_ERR_BAD_VALUE",
+    10: "LUSTRINE_ERR_TOO_LARGE",
 }
 MODE_REFERENCE, MODE_PBF = 0, 1
 PRECISION_FP32, PRECISION_MIXED = 0, 1
@@ -129,6 +130,7 @@ SIGNATURES = {
     "lustrine_pbf_get_tuning": (C.c_int, [_P, C.POINTER(PbfTuning)]),
     "lustrine_pbf_autotune": (C.c_int, [_P, C.c_float, C.c_int, C.POINTER(PbfTuning), _FP]),
     "lustrine_counting_sort": (C.c_int, [_P, _P, C.c_size_t, C.c_size_t, _P, _P]),
+    "lustrine_counting_sort_noalloc": (C.c_int, [_P, _P, C.c_size_t, C.c_size_t, _P, _P]),
     "lustrine_error_string": (C.c_char_p, [C.c_int]),
 }
 

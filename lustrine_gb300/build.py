@@ -29,6 +29,7 @@ UNITS = {
     "pbf_solver.cu": [],
     "pbf_context.cu": [],
     "pbf_sort_api.cu": [],
+    "pbf_sort_noalloc.cu": [],
     "lustrine_wrapper.cpp": [],
 }
 

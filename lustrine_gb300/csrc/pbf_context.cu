@@ -842,6 +842,7 @@ extern "C" const char* lustrine_error_string(int code) {
     case LUSTRINE_ERR_NO_SIMULATION: return "no simulation initialised";
     case LUSTRINE_ERR_TIMEOUT: return "device wait timed out";
     case LUSTRINE_ERR_BAD_VALUE: return "non-finite particle state";
+    case LUSTRINE_ERR_TOO_LARGE: return "input exceeds the fixed scratch limit";
     default: return "unknown status";
     }
 }
