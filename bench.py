@@ -370,6 +370,65 @@ def run_variants(args, flush):
                                "launch_shape": sim.tuned["tuning"],
                                "stage_ms": {a: round(b[0], 4) for a, b in prof.items()}}
     sim.close()
+    out["config3_batched_vs_plain"] = run_config3(max(3, min(args.steps, 10)), flush)
+    return out
+
+
+def run_config3(steps, flush):
+    """512 independent scenes (log-uniform 1,024-65,536 particles): the batched
+    step (one launch per stage for all scenes, fp32 and mixed precision)
+    against the plain step applied scene by scene (one context and stream per
+    scene).  Wall-clock time per step of all scenes, device synchronised,
+    L2 flushed before each step; the equal-error condition (batched mixed
+    density within 1e-4 of FP64) is asserted by tests/test_gpu_batch.py."""
+    import torch
+    from lustrine_gb300 import PRECISION_MIXED, PbfSim, pbf_params, scenes, tuning
+    scs = scenes.config3()
+    total = sum(sc.n for sc in scs)
+    dt = scs[0].dt
+    x_all = np.concatenate([sc.x for sc in scs])
+    out = {"scenes": len(scs), "fluid_particles": total, "iterations": 4}
+
+    def wall(step_all):
+        ts = []
+        for _ in range(steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            step_all()
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - t0)
+        return statistics.median(ts)
+
+    for name, prec in (("batched_fp32", 0), ("batched_mixed", PRECISION_MIXED)):
+        b = PbfSim.batch(pbf_params(8, 8, 8, iterations=4, precision=prec), [sc.domain for sc in scs],
+                         [sc.n for sc in scs])
+        b.upload(x_all)
+        b.step(dt, 3)
+        tuned = tuning.tune(b, dt, steps=2, cache=None)
+        b.step(dt, 2)
+        t = wall(lambda: b.step(dt))
+        out[name] = {"value": total * 4 / t, "ms_per_step": t * 1e3, "status": b.status(),
+                     "launch_shape": tuned["tuning"], "launches_per_step": b.launches_per_step()}
+        b.close()
+    sims = []
+    for sc in scs:
+        s = PbfSim(pbf_params(*sc.domain, iterations=4), sc.n)
+        s.upload(sc.x)
+        s.step(dt, 2)
+        sims.append(s)
+
+    def step_each():
+        for s in sims:
+            s.step(dt)
+
+    t = wall(step_each)
+    out["plain_per_scene"] = {"value": total * 4 / t, "ms_per_step": t * 1e3,
+                              "status": max(s.status() for s in sims),
+                              "launches_per_step": sum(s.launches_per_step() for s in sims)}
+    for s in sims:
+        s.close()
+    out["batched_mixed_over_plain"] = out["batched_mixed"]["value"] / out["plain_per_scene"]["value"]
     return out
 
 

@@ -181,6 +181,15 @@ LUSTRINE_API void lustrine_pbf_params_reference(lustrine_pbf_params* p, int X, i
 LUSTRINE_API int lustrine_pbf_create(const lustrine_pbf_params* p, int n_fluid, int n_solid,
                                      lustrine_pbf** out);
 LUSTRINE_API int lustrine_pbf_destroy(lustrine_pbf* s);
+/* A batch of independent scenes stepped together (PBF mode): scene k has the
+ * box domains[3k..3k+2], n_fluid[k] fluid and n_solid[k] solid particles
+ * (n_solid may be NULL: none).  Same physics for all scenes (p; p->domain is
+ * ignored).  The returned context works with every lustrine_pbf_* call;
+ * particle ids run scene after scene (upload and download concatenate the
+ * scenes in order, each in its own box coordinates).  One step advances all
+ * scenes with one launch per stage. */
+LUSTRINE_API int lustrine_batch_create(const lustrine_pbf_params* p, int num_scenes, const int* domains,
+                                       const int* n_fluid, const int* n_solid, lustrine_pbf** out);
 /* Change parameters (same mode/precision/domain/max_neighbors as at create). */
 LUSTRINE_API int lustrine_pbf_set_params(lustrine_pbf* s, const lustrine_pbf_params* p);
 LUSTRINE_API int lustrine_pbf_get_params(const lustrine_pbf* s, lustrine_pbf_params* p);

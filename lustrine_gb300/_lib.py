@@ -108,6 +108,7 @@ SIGNATURES = {
                                              C.c_float, C.c_float]),
     "lustrine_pbf_create": (C.c_int, [C.POINTER(PbfParams), C.c_int, C.c_int, C.POINTER(_P)]),
     "lustrine_pbf_destroy": (C.c_int, [_P]),
+    "lustrine_batch_create": (C.c_int, [C.POINTER(PbfParams), C.c_int, _P, _P, _P, C.POINTER(_P)]),
     "lustrine_pbf_set_params": (C.c_int, [_P, C.POINTER(PbfParams)]),
     "lustrine_pbf_get_params": (C.c_int, [_P, C.POINTER(PbfParams)]),
     "lustrine_pbf_counts": (C.c_int, [_P, _IP, _IP]),

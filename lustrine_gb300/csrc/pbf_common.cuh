@@ -28,8 +28,22 @@ enum : int {
     ST_BAD_VALUE = 8,     // a non-finite position was met
 };
 
+// One scene of a batch: its grid, the offset of its cells in the batch's
+// cell numbering and its box.  The scenes' particles occupy fixed slot
+// ranges (a scene's cells are contiguous in the global numbering, so the
+// counting sort keeps every scene in its range).
+struct SceneInfo {
+    int gx, gy, gz, cell_off;
+    float lox, loy, loz, hix, hiy, hiz;
+};
+
 // Everything a step kernel reads, passed by value (constant bank).
 struct StepParams {
+    // batches (nullptr for one scene): per-scene table, scene of each fluid
+    // slot and of each solid slot
+    const SceneInfo* scenes;
+    const int* scene_of;
+    const int* solid_scene_of;
     int n, ns;            // fluid, solid particle counts
     int gx, gy, gz;       // grid dims
     int num_cells;

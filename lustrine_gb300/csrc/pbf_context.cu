@@ -1,6 +1,7 @@
 // pbf_context.cu -- lustrine_pbf_* context API: device state, one step as a
 // fixed sequence of kernel launches on the context stream, optionally
 // replayed from a captured CUDA graph (one graph per state buffer parity).
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -168,7 +169,8 @@ lustrine_pbf::~lustrine_pbf() {
         if (graph_exec[k]) cudaGraphExecDestroy(graph_exec[k]);
     void* ptrs[] = {x[0], x[1], xs[0], xs[1], v[0], v[1], id[0], id[1], xs_alt, vtmp, key, key_sorted,
                     rank, tmp, perm, count, start, block_sums, solid, solid_raw, sstart, nbr, cnt, lam,
-                    lam_by_id, rho, status, red, out3, out3d, iota, solid_id};
+                    lam_by_id, rho, status, red, out3, out3d, iota, solid_id, d_scenes, d_scene_of,
+                    d_solid_scene_of};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     if (stream) cudaStreamDestroy(stream);
@@ -252,6 +254,105 @@ extern "C" int lustrine_pbf_create(const lustrine_pbf_params* p, int n_fluid, in
     return LUSTRINE_OK;
 }
 
+// Batch geometry: every scene's grid and box, cells numbered scene after
+// scene; the mixed-precision packing is sized by the largest box per axis.
+static int derive_batch(const lustrine_pbf_params& q0, const std::vector<int>& dom,
+                        const std::vector<int>& nf, const std::vector<int>& nsv, StepParams* sp,
+                        CellPack* cp, std::vector<SceneInfo>* table) {
+    const int S = (int)nf.size();
+    long long n = 0, ns = 0;
+    lustrine_pbf_params q = q0;
+    q.domain[0] = q.domain[1] = q.domain[2] = 1;
+    for (int k = 0; k < S; k++) {
+        if (dom[3 * k] <= 0 || dom[3 * k + 1] <= 0 || dom[3 * k + 2] <= 0 || nf[k] < 0 || nsv[k] < 0)
+            return LUSTRINE_ERR_ARGS;
+        for (int a = 0; a < 3; a++) q.domain[a] = std::max(q.domain[a], dom[3 * k + a]);
+        n += nf[k];
+        ns += nsv[k];
+    }
+    if (n >= (1LL << 26) || ns >= (1LL << 26)) return LUSTRINE_ERR_UNSUPPORTED;
+    int rc = derive(q, (int)n, (int)ns, sp, cp);
+    if (rc) return rc;
+    table->clear();
+    long long off = 0;
+    const float r = q.particle_radius;
+    for (int k = 0; k < S; k++) {
+        SceneInfo si;
+        const float dX = (float)dom[3 * k], dY = (float)dom[3 * k + 1], dZ = (float)dom[3 * k + 2];
+        si.gx = (int)(dX / q.cell_size) + 1;
+        si.gy = (int)(dY / q.cell_size) + 1;
+        si.gz = (int)(dZ / q.cell_size) + 1;
+        si.cell_off = (int)off;
+        si.lox = si.loy = si.loz = r;
+        si.hix = dX - r;
+        si.hiy = dY - r;
+        si.hiz = dZ - r;
+        table->push_back(si);
+        off += (long long)si.gx * si.gy * si.gz;
+        if (off > (1LL << 31) - 2) return LUSTRINE_ERR_UNSUPPORTED;
+    }
+    sp->num_cells = (int)off;
+    return LUSTRINE_OK;
+}
+
+extern "C" int lustrine_batch_create(const lustrine_pbf_params* p, int num_scenes, const int* domains,
+                                     const int* n_fluid, const int* n_solid, lustrine_pbf** out) {
+    if (!p || !out || num_scenes < 1 || !domains || !n_fluid) return LUSTRINE_ERR_ARGS;
+    *out = nullptr;
+    if (p->mode != LUSTRINE_MODE_PBF) return LUSTRINE_ERR_UNSUPPORTED;
+    lustrine_pbf* s = new (std::nothrow) lustrine_pbf();
+    if (!s) return LUSTRINE_ERR_NOMEM;
+    s->b_domains.assign(domains, domains + 3 * (size_t)num_scenes);
+    s->b_nfluid.assign(n_fluid, n_fluid + num_scenes);
+    s->b_nsolid.assign((size_t)num_scenes, 0);
+    if (n_solid) s->b_nsolid.assign(n_solid, n_solid + num_scenes);
+    std::vector<SceneInfo> table;
+    int rc = derive_batch(*p, s->b_domains, s->b_nfluid, s->b_nsolid, &s->sp, &s->cp, &table);
+    if (rc) {
+        delete s;
+        return rc;
+    }
+    s->prm = *p;
+    for (int a = 0; a < 3; a++) {
+        int m = 1;
+        for (int k = 0; k < num_scenes; k++) m = std::max(m, domains[3 * k + a]);
+        s->prm.domain[a] = m;
+    }
+    s->n = s->sp.n;
+    s->ns = s->sp.ns;
+    if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete s;
+        return LUSTRINE_ERR_CUDA;
+    }
+    rc = ctx_alloc(s);
+    // static maps: scene of every fluid and solid slot (scenes are contiguous slot ranges)
+    std::vector<int> sof((size_t)s->n), ssof((size_t)s->ns);
+    for (int k = 0, i = 0, j = 0; k < num_scenes; k++) {
+        for (int c = 0; c < s->b_nfluid[k]; c++) sof[(size_t)i++] = k;
+        for (int c = 0; c < s->b_nsolid[k]; c++) ssof[(size_t)j++] = k;
+    }
+    if (!rc) rc = dalloc(&s->d_scenes, table.size());
+    if (!rc) rc = dalloc(&s->d_scene_of, sof.size());
+    if (!rc) rc = dalloc(&s->d_solid_scene_of, ssof.size());
+    if (!rc && cudaMemcpy(s->d_scenes, table.data(), table.size() * sizeof(SceneInfo), cudaMemcpyHostToDevice) != cudaSuccess)
+        rc = LUSTRINE_ERR_CUDA;
+    if (!rc && !sof.empty() &&
+        cudaMemcpy(s->d_scene_of, sof.data(), sof.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess)
+        rc = LUSTRINE_ERR_CUDA;
+    if (!rc && !ssof.empty() &&
+        cudaMemcpy(s->d_solid_scene_of, ssof.data(), ssof.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess)
+        rc = LUSTRINE_ERR_CUDA;
+    if (rc) {
+        delete s;
+        return rc;
+    }
+    s->sp.scenes = s->d_scenes;
+    s->sp.scene_of = s->d_scene_of;
+    s->sp.solid_scene_of = s->d_solid_scene_of;
+    *out = s;
+    return LUSTRINE_OK;
+}
+
 extern "C" int lustrine_pbf_destroy(lustrine_pbf* s) {
     if (!s) return LUSTRINE_ERR_ARGS;
     cudaStreamSynchronize(s->stream);
@@ -268,7 +369,21 @@ extern "C" int lustrine_pbf_set_params(lustrine_pbf* s, const lustrine_pbf_param
         return LUSTRINE_ERR_ARGS;
     StepParams sp;
     CellPack cp;
-    int rc = derive(*p, s->n, s->ns, &sp, &cp);
+    int rc;
+    if (s->is_batch()) {
+        if (p->mode != LUSTRINE_MODE_PBF) return LUSTRINE_ERR_UNSUPPORTED;
+        std::vector<SceneInfo> table;
+        rc = derive_batch(*p, s->b_domains, s->b_nfluid, s->b_nsolid, &sp, &cp, &table);
+        sp.scenes = s->sp.scenes;
+        sp.scene_of = s->sp.scene_of;
+        sp.solid_scene_of = s->sp.solid_scene_of;
+        sp.dt = s->sp.dt;
+        sp.inv_dt = s->sp.inv_dt;
+    } else {
+        rc = derive(*p, s->n, s->ns, &sp, &cp);
+        sp.dt = s->sp.dt;
+        sp.inv_dt = s->sp.inv_dt;
+    }
     if (rc) return rc;
     s->prm = *p;
     s->sp = sp;
@@ -322,9 +437,10 @@ static int setup_solids(lustrine_pbf* s) {
 static int pack_fluid(lustrine_pbf* s, const float* dx, const float* dv) {
     const int n = s->n, c = s->cur;
     if (!n) return LUSTRINE_OK;
-    launch_pack_pos(s->mixed(), s->sp, s->cp, dx, n, s->x[c], s->stream);
+    // caller order = slot order here; in a batch, particles come scene by scene
+    launch_pack_pos(s->mixed(), s->sp, s->cp, dx, n, s->sp.scene_of, s->x[c], s->stream);
     if (dv)
-        launch_pack_pos(false, s->sp, s->cp, dv, n, s->v[c], s->stream);
+        launch_pack_pos(false, s->sp, s->cp, dv, n, nullptr, s->v[c], s->stream);
     else
         CK(cudaMemsetAsync(s->v[c], 0, (size_t)n * sizeof(float4), s->stream));
     CK(cudaMemcpyAsync(s->id[c], s->iota, (size_t)n * sizeof(int), cudaMemcpyDeviceToDevice, s->stream));
@@ -333,7 +449,8 @@ static int pack_fluid(lustrine_pbf* s, const float* dx, const float* dv) {
 }
 
 static int pack_solids(lustrine_pbf* s, const float* dsolid) {
-    if (s->ns > 0) launch_pack_pos(s->mixed(), s->sp, s->cp, dsolid, s->ns, s->solid_raw, s->stream);
+    if (s->ns > 0)
+        launch_pack_pos(s->mixed(), s->sp, s->cp, dsolid, s->ns, s->sp.solid_scene_of, s->solid_raw, s->stream);
     CK(cudaGetLastError());
     int rc = setup_solids(s);
     if (rc) return rc;

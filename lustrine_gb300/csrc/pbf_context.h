@@ -3,6 +3,8 @@
 
 #include <cuda_runtime.h>
 
+#include <vector>
+
 #include "lustrine_gb300.h"
 #include "pbf_common.cuh"
 
@@ -55,6 +57,13 @@ struct lustrine_pbf {
     double* red = nullptr;
     float* out3 = nullptr;    // 3 * max(n, ns) floats of staging
     double* out3d = nullptr;  // 3 * n doubles of staging
+
+    // batch of independent scenes (empty for one scene)
+    std::vector<int> b_domains, b_nfluid, b_nsolid;
+    lgb::SceneInfo* d_scenes = nullptr;
+    int* d_scene_of = nullptr;
+    int* d_solid_scene_of = nullptr;
+    bool is_batch() const { return !b_nfluid.empty(); }
 
     cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};
     int launches = 0;

@@ -78,6 +78,7 @@ void launch_unpermute_pos(bool mixed, const StepParams& p, const CellPack& cp, c
 void launch_unpermute_pos_d(bool mixed, const StepParams& p, const CellPack& cp, const float4* a,
                             const int* id, int n, double* out, cudaStream_t st);
 void launch_pack_pos(bool mixed, const StepParams& p, const CellPack& cp, const float* in, int n,
+                     const int* scene_of,
                      float4* out, cudaStream_t st);
 void launch_reduce(bool mixed, const StepParams& p, const CellPack& cp, const float4* x,
                    const float4* v, const float* rho, double* out, cudaStream_t st);

@@ -50,24 +50,46 @@ __device__ __forceinline__ float pack_cell(const CellPack& cp, int cx, int cy, i
     return __uint_as_float(u);
 }
 
-__device__ __forceinline__ int linear_cell(const StepParams& p, int3 c) {
-    return c.y * p.gx * p.gz + c.x * p.gz + c.z;
+// Grid and box of the scene a particle belongs to: the step's own for one
+// scene, the batch table's entry otherwise.
+struct Geo {
+    int gx, gy, gz, off;
+    float lox, loy, loz, hix, hiy, hiz;
+};
+
+__device__ __forceinline__ Geo geo_single(const StepParams& p) {
+    return Geo{p.gx, p.gy, p.gz, 0, p.lox, p.loy, p.loz, p.hix, p.hiy, p.hiz};
 }
 
-__device__ __forceinline__ int3 decode_cell(const StepParams& p, int key) {
-    const int slab = p.gx * p.gz;
-    const int y = key / slab;
-    const int r = key - y * slab;
-    const int x = r / p.gz;
-    return make_int3(x, y, r - x * p.gz);
+__device__ __forceinline__ Geo geo_scene(const StepParams& p, int scene) {
+    const SceneInfo si = p.scenes[scene];
+    return Geo{si.gx, si.gy, si.gz, si.cell_off, si.lox, si.loy, si.loz, si.hix, si.hiy, si.hiz};
+}
+
+// geometry of fluid slot s (slots of a scene are a fixed range)
+__device__ __forceinline__ Geo geo_slot(const StepParams& p, int s) {
+    return p.scenes ? geo_scene(p, __ldg(&p.scene_of[s])) : geo_single(p);
+}
+
+__device__ __forceinline__ int linear_cell(const Geo& g, int3 c) {
+    return g.off + c.y * g.gx * g.gz + c.x * g.gz + c.z;
+}
+
+__device__ __forceinline__ int3 decode_cell(const Geo& g, int key) {
+    const int slab = g.gx * g.gz;
+    const int local = key - g.off;
+    const int y = local / slab;
+    const int r = local - y * slab;
+    const int x = r / g.gz;
+    return make_int3(x, y, r - x * g.gz);
 }
 
 __device__ __forceinline__ float clampf(float v, float lo, float hi) { return fminf(fmaxf(v, lo), hi); }
 
-__device__ __forceinline__ int3 plain_cell(const StepParams& p, float x, float y, float z) {
+__device__ __forceinline__ int3 plain_cell(const StepParams& p, const Geo& g, float x, float y, float z) {
     int cx = (int)floorf(x * p.inv_cell), cy = (int)floorf(y * p.inv_cell),
         cz = (int)floorf(z * p.inv_cell);
-    return make_int3(min(max(cx, 0), p.gx - 1), min(max(cy, 0), p.gy - 1), min(max(cz, 0), p.gz - 1));
+    return make_int3(min(max(cx, 0), g.gx - 1), min(max(cy, 0), g.gy - 1), min(max(cz, 0), g.gz - 1));
 }
 
 // Offset of the neighbour's cell from the particle's: code -> -(c_j - c_i) * cell
@@ -175,34 +197,37 @@ __global__ void k_predict(StepParams p, CellPack cp, const float4* __restrict__ 
     vi.z += p.gzv * p.dt;
     v[i] = vi;
     const float4 xi = x[i];
+    const Geo g = geo_slot(p, i);
     int3 c;
     float4 s;
     if (!MIXED) {
-        s = make_float4(clampf(xi.x + vi.x * p.dt, p.lox, p.hix), clampf(xi.y + vi.y * p.dt, p.loy, p.hiy),
-                        clampf(xi.z + vi.z * p.dt, p.loz, p.hiz), 0.0f);
-        c = plain_cell(p, s.x, s.y, s.z);
+        s = make_float4(clampf(xi.x + vi.x * p.dt, g.lox, g.hix), clampf(xi.y + vi.y * p.dt, g.loy, g.hiy),
+                        clampf(xi.z + vi.z * p.dt, g.loz, g.hiz), 0.0f);
+        c = plain_cell(p, g, s.x, s.y, s.z);
     } else {
         c = unpack_cell(cp, xi.w);
         float ox = xi.x + vi.x * p.dt, oy = xi.y + vi.y * p.dt, oz = xi.z + vi.z * p.dt;
-        renorm_axis(p, ox, c.x, p.lox, p.hix);
-        renorm_axis(p, oy, c.y, p.loy, p.hiy);
-        renorm_axis(p, oz, c.z, p.loz, p.hiz);
+        renorm_axis(p, ox, c.x, g.lox, g.hix);
+        renorm_axis(p, oy, c.y, g.loy, g.hiy);
+        renorm_axis(p, oz, c.z, g.loz, g.hiz);
         s = make_float4(ox, oy, oz, 0.0f);
     }
     xs[i] = s;
-    const int k = linear_cell(p, c);
+    const int k = linear_cell(g, c);
     key[i] = k;
     rank[i] = atomicAdd(&count[k], 1);
 }
 
+// Cell key and histogram of static particles (solids; scene from solid_scene_of).
 template <bool MIXED>
 __global__ void k_key(StepParams p, CellPack cp, const float4* __restrict__ pos, int m,
                       int* __restrict__ key, int* __restrict__ rank, int* __restrict__ count) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m) return;
     float4 q = pos[i];
-    int3 c = MIXED ? unpack_cell(cp, q.w) : plain_cell(p, q.x, q.y, q.z);
-    int k = linear_cell(p, c);
+    const Geo g = p.scenes ? geo_scene(p, p.solid_scene_of[i]) : geo_single(p);
+    int3 c = MIXED ? unpack_cell(cp, q.w) : plain_cell(p, g, q.x, q.y, q.z);
+    int k = linear_cell(g, c);
     key[i] = k;
     rank[i] = atomicAdd(&count[k], 1);
 }
@@ -251,9 +276,9 @@ __device__ __forceinline__ float lambda_of(const StepParams& p, const LambdaAcc&
 template <bool MIXED, bool SOLID>
 __device__ __forceinline__ void walk_row(const StepParams& p, const float4& self, int s,
                                          const float4* __restrict__ pos, const int* __restrict__ start,
-                                         int row, int zc, int dx, int dy, LambdaAcc& a, int& c_n,
+                                         int row, int zc, int gz, int dx, int dy, LambdaAcc& a, int& c_n,
                                          int* __restrict__ nbr) {
-    const int z0 = max(zc - 1, 0), z1 = min(zc + 1, p.gz - 1);
+    const int z0 = max(zc - 1, 0), z1 = min(zc + 1, gz - 1);
     int b[4];
 #pragma unroll
     for (int k = 0; k < 4; k++) b[k] = (z0 + k <= z1 + 1) ? start[row + z0 + k] : 0;
@@ -295,19 +320,21 @@ __global__ void __launch_bounds__(B) k_lists_lambda(StepParams p, float4* __rest
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= p.n) return;
     const float4 self = xs[s];
-    const int3 c = decode_cell(p, key_sorted[s]);
+    const Geo g = geo_slot(p, s);
+    const int3 c = decode_cell(g, key_sorted[s]);
     LambdaAcc a = lambda_init(p);
     int c_n = 0;
-    const int slab = p.gx * p.gz;
+    const int slab = g.gx * g.gz;
     for (int dy = -1; dy <= 1; dy++) {
         const int y = c.y + dy;
-        if (y < 0 || y >= p.gy) continue;
+        if (y < 0 || y >= g.gy) continue;
         for (int dx = -1; dx <= 1; dx++) {
             const int xx = c.x + dx;
-            if (xx < 0 || xx >= p.gx) continue;
-            const int row = y * slab + xx * p.gz;
-            walk_row<MIXED, false>(p, self, s, xs, fstart, row, c.z, dx, dy, a, c_n, nbr);
-            if (p.ns > 0) walk_row<MIXED, true>(p, self, s, solid, sstart, row, c.z, dx, dy, a, c_n, nbr);
+            if (xx < 0 || xx >= g.gx) continue;
+            const int row = g.off + y * slab + xx * g.gz;
+            walk_row<MIXED, false>(p, self, s, xs, fstart, row, c.z, g.gz, dx, dy, a, c_n, nbr);
+            if (p.ns > 0)
+                walk_row<MIXED, true>(p, self, s, solid, sstart, row, c.z, g.gz, dx, dy, a, c_n, nbr);
         }
     }
     if (c_n > p.max_nbrs) {
@@ -408,14 +435,15 @@ __global__ void __launch_bounds__(B) k_delta(StepParams p, CellPack cp, const fl
     }
     float4 out;
     int3 cs = make_int3(0, 0, 0);
+    const Geo g = geo_slot(p, s);
     if (!MIXED) {
-        out = make_float4(clampf(self.x + dx, p.lox, p.hix), clampf(self.y + dy, p.loy, p.hiy),
-                          clampf(self.z + dz, p.loz, p.hiz), 0.0f);
+        out = make_float4(clampf(self.x + dx, g.lox, g.hix), clampf(self.y + dy, g.loy, g.hiy),
+                          clampf(self.z + dz, g.loz, g.hiz), 0.0f);
     } else {
-        cs = decode_cell(p, key_sorted[s]);
-        out = make_float4(clamp_offset(p, self.x + dx, cs.x, p.lox, p.hix),
-                          clamp_offset(p, self.y + dy, cs.y, p.loy, p.hiy),
-                          clamp_offset(p, self.z + dz, cs.z, p.loz, p.hiz), 0.0f);
+        cs = decode_cell(g, key_sorted[s]);
+        out = make_float4(clamp_offset(p, self.x + dx, cs.x, g.lox, g.hix),
+                          clamp_offset(p, self.y + dy, cs.y, g.loy, g.hiy),
+                          clamp_offset(p, self.z + dz, cs.z, g.loz, g.hiz), 0.0f);
     }
     xs_out[s] = out;
     if (v_out) {
@@ -476,7 +504,7 @@ __global__ void __launch_bounds__(B) k_xsph(StepParams p, CellPack cp, const flo
     if (!MIXED) {
         x_out[s] = make_float4(self.x, self.y, self.z, 0.0f);
     } else {
-        int3 cs = decode_cell(p, key_sorted[s]);
+        int3 cs = decode_cell(geo_slot(p, s), key_sorted[s]);
         x_out[s] = make_float4(self.x, self.y, self.z, pack_cell(cp, cs.x, cs.y, cs.z));
     }
 }
@@ -522,9 +550,10 @@ __global__ void k_unpermute_pos_d(StepParams p, CellPack cp, const float4* __res
 }
 
 // Caller positions (float3, id order) into the state representation, slot = id.
+// scene_of: scene of each packed element in a batch (nullptr for one scene).
 template <bool MIXED>
 __global__ void k_pack_pos(StepParams p, CellPack cp, const float* __restrict__ in, int n,
-                           float4* __restrict__ out) {
+                           const int* __restrict__ scene_of, float4* __restrict__ out) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float x = in[3 * (size_t)i], y = in[3 * (size_t)i + 1], z = in[3 * (size_t)i + 2];
@@ -536,9 +565,10 @@ __global__ void k_pack_pos(StepParams p, CellPack cp, const float* __restrict__ 
     // packed field widths); the offset keeps the exact position, so a caller
     // position outside the box stays where it is (it may then lie outside
     // [0, cell)) and the next prediction clamps it like the plain form does.
-    int cx = min(max((int)floorf(x * p.inv_cell), 0), (int)floorf(p.hix * p.inv_cell));
-    int cy = min(max((int)floorf(y * p.inv_cell), 0), (int)floorf(p.hiy * p.inv_cell));
-    int cz = min(max((int)floorf(z * p.inv_cell), 0), (int)floorf(p.hiz * p.inv_cell));
+    const Geo g = (p.scenes && scene_of) ? geo_scene(p, scene_of[i]) : geo_single(p);
+    int cx = min(max((int)floorf(x * p.inv_cell), 0), (int)floorf(g.hix * p.inv_cell));
+    int cy = min(max((int)floorf(y * p.inv_cell), 0), (int)floorf(g.hiy * p.inv_cell));
+    int cz = min(max((int)floorf(z * p.inv_cell), 0), (int)floorf(g.hiz * p.inv_cell));
     out[i] = make_float4(x - (float)cx * p.cell, y - (float)cy * p.cell, z - (float)cz * p.cell,
                          pack_cell(cp, cx, cy, cz));
 }
@@ -711,9 +741,9 @@ void launch_unpermute_pos_d(bool mixed, const StepParams& p, const CellPack& cp,
 }
 
 void launch_pack_pos(bool mixed, const StepParams& p, const CellPack& cp, const float* in, int n,
-                     float4* out, cudaStream_t st) {
+                     const int* scene_of, float4* out, cudaStream_t st) {
     if (n <= 0) return;
-    LGB_DISPATCH(mixed, k_pack_pos, blocks_for(n, 256), 256, st, p, cp, in, n, out);
+    LGB_DISPATCH(mixed, k_pack_pos, blocks_for(n, 256), 256, st, p, cp, in, n, scene_of, out);
 }
 
 void launch_reduce(bool mixed, const StepParams& p, const CellPack& cp, const float4* x,

@@ -78,6 +78,26 @@ class PbfSim:
               "lustrine_pbf_create")
         self.h = h
 
+    @classmethod
+    def batch(cls, params: PbfParams, domains, n_fluid, n_solid=None) -> "PbfSim":
+        """Independent scenes stepped together (one launch per stage).
+        domains: (S, 3) ints; n_fluid, n_solid: S ints.  Arrays passed to
+        upload/download concatenate the scenes in order."""
+        self = cls.__new__(cls)
+        self.lib = _lib.load()
+        self.params = params
+        dom = np.ascontiguousarray(domains, np.int32).reshape(-1)
+        nf = np.ascontiguousarray(n_fluid, np.int32)
+        nsol = None if n_solid is None else np.ascontiguousarray(n_solid, np.int32)
+        self.n = int(nf.sum())
+        self.ns = 0 if nsol is None else int(nsol.sum())
+        self.scene_counts = nf.copy()
+        h = C.c_void_p()
+        check(self.lib.lustrine_batch_create(C.byref(params), len(nf), _ptr(dom), _ptr(nf), _ptr(nsol),
+                                             C.byref(h)), "lustrine_batch_create")
+        self.h = h
+        return self
+
     # lifecycle -------------------------------------------------------------
     def close(self):
         if getattr(self, "h", None) and self.h.value:
