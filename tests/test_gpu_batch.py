@@ -64,10 +64,11 @@ def test_batch_mixed_density_error_vs_fp64(orc):
     p1 = _params(PRECISION_MIXED)
     p1.iterations = 1
     e = PbfSim.batch(p1, [sc.domain for sc in scs], [sc.n for sc in scs])
-    e.upload(xd.astype(np.float32))
+    x_up = xd.astype(np.float32)
+    e.upload(x_up)
     e.step(1e-7)
-    rho = e.density()
-    x_eval = e.positions_f64()
+    rho = e.density()  # the lambda pass ran at the uploaded positions
+    x_eval = x_up.astype(np.float64)
     off = 0
     worst = 0.0
     for sc in scs:
