@@ -347,6 +347,41 @@ __global__ void __launch_bounds__(B) k_lists_lambda(StepParams p, float4* __rest
     if (rho) rho[s] = a.density;
 }
 
+// Walk a particle's list U entries at a time, calling f(entry, position)
+// for each.  The first U entries are loaded together with the count and
+// every next chunk's entries while the current chunk's positions are
+// gathered: the list buffer holds max_nbrs rows for every particle, so these
+// loads stay in bounds, and entries at or past the count are replaced by
+// the particle itself before any position is gathered.
+template <int U, class F>
+__device__ __forceinline__ void for_each_entry(const StepParams& p, const int* __restrict__ col,
+                                               const int* __restrict__ cnt, int s,
+                                               const float4* __restrict__ xs,
+                                               const float4* __restrict__ solid, F&& f) {
+    int nx[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) nx[u] = u < p.max_nbrs ? __ldg(&col[(size_t)u * p.n]) : s;
+    const int c = __ldg(&cnt[s]);
+    for (int k = 0; k < c; k += U) {
+        int e[U];
+        float4 q[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) e[u] = k + u < c ? nx[u] : s;
+        if (k + U < c) {
+#pragma unroll
+            for (int u = 0; u < U; u++)
+                nx[u] = k + U + u < p.max_nbrs ? __ldg(&col[(size_t)(k + U + u) * p.n]) : s;
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) q[u] = load_entry(e[u], xs, solid);
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            if (k + u >= c) break;
+            f(e[u], q[u]);
+        }
+    }
+}
+
 // Lambda pass over the lists (iterations after the first); U neighbour
 // gathers in flight per thread.
 template <bool MIXED, int U, int B>
@@ -358,23 +393,11 @@ __global__ void __launch_bounds__(B) k_lambda(StepParams p, float4* __restrict__
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= p.n) return;
     const float4 self = xs[s];
-    const int c = cnt[s];
-    const int* __restrict__ col = nbr + s;
     LambdaAcc a = lambda_init(p);
-    for (int k = 0; k < c; k += U) {
-        int e[U];
-        float4 q[U];
-#pragma unroll
-        for (int u = 0; u < U; u++) e[u] = k + u < c ? __ldg(&col[(size_t)(k + u) * p.n]) : s;
-#pragma unroll
-        for (int u = 0; u < U; u++) q[u] = load_entry(e[u], xs, solid);
-#pragma unroll
-        for (int u = 0; u < U; u++) {
-            if (k + u >= c) break;
-            float3 d = rel_e<MIXED>(p, self, q[u], e[u]);
-            lambda_accumulate<MIXED>(p, a, d, entry_solid(e[u]));
-        }
-    }
+    for_each_entry<U>(p, nbr + s, cnt, s, xs, solid, [&](int e, float4 q) {
+        float3 d = rel_e<MIXED>(p, self, q, e);
+        lambda_accumulate<MIXED>(p, a, d, entry_solid(e));
+    });
     reinterpret_cast<float*>(xs)[4 * (size_t)s + 3] = lambda_of(p, a);
     if (rho) rho[s] = a.density;
 }
@@ -393,39 +416,27 @@ __global__ void __launch_bounds__(B) k_delta(StepParams p, CellPack cp, const fl
     if (s >= p.n) return;
     const float4 self = xs[s];
     const float li = self.w;
-    const int c = cnt[s];
-    const int* __restrict__ col = nbr + s;
     float px = 0.0f, py = 0.0f, pz = 0.0f;
     float cx = 0.0f, cy = 0.0f, cz = 0.0f;
     int nct = 0;
-    for (int k = 0; k < c; k += U) {
-        int e[U];
-        float4 q[U];
-#pragma unroll
-        for (int u = 0; u < U; u++) e[u] = k + u < c ? __ldg(&col[(size_t)(k + u) * p.n]) : s;
-#pragma unroll
-        for (int u = 0; u < U; u++) q[u] = load_entry(e[u], xs, solid);
-#pragma unroll
-        for (int u = 0; u < U; u++) {
-            if (k + u >= c) break;
-            const bool sol = entry_solid(e[u]);
-            float3 d = rel_e<MIXED>(p, self, q[u], e[u]);
-            const float r2 = dot3(d.x, d.y, d.z);
-            const PairR pr = pair_r(r2);
-            const float lj = sol ? li : q[u].w;
-            const float w = (li + lj + scorr(p, r2)) * spiky_factor(p, pr);
-            px += w * d.x;
-            py += w * d.y;
-            pz += w * d.z;
-            if (sol && pr.r < p.contact && pr.inv_r > 0.0f) {
-                const float t = (p.contact - pr.r) * pr.inv_r;
-                cx += t * d.x;
-                cy += t * d.y;
-                cz += t * d.z;
-                nct++;
-            }
+    for_each_entry<U>(p, nbr + s, cnt, s, xs, solid, [&](int e, float4 q) {
+        const bool sol = entry_solid(e);
+        float3 d = rel_e<MIXED>(p, self, q, e);
+        const float r2 = dot3(d.x, d.y, d.z);
+        const PairR pr = pair_r(r2);
+        const float lj = sol ? li : q.w;
+        const float w = (li + lj + scorr(p, r2)) * spiky_factor(p, pr);
+        px += w * d.x;
+        py += w * d.y;
+        pz += w * d.z;
+        if (sol && pr.r < p.contact && pr.inv_r > 0.0f) {
+            const float t = (p.contact - pr.r) * pr.inv_r;
+            cx += t * d.x;
+            cy += t * d.y;
+            cz += t * d.z;
+            nct++;
         }
-    }
+    });
     float dx = px * p.mr, dy = py * p.mr, dz = pz * p.mr;
     if (nct) {
         const float inv = __frcp_rn((float)nct);
