@@ -371,6 +371,19 @@ def run_variants(args, flush):
                                "stage_ms": {a: round(b[0], 4) for a, b in prof.items()}}
     sim.close()
     out["config3_batched_vs_plain"] = run_config3(max(3, min(args.steps, 10)), flush)
+    # 4,194,304 particles in a 4096 x 256 x 4096 box: 4.3e9 cells, so the
+    # grid is hashed (2^23 buckets); mixed precision is the mode the box needs
+    sc = scenes.config4()
+    for name, prec in (("config4_mixed_hashed_4M", PRECISION_MIXED), ("config4_fp32_hashed_4M", 0)):
+        p = pbf_params(*sc.domain, iterations=sc.iterations, c_xsph=sc.c_xsph, precision=prec)
+        sim, _, ms, st = run_scene(sc, p, k, 3, flush)
+        prof = profile_stages(sim, sc.dt, reps=2)
+        out[name] = {"value": sc.n * p.iterations / (np.mean(ms) * 1e-3),
+                     "ms_per_step": float(np.mean(ms)), "status": st,
+                     "launch_shape": sim.tuned["tuning"],
+                     "max_density_error": sim.reduce()["max_density_error"],
+                     "stage_ms": {a: round(b[0], 4) for a, b in prof.items()}}
+        sim.close()
     return out
 
 

@@ -169,7 +169,14 @@ typedef struct lustrine_pbf_params {
     int max_neighbors;        /* neighbour list capacity per particle */
     int clamp_cells;          /* reference mode: clamp cell coordinates to the grid */
     int use_graph;            /* replay each step from a captured CUDA graph */
+    int grid_mode;            /* LUSTRINE_GRID_*: dense cell table or hashed cells (PBF mode) */
 } lustrine_pbf_params;
+
+enum {
+    LUSTRINE_GRID_AUTO = 0,   /* dense unless the box has far more cells than particles */
+    LUSTRINE_GRID_DENSE = 1,  /* one table entry per cell of the box */
+    LUSTRINE_GRID_HASHED = 2  /* 2^k hash buckets (k from the particle count); any box size */
+};
 
 typedef struct lustrine_pbf lustrine_pbf;
 

@@ -70,7 +70,11 @@ class PbfParams(C.Structure):
                 ("relaxation_epsilon", C.c_float), ("s_corr_dq", C.c_float),
                 ("s_corr_k", C.c_float), ("s_corr_n", C.c_float), ("c_xsph", C.c_float),
                 ("solid_contact", C.c_float), ("iterations", C.c_int),
-                ("max_neighbors", C.c_int), ("clamp_cells", C.c_int), ("use_graph", C.c_int)]
+                ("max_neighbors", C.c_int), ("clamp_cells", C.c_int), ("use_graph", C.c_int),
+                ("grid_mode", C.c_int)]
+
+
+GRID_AUTO, GRID_DENSE, GRID_HASHED = 0, 1, 2
 
 
 class PbfTuning(C.Structure):

@@ -44,9 +44,12 @@ struct StepParams {
     const SceneInfo* scenes;
     const int* scene_of;
     const int* solid_scene_of;
+    // hashed grid: packed cell of every sorted fluid slot (nullptr when dense)
+    const int* cell_sorted;
     int n, ns;            // fluid, solid particle counts
     int gx, gy, gz;       // grid dims
-    int num_cells;
+    int num_cells;        // dense: cells; hashed: buckets (1 << hash_bits)
+    int hash_bits;        // 0: dense cell grid; > 0: hashed grid of 2^hash_bits buckets
     int max_nbrs;
     int clamp_cells;      // compat mode: clamp cell coords per axis
     float cell, inv_cell;

@@ -92,10 +92,24 @@ static int derive(const lustrine_pbf_params& q, int n, int ns, StepParams* sp, C
     p.gy = (int)(dY / q.cell_size) + 1;
     p.gz = (int)(dZ / q.cell_size) + 1;
     const long long C = (long long)p.gx * p.gy * p.gz;
-    if (C > (1LL << 31) - 2) return LUSTRINE_ERR_UNSUPPORTED;
-    // PBF neighbour entries hold a 26-bit slot
-    if (q.mode == LUSTRINE_MODE_PBF && (n >= (1 << 26) || ns >= (1 << 26))) return LUSTRINE_ERR_UNSUPPORTED;
-    p.num_cells = (int)C;
+    // hashed grid: requested, or (auto) when the box has far more cells than
+    // particles -- up to 2^32 cells for a 4096 x 256 x 4096 box
+    const long long parts = (long long)n + ns;
+    const bool hashed = q.mode == LUSTRINE_MODE_PBF &&
+                        (q.grid_mode == LUSTRINE_GRID_HASHED ||
+                         (q.grid_mode == LUSTRINE_GRID_AUTO && (C > (1LL << 31) - 2 || C > 32 * parts + (1LL << 24))));
+    if (q.grid_mode == LUSTRINE_GRID_HASHED && q.mode != LUSTRINE_MODE_PBF) return LUSTRINE_ERR_UNSUPPORTED;
+    if (!hashed && C > (1LL << 31) - 2) return LUSTRINE_ERR_UNSUPPORTED;
+    // PBF neighbour entries hold a 25-bit slot
+    if (q.mode == LUSTRINE_MODE_PBF && (n >= (1 << 25) || ns >= (1 << 25))) return LUSTRINE_ERR_UNSUPPORTED;
+    if (hashed) {
+        int bits = 10;
+        while ((1LL << bits) < 2 * parts && bits < 30) bits++;
+        p.hash_bits = bits;
+        p.num_cells = 1 << bits;
+    } else {
+        p.num_cells = (int)C;
+    }
     p.max_nbrs = q.max_neighbors;
     p.clamp_cells = q.clamp_cells;
     p.cell = q.cell_size;
@@ -147,7 +161,7 @@ static int derive(const lustrine_pbf_params& q, int n, int ns, StepParams* sp, C
     }
     CellPack c;
     std::memset(&c, 0, sizeof(c));
-    if (q.precision == LUSTRINE_PRECISION_MIXED) {
+    if (q.precision == LUSTRINE_PRECISION_MIXED || hashed) {
         // cells a clamped position can occupy: 0 .. floor(hi / cell)
         int vx = (int)std::floor(p.hix / p.cell) + 1, vy = (int)std::floor(p.hiy / p.cell) + 1,
             vz = (int)std::floor(p.hiz / p.cell) + 1;
@@ -170,7 +184,7 @@ lustrine_pbf::~lustrine_pbf() {
     void* ptrs[] = {x[0], x[1], xs[0], xs[1], v[0], v[1], id[0], id[1], xs_alt, vtmp, key, key_sorted,
                     rank, tmp, perm, count, start, block_sums, solid, solid_raw, sstart, nbr, cnt, lam,
                     lam_by_id, rho, status, red, out3, out3d, iota, solid_id, d_scenes, d_scene_of,
-                    d_solid_scene_of};
+                    d_solid_scene_of, cellk, cell_sorted, solid_cell};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     if (stream) cudaStreamDestroy(stream);
@@ -210,6 +224,12 @@ static int ctx_alloc(lustrine_pbf* s) {
     rc = rc ? rc : dalloc(&s->out3d, (size_t)3 * n);
     rc = rc ? rc : dalloc(&s->iota, n);
     rc = rc ? rc : dalloc(&s->solid_id, ns);
+    if (s->sp.hash_bits) {  // hashed grid: packed cells, unsorted and sorted
+        rc = rc ? rc : dalloc(&s->cellk, m);
+        rc = rc ? rc : dalloc(&s->cell_sorted, n);
+        rc = rc ? rc : dalloc(&s->solid_cell, ns);
+        s->sp.cell_sorted = s->cell_sorted;
+    }
     if (rc) return rc;
     if (n) {
         std::vector<int> ids((size_t)n);
@@ -263,6 +283,7 @@ static int derive_batch(const lustrine_pbf_params& q0, const std::vector<int>& d
     long long n = 0, ns = 0;
     lustrine_pbf_params q = q0;
     q.domain[0] = q.domain[1] = q.domain[2] = 1;
+    q.grid_mode = LUSTRINE_GRID_DENSE;  // scenes' cells are numbered one after another
     for (int k = 0; k < S; k++) {
         if (dom[3 * k] <= 0 || dom[3 * k + 1] <= 0 || dom[3 * k + 2] <= 0 || nf[k] < 0 || nsv[k] < 0)
             return LUSTRINE_ERR_ARGS;
@@ -365,7 +386,7 @@ extern "C" int lustrine_pbf_set_params(lustrine_pbf* s, const lustrine_pbf_param
     if (p->precision != s->prm.precision ||
         p->domain[0] != s->prm.domain[0] || p->domain[1] != s->prm.domain[1] ||
         p->domain[2] != s->prm.domain[2] || p->max_neighbors != s->prm.max_neighbors ||
-        p->cell_size != s->prm.cell_size)
+        p->cell_size != s->prm.cell_size || p->grid_mode != s->prm.grid_mode)
         return LUSTRINE_ERR_ARGS;
     StepParams sp;
     CellPack cp;
@@ -383,8 +404,11 @@ extern "C" int lustrine_pbf_set_params(lustrine_pbf* s, const lustrine_pbf_param
         rc = derive(*p, s->n, s->ns, &sp, &cp);
         sp.dt = s->sp.dt;
         sp.inv_dt = s->sp.inv_dt;
+        sp.cell_sorted = s->sp.cell_sorted;
     }
     if (rc) return rc;
+    // the grid's table (dense cells or hash buckets) was sized at creation
+    if (sp.hash_bits != s->sp.hash_bits || sp.num_cells != s->sp.num_cells) return LUSTRINE_ERR_UNSUPPORTED;
     s->prm = *p;
     s->sp = sp;
     s->cp = cp;
@@ -423,11 +447,13 @@ static int setup_solids(lustrine_pbf* s) {
         if (s->prm.mode == LUSTRINE_MODE_REFERENCE)
             launch_key_ref(p, s->solid_raw, ns, s->key, s->rank, s->count, s->status, s->stream);
         else
-            launch_key(s->mixed(), p, s->cp, s->solid_raw, ns, s->key, s->rank, s->count, s->stream);
+            launch_key(s->mixed(), p, s->cp, s->solid_raw, ns, s->key, s->rank, s->count, s->cellk,
+                       s->stream);
     }
     launch_scan(s->count, C, s->block_sums, s->sstart, s->stream);
     launch_sort_tail(s->key, s->rank, s->sstart, nullptr, ns, s->tmp, s->perm, s->stream);
     launch_gather_solid(s->perm, ns, s->solid_raw, s->solid, s->stream);
+    if (p.hash_bits) launch_gather_int(s->perm, ns, s->cellk, s->solid_cell, s->stream);
     CK(cudaGetLastError());
     return LUSTRINE_OK;
 }
@@ -531,7 +557,7 @@ static int enqueue_step(lustrine_pbf* s, cudaStream_t st, StageMarks* mk = nullp
     if (s->prm.mode == LUSTRINE_MODE_REFERENCE)
         launch_predict_ref(p, s->x[c], s->v[c], s->xs[c], s->key, s->rank, s->count, s->status, st);
     else
-        launch_predict(mixed, p, s->cp, s->x[c], s->v[c], s->xs[c], s->key, s->rank, s->count, st);
+        launch_predict(mixed, p, s->cp, s->x[c], s->v[c], s->xs[c], s->key, s->rank, s->count, s->cellk, st);
     k += 1;
     if (mk) mk->mark(LUSTRINE_STAGE_PREDICT, st);
     launch_scan(s->count, C, s->block_sums, s->start, st);
@@ -541,7 +567,8 @@ static int enqueue_step(lustrine_pbf* s, cudaStream_t st, StageMarks* mk = nullp
     // reference's list order), by the previous slot otherwise
     const int* tie = s->prm.mode == LUSTRINE_MODE_REFERENCE ? s->id[c] : nullptr;
     launch_sort_state(s->key, s->rank, s->start, tie, n, s->tmp, s->x[c], s->xs[c], s->v[c], s->id[c],
-                      s->key_sorted, s->x[o], s->xs[o], s->v[o], s->id[o], st);
+                      s->key_sorted, s->x[o], s->xs[o], s->v[o], s->id[o], p.hash_bits ? s->cellk : nullptr,
+                      s->cell_sorted, st);
     k += 2;
     if (mk) mk->mark(LUSTRINE_STAGE_SORT, st);
     if (s->prm.mode == LUSTRINE_MODE_REFERENCE) {
@@ -563,8 +590,8 @@ static int enqueue_step(lustrine_pbf* s, cudaStream_t st, StageMarks* mk = nullp
         for (int it = 0; it < iters; it++) {
             float* rho = it == iters - 1 ? s->rho : nullptr;  // densities of the last pass only
             if (it == 0) {
-                launch_lists_lambda(mixed, tu, p, a, s->key_sorted, s->start, s->solid, s->sstart,
-                                    s->nbr, s->cnt, rho, s->status, st);
+                launch_lists_lambda(mixed, tu, p, s->cp, a, s->key_sorted, s->cell_sorted, s->start,
+                                    s->solid, s->solid_cell, s->sstart, s->nbr, s->cnt, rho, s->status, st);
                 if (mk) mk->mark(LUSTRINE_STAGE_LISTS, st);
             } else {
                 launch_lambda(mixed, tu, p, a, s->nbr, s->cnt, s->solid, rho, st);
@@ -902,8 +929,8 @@ extern "C" int lustrine_pbf_neighbors(lustrine_pbf* s, int* count, int* idx, int
             int j = nbr[(size_t)e * n + k];
             if (ref)
                 idx[(size_t)i * cap + e] = j >= 0 ? ids[(size_t)j] : n + sid[(size_t)(-1 - j)];
-            else  // PBF entry: slot in bits 0-25, solid flag in bit 31
-                idx[(size_t)i * cap + e + 1] = j >= 0 ? ids[(size_t)(j & 0x3FFFFFF)] : n + sid[(size_t)(j & 0x3FFFFFF)];
+            else  // PBF entry: slot in bits 0-24, solid flag in bit 31
+                idx[(size_t)i * cap + e + 1] = j >= 0 ? ids[(size_t)(j & 0x1FFFFFF)] : n + sid[(size_t)(j & 0x1FFFFFF)];
         }
     }
     return rc;

@@ -42,6 +42,11 @@ struct lustrine_pbf {
     // static solids, sorted by cell
     float4* solid = nullptr;
     float4* solid_raw = nullptr;
+    // hashed grid: packed cell of each particle (unsorted), of each sorted
+    // fluid slot, of each sorted solid slot
+    int* cellk = nullptr;
+    int* cell_sorted = nullptr;
+    int* solid_cell = nullptr;
     int* solid_id = nullptr;   // caller's solid index of each sorted slot
     int* sstart = nullptr;
 

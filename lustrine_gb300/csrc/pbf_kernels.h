@@ -34,10 +34,13 @@ CountingSortScratch counting_sort_scratch(int* base, int n, int num_cells);
 void launch_counting_sort(const int* keys, int n, int num_cells, CountingSortScratch w, int* start,
                           int* sorted, cudaStream_t st);
 // index scatter + stabilisation fused with the reorder of the particle state
+// (aux: an optional int per particle carried into the new order, e.g. the
+// packed cells of a hashed grid)
 void launch_sort_state(const int* key, const int* rank, const int* start, const int* tie, int n,
                        int* tmp, const float4* x, const float4* xs, const float4* v, const int* id,
                        int* key_out, float4* x_out, float4* xs_out, float4* v_out, int* id_out,
-                       cudaStream_t st);
+                       const int* aux, int* aux_out, cudaStream_t st);
+void launch_gather_int(const int* perm, int n, const int* src, int* dst, cudaStream_t st);
 
 // pbf_compat.cu (reference semantics, no FMA contraction)
 void launch_predict_ref(const StepParams& p, const float4* x, float4* v, float4* xs, int* key,
@@ -55,15 +58,16 @@ void launch_delta_ref(const StepParams& p, const float4* xs, float4* xs_out, flo
                       const float* lam_by_id, cudaStream_t st);
 
 // pbf_solver.cu (PBF; mixed = cell index + offset representation)
+// cellk: packed cell of every particle on a hashed grid (nullptr when dense)
 void launch_predict(bool mixed, const StepParams& p, const CellPack& cp, const float4* x, float4* v,
-                    float4* xs, int* key, int* rank, int* count, cudaStream_t st);
+                    float4* xs, int* key, int* rank, int* count, int* cellk, cudaStream_t st);
 void launch_key(bool mixed, const StepParams& p, const CellPack& cp, const float4* pos, int m,
-                int* key, int* rank, int* count, cudaStream_t st);
+                int* key, int* rank, int* count, int* cellk, cudaStream_t st);
 // neighbour lists + first lambda pass (lambda stored in xs.w)
-void launch_lists_lambda(bool mixed, const Tuning& tu, const StepParams& p, float4* xs,
-                         const int* key_sorted, const int* fstart, const float4* solid,
-                         const int* sstart, int* nbr, int* cnt, float* rho, int* status,
-                         cudaStream_t st);
+void launch_lists_lambda(bool mixed, const Tuning& tu, const StepParams& p, const CellPack& cp,
+                         float4* xs, const int* key_sorted, const int* cell_sorted, const int* fstart,
+                         const float4* solid, const int* solid_cell, const int* sstart, int* nbr,
+                         int* cnt, float* rho, int* status, cudaStream_t st);
 void launch_lambda(bool mixed, const Tuning& tu, const StepParams& p, float4* xs, const int* nbr,
                    const int* cnt, const float4* solid, float* rho, cudaStream_t st);
 void launch_delta(bool mixed, const Tuning& tu, const StepParams& p, const CellPack& cp,

@@ -18,24 +18,45 @@
 // lambda, written in place by the lambda pass, so the position pass gathers
 // one float4 per neighbour.
 //
-// Neighbour list entry (int32): bits 0-25 slot, bits 26-30 the neighbour's
-// cell offset code (dx + 1) + 3 (dz + 1) + 9 (dy + 1), bit 31 set for solids.
+// Neighbour list entry (int32): bits 0-24 slot, then the neighbour's cell
+// offset from the particle's cell, 2 bits per axis as d + 1 (x in 25-26, y in
+// 27-28, z in 29-30), bit 31 set for solids.
+//
+// Grids: dense (cell id = offset + y gX gZ + x gZ + z; the three cells of a
+// stencil row are consecutive ids) or hashed (the counting sort runs over
+// hash buckets of cells, see cell_bucket; each slot keeps its packed cell,
+// so the 27-cell walk rejects particles of other cells sharing a bucket --
+// used for domains with more cells than fit a dense table).
 #include "pbf_common.cuh"
 #include "pbf_kernels.h"
 
 namespace lgb {
 
-constexpr int SLOT_BITS = 26;
+constexpr int SLOT_BITS = 25;
 constexpr int SLOT_MASK = (1 << SLOT_BITS) - 1;
 
-__device__ __forceinline__ int entry(int slot, int code, bool solid) {
-    return slot | (code << SLOT_BITS) | (solid ? (int)0x80000000u : 0);
+__device__ __forceinline__ int entry(int slot, int dx, int dy, int dz, bool solid) {
+    return slot | ((dx + 1) << 25) | ((dy + 1) << 27) | ((dz + 1) << 29) | (solid ? (int)0x80000000u : 0);
 }
 __device__ __forceinline__ int entry_slot(int e) { return e & SLOT_MASK; }
 __device__ __forceinline__ bool entry_solid(int e) { return e < 0; }
-__device__ __forceinline__ int entry_code(int e) { return (e >> SLOT_BITS) & 31; }
 // the particle itself: a fluid entry of its own slot (any cell code)
 __device__ __forceinline__ bool entry_is(int e, int s) { return (e & (SLOT_MASK | (int)0x80000000u)) == s; }
+
+// Bucket of a cell in a table of 2^bits buckets.  Cells are grouped in
+// bricks of 4 (x) x 4 (y) x 8 (z); a brick starts at a hashed base
+// (multiply-xorshift mix of its coordinates) and its 128 cells take the
+// consecutive buckets after it (mod the table), so the sort keeps the
+// particles of a brick together and a warp's particles stay neighbours.
+__device__ __forceinline__ int cell_bucket(int3 c, int bits) {
+    unsigned h = ((unsigned)(c.x >> 2) * 0x9E3779B1u) ^ ((unsigned)(c.y >> 2) * 0x85EBCA77u) ^
+                 ((unsigned)(c.z >> 3) * 0xC2B2AE3Du);
+    h ^= h >> 15;
+    h *= 0x2C1B3C6Du;
+    h ^= h >> 13;
+    const unsigned local = (unsigned)((((c.y & 3) << 2) | (c.x & 3)) << 3 | (c.z & 7));
+    return (int)(((h >> (32 - bits)) + local) & ((1u << bits) - 1u));
+}
 
 // ---------------------------------------------------------------- helpers --
 
@@ -92,21 +113,21 @@ __device__ __forceinline__ int3 plain_cell(const StepParams& p, const Geo& g, fl
     return make_int3(min(max(cx, 0), g.gx - 1), min(max(cy, 0), g.gy - 1), min(max(cz, 0), g.gz - 1));
 }
 
-// Offset of the neighbour's cell from the particle's: code -> -(c_j - c_i) * cell
-// as the vector to add to (o_i - o_j).
-__device__ __forceinline__ float3 code_shift(const StepParams& p, int code) {
-    const int dx = code % 3 - 1, dz = (code / 3) % 3 - 1, dy = code / 9 - 1;
-    return make_float3(-(float)dx * p.cell, -(float)dy * p.cell, -(float)dz * p.cell);
+// One axis of the cell shift of an entry: the neighbour's cell is
+// c_i + (bits - 1) on that axis, so (c_i - c_j) * cell = (1 - bits) * cell.
+__device__ __forceinline__ float axis_shift(float cell, int e, int at) {
+    const int b = (e >> at) & 3;
+    return b == 1 ? 0.0f : (b == 0 ? cell : -cell);
 }
 
+// x_i - x_j of a pair from the two stored positions and the list entry.
 template <bool MIXED>
 __device__ __forceinline__ float3 rel_e(const StepParams& p, float4 a, float4 b, int e) {
     float3 d = make_float3(a.x - b.x, a.y - b.y, a.z - b.z);
     if (MIXED) {
-        float3 s = code_shift(p, entry_code(e));
-        d.x += s.x;
-        d.y += s.y;
-        d.z += s.z;
+        d.x += axis_shift(p.cell, e, 25);
+        d.y += axis_shift(p.cell, e, 27);
+        d.z += axis_shift(p.cell, e, 29);
     }
     return d;
 }
@@ -183,11 +204,26 @@ __device__ __forceinline__ float clamp_offset(const StepParams& p, float o, int 
 
 // ---------------------------------------------------------------- kernels --
 
+__device__ __forceinline__ unsigned pack_bits(const CellPack& cp, int3 c) {
+    return (unsigned)c.x | ((unsigned)c.y << cp.by_shift) | ((unsigned)c.z << cp.bz_shift);
+}
+
+// Sort key of a cell: its dense id, or its hash bucket (the packed cell then
+// goes to cellk so the neighbour walk can tell cells sharing a bucket apart).
+__device__ __forceinline__ int cell_key(const StepParams& p, const CellPack& cp, const Geo& g, int3 c,
+                                        int* cellk, int i) {
+    if (!p.hash_bits) return linear_cell(g, c);
+    // a static particle outside the box joins the last packable cell
+    c = make_int3(min(c.x, (int)cp.mx), min(c.y, (int)cp.my), min(c.z, (int)cp.mz));
+    cellk[i] = (int)pack_bits(cp, c);
+    return cell_bucket(c, p.hash_bits);
+}
+
 // Prediction with the box clamp, cell key and histogram.
 template <bool MIXED>
 __global__ void k_predict(StepParams p, CellPack cp, const float4* __restrict__ x,
                           float4* __restrict__ v, float4* __restrict__ xs, int* __restrict__ key,
-                          int* __restrict__ rank, int* __restrict__ count) {
+                          int* __restrict__ rank, int* __restrict__ count, int* __restrict__ cellk) {
     pdl_wait();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
@@ -213,7 +249,7 @@ __global__ void k_predict(StepParams p, CellPack cp, const float4* __restrict__ 
         s = make_float4(ox, oy, oz, 0.0f);
     }
     xs[i] = s;
-    const int k = linear_cell(g, c);
+    const int k = cell_key(p, cp, g, c, cellk, i);
     key[i] = k;
     rank[i] = atomicAdd(&count[k], 1);
 }
@@ -221,13 +257,14 @@ __global__ void k_predict(StepParams p, CellPack cp, const float4* __restrict__ 
 // Cell key and histogram of static particles (solids; scene from solid_scene_of).
 template <bool MIXED>
 __global__ void k_key(StepParams p, CellPack cp, const float4* __restrict__ pos, int m,
-                      int* __restrict__ key, int* __restrict__ rank, int* __restrict__ count) {
+                      int* __restrict__ key, int* __restrict__ rank, int* __restrict__ count,
+                      int* __restrict__ cellk) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m) return;
     float4 q = pos[i];
     const Geo g = p.scenes ? geo_scene(p, p.solid_scene_of[i]) : geo_single(p);
     int3 c = MIXED ? unpack_cell(cp, q.w) : plain_cell(p, g, q.x, q.y, q.z);
-    int k = linear_cell(g, c);
+    int k = cell_key(p, cp, g, c, cellk, i);
     key[i] = k;
     rank[i] = atomicAdd(&count[k], 1);
 }
@@ -288,7 +325,6 @@ __device__ __forceinline__ void walk_row(const StepParams& p, const float4& self
         const int z = z0 + k;
         if (z > z1) break;
         const int dz = z - zc;
-        const int code = (dx + 1) + 3 * (dz + 1) + 9 * (dy + 1);
         const float sz = -(float)dz * p.cell;
         for (int t = b[k]; t < b[k + 1]; t++) {
             if (!SOLID && t == s) continue;
@@ -300,7 +336,7 @@ __device__ __forceinline__ void walk_row(const StepParams& p, const float4& self
                 d.z += sz;
             }
             if (dot3(d.x, d.y, d.z) <= p.h2) {
-                if (c_n < p.max_nbrs) nbr[(size_t)c_n * p.n + s] = entry(t, code, SOLID);
+                if (c_n < p.max_nbrs) nbr[(size_t)c_n * p.n + s] = entry(t, dx, dy, dz, SOLID);
                 c_n++;
                 lambda_accumulate<MIXED>(p, a, d, SOLID);
             }
@@ -308,11 +344,55 @@ __device__ __forceinline__ void walk_row(const StepParams& p, const float4& self
     }
 }
 
+// One cell of the stencil on a hashed grid: the particles of its bucket,
+// kept only if they belong to that cell.
+template <bool MIXED, bool SOLID>
+__device__ __forceinline__ void walk_hashed_cell(const StepParams& p, const CellPack& cp,
+                                                 const float4& self, int s,
+                                                 const float4* __restrict__ pos,
+                                                 const int* __restrict__ start,
+                                                 const int* __restrict__ cells, int3 cn, int dx,
+                                                 int dy, int dz, LambdaAcc& a, int& c_n,
+                                                 int* __restrict__ nbr) {
+    const int packed = (int)pack_bits(cp, cn);
+    const int b = cell_bucket(cn, p.hash_bits);
+    const float sx = -(float)dx * p.cell, sy = -(float)dy * p.cell, sz = -(float)dz * p.cell;
+    for (int t = start[b], e = start[b + 1]; t < e; t++) {
+        if ((!SOLID && t == s) || __ldg(&cells[t]) != packed) continue;
+        const float4 q = SOLID ? __ldg(&pos[t]) : pos[t];
+        float3 d = make_float3(self.x - q.x, self.y - q.y, self.z - q.z);
+        if (MIXED) {
+            d.x += sx;
+            d.y += sy;
+            d.z += sz;
+        }
+        if (dot3(d.x, d.y, d.z) <= p.h2) {
+            if (c_n < p.max_nbrs) nbr[(size_t)c_n * p.n + s] = entry(t, dx, dy, dz, SOLID);
+            c_n++;
+            lambda_accumulate<MIXED>(p, a, d, SOLID);
+        }
+    }
+}
+
+// Cell of fluid slot s in the current step: from its packed cell on a
+// hashed grid, from its dense key otherwise.
+__device__ __forceinline__ int3 slot_cell(const StepParams& p, const CellPack& cp, const Geo& g,
+                                          const int* __restrict__ key_sorted,
+                                          const int* __restrict__ cell_sorted, int s) {
+    if (p.hash_bits) {
+        const unsigned u = (unsigned)__ldg(&cell_sorted[s]);
+        return make_int3((int)(u & cp.mx), (int)((u >> cp.by_shift) & cp.my), (int)((u >> cp.bz_shift) & cp.mz));
+    }
+    return decode_cell(g, __ldg(&key_sorted[s]));
+}
+
 template <bool MIXED, int B>
-__global__ void __launch_bounds__(B) k_lists_lambda(StepParams p, float4* __restrict__ xs,
+__global__ void __launch_bounds__(B) k_lists_lambda(StepParams p, CellPack cp, float4* __restrict__ xs,
                                                     const int* __restrict__ key_sorted,
+                                                    const int* __restrict__ cell_sorted,
                                                     const int* __restrict__ fstart,
                                                     const float4* __restrict__ solid,
+                                                    const int* __restrict__ solid_cell,
                                                     const int* __restrict__ sstart,
                                                     int* __restrict__ nbr, int* __restrict__ cnt,
                                                     float* __restrict__ rho, int* status) {
@@ -321,7 +401,7 @@ __global__ void __launch_bounds__(B) k_lists_lambda(StepParams p, float4* __rest
     if (s >= p.n) return;
     const float4 self = xs[s];
     const Geo g = geo_slot(p, s);
-    const int3 c = decode_cell(g, key_sorted[s]);
+    const int3 c = slot_cell(p, cp, g, key_sorted, cell_sorted, s);
     LambdaAcc a = lambda_init(p);
     int c_n = 0;
     const int slab = g.gx * g.gz;
@@ -331,6 +411,20 @@ __global__ void __launch_bounds__(B) k_lists_lambda(StepParams p, float4* __rest
         for (int dx = -1; dx <= 1; dx++) {
             const int xx = c.x + dx;
             if (xx < 0 || xx >= g.gx) continue;
+            if (p.hash_bits) {
+                // cells past the packed field widths hold no particle
+                if (xx > (int)cp.mx || y > (int)cp.my) continue;
+                // the dense walk's entry order: the row's fluid cells, then its solid cells
+                const int z0 = max(c.z - 1, 0), z1 = min(min(c.z + 1, g.gz - 1), (int)cp.mz);
+                for (int z = z0; z <= z1; z++)
+                    walk_hashed_cell<MIXED, false>(p, cp, self, s, xs, fstart, cell_sorted, make_int3(xx, y, z),
+                                                   dx, dy, z - c.z, a, c_n, nbr);
+                if (p.ns > 0)
+                    for (int z = z0; z <= z1; z++)
+                        walk_hashed_cell<MIXED, true>(p, cp, self, s, solid, sstart, solid_cell,
+                                                      make_int3(xx, y, z), dx, dy, z - c.z, a, c_n, nbr);
+                continue;
+            }
             const int row = g.off + y * slab + xx * g.gz;
             walk_row<MIXED, false>(p, self, s, xs, fstart, row, c.z, g.gz, dx, dy, a, c_n, nbr);
             if (p.ns > 0)
@@ -451,7 +545,7 @@ __global__ void __launch_bounds__(B) k_delta(StepParams p, CellPack cp, const fl
         out = make_float4(clampf(self.x + dx, g.lox, g.hix), clampf(self.y + dy, g.loy, g.hiy),
                           clampf(self.z + dz, g.loz, g.hiz), 0.0f);
     } else {
-        cs = decode_cell(g, key_sorted[s]);
+        cs = slot_cell(p, cp, g, key_sorted, p.cell_sorted, s);
         out = make_float4(clamp_offset(p, self.x + dx, cs.x, g.lox, g.hix),
                           clamp_offset(p, self.y + dy, cs.y, g.loy, g.hiy),
                           clamp_offset(p, self.z + dz, cs.z, g.loz, g.hiz), 0.0f);
@@ -515,7 +609,7 @@ __global__ void __launch_bounds__(B) k_xsph(StepParams p, CellPack cp, const flo
     if (!MIXED) {
         x_out[s] = make_float4(self.x, self.y, self.z, 0.0f);
     } else {
-        int3 cs = decode_cell(geo_slot(p, s), key_sorted[s]);
+        int3 cs = slot_cell(p, cp, geo_slot(p, s), key_sorted, p.cell_sorted, s);
         x_out[s] = make_float4(self.x, self.y, self.z, pack_cell(cp, cs.x, cs.y, cs.z));
     }
 }
@@ -655,15 +749,15 @@ static inline int blocks_for(int n, int t) { return (n + t - 1) / t; }
     } while (0)
 
 void launch_predict(bool mixed, const StepParams& p, const CellPack& cp, const float4* x, float4* v,
-                    float4* xs, int* key, int* rank, int* count, cudaStream_t st) {
+                    float4* xs, int* key, int* rank, int* count, int* cellk, cudaStream_t st) {
     if (p.n <= 0) return;
-    LGB_DISPATCH(mixed, k_predict, blocks_for(p.n, 256), 256, st, p, cp, x, v, xs, key, rank, count);
+    LGB_DISPATCH(mixed, k_predict, blocks_for(p.n, 256), 256, st, p, cp, x, v, xs, key, rank, count, cellk);
 }
 
 void launch_key(bool mixed, const StepParams& p, const CellPack& cp, const float4* pos, int m,
-                int* key, int* rank, int* count, cudaStream_t st) {
+                int* key, int* rank, int* count, int* cellk, cudaStream_t st) {
     if (m <= 0) return;
-    LGB_DISPATCH(mixed, k_key, blocks_for(m, 256), 256, st, p, cp, pos, m, key, rank, count);
+    LGB_DISPATCH(mixed, k_key, blocks_for(m, 256), 256, st, p, cp, pos, m, key, rank, count, cellk);
 }
 
 // Kernels templated on (MIXED, U, B) are instantiated for U in {1, 2, 4} and
@@ -696,16 +790,16 @@ void launch_key(bool mixed, const StepParams& p, const CellPack& cp, const float
             TUNE_CASE(KERNEL, false, tu, N, ST, __VA_ARGS__);                                   \
     } while (0)
 
-void launch_lists_lambda(bool mixed, const Tuning& tu, const StepParams& p, float4* xs,
-                         const int* key_sorted, const int* fstart, const float4* solid,
-                         const int* sstart, int* nbr, int* cnt, float* rho, int* status,
-                         cudaStream_t st) {
+void launch_lists_lambda(bool mixed, const Tuning& tu, const StepParams& p, const CellPack& cp,
+                         float4* xs, const int* key_sorted, const int* cell_sorted, const int* fstart,
+                         const float4* solid, const int* solid_cell, const int* sstart, int* nbr,
+                         int* cnt, float* rho, int* status, cudaStream_t st) {
     if (p.n <= 0) return;
     const int B = tu.list_block <= 64 ? 64 : (tu.list_block <= 128 ? 128 : 256);
     const bool pdl = pdl_enabled();
 #define LGB_LISTS(MIX, BB)                                                                      \
-    launch_k(k_lists_lambda<MIX, BB>, blocks_for(p.n, BB), BB, st, pdl, p, xs, key_sorted, fstart, \
-             solid, sstart, nbr, cnt, rho, status)
+    launch_k(k_lists_lambda<MIX, BB>, blocks_for(p.n, BB), BB, st, pdl, p, cp, xs, key_sorted,  \
+             cell_sorted, fstart, solid, solid_cell, sstart, nbr, cnt, rho, status)
     if (mixed) {
         if (B == 64) LGB_LISTS(true, 64);
         else if (B == 128) LGB_LISTS(true, 128);

@@ -34,7 +34,8 @@ def reference_params(X, Y, Z, radius=0.5, kernel_radius_scale=2.0) -> PbfParams:
 
 def pbf_params(X, Y, Z, *, radius=0.5, h=1.0, rest_density=1.0, mass=1.0, gravity=-9.81,
                iterations=4, s_corr_k=0.1, s_corr_n=4.0, s_corr_dq_frac=0.2, c_xsph=0.01,
-               epsilon=10.0, precision=PRECISION_FP32, max_neighbors=64, use_graph=True) -> PbfParams:
+               epsilon=10.0, precision=PRECISION_FP32, max_neighbors=64, use_graph=True,
+               grid_mode=0) -> PbfParams:
     """PBF-mode parameters of the benchmark scenes (dam breaks at unit spacing)."""
     p = reference_params(X, Y, Z, radius, h / radius)
     p.mode = MODE_PBF
@@ -51,6 +52,7 @@ def pbf_params(X, Y, Z, *, radius=0.5, h=1.0, rest_density=1.0, mass=1.0, gravit
     p.solid_contact = 2.0 * radius
     p.max_neighbors = max_neighbors
     p.use_graph = 1 if use_graph else 0
+    p.grid_mode = grid_mode
     return p
 
 

@@ -2,6 +2,7 @@
 statistics.
 
     python -m lustrine_gb300.run_scene --config config2 --steps 5 [--mixed] [--no-graph]
+        [--grid auto|dense|hashed] [--stages]
 
 Used for profiling captures of a single configuration (a fixed, short
 sequence of launches) and as a quick end-to-end check of an installation.
@@ -17,16 +18,19 @@ from . import PRECISION_FP32, PRECISION_MIXED, PbfSim, pbf_params, scenes
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("--config", default="config1", choices=["config0", "config1", "config2"])
+    ap.add_argument("--config", default="config1", choices=["config0", "config1", "config2", "config4"])
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--mixed", action="store_true")
     ap.add_argument("--no-graph", action="store_true")
     ap.add_argument("--max-neighbors", type=int, default=64)
+    ap.add_argument("--grid", default="auto", choices=["auto", "dense", "hashed"])
+    ap.add_argument("--stages", action="store_true", help="also print per-stage device ms")
     a = ap.parse_args(argv)
     sc = getattr(scenes, a.config)()
     p = pbf_params(*sc.domain, iterations=sc.iterations, c_xsph=sc.c_xsph,
                    precision=PRECISION_MIXED if a.mixed else PRECISION_FP32,
-                   max_neighbors=a.max_neighbors, use_graph=not a.no_graph)
+                   max_neighbors=a.max_neighbors, use_graph=not a.no_graph,
+                   grid_mode=["auto", "dense", "hashed"].index(a.grid))
     with PbfSim(p, sc.n, sc.ns) as sim:
         sim.upload(sc.x, None, sc.solid if sc.ns else None)
         t0 = time.perf_counter()
@@ -37,6 +41,8 @@ def main(argv=None):
         out = {"config": sc.name, "n": sc.n, "ns": sc.ns, "steps": a.steps,
                "wall_ms_per_step": wall / max(a.steps, 1) * 1e3, "status": sim.status(),
                "kinetic": r["kinetic"], "com": r["com"], "max_density_error": r["max_density_error"]}
+        if a.stages:
+            out["stage_ms"] = {k: round(v[0], 4) for k, v in sim.profile_step(sc.dt).items()}
     print(json.dumps(out))
     return 0 if out["status"] == 0 else 1
 

@@ -37,7 +37,7 @@ def test_struct_layouts_match_reference_abi():
     assert GridWrapper.color.offset == 16 and GridWrapper.position.offset == 32
     assert GridWrapper.has_one_color_per_cell.offset == 44 and GridWrapper.X.offset == 48
     assert GridWrapper.type.offset == 68 and C.sizeof(GridWrapper) == 72
-    assert C.sizeof(PbfParams) == 4 * 24  # 24 four-byte fields
+    assert C.sizeof(PbfParams) == 4 * 25  # 25 four-byte fields
 
 
 def test_error_strings_and_reference_params_need_no_gpu():
