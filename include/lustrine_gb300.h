@@ -257,7 +257,7 @@ LUSTRINE_API int lustrine_pbf_profile_step(lustrine_pbf* s, float dt, double* st
                                            int* stage_launches, int num_stages);
 /* Launch shape of the PBF iteration kernels (lambda, delta-p, XSPH) and of
  * the neighbour-list build.  block and list_block: 64, 128 or 256 threads;
- * unroll: neighbour gathers in flight per thread, 1, 2 or 4. */
+ * unroll: neighbour gathers in flight per thread, 1, 2, 4 or 8. */
 typedef struct lustrine_pbf_tuning {
     int block;
     int unroll;

@@ -58,6 +58,8 @@ struct StepParams {
     float kfac, cubic_k, cubic_l;
     // PBF kernels: poly6 K6 (h^2 - r^2)^3, spiky gradient -Ks (h - r)^2 d / r
     float k6, ks, inv_w_dq;
+    float k6m;            // m K6
+    float inv_hdq2;       // 1 / (h^2 - dq^2) (0 when dq >= h: no s_corr)
     float mass, rho0, eps;
     float mr;             // mass / rho0
     float self_density;   // m W(0) = m K6 h^6 (the particle's own density term)

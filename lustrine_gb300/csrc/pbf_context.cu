@@ -130,7 +130,9 @@ static int derive(const lustrine_pbf_params& q, int n, int ns, StepParams* sp, C
         double d = h * h - (double)q.s_corr_dq * (double)q.s_corr_dq;
         double wdq = q.s_corr_dq <= q.kernel_radius ? 315.0 / (64.0 * kPi * std::pow(h, 9)) * d * d * d : 0.0;
         p.inv_w_dq = wdq > 0.0 ? (float)(1.0 / wdq) : 0.0f;
+        p.inv_hdq2 = (wdq > 0.0 && q.s_corr_k != 0.0f) ? (float)(1.0 / d) : 0.0f;
     }
+    p.k6m = (float)((double)q.mass * 315.0 / (64.0 * kPi * std::pow(h, 9)));
     p.mass = q.mass;
     p.rho0 = q.rest_density;
     p.mr = q.mass / q.rest_density;
@@ -707,7 +709,7 @@ extern "C" int lustrine_pbf_profile_step(lustrine_pbf* s, float dt, double* stag
 extern "C" int lustrine_pbf_set_tuning(lustrine_pbf* s, const lustrine_pbf_tuning* t) {
     if (!s || !t) return LUSTRINE_ERR_ARGS;
     auto ok = [](int b) { return b == 64 || b == 128 || b == 256; };
-    if (!ok(t->block) || !ok(t->list_block) || (t->unroll != 1 && t->unroll != 2 && t->unroll != 4))
+    if (!ok(t->block) || !ok(t->list_block) || (t->unroll != 1 && t->unroll != 2 && t->unroll != 4 && t->unroll != 8))
         return LUSTRINE_ERR_ARGS;
     s->tune = Tuning{t->block, t->unroll, t->list_block};
     s->invalidate_graphs();
@@ -795,10 +797,10 @@ extern "C" int lustrine_pbf_autotune(lustrine_pbf* s, float dt, int steps, lustr
     Tuning keep = s->tune, top = s->tune;
     float top_ms = 3.4e38f;
     static const int blocks[3] = {64, 128, 256};
-    static const int unrolls[3] = {1, 2, 4};
+    static const int unrolls[4] = {1, 2, 4, 8};
     // the iteration kernels' shape first, then the list build's block size
     for (int bi = 0; bi < 3 && !rc; bi++)
-        for (int ui = 0; ui < 3 && !rc; ui++) {
+        for (int ui = 0; ui < 4 && !rc; ui++) {
             s->tune = Tuning{blocks[bi], unrolls[ui], keep.list_block};
             s->invalidate_graphs();
             float ms = 0.0f;

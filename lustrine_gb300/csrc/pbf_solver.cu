@@ -48,14 +48,19 @@ __device__ __forceinline__ bool entry_is(int e, int s) { return (e & (SLOT_MASK 
 // (multiply-xorshift mix of its coordinates) and its 128 cells take the
 // consecutive buckets after it (mod the table), so the sort keeps the
 // particles of a brick together and a warp's particles stay neighbours.
-__device__ __forceinline__ int cell_bucket(int3 c, int bits) {
-    unsigned h = ((unsigned)(c.x >> 2) * 0x9E3779B1u) ^ ((unsigned)(c.y >> 2) * 0x85EBCA77u) ^
-                 ((unsigned)(c.z >> 3) * 0xC2B2AE3Du);
+__device__ __forceinline__ unsigned brick_base(int bx, int by, int bz, int bits) {
+    unsigned h = ((unsigned)bx * 0x9E3779B1u) ^ ((unsigned)by * 0x85EBCA77u) ^ ((unsigned)bz * 0xC2B2AE3Du);
     h ^= h >> 15;
     h *= 0x2C1B3C6Du;
     h ^= h >> 13;
+    return h >> (32 - bits);
+}
+__device__ __forceinline__ int brick_bucket(unsigned base, int3 c, int bits) {
     const unsigned local = (unsigned)((((c.y & 3) << 2) | (c.x & 3)) << 3 | (c.z & 7));
-    return (int)(((h >> (32 - bits)) + local) & ((1u << bits) - 1u));
+    return (int)((base + local) & ((1u << bits) - 1u));
+}
+__device__ __forceinline__ int cell_bucket(int3 c, int bits) {
+    return brick_bucket(brick_base(c.x >> 2, c.y >> 2, c.z >> 3, bits), c, bits);
 }
 
 // ---------------------------------------------------------------- helpers --
@@ -132,39 +137,36 @@ __device__ __forceinline__ float3 rel_e(const StepParams& p, float4 a, float4 b,
     return d;
 }
 
-__device__ __forceinline__ float poly6(const StepParams& p, float r2) {
-    float d = p.h2 - r2;
-    return r2 <= p.h2 ? p.k6 * d * d * d : 0.0f;
+// Pair terms.  The kernels are issue-bound, so the pair loops keep only the
+// r-dependent factors and the constants are applied once per particle:
+//   poly6        W(r)  = K6 hd^3,            hd = max(h^2 - r^2, 0)
+//   spiky        dW(d) = -Ks g d,            g  = max(h - r, 0)^2 / r
+//   s_corr       -k (W(r) / W(dq))^n,        W(r) / W(dq) = (hd / (h^2 - dq^2))^3
+// r and 1/r come from one reciprocal square root of max(r^2, 1e-30): at
+// r = 0 the offset d is 0 and every pair term with it.
+__device__ __forceinline__ float hdiff(const StepParams& p, float r2) { return fmaxf(p.h2 - r2, 0.0f); }
+
+__device__ __forceinline__ float inv_r_of(float r2) { return rsqrtf(fmaxf(r2, 1e-30f)); }
+
+__device__ __forceinline__ float spiky_g(const StepParams& p, float r, float inv_r) {
+    const float f = fmaxf(p.h - r, 0.0f);
+    return f * f * inv_r;
 }
 
-// Distance terms of a pair from r^2: r and 1/r from one reciprocal square
-// root (the PBF kernels are issue-bound; an IEEE sqrt and divide per pair
-// cost more than the rest of the pair's arithmetic).
-struct PairR {
-    float r, inv_r;
-};
-__device__ __forceinline__ PairR pair_r(float r2) {
-    const float inv_r = r2 > 0.0f ? rsqrtf(r2) : 0.0f;
-    return PairR{r2 * inv_r, inv_r};
-}
-
-// spiky gradient as a factor on the offset: dW(d) = f * d
-__device__ __forceinline__ float spiky_factor(const StepParams& p, PairR q) {
-    const float f = p.h - q.r;
-    return (q.inv_r > 0.0f && q.r <= p.h) ? -p.ks * f * f * q.inv_r : 0.0f;
-}
-
-__device__ __forceinline__ float scorr(const StepParams& p, float r2) {
-    float t = poly6(p, r2) * p.inv_w_dq;
+__device__ __forceinline__ float scorr_hd(const StepParams& p, float hd) {
+    const float x = hd * p.inv_hdq2;
     float pw;
-    if (p.sn_int == 4) {
-        float t2 = t * t;
-        pw = t2 * t2;
-    } else if (p.sn_int >= 0) {
-        pw = 1.0f;
-        for (int e = 0; e < p.sn_int; e++) pw *= t;
+    if (p.sn_int == 4) {  // (x^3)^4
+        const float x2 = x * x, x4 = x2 * x2;
+        pw = x4 * x4 * x4;
     } else {
-        pw = powf(t, p.sn);
+        const float t = x * x * x;
+        if (p.sn_int >= 0) {
+            pw = 1.0f;
+            for (int e = 0; e < p.sn_int; e++) pw *= t;
+        } else {
+            pw = powf(t, p.sn);
+        }
     }
     return -p.sk * pw;
 }
@@ -274,37 +276,45 @@ __global__ void k_key(StepParams p, CellPack cp, const float4* __restrict__ pos,
 // constraint over the accepted neighbours.  The particle itself is not in
 // its list: its density term m W(0) starts the sum and it has no gradient.
 struct LambdaAcc {
-    float density, comp, S, gx, gy, gz;
+    float wsum, comp, S, gx, gy, gz;  // sum of hd^3 (compensated in mixed), sum g^2 r^2, sum g d
 };
 
-__device__ __forceinline__ LambdaAcc lambda_init(const StepParams& p) {
-    return LambdaAcc{p.self_density, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+__device__ __forceinline__ LambdaAcc lambda_init(const StepParams&) {
+    return LambdaAcc{0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
 }
 
 template <bool MIXED>
 __device__ __forceinline__ void lambda_accumulate(const StepParams& p, LambdaAcc& a, float3 d,
                                                   bool solid) {
     const float r2 = dot3(d.x, d.y, d.z);
-    const float w = p.mass * poly6(p, r2);
+    const float hd = hdiff(p, r2);
+    const float w = hd * hd * hd;
     if (MIXED) {
         float y = w - a.comp;
-        float t = a.density + y;
-        a.comp = (t - a.density) - y;
-        a.density = t;
+        float t = a.wsum + y;
+        a.comp = (t - a.wsum) - y;
+        a.wsum = t;
     } else {
-        a.density += w;
+        a.wsum += w;
     }
-    const float f = spiky_factor(p, pair_r(r2)) * p.mr;
-    const float ax = f * d.x, ay = f * d.y, az = f * d.z;
-    if (!solid) a.S += dot3(ax, ay, az);
-    a.gx += ax;
-    a.gy += ay;
-    a.gz += az;
+    const float inv_r = inv_r_of(r2);
+    const float g = spiky_g(p, r2 * inv_r, inv_r);
+    if (!solid) a.S += g * g * r2;
+    a.gx += g * d.x;
+    a.gy += g * d.y;
+    a.gz += g * d.z;
 }
 
+// rho = m W(0) + m K6 sum hd^3
+__device__ __forceinline__ float density_of(const StepParams& p, const LambdaAcc& a) {
+    return p.self_density + p.k6m * a.wsum;
+}
+
+// lambda = -(rho / rho0 - 1) / (S + eps), S = (Ks m / rho0)^2 (sum g^2 r^2 + |sum g d|^2)
 __device__ __forceinline__ float lambda_of(const StepParams& p, const LambdaAcc& a) {
-    const float S = a.S + dot3(a.gx, a.gy, a.gz);
-    return -(a.density / p.rho0 - 1.0f) / (S + p.eps);
+    const float c = p.ks * p.mr;
+    const float S = c * c * (a.S + dot3(a.gx, a.gy, a.gz));
+    return -(density_of(p, a) / p.rho0 - 1.0f) / (S + p.eps);
 }
 
 // One row (dy, dx) of the stencil: the cells z0..z1 of a row are consecutive
@@ -347,15 +357,12 @@ __device__ __forceinline__ void walk_row(const StepParams& p, const float4& self
 // One cell of the stencil on a hashed grid: the particles of its bucket,
 // kept only if they belong to that cell.
 template <bool MIXED, bool SOLID>
-__device__ __forceinline__ void walk_hashed_cell(const StepParams& p, const CellPack& cp,
-                                                 const float4& self, int s,
+__device__ __forceinline__ void walk_hashed_cell(const StepParams& p, const float4& self, int s,
                                                  const float4* __restrict__ pos,
                                                  const int* __restrict__ start,
-                                                 const int* __restrict__ cells, int3 cn, int dx,
-                                                 int dy, int dz, LambdaAcc& a, int& c_n,
+                                                 const int* __restrict__ cells, int b, int packed,
+                                                 int dx, int dy, int dz, LambdaAcc& a, int& c_n,
                                                  int* __restrict__ nbr) {
-    const int packed = (int)pack_bits(cp, cn);
-    const int b = cell_bucket(cn, p.hash_bits);
     const float sx = -(float)dx * p.cell, sy = -(float)dy * p.cell, sz = -(float)dz * p.cell;
     for (int t = start[b], e = start[b + 1]; t < e; t++) {
         if ((!SOLID && t == s) || __ldg(&cells[t]) != packed) continue;
@@ -386,7 +393,7 @@ __device__ __forceinline__ int3 slot_cell(const StepParams& p, const CellPack& c
     return decode_cell(g, __ldg(&key_sorted[s]));
 }
 
-template <bool MIXED, int B>
+template <bool MIXED, bool HASHED, int B>
 __global__ void __launch_bounds__(B) k_lists_lambda(StepParams p, CellPack cp, float4* __restrict__ xs,
                                                     const int* __restrict__ key_sorted,
                                                     const int* __restrict__ cell_sorted,
@@ -411,18 +418,24 @@ __global__ void __launch_bounds__(B) k_lists_lambda(StepParams p, CellPack cp, f
         for (int dx = -1; dx <= 1; dx++) {
             const int xx = c.x + dx;
             if (xx < 0 || xx >= g.gx) continue;
-            if (p.hash_bits) {
+            if (HASHED) {
                 // cells past the packed field widths hold no particle
                 if (xx > (int)cp.mx || y > (int)cp.my) continue;
                 // the dense walk's entry order: the row's fluid cells, then its solid cells
                 const int z0 = max(c.z - 1, 0), z1 = min(min(c.z + 1, g.gz - 1), (int)cp.mz);
-                for (int z = z0; z <= z1; z++)
-                    walk_hashed_cell<MIXED, false>(p, cp, self, s, xs, fstart, cell_sorted, make_int3(xx, y, z),
+                for (int z = z0; z <= z1; z++) {
+                    const int3 cn = make_int3(xx, y, z);
+                    walk_hashed_cell<MIXED, false>(p, self, s, xs, fstart, cell_sorted,
+                                                   cell_bucket(cn, p.hash_bits), (int)pack_bits(cp, cn),
                                                    dx, dy, z - c.z, a, c_n, nbr);
+                }
                 if (p.ns > 0)
-                    for (int z = z0; z <= z1; z++)
-                        walk_hashed_cell<MIXED, true>(p, cp, self, s, solid, sstart, solid_cell,
-                                                      make_int3(xx, y, z), dx, dy, z - c.z, a, c_n, nbr);
+                    for (int z = z0; z <= z1; z++) {
+                        const int3 cn = make_int3(xx, y, z);
+                        walk_hashed_cell<MIXED, true>(p, self, s, solid, sstart, solid_cell,
+                                                      cell_bucket(cn, p.hash_bits), (int)pack_bits(cp, cn),
+                                                      dx, dy, z - c.z, a, c_n, nbr);
+                    }
                 continue;
             }
             const int row = g.off + y * slab + xx * g.gz;
@@ -438,7 +451,7 @@ __global__ void __launch_bounds__(B) k_lists_lambda(StepParams p, CellPack cp, f
     cnt[s] = c_n;
     // lambda into w in place: neighbours read only xyz of this element here
     reinterpret_cast<float*>(xs)[4 * (size_t)s + 3] = lambda_of(p, a);
-    if (rho) rho[s] = a.density;
+    if (rho) rho[s] = density_of(p, a);
 }
 
 // Walk a particle's list U entries at a time, calling f(entry, position)
@@ -493,7 +506,7 @@ __global__ void __launch_bounds__(B) k_lambda(StepParams p, float4* __restrict__
         lambda_accumulate<MIXED>(p, a, d, entry_solid(e));
     });
     reinterpret_cast<float*>(xs)[4 * (size_t)s + 3] = lambda_of(p, a);
-    if (rho) rho[s] = a.density;
+    if (rho) rho[s] = density_of(p, a);
 }
 
 // Position correction with s_corr, solid push-out and box clamp (Jacobi).
@@ -517,21 +530,24 @@ __global__ void __launch_bounds__(B) k_delta(StepParams p, CellPack cp, const fl
         const bool sol = entry_solid(e);
         float3 d = rel_e<MIXED>(p, self, q, e);
         const float r2 = dot3(d.x, d.y, d.z);
-        const PairR pr = pair_r(r2);
+        const float inv_r = inv_r_of(r2);
+        const float r = r2 * inv_r;
         const float lj = sol ? li : q.w;
-        const float w = (li + lj + scorr(p, r2)) * spiky_factor(p, pr);
+        const float w = (li + lj + scorr_hd(p, hdiff(p, r2))) * spiky_g(p, r, inv_r);
         px += w * d.x;
         py += w * d.y;
         pz += w * d.z;
-        if (sol && pr.r < p.contact && pr.inv_r > 0.0f) {
-            const float t = (p.contact - pr.r) * pr.inv_r;
+        if (sol && r < p.contact && r2 > 0.0f) {
+            const float t = (p.contact - r) * inv_r;
             cx += t * d.x;
             cy += t * d.y;
             cz += t * d.z;
             nct++;
         }
     });
-    float dx = px * p.mr, dy = py * p.mr, dz = pz * p.mr;
+    // dp = (m / rho0) sum (lambda_i + lambda_j + s_corr) dW, dW = -Ks g d
+    const float kd = -p.ks * p.mr;
+    float dx = px * kd, dy = py * kd, dz = pz * kd;
     if (nct) {
         const float inv = __frcp_rn((float)nct);
         dx += cx * inv;
@@ -598,14 +614,17 @@ __global__ void __launch_bounds__(B) k_xsph(StepParams p, CellPack cp, const flo
                 if (k + u >= c) break;
                 if (entry_is(e[u], s)) continue;
                 float3 d = rel_e<MIXED>(p, self, q[u], e[u]);
-                const float w = poly6(p, dot3(d.x, d.y, d.z));
+                const float hd = hdiff(p, dot3(d.x, d.y, d.z));
+                const float w = hd * hd * hd;
                 ax += (vj[u].x - vi.x) * w;
                 ay += (vj[u].y - vi.y) * w;
                 az += (vj[u].z - vi.z) * w;
             }
         }
     }
-    v_out[s] = make_float4(vi.x + p.c_xsph * ax, vi.y + p.c_xsph * ay, vi.z + p.c_xsph * az, 0.0f);
+    // v += c sum (v_j - v_i) W, W = K6 hd^3
+    const float cx = p.c_xsph * p.k6;
+    v_out[s] = make_float4(vi.x + cx * ax, vi.y + cx * ay, vi.z + cx * az, 0.0f);
     if (!MIXED) {
         x_out[s] = make_float4(self.x, self.y, self.z, 0.0f);
     } else {
@@ -779,8 +798,10 @@ void launch_key(bool mixed, const StepParams& p, const CellPack& cp, const float
             TUNE_BLOCKS(KERNEL, MIX, 1, tu, N, ST, __VA_ARGS__);                                \
         else if (tu.unroll == 2)                                                                \
             TUNE_BLOCKS(KERNEL, MIX, 2, tu, N, ST, __VA_ARGS__);                                \
-        else                                                                                    \
+        else if (tu.unroll == 4)                                                                \
             TUNE_BLOCKS(KERNEL, MIX, 4, tu, N, ST, __VA_ARGS__);                                \
+        else                                                                                    \
+            TUNE_BLOCKS(KERNEL, MIX, 8, tu, N, ST, __VA_ARGS__);                                \
     } while (0)
 #define TUNE_DISPATCH(KERNEL, mixed, tu, N, ST, ...)                                            \
     do {                                                                                        \
@@ -797,9 +818,14 @@ void launch_lists_lambda(bool mixed, const Tuning& tu, const StepParams& p, cons
     if (p.n <= 0) return;
     const int B = tu.list_block <= 64 ? 64 : (tu.list_block <= 128 ? 128 : 256);
     const bool pdl = pdl_enabled();
-#define LGB_LISTS(MIX, BB)                                                                      \
-    launch_k(k_lists_lambda<MIX, BB>, blocks_for(p.n, BB), BB, st, pdl, p, cp, xs, key_sorted,  \
+#define LGB_LISTS_H(MIX, H, BB)                                                                 \
+    launch_k(k_lists_lambda<MIX, H, BB>, blocks_for(p.n, BB), BB, st, pdl, p, cp, xs, key_sorted, \
              cell_sorted, fstart, solid, solid_cell, sstart, nbr, cnt, rho, status)
+#define LGB_LISTS(MIX, BB)                       \
+    do {                                         \
+        if (p.hash_bits) LGB_LISTS_H(MIX, true, BB); \
+        else LGB_LISTS_H(MIX, false, BB);        \
+    } while (0)
     if (mixed) {
         if (B == 64) LGB_LISTS(true, 64);
         else if (B == 128) LGB_LISTS(true, 128);
@@ -810,6 +836,7 @@ void launch_lists_lambda(bool mixed, const Tuning& tu, const StepParams& p, cons
         else LGB_LISTS(false, 256);
     }
 #undef LGB_LISTS
+#undef LGB_LISTS_H
 }
 
 void launch_lambda(bool mixed, const Tuning& tu, const StepParams& p, float4* xs, const int* nbr,

@@ -94,9 +94,11 @@ def _density_at(sim_params, x, n):
 
 @pytest.mark.parametrize("offset", [0.0, 3900.0])
 def test_density_error_vs_fp64_near_and_far_from_origin(orc, offset):
-    """The same 10k block at the origin and 3,900 cells away: mixed precision
-    (cell index + offset, Kahan sums) stays within 1e-4 relative density error
-    of FP64 at both; plain fp32 positions lose resolution far away."""
+    """The same 10k block at the origin and 3,900 cells away: the lambda pass
+    at given positions stays within 1e-4 relative density error of FP64 in
+    both precisions (pair offsets of nearby fp32 positions are exact; the
+    resolution plain fp32 loses far away shows along a trajectory, which
+    tests/test_gpu_hashed.py::test_far_blob_trajectory_vs_fp64 checks)."""
     from lustrine_gb300 import PRECISION_MIXED, pbf_params, scenes
     rng = np.random.default_rng(31)
     # the block starts one cell above the floor so no particle is clamped by
@@ -112,10 +114,7 @@ def test_density_error_vs_fp64_near_and_far_from_origin(orc, offset):
         rho64 = orc.pbf_density(q, x.astype(np.float64))
         errs[prec] = np.abs(rho - rho64).max() / np.abs(rho64).max()
     assert errs[PRECISION_MIXED] <= 1e-4, errs
-    if offset == 0.0:
-        assert errs[0] <= 1e-4, errs
-    else:
-        assert errs[0] > errs[PRECISION_MIXED], errs
+    assert errs[0] <= 1e-4, errs
 
 
 def test_mixed_one_step_matches_fp64_oracle(orc):
@@ -160,11 +159,11 @@ def test_autotune_keeps_state_and_all_shapes_agree():
     best, ms = sim.autotune(sc.dt, steps=2)
     after = sim.download()
     assert np.array_equal(before[0], after[0]) and np.array_equal(before[1], after[1])
-    assert best["block"] in (64, 128, 256) and best["unroll"] in (1, 2, 4) and ms > 0
+    assert best["block"] in (64, 128, 256) and best["unroll"] in (1, 2, 4, 8) and ms > 0
     assert sim.get_tuning() == best
     # every launch shape computes the same step (same summation order)
     ref = None
-    for blk, unr in ((64, 1), (128, 2), (256, 4)):
+    for blk, unr in ((64, 1), (128, 2), (256, 4), (128, 8)):
         sim.upload(before[0], before[1])
         sim.set_tuning(blk, unr, blk)
         sim.step(sc.dt)
