@@ -123,6 +123,13 @@ inline void launch_k(void (*kernel)(KArgs...), int grid, int block, cudaStream_t
 void set_pdl(bool on);
 bool pdl_enabled();
 
+// Cell scan of the step: tiles of CELL_TILE cells, one block each.
+constexpr int CELL_SCAN_THREADS = 256;
+constexpr int CELL_SCAN_ITEMS = 16;
+constexpr int CELL_TILE_SHIFT = 12;
+constexpr int CELL_TILE = 1 << CELL_TILE_SHIFT;  // CELL_SCAN_THREADS * CELL_SCAN_ITEMS
+constexpr int CELL_SCAN_MAX_TILES = 4096;         // 16.7 M cells
+
 __device__ __forceinline__ void set_status(int* status, int bit) {
     if ((*(volatile int*)status & bit) == 0) atomicOr(status, bit);
 }

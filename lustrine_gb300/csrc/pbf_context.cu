@@ -184,7 +184,7 @@ lustrine_pbf::~lustrine_pbf() {
     for (int k = 0; k < 2; k++)
         if (graph_exec[k]) cudaGraphExecDestroy(graph_exec[k]);
     void* ptrs[] = {x[0], x[1], xs[0], xs[1], v[0], v[1], id[0], id[1], xs_alt, vtmp, key, key_sorted,
-                    rank, tmp, perm, count, start, block_sums, solid, solid_raw, sstart, nbr, cnt, lam,
+                    rank, tmp, perm, count, start, block_sums, tile_sum, solid, solid_raw, sstart, nbr, cnt, lam,
                     lam_by_id, rho, status, red, out3, out3d, iota, solid_id, d_scenes, d_scene_of,
                     d_solid_scene_of, cellk, cell_sorted, solid_cell};
     for (void* q : ptrs)
@@ -211,6 +211,8 @@ static int ctx_alloc(lustrine_pbf* s) {
     rc = rc ? rc : dalloc(&s->count, C);
     rc = rc ? rc : dalloc(&s->start, (size_t)C + 1);
     rc = rc ? rc : dalloc(&s->block_sums, scan_block_sums_size(C));
+    const bool tiled_scan = cell_scan_tiles(C) <= CELL_SCAN_MAX_TILES;
+    if (tiled_scan) rc = rc ? rc : dalloc(&s->tile_sum, cell_scan_tiles(C));
     rc = rc ? rc : dalloc(&s->solid, ns);
     rc = rc ? rc : dalloc(&s->solid_raw, ns);
     rc = rc ? rc : dalloc(&s->sstart, (size_t)C + 1);
@@ -553,8 +555,8 @@ static int enqueue_step(lustrine_pbf* s, cudaStream_t st, StageMarks* mk = nullp
     const bool mixed = s->mixed();
     int k = 0;
     if (mk) mk->mark(-1, st);
-    // count[] is all zero here: zeroed at allocation and by every scan's
-    // down-sweep.  Step kernels use programmatic dependent launch.
+    // count[] is all zero here: zeroed at allocation and by every scan.
+    // Step kernels use programmatic dependent launch.
     set_pdl(s->use_pdl);
     if (s->prm.mode == LUSTRINE_MODE_REFERENCE)
         launch_predict_ref(p, s->x[c], s->v[c], s->xs[c], s->key, s->rank, s->count, s->status, st);
@@ -562,8 +564,13 @@ static int enqueue_step(lustrine_pbf* s, cudaStream_t st, StageMarks* mk = nullp
         launch_predict(mixed, p, s->cp, s->x[c], s->v[c], s->xs[c], s->key, s->rank, s->count, s->cellk, st);
     k += 1;
     if (mk) mk->mark(LUSTRINE_STAGE_PREDICT, st);
-    launch_scan(s->count, C, s->block_sums, s->start, st);
-    k += 3;
+    if (s->tile_sum) {
+        launch_scan_tiles(s->count, C, s->tile_sum, s->start, st);
+        k += 2;
+    } else {
+        launch_scan(s->count, C, s->block_sums, s->start, st);
+        k += 3;
+    }
     if (mk) mk->mark(LUSTRINE_STAGE_SCAN, st);
     // stable within a cell: by the caller's id in reference mode (the
     // reference's list order), by the previous slot otherwise

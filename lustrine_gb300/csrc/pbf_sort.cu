@@ -5,9 +5,11 @@
 // scatter.  The GPU form:
 //   1. histogram: the prediction kernel does atomicAdd(count[key]) and keeps
 //      the returned value as the particle's provisional rank in its cell;
-//   2. exclusive scan of count over all cells (reduce, scan of the tile
-//      sums, down-sweep; no inter-block waits); the down-sweep also zeroes
-//      count for the next step's histogram;
+//   2. exclusive scan of count over all cells: tile totals, then every tile
+//      scanned from the sum of the totals before it (k_tile_sums,
+//      k_scan_tiles), or reduce / scan of the tile sums / down-sweep (grids
+//      of more than CELL_SCAN_MAX_TILES tiles, the standalone sort entry
+//      points); the scan also zeroes count for the next step's histogram;
 //   3. scatter of particle indices to start[key] + rank;
 //   4. stabilisation: atomic arrival order is arbitrary, so each slot counts
 //      the members of its cell with a smaller tie key (previous slot, or the
@@ -129,6 +131,95 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_down(int* __restrict__ co
     if (blockIdx.x == gridDim.x - 1 && threadIdx.x == SCAN_THREADS - 1) start[C] = ex;
 }
 
+// Exclusive scan of the step in two passes with no inter-block waits:
+// k_tile_sums writes the total of every tile of CELL_TILE cells, then each
+// block of k_scan_tiles finds its tile's offset by summing the totals of the
+// tiles before it (at most CELL_SCAN_MAX_TILES values, L2-resident) and
+// scans its tile.
+__device__ __forceinline__ void load_tile_items(const int* __restrict__ count, int C, long long base,
+                                                int (&v)[CELL_SCAN_ITEMS]) {
+    if (base + CELL_SCAN_ITEMS <= C) {
+        const int4* c4 = reinterpret_cast<const int4*>(count + base);
+#pragma unroll
+        for (int q = 0; q < CELL_SCAN_ITEMS / 4; q++) {
+            const int4 t = c4[q];
+            v[4 * q] = t.x;
+            v[4 * q + 1] = t.y;
+            v[4 * q + 2] = t.z;
+            v[4 * q + 3] = t.w;
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < CELL_SCAN_ITEMS; k++) v[k] = base + k < C ? count[base + k] : 0;
+    }
+}
+
+__global__ void __launch_bounds__(CELL_SCAN_THREADS) k_tile_sums(const int* __restrict__ count, int C,
+                                                                 int* __restrict__ tile_sum) {
+    pdl_wait();
+    const long long base = (long long)blockIdx.x * CELL_TILE + (long long)threadIdx.x * CELL_SCAN_ITEMS;
+    int v[CELL_SCAN_ITEMS];
+    load_tile_items(count, C, base, v);
+    int sum = 0;
+#pragma unroll
+    for (int k = 0; k < CELL_SCAN_ITEMS; k++) sum += v[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    __shared__ int warp_total[CELL_SCAN_THREADS / 32];
+    if ((threadIdx.x & 31) == 0) warp_total[threadIdx.x >> 5] = sum;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int t = 0;
+#pragma unroll
+        for (int w = 0; w < CELL_SCAN_THREADS / 32; w++) t += warp_total[w];
+        tile_sum[blockIdx.x] = t;
+    }
+}
+
+__global__ void __launch_bounds__(CELL_SCAN_THREADS) k_scan_tiles(int* __restrict__ count, int C,
+                                                                  const int* __restrict__ tile_sum,
+                                                                  int* __restrict__ start) {
+    pdl_wait();
+    const int tile = blockIdx.x;
+    const long long base = (long long)tile * CELL_TILE + (long long)threadIdx.x * CELL_SCAN_ITEMS;
+    const bool full = base + CELL_SCAN_ITEMS <= C;
+    int v[CELL_SCAN_ITEMS];
+    load_tile_items(count, C, base, v);
+    int part = 0;
+    for (int j = threadIdx.x; j < tile; j += CELL_SCAN_THREADS) part += __ldg(&tile_sum[j]);
+    int sum = 0;
+#pragma unroll
+    for (int k = 0; k < CELL_SCAN_ITEMS; k++) sum += v[k];
+    int total, offset;
+    block_exclusive_scan<CELL_SCAN_THREADS>(part, &offset);
+    int ex = block_exclusive_scan<CELL_SCAN_THREADS>(sum, &total) + offset;
+    if (full) {
+        int4* s4 = reinterpret_cast<int4*>(start + base);
+        int4* c4 = reinterpret_cast<int4*>(count + base);
+#pragma unroll
+        for (int q = 0; q < CELL_SCAN_ITEMS / 4; q++) {
+            int4 o;
+            o.x = ex;
+            o.y = o.x + v[4 * q];
+            o.z = o.y + v[4 * q + 1];
+            o.w = o.z + v[4 * q + 2];
+            ex = o.w + v[4 * q + 3];
+            s4[q] = o;
+            if (v[4 * q] | v[4 * q + 1] | v[4 * q + 2] | v[4 * q + 3]) c4[q] = make_int4(0, 0, 0, 0);
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < CELL_SCAN_ITEMS; k++) {
+            if (base + k < C) {
+                start[base + k] = ex;
+                if (v[k]) count[base + k] = 0;
+            }
+            ex += v[k];
+        }
+    }
+    if (tile == gridDim.x - 1 && threadIdx.x == 0) start[C] = offset + total;
+}
+
 __global__ void k_scatter_index(const int* __restrict__ key, const int* __restrict__ rank,
                                 const int* __restrict__ start, int n, int* __restrict__ tmp) {
     pdl_wait();
@@ -227,6 +318,15 @@ void launch_scan(int* count, int C, int* block_sums, int* start, cudaStream_t st
 }
 
 int scan_block_sums_size(int C) { return blocks_for(C, SCAN_TILE) + 1; }
+
+int cell_scan_tiles(int C) { return blocks_for(C, CELL_TILE); }
+
+void launch_scan_tiles(int* count, int C, int* tile_sum, int* start, cudaStream_t st) {
+    const bool pdl = pdl_enabled();
+    launch_k(k_tile_sums, cell_scan_tiles(C), CELL_SCAN_THREADS, st, pdl, (const int*)count, C, tile_sum);
+    launch_k(k_scan_tiles, cell_scan_tiles(C), CELL_SCAN_THREADS, st, pdl, count, C, (const int*)tile_sum,
+             start);
+}
 
 void launch_sort_tail(const int* key, const int* rank, const int* start, const int* tie, int n,
                       int* tmp, int* perm, cudaStream_t st) {
