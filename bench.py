@@ -70,27 +70,48 @@ def measured_peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
-
+    """nvidia-smi clock and throttle-reason samples (every 200 ms), each
+    stamped with the host time it arrived.  A timed region of a few
+    milliseconds falls between two samples, so the sampler runs from before
+    the warm-up (the GPU under the same load) and stop() keeps the samples
+    within `margin` seconds of the timed region."""
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self):
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        self.lines = []
+        self.t0 = self.t1 = None
 
     def start(self):
+        import threading
         try:
-            os.makedirs(os.path.dirname(self.path), exist_ok=True)
-            self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}",
                                           "--format=csv,noheader,nounits", "-lms", "200"],
-                                         stdout=self.f, stderr=subprocess.DEVNULL)
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except (OSError, FileNotFoundError):
             self.proc = None
+            return
 
-    def stop(self, gpu_index=0):
+        def pump():
+            for line in self.proc.stdout:
+                self.lines.append((time.time(), line))
+
+        self.thread = threading.Thread(target=pump, daemon=True)
+        self.thread.start()
+        # wait (up to 5 s) for the first sample so the timed region is covered
+        t_end = time.time() + 5.0
+        while not self.lines and time.time() < t_end and self.proc.poll() is None:
+            time.sleep(0.02)
+
+    def mark_start(self):
+        self.t0 = time.time()
+
+    def mark_end(self):
+        self.t1 = time.time()
+
+    def stop(self, gpu_index=0, margin=1.0):
         if not self.proc:
             return None
         self.proc.terminate()
@@ -98,10 +119,14 @@ class ClockSampler:
             self.proc.wait(5)
         except subprocess.TimeoutExpired:
             self.proc.kill()
-        self.f.close()
+        self.thread.join(2)
+        lo = (self.t0 or 0.0) - margin
+        hi = (self.t1 or time.time()) + margin
         sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in open(self.path):
+        for t, line in self.lines:
+            if not lo <= t <= hi:
+                continue
             parts = [p.strip() for p in line.split(",")]
             if len(parts) < 9 or not parts[0].isdigit() or int(parts[0]) != gpu_index:
                 continue
@@ -115,8 +140,11 @@ class ClockSampler:
                     reasons.add(nm)
         if not sm:
             return None
+        region = (self.t1 - self.t0) if (self.t0 and self.t1) else None
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "window": f"timed region ({region:.3f} s) +- {margin} s, "
+                                              f"GPU stepping the workload throughout"
+                if region is not None else "whole run"}
 
 
 def dist_setup(args):
@@ -251,13 +279,21 @@ def run_ours(args, world, rank, local):
     params = pbf_params(*sc.domain, iterations=sc.iterations, c_xsph=sc.c_xsph)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     clocks = ClockSampler()
+    clocks.start()  # runs through the warm-up: the timed region is milliseconds long
 
     sim, ext, _, _ = run_scene(sc, params, 1, args.warmup, flush)  # warm-up, graph capture
     barrier(world)
-    clocks.start()
+    clocks.mark_start()
     ms = time_steps(sim, sc.dt, args.steps, flush, ext)
-    clk = clocks.stop(local)
+    clocks.mark_end()
     status = sim.status()
+    # keep the GPU on the workload (untimed) while the samples after the
+    # timed region arrive
+    t_busy = time.time() + 0.5
+    while time.time() < t_busy:
+        sim.step(sc.dt, 20)
+        sim.synchronize()
+    clk = clocks.stop(local, margin=0.5)
     barrier(world)
     ms_step = dist_max(sum(ms) / len(ms), world)
     iters = params.iterations
