@@ -51,6 +51,7 @@ struct StepParams {
     int num_cells;        // dense: cells; hashed: buckets (1 << hash_bits)
     int hash_bits;        // 0: dense cell grid; > 0: hashed grid of 2^hash_bits buckets
     int max_nbrs;
+    int pad;              // PBF lists padded with sentinel entries to a multiple of pad (1, 2, 4, 8)
     int clamp_cells;      // compat mode: clamp cell coords per axis
     float cell, inv_cell;
     float h, h2;
@@ -122,6 +123,11 @@ inline void launch_k(void (*kernel)(KArgs...), int grid, int block, cudaStream_t
 // launch (set by the context around a step's launches).
 void set_pdl(bool on);
 bool pdl_enabled();
+
+// PBF neighbour lists: rows allocated = max_nbrs rounded up to LIST_PAD_MAX;
+// the sentinel slot n sits at SENTINEL_POS on every axis.
+constexpr int LIST_PAD_MAX = 8;
+constexpr float SENTINEL_POS = 1e18f;
 
 // Cell scan of the step: tiles of CELL_TILE cells, one block each.
 constexpr int CELL_SCAN_THREADS = 256;

@@ -6,6 +6,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <initializer_list>
 #include <vector>
 
 #include "lustrine_gb300.h"
@@ -80,6 +81,7 @@ static int derive(const lustrine_pbf_params& q, int n, int ns, StepParams* sp, C
     if (!(q.kernel_radius > 0.0f) || !(q.cell_size > 0.0f) || !(q.rest_density > 0.0f))
         return LUSTRINE_ERR_ARGS;
     if (q.max_neighbors <= 0 || q.iterations < 1 || q.iterations > 1000) return LUSTRINE_ERR_ARGS;
+    if (!(q.s_corr_n >= 0.0f)) return LUSTRINE_ERR_ARGS;  // (W / W(dq))^n with W = 0 at r = h
     if (q.mode != LUSTRINE_MODE_REFERENCE && q.mode != LUSTRINE_MODE_PBF) return LUSTRINE_ERR_ARGS;
     if (q.precision == LUSTRINE_PRECISION_MIXED && q.mode != LUSTRINE_MODE_PBF)
         return LUSTRINE_ERR_UNSUPPORTED;
@@ -111,6 +113,7 @@ static int derive(const lustrine_pbf_params& q, int n, int ns, StepParams* sp, C
         p.num_cells = (int)C;
     }
     p.max_nbrs = q.max_neighbors;
+    p.pad = 1;  // set per launch of the list build
     p.clamp_cells = q.clamp_cells;
     p.cell = q.cell_size;
     p.inv_cell = 1.0f / q.cell_size;
@@ -197,12 +200,12 @@ static int ctx_alloc(lustrine_pbf* s) {
     int rc = LUSTRINE_OK;
     for (int k = 0; k < 2 && !rc; k++) {
         rc = rc ? rc : dalloc(&s->x[k], n);
-        rc = rc ? rc : dalloc(&s->xs[k], n);
+        rc = rc ? rc : dalloc(&s->xs[k], (size_t)n + 1);  // + the sentinel slot n
         rc = rc ? rc : dalloc(&s->v[k], n);
         rc = rc ? rc : dalloc(&s->id[k], n);
     }
-    rc = rc ? rc : dalloc(&s->xs_alt, n);
-    rc = rc ? rc : dalloc(&s->vtmp, n);
+    rc = rc ? rc : dalloc(&s->xs_alt, (size_t)n + 1);
+    rc = rc ? rc : dalloc(&s->vtmp, (size_t)n + 1);
     rc = rc ? rc : dalloc(&s->key, m);
     rc = rc ? rc : dalloc(&s->key_sorted, n);
     rc = rc ? rc : dalloc(&s->rank, m);
@@ -216,7 +219,8 @@ static int ctx_alloc(lustrine_pbf* s) {
     rc = rc ? rc : dalloc(&s->solid, ns);
     rc = rc ? rc : dalloc(&s->solid_raw, ns);
     rc = rc ? rc : dalloc(&s->sstart, (size_t)C + 1);
-    rc = rc ? rc : dalloc(&s->nbr, (size_t)s->sp.max_nbrs * (size_t)n);
+    const size_t list_rows = (size_t)((s->sp.max_nbrs + LIST_PAD_MAX - 1) / LIST_PAD_MAX * LIST_PAD_MAX);
+    rc = rc ? rc : dalloc(&s->nbr, list_rows * (size_t)n);
     rc = rc ? rc : dalloc(&s->cnt, n);
     rc = rc ? rc : dalloc(&s->lam, n);
     s->lam_by_id_len = (size_t)(n + ns > s->sp.max_nbrs ? n + ns : s->sp.max_nbrs) + 1;
@@ -239,6 +243,12 @@ static int ctx_alloc(lustrine_pbf* s) {
         std::vector<int> ids((size_t)n);
         for (int i = 0; i < n; i++) ids[(size_t)i] = i;
         CK(cudaMemcpy(s->iota, ids.data(), (size_t)n * sizeof(int), cudaMemcpyHostToDevice));
+    }
+    {  // the sentinel particle of the padded neighbour lists
+        const float4 far = make_float4(SENTINEL_POS, SENTINEL_POS, SENTINEL_POS, 0.0f);
+        for (float4* a : {s->xs[0], s->xs[1], s->xs_alt})
+            CK(cudaMemcpy(a + n, &far, sizeof(float4), cudaMemcpyHostToDevice));
+        CK(cudaMemset(s->vtmp + n, 0, sizeof(float4)));
     }
     CK(cudaMemsetAsync(s->lam_by_id, 0, s->lam_by_id_len * sizeof(float), s->stream));
     CK(cudaMemsetAsync(s->lam, 0, (size_t)(n ? n : 1) * sizeof(float), s->stream));

@@ -40,8 +40,12 @@ __device__ __forceinline__ int entry(int slot, int dx, int dy, int dz, bool soli
 }
 __device__ __forceinline__ int entry_slot(int e) { return e & SLOT_MASK; }
 __device__ __forceinline__ bool entry_solid(int e) { return e < 0; }
-// the particle itself: a fluid entry of its own slot (any cell code)
-__device__ __forceinline__ bool entry_is(int e, int s) { return (e & (SLOT_MASK | (int)0x80000000u)) == s; }
+// Lists are padded to a multiple of StepParams::pad with entries of the
+// sentinel slot n, a particle at (1e18, 1e18, 1e18) with zero velocity and
+// lambda in every position and velocity array the passes gather from: every
+// pair term with it is exactly zero (h^2 - r^2 and h - r clamp to 0), so the
+// neighbour loops run whole chunks without per-entry checks.
+__device__ __forceinline__ int sentinel_entry(const StepParams& p) { return entry(p.n, 0, 0, 0, false); }
 
 // Bucket of a cell in a table of 2^bits buckets.  Cells are grouped in
 // bricks of 4 (x) x 4 (y) x 8 (z); a brick starts at a hashed base
@@ -449,6 +453,9 @@ __global__ void __launch_bounds__(B) k_lists_lambda(StepParams p, CellPack cp, f
         c_n = p.max_nbrs;
     }
     cnt[s] = c_n;
+    // sentinel entries up to a multiple of the passes' chunk (pad divides the
+    // buffer's rows: max_nbrs rounded up to LIST_PAD_MAX)
+    for (int k = c_n; k % p.pad != 0; k++) nbr[(size_t)k * p.n + s] = sentinel_entry(p);
     // lambda into w in place: neighbours read only xyz of this element here
     reinterpret_cast<float*>(xs)[4 * (size_t)s + 3] = lambda_of(p, a);
     if (rho) rho[s] = density_of(p, a);
@@ -457,9 +464,9 @@ __global__ void __launch_bounds__(B) k_lists_lambda(StepParams p, CellPack cp, f
 // Walk a particle's list U entries at a time, calling f(entry, position)
 // for each.  The first U entries are loaded together with the count and
 // every next chunk's entries while the current chunk's positions are
-// gathered: the list buffer holds max_nbrs rows for every particle, so these
-// loads stay in bounds, and entries at or past the count are replaced by
-// the particle itself before any position is gathered.
+// gathered.  The list is padded with sentinel entries to a multiple of U
+// (the list build's pad), and the buffer holds at least 8 rows, so every
+// entry of a chunk below the count is valid and every load in bounds.
 template <int U, class F>
 __device__ __forceinline__ void for_each_entry(const StepParams& p, const int* __restrict__ col,
                                                const int* __restrict__ cnt, int s,
@@ -467,25 +474,21 @@ __device__ __forceinline__ void for_each_entry(const StepParams& p, const int* _
                                                const float4* __restrict__ solid, F&& f) {
     int nx[U];
 #pragma unroll
-    for (int u = 0; u < U; u++) nx[u] = u < p.max_nbrs ? __ldg(&col[(size_t)u * p.n]) : s;
+    for (int u = 0; u < U; u++) nx[u] = __ldg(&col[(size_t)u * p.n]);
     const int c = __ldg(&cnt[s]);
     for (int k = 0; k < c; k += U) {
         int e[U];
         float4 q[U];
 #pragma unroll
-        for (int u = 0; u < U; u++) e[u] = k + u < c ? nx[u] : s;
+        for (int u = 0; u < U; u++) e[u] = nx[u];
         if (k + U < c) {
 #pragma unroll
-            for (int u = 0; u < U; u++)
-                nx[u] = k + U + u < p.max_nbrs ? __ldg(&col[(size_t)(k + U + u) * p.n]) : s;
+            for (int u = 0; u < U; u++) nx[u] = __ldg(&col[(size_t)(k + U + u) * p.n]);
         }
 #pragma unroll
         for (int u = 0; u < U; u++) q[u] = load_entry(e[u], xs, solid);
 #pragma unroll
-        for (int u = 0; u < U; u++) {
-            if (k + u >= c) break;
-            f(e[u], q[u]);
-        }
+        for (int u = 0; u < U; u++) f(e[u], q[u]);
     }
 }
 
@@ -596,13 +599,14 @@ __global__ void __launch_bounds__(B) k_xsph(StepParams p, CellPack cp, const flo
     const int* __restrict__ col = nbr + s;
     float ax = 0.0f, ay = 0.0f, az = 0.0f;
     if (p.c_xsph != 0.0f) {
+        const int sent = sentinel_entry(p);
         for (int k = 0; k < c; k += U) {
             int e[U];
             float4 q[U], vj[U];
 #pragma unroll
             for (int u = 0; u < U; u++) {
-                int t = k + u < c ? __ldg(&col[(size_t)(k + u) * p.n]) : s;
-                e[u] = entry_solid(t) ? s : t;  // solids take no part (skipped as s)
+                const int t = __ldg(&col[(size_t)(k + u) * p.n]);  // padded list: valid below roundup(c, U)
+                e[u] = entry_solid(t) ? sent : t;  // solids take no part (their term is the sentinel's zero)
             }
 #pragma unroll
             for (int u = 0; u < U; u++) {
@@ -611,8 +615,6 @@ __global__ void __launch_bounds__(B) k_xsph(StepParams p, CellPack cp, const flo
             }
 #pragma unroll
             for (int u = 0; u < U; u++) {
-                if (k + u >= c) break;
-                if (entry_is(e[u], s)) continue;
                 float3 d = rel_e<MIXED>(p, self, q[u], e[u]);
                 const float hd = hdiff(p, dot3(d.x, d.y, d.z));
                 const float w = hd * hd * hd;
@@ -817,9 +819,11 @@ void launch_lists_lambda(bool mixed, const Tuning& tu, const StepParams& p, cons
                          int* cnt, float* rho, int* status, cudaStream_t st) {
     if (p.n <= 0) return;
     const int B = tu.list_block <= 64 ? 64 : (tu.list_block <= 128 ? 128 : 256);
+    StepParams pp = p;  // lists padded for the chunk of the passes that read them
+    pp.pad = tu.unroll >= 8 ? 8 : (tu.unroll >= 4 ? 4 : (tu.unroll >= 2 ? 2 : 1));
     const bool pdl = pdl_enabled();
 #define LGB_LISTS_H(MIX, H, BB)                                                                 \
-    launch_k(k_lists_lambda<MIX, H, BB>, blocks_for(p.n, BB), BB, st, pdl, p, cp, xs, key_sorted, \
+    launch_k(k_lists_lambda<MIX, H, BB>, blocks_for(p.n, BB), BB, st, pdl, pp, cp, xs, key_sorted, \
              cell_sorted, fstart, solid, solid_cell, sstart, nbr, cnt, rho, status)
 #define LGB_LISTS(MIX, BB)                       \
     do {                                         \
