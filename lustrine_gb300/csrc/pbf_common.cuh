@@ -46,6 +46,9 @@ struct StepParams {
     const int* solid_scene_of;
     // hashed grid: packed cell of every sorted fluid slot (nullptr when dense)
     const int* cell_sorted;
+    // per cell (bucket): whether a static particle lies in its 27-cell
+    // neighbourhood (nullptr: no static particles)
+    const unsigned char* solid_near;
     int n, ns;            // fluid, solid particle counts
     int gx, gy, gz;       // grid dims
     int num_cells;        // dense: cells; hashed: buckets (1 << hash_bits)

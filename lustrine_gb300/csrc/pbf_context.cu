@@ -187,7 +187,7 @@ lustrine_pbf::~lustrine_pbf() {
     for (int k = 0; k < 2; k++)
         if (graph_exec[k]) cudaGraphExecDestroy(graph_exec[k]);
     void* ptrs[] = {x[0], x[1], xs[0], xs[1], v[0], v[1], id[0], id[1], xs_alt, vtmp, key, key_sorted,
-                    rank, tmp, perm, count, start, block_sums, tile_sum, solid, solid_raw, sstart, nbr, cnt, lam,
+                    rank, tmp, perm, count, start, block_sums, tile_sum, solid_near, solid, solid_raw, sstart, nbr, cnt, lam,
                     lam_by_id, rho, status, red, out3, out3d, iota, solid_id, d_scenes, d_scene_of,
                     d_solid_scene_of, cellk, cell_sorted, solid_cell};
     for (void* q : ptrs)
@@ -232,6 +232,10 @@ static int ctx_alloc(lustrine_pbf* s) {
     rc = rc ? rc : dalloc(&s->out3d, (size_t)3 * n);
     rc = rc ? rc : dalloc(&s->iota, n);
     rc = rc ? rc : dalloc(&s->solid_id, ns);
+    if (ns > 0) {
+        rc = rc ? rc : dalloc(&s->solid_near, (size_t)C);
+        s->sp.solid_near = s->solid_near;
+    }
     if (s->sp.hash_bits) {  // hashed grid: packed cells, unsorted and sorted
         rc = rc ? rc : dalloc(&s->cellk, m);
         rc = rc ? rc : dalloc(&s->cell_sorted, n);
@@ -420,6 +424,7 @@ extern "C" int lustrine_pbf_set_params(lustrine_pbf* s, const lustrine_pbf_param
         sp.inv_dt = s->sp.inv_dt;
         sp.cell_sorted = s->sp.cell_sorted;
     }
+    sp.solid_near = s->sp.solid_near;
     if (rc) return rc;
     // the grid's table (dense cells or hash buckets) was sized at creation
     if (sp.hash_bits != s->sp.hash_bits || sp.num_cells != s->sp.num_cells) return LUSTRINE_ERR_UNSUPPORTED;
@@ -468,6 +473,10 @@ static int setup_solids(lustrine_pbf* s) {
     launch_sort_tail(s->key, s->rank, s->sstart, nullptr, ns, s->tmp, s->perm, s->stream);
     launch_gather_solid(s->perm, ns, s->solid_raw, s->solid, s->stream);
     if (p.hash_bits) launch_gather_int(s->perm, ns, s->cellk, s->solid_cell, s->stream);
+    if (ns > 0) {  // PBF geometry (the reference-mode list build walks every cell)
+        CK(cudaMemsetAsync(s->solid_near, 0, (size_t)C, s->stream));
+        launch_mark_solid_near(s->mixed(), p, s->cp, s->solid_raw, ns, s->solid_near, s->stream);
+    }
     CK(cudaGetLastError());
     return LUSTRINE_OK;
 }

@@ -49,6 +49,7 @@ struct lustrine_pbf {
     int* cell_sorted = nullptr;
     int* solid_cell = nullptr;
     int* solid_id = nullptr;   // caller's solid index of each sorted slot
+    unsigned char* solid_near = nullptr;  // cells within one cell of a solid (PBF list build)
     int* sstart = nullptr;
 
     // neighbour lists and per-particle outputs

@@ -67,6 +67,10 @@ void launch_predict(bool mixed, const StepParams& p, const CellPack& cp, const f
                     float4* xs, int* key, int* rank, int* count, int* cellk, cudaStream_t st);
 void launch_key(bool mixed, const StepParams& p, const CellPack& cp, const float4* pos, int m,
                 int* key, int* rank, int* count, int* cellk, cudaStream_t st);
+// near[key] = 1 for every cell (bucket) within one cell of a static particle
+// (near: num_cells bytes, zero on entry)
+void launch_mark_solid_near(bool mixed, const StepParams& p, const CellPack& cp, const float4* pos, int m,
+                            unsigned char* near, cudaStream_t st);
 // neighbour lists + first lambda pass (lambda stored in xs.w)
 void launch_lists_lambda(bool mixed, const Tuning& tu, const StepParams& p, const CellPack& cp,
                          float4* xs, const int* key_sorted, const int* cell_sorted, const int* fstart,

@@ -275,6 +275,33 @@ __global__ void k_key(StepParams p, CellPack cp, const float4* __restrict__ pos,
     rank[i] = atomicAdd(&count[k], 1);
 }
 
+// Cells (hash buckets) with a static particle in their 27-cell
+// neighbourhood, marked once when the solids are set: the list build walks
+// the solids only from those (a bucket shared with another cell is a false
+// positive, which only costs a walk).
+template <bool MIXED>
+__global__ void k_mark_solid_near(StepParams p, CellPack cp, const float4* __restrict__ pos, int m,
+                                  unsigned char* __restrict__ near) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    float4 q = pos[i];
+    const Geo g = p.scenes ? geo_scene(p, p.solid_scene_of[i]) : geo_single(p);
+    int3 c = MIXED ? unpack_cell(cp, q.w) : plain_cell(p, g, q.x, q.y, q.z);
+    if (p.hash_bits) c = make_int3(min(c.x, (int)cp.mx), min(c.y, (int)cp.my), min(c.z, (int)cp.mz));
+    for (int dy = -1; dy <= 1; dy++)
+        for (int dx = -1; dx <= 1; dx++)
+            for (int dz = -1; dz <= 1; dz++) {
+                const int3 cn = make_int3(c.x + dx, c.y + dy, c.z + dz);
+                if (cn.x < 0 || cn.y < 0 || cn.z < 0 || cn.x >= g.gx || cn.y >= g.gy || cn.z >= g.gz) continue;
+                if (p.hash_bits) {
+                    if (cn.x > (int)cp.mx || cn.y > (int)cp.my || cn.z > (int)cp.mz) continue;
+                    near[cell_bucket(cn, p.hash_bits)] = 1;
+                } else {
+                    near[linear_cell(g, cn)] = 1;
+                }
+            }
+}
+
 // Neighbour search fused with the first lambda pass: walks the 27 cells
 // around the particle's cell, writes the list and accumulates the density
 // constraint over the accepted neighbours.  The particle itself is not in
@@ -416,6 +443,8 @@ __global__ void __launch_bounds__(B) k_lists_lambda(StepParams p, CellPack cp, f
     LambdaAcc a = lambda_init(p);
     int c_n = 0;
     const int slab = g.gx * g.gz;
+    // static particles only where the cell's neighbourhood holds some
+    const bool solids = p.ns > 0 && p.solid_near && __ldg(&p.solid_near[__ldg(&key_sorted[s])]);
     for (int dy = -1; dy <= 1; dy++) {
         const int y = c.y + dy;
         if (y < 0 || y >= g.gy) continue;
@@ -433,7 +462,7 @@ __global__ void __launch_bounds__(B) k_lists_lambda(StepParams p, CellPack cp, f
                                                    cell_bucket(cn, p.hash_bits), (int)pack_bits(cp, cn),
                                                    dx, dy, z - c.z, a, c_n, nbr);
                 }
-                if (p.ns > 0)
+                if (solids)
                     for (int z = z0; z <= z1; z++) {
                         const int3 cn = make_int3(xx, y, z);
                         walk_hashed_cell<MIXED, true>(p, self, s, solid, sstart, solid_cell,
@@ -444,7 +473,7 @@ __global__ void __launch_bounds__(B) k_lists_lambda(StepParams p, CellPack cp, f
             }
             const int row = g.off + y * slab + xx * g.gz;
             walk_row<MIXED, false>(p, self, s, xs, fstart, row, c.z, g.gz, dx, dy, a, c_n, nbr);
-            if (p.ns > 0)
+            if (solids)
                 walk_row<MIXED, true>(p, self, s, solid, sstart, row, c.z, g.gz, dx, dy, a, c_n, nbr);
         }
     }
@@ -773,6 +802,12 @@ void launch_predict(bool mixed, const StepParams& p, const CellPack& cp, const f
                     float4* xs, int* key, int* rank, int* count, int* cellk, cudaStream_t st) {
     if (p.n <= 0) return;
     LGB_DISPATCH(mixed, k_predict, blocks_for(p.n, 256), 256, st, p, cp, x, v, xs, key, rank, count, cellk);
+}
+
+void launch_mark_solid_near(bool mixed, const StepParams& p, const CellPack& cp, const float4* pos, int m,
+                            unsigned char* near, cudaStream_t st) {
+    if (m <= 0) return;
+    LGB_DISPATCH(mixed, k_mark_solid_near, blocks_for(m, 256), 256, st, p, cp, pos, m, near);
 }
 
 void launch_key(bool mixed, const StepParams& p, const CellPack& cp, const float4* pos, int m,
