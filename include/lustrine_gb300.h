@@ -133,6 +133,9 @@ LUSTRINE_API void init_grid_box(const SimulationParameters* parameters, GridWrap
 LUSTRINE_API int get_num_sand_particles(void);
 /* LustrineWrapper.cpp:705-707 (returns the float cell size converted to int) */
 LUSTRINE_API int get_grid_cell_size(void);
+/* LustrineWrapper.hpp:184 / LustrineWrapper.cpp:288-291: particles in the
+ * cells of the box [min, max] after the last step (lustrine_pbf_query_cell_count). */
+LUSTRINE_API int query_cell_num_particles(Vec3 min, Vec3 max, bool include_solid);
 /* LustrineWrapper.cpp:666-677.  0 and 1 select the reference's sand solvers,
  * which this library does not provide (LUSTRINE_ERR_UNSUPPORTED, step
  * unchanged); 2 selects the fluid step with reference semantics; 3 the PBF
@@ -235,6 +238,13 @@ LUSTRINE_API int lustrine_pbf_neighbors(lustrine_pbf* s, int* count, int* idx, i
  * energy, [5..7] centre of mass, [8] max |rho / rho0 - 1| of the last lambda
  * pass.  Synchronises. */
 LUSTRINE_API int lustrine_pbf_reduce(lustrine_pbf* s, double out[9]);
+/* Particles the last step binned in the grid cells of the box [min_pos,
+ * max_pos] (Lustrine::query_cell_num_particles, Lustrine.cpp:864-914: corners
+ * clamped to [cell/2, domain - cell/2] and truncated to cell indices; fluid
+ * binned at the step's predicted positions; solids counted when
+ * include_solid).  0 before the first step.  One scene only.  Synchronises. */
+LUSTRINE_API int lustrine_pbf_query_cell_count(lustrine_pbf* s, const float min_pos[3],
+                                               const float max_pos[3], int include_solid, int* count);
 /* Device-side error bits since the last call, as a status code (synchronises). */
 LUSTRINE_API int lustrine_pbf_status(lustrine_pbf* s);
 /* The context's cudaStream_t, as void*. */

@@ -104,6 +104,7 @@ SIGNATURES = {
     "get_num_sand_particles": (C.c_int, []),
     "get_grid_cell_size": (C.c_int, []),
     "set_simulate_function": (None, [C.c_int]),
+    "query_cell_num_particles": (C.c_int, [Vec3, Vec3, C.c_bool]),
     "lustrine_last_status": (C.c_int, []),
     "lustrine_global_context": (_P, []),
     "lustrine_free_grid": (None, [C.POINTER(GridWrapper)]),
@@ -127,6 +128,7 @@ SIGNATURES = {
     "lustrine_pbf_download_positions_f64": (C.c_int, [_P, _P]),
     "lustrine_pbf_neighbors": (C.c_int, [_P, _P, _P, C.c_int]),
     "lustrine_pbf_reduce": (C.c_int, [_P, _DP]),
+    "lustrine_pbf_query_cell_count": (C.c_int, [_P, _FP, _FP, C.c_int, _IP]),
     "lustrine_pbf_status": (C.c_int, [_P]),
     "lustrine_pbf_stream": (C.c_int, [_P, C.POINTER(_P)]),
     "lustrine_pbf_launches_per_step": (C.c_int, [_P]),

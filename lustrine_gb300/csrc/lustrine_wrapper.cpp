@@ -193,6 +193,17 @@ int get_num_sand_particles(void) { return g_num_sand; }
 
 int get_grid_cell_size(void) { return (int)g_cell_size; }
 
+int query_cell_num_particles(Vec3 min, Vec3 max, bool include_solid) {
+    if (!g_ctx) {
+        g_status = LUSTRINE_ERR_NO_SIMULATION;
+        return 0;
+    }
+    const float lo[3] = {min.x, min.y, min.z}, hi[3] = {max.x, max.y, max.z};
+    int count = 0;
+    g_status = lustrine_pbf_query_cell_count(g_ctx, lo, hi, include_solid ? 1 : 0, &count);
+    return count;
+}
+
 void set_simulate_function(int index) {
     if (!g_ctx) {
         g_status = LUSTRINE_ERR_NO_SIMULATION;

@@ -188,7 +188,7 @@ lustrine_pbf::~lustrine_pbf() {
         if (graph_exec[k]) cudaGraphExecDestroy(graph_exec[k]);
     void* ptrs[] = {x[0], x[1], xs[0], xs[1], v[0], v[1], id[0], id[1], xs_alt, vtmp, key, key_sorted,
                     rank, tmp, perm, count, start, block_sums, tile_sum, solid_near, solid, solid_raw, sstart, nbr, cnt, lam,
-                    lam_by_id, rho, status, red, out3, out3d, iota, solid_id, d_scenes, d_scene_of,
+                    lam_by_id, rho, status, red, qcount, out3, out3d, iota, solid_id, d_scenes, d_scene_of,
                     d_solid_scene_of, cellk, cell_sorted, solid_cell};
     for (void* q : ptrs)
         if (q) cudaFree(q);
@@ -228,6 +228,7 @@ static int ctx_alloc(lustrine_pbf* s) {
     rc = rc ? rc : dalloc(&s->rho, n);
     rc = rc ? rc : dalloc(&s->status, 4);
     rc = rc ? rc : dalloc(&s->red, 9);
+    rc = rc ? rc : dalloc(&s->qcount, 1);
     rc = rc ? rc : dalloc(&s->out3, (size_t)3 * m);
     rc = rc ? rc : dalloc(&s->out3d, (size_t)3 * n);
     rc = rc ? rc : dalloc(&s->iota, n);
@@ -973,6 +974,42 @@ extern "C" int lustrine_pbf_reduce(lustrine_pbf* s, double out[9]) {
     CK(cudaStreamSynchronize(s->stream));
     if (out[0] > 0.0)
         for (int k = 5; k < 8; k++) out[k] /= out[0];
+    return LUSTRINE_OK;
+}
+
+// Lustrine.cpp:864-914 with get_cell_indices (neighbors/Utils.hpp:13-21): the
+// corners are clamped to [cell / 2, domain - cell / 2] per axis (float,
+// bounds formed in double as glm does) and truncated to cell indices; the
+// count is that of the particles the last step binned in those cells.
+extern "C" int lustrine_pbf_query_cell_count(lustrine_pbf* s, const float min_pos[3],
+                                             const float max_pos[3], int include_solid, int* count) {
+    if (!s || !min_pos || !max_pos || !count) return LUSTRINE_ERR_ARGS;
+    if (s->is_batch()) return LUSTRINE_ERR_UNSUPPORTED;
+    *count = 0;
+    const float cell = s->prm.cell_size;
+    const int g[3] = {s->sp.gx, s->sp.gy, s->sp.gz};
+    int box[6];
+    for (int a = 0; a < 3; a++) {
+        const float lo = (float)((double)cell * 0.5);
+        const float hi = (float)((double)(float)s->prm.domain[a] - (double)cell * 0.5);
+        int i0 = (int)(std::fmin(std::fmax(min_pos[a], lo), hi) / cell);
+        int i1 = (int)(std::fmin(std::fmax(max_pos[a], lo), hi) / cell);
+        i0 = std::min(std::max(i0, 0), g[a] - 1);
+        i1 = std::min(std::max(i1, 0), g[a] - 1);
+        box[2 * a] = i0;
+        box[2 * a + 1] = i1;
+    }
+    // an empty range (min above max on an axis) counts nothing, as the
+    // reference's loops do
+    if (box[0] > box[1] || box[2] > box[3] || box[4] > box[5]) return LUSTRINE_OK;
+    if (!s->lists_valid) return LUSTRINE_OK;  // no step yet: the cell table is empty
+    CK(cudaMemsetAsync(s->qcount, 0, sizeof(int), s->stream));
+    const bool solids = include_solid && s->ns > 0;
+    launch_query_cells(s->sp, s->cp, box, s->start, solids ? s->sstart : nullptr, s->cell_sorted,
+                       solids ? s->solid_cell : nullptr, s->qcount, s->stream);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(count, s->qcount, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
     return LUSTRINE_OK;
 }
 

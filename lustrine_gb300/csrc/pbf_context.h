@@ -62,6 +62,7 @@ struct lustrine_pbf {
     float* rho = nullptr;
     int* status = nullptr;
     double* red = nullptr;
+    int* qcount = nullptr;    // cell-count query result
     float* out3 = nullptr;    // 3 * max(n, ns) floats of staging
     double* out3d = nullptr;  // 3 * n doubles of staging
 

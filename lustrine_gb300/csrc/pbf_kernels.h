@@ -92,6 +92,12 @@ void launch_unpermute_pos_d(bool mixed, const StepParams& p, const CellPack& cp,
 void launch_pack_pos(bool mixed, const StepParams& p, const CellPack& cp, const float* in, int n,
                      const int* scene_of,
                      float4* out, cudaStream_t st);
+// count of the particles the last step binned in the cells x0..x1, y0..y1,
+// z0..z1 (box[6], inclusive, inside the grid), added to *out (device int);
+// sstart / solid_cell nullptr: fluid only
+void launch_query_cells(const StepParams& p, const CellPack& cp, const int box[6], const int* fstart,
+                        const int* sstart, const int* cell_sorted, const int* solid_cell, int* out,
+                        cudaStream_t st);
 void launch_reduce(bool mixed, const StepParams& p, const CellPack& cp, const float4* x,
                    const float4* v, const float* rho, double* out, cudaStream_t st);
 

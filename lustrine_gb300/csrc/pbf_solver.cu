@@ -728,6 +728,58 @@ __global__ void k_pack_pos(StepParams p, CellPack cp, const float* __restrict__ 
                          pack_cell(cp, cx, cy, cz));
 }
 
+// Particles binned in a box of cells by the last step (the sorted cell table
+// of its prediction), Lustrine.cpp:864-914.  Dense grid: one thread per
+// (y, x) row of the box, the row's z range being one slot range of each
+// table.  Hashed grid: one thread per particle, its packed cell tested.
+__global__ void k_query_rows(int gx, int gz, int x0, int x1, int y0, int y1, int z0, int z1,
+                             const int* __restrict__ fstart, const int* __restrict__ sstart,
+                             int* __restrict__ out) {
+    const int nx = x1 - x0 + 1;
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    int c = 0;
+    if (r < nx * (y1 - y0 + 1)) {
+        const int y = y0 + r / nx, x = x0 + r % nx;
+        const int row = y * gx * gz + x * gz;
+        c = fstart[row + z1 + 1] - fstart[row + z0];
+        if (sstart) c += sstart[row + z1 + 1] - sstart[row + z0];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, c);
+}
+
+__global__ void k_query_packed(CellPack cp, const int* __restrict__ cells, int m, int x0, int x1, int y0,
+                               int y1, int z0, int z1, int* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int c = 0;
+    if (i < m) {
+        const unsigned u = (unsigned)cells[i];
+        const int x = (int)(u & cp.mx), y = (int)((u >> cp.by_shift) & cp.my), z = (int)((u >> cp.bz_shift) & cp.mz);
+        c = (x >= x0 && x <= x1 && y >= y0 && y <= y1 && z >= z0 && z <= z1) ? 1 : 0;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, c);
+}
+
+void launch_query_cells(const StepParams& p, const CellPack& cp, const int box[6], const int* fstart,
+                        const int* sstart, const int* cell_sorted, const int* solid_cell, int* out,
+                        cudaStream_t st) {
+    const int x0 = box[0], x1 = box[1], y0 = box[2], y1 = box[3], z0 = box[4], z1 = box[5];
+    if (!p.hash_bits) {
+        const int rows = (x1 - x0 + 1) * (y1 - y0 + 1);
+        k_query_rows<<<(rows + 255) / 256, 256, 0, st>>>(p.gx, p.gz, x0, x1, y0, y1, z0, z1, fstart,
+                                                            sstart, out);
+        return;
+    }
+    if (p.n > 0)
+        k_query_packed<<<(p.n + 255) / 256, 256, 0, st>>>(cp, cell_sorted, p.n, x0, x1, y0, y1, z0, z1, out);
+    if (solid_cell && p.ns > 0)
+        k_query_packed<<<(p.ns + 255) / 256, 256, 0, st>>>(cp, solid_cell, p.ns, x0, x1, y0, y1, z0, z1,
+                                                              out);
+}
+
 // FP64 reductions over the fluid: [0] mass, [1..3] momentum, [4] kinetic
 // energy, [5..7] mass-weighted position sum, [8] max |rho / rho0 - 1|.
 __device__ __forceinline__ void atomic_max_pos_double(double* addr, double val) {

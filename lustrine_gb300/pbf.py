@@ -236,5 +236,15 @@ class PbfSim:
               "profile_step")
         return {k: (ms[i], cnt[i]) for i, k in enumerate(self.STAGES)}
 
+    def query_cell_count(self, min_pos, max_pos, include_solid: bool = False) -> int:
+        """Particles the last step binned in the cells of the box
+        (Lustrine::query_cell_num_particles)."""
+        lo = (C.c_float * 3)(*[float(a) for a in min_pos])
+        hi = (C.c_float * 3)(*[float(a) for a in max_pos])
+        out = C.c_int(0)
+        check(self.lib.lustrine_pbf_query_cell_count(self.h, lo, hi, 1 if include_solid else 0,
+                                                     C.byref(out)), "query_cell_count")
+        return int(out.value)
+
     def status(self) -> int:
         return int(self.lib.lustrine_pbf_status(self.h))

@@ -14,6 +14,7 @@ from . import _lib
 from ._lib import Color, GridWrapper, SimulationData, SimulationParameters, Vec3
 
 __all__ = ["SimulationParameters", "SimulationData", "GridWrapper", "Vec3", "Color",
+           "query_cell_num_particles",
            "init_grid_box", "init_simulation", "init_simulation_extra_parameters", "simulate",
            "simulate_no_flags", "simulation_bind_positions_copy", "cleanup_simulation",
            "get_num_sand_particles", "get_grid_cell_size", "set_simulate_function",
@@ -100,6 +101,10 @@ def get_num_sand_particles() -> int:
 
 def get_grid_cell_size() -> int:
     return int(_lib_().get_grid_cell_size())
+
+
+def query_cell_num_particles(min_pos, max_pos, include_solid: bool = False) -> int:
+    return int(_lib_().query_cell_num_particles(Vec3(*min_pos), Vec3(*max_pos), bool(include_solid)))
 
 
 def set_simulate_function(index: int):
