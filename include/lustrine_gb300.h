@@ -133,6 +133,26 @@ LUSTRINE_API void init_grid_box(const SimulationParameters* parameters, GridWrap
 LUSTRINE_API int get_num_sand_particles(void);
 /* LustrineWrapper.cpp:705-707 (returns the float cell size converted to int) */
 LUSTRINE_API int get_grid_cell_size(void);
+/* LustrineWrapper.hpp:162-169 / LustrineWrapper.cpp:679-703, Lustrine.cpp:916-1017:
+ * particle sources and sinks, run by simulate around each step as
+ * Lustrine::simulate does (Lustrine.cpp:745-861): a source's timer grows by
+ * 0.016 per call; when it reaches freq (and the source is on, below its
+ * capacity, with room left) the pattern grid's particles are appended at the
+ * pattern positions shifted along the normalised direction by
+ * freq - fmod(total_time, freq), with velocity direction * 2r / freq (the
+ * middle particle + 0.001 per axis); after the step every sink whose timer
+ * (+= dt per call, never reset) reached its frequency evicts the particles
+ * binned in its cells (lustrine_pbf_despawn_cells).  Room for spawned
+ * particles: the reference's allocation, max(n + ns, X Y Z sub^3) - 1 - ns
+ * - n, reserved up to 2^22.  get_sink_despawned returns the reference's
+ * counter, which it never increments (0).  Index arguments out of range
+ * record LUSTRINE_ERR_ARGS. */
+LUSTRINE_API int add_particle_source(GridWrapper* pattern, Vec3 direction, float freq, int capacity);
+LUSTRINE_API int add_particle_sink(Vec3 min_pos, Vec3 max_pos, float frequency);
+LUSTRINE_API void set_source_state(int index, int state);
+LUSTRINE_API void set_sink_state(int index, int state);
+LUSTRINE_API int get_source_spawned(int index);
+LUSTRINE_API int get_sink_despawned(int index);
 /* LustrineWrapper.hpp:184 / LustrineWrapper.cpp:288-291: particles in the
  * cells of the box [min, max] after the last step (lustrine_pbf_query_cell_count). */
 LUSTRINE_API int query_cell_num_particles(Vec3 min, Vec3 max, bool include_solid);
@@ -245,6 +265,26 @@ LUSTRINE_API int lustrine_pbf_reduce(lustrine_pbf* s, double out[9]);
  * include_solid).  0 before the first step.  One scene only.  Synchronises. */
 LUSTRINE_API int lustrine_pbf_query_cell_count(lustrine_pbf* s, const float min_pos[3],
                                                const float max_pos[3], int include_solid, int* count);
+/* Particles entering and leaving (the device side of the reference's sources
+ * and sinks, Lustrine.cpp:745-836).  One scene only.
+ *
+ * reserve: buffers for up to capacity fluid particles; call before the first
+ * upload (LUSTRINE_ERR_UNSUPPORTED after it).  The fluid count of the
+ * context stays n_fluid until particles are spawned.
+ * spawn: appends m particles (host xyz triples; v may be NULL for zero) as
+ * caller indices n, n+1, ...; LUSTRINE_ERR_TOO_LARGE past the capacity.
+ * despawn_cells: removes the fluid particles the last step binned in the
+ * listed cells (dense cell ids y*gX*gZ + x*gZ + z, repeats allowed), with
+ * the reference's index semantics: in list order, ascending index within a
+ * cell, every evicted index takes the data of the current last particle and
+ * the count drops by one (so an eviction list that reaches the tail moves
+ * and drops particles exactly as the reference does).  *removed = how many
+ * the count dropped.  Hashed grids: LUSTRINE_ERR_UNSUPPORTED.
+ * Both synchronise; lambdas and densities of the last step read as 0 after
+ * either until the next step. */
+LUSTRINE_API int lustrine_pbf_reserve(lustrine_pbf* s, int capacity);
+LUSTRINE_API int lustrine_pbf_spawn(lustrine_pbf* s, const float* x, const float* v, int m);
+LUSTRINE_API int lustrine_pbf_despawn_cells(lustrine_pbf* s, const int* cells, int ncells, int* removed);
 /* Device-side error bits since the last call, as a status code (synchronises). */
 LUSTRINE_API int lustrine_pbf_status(lustrine_pbf* s);
 /* The context's cudaStream_t, as void*. */

@@ -105,6 +105,12 @@ SIGNATURES = {
     "get_grid_cell_size": (C.c_int, []),
     "set_simulate_function": (None, [C.c_int]),
     "query_cell_num_particles": (C.c_int, [Vec3, Vec3, C.c_bool]),
+    "add_particle_source": (C.c_int, [C.POINTER(GridWrapper), Vec3, C.c_float, C.c_int]),
+    "add_particle_sink": (C.c_int, [Vec3, Vec3, C.c_float]),
+    "set_source_state": (None, [C.c_int, C.c_int]),
+    "set_sink_state": (None, [C.c_int, C.c_int]),
+    "get_source_spawned": (C.c_int, [C.c_int]),
+    "get_sink_despawned": (C.c_int, [C.c_int]),
     "lustrine_last_status": (C.c_int, []),
     "lustrine_global_context": (_P, []),
     "lustrine_free_grid": (None, [C.POINTER(GridWrapper)]),
@@ -129,6 +135,9 @@ SIGNATURES = {
     "lustrine_pbf_neighbors": (C.c_int, [_P, _P, _P, C.c_int]),
     "lustrine_pbf_reduce": (C.c_int, [_P, _DP]),
     "lustrine_pbf_query_cell_count": (C.c_int, [_P, _FP, _FP, C.c_int, _IP]),
+    "lustrine_pbf_reserve": (C.c_int, [_P, C.c_int]),
+    "lustrine_pbf_spawn": (C.c_int, [_P, _P, _P, C.c_int]),
+    "lustrine_pbf_despawn_cells": (C.c_int, [_P, _P, C.c_int, _IP]),
     "lustrine_pbf_status": (C.c_int, [_P]),
     "lustrine_pbf_stream": (C.c_int, [_P, C.POINTER(_P)]),
     "lustrine_pbf_launches_per_step": (C.c_int, [_P]),

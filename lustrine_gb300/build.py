@@ -28,9 +28,12 @@ UNITS = {
     "pbf_compat.cu": ["--fmad=false"],
     "pbf_solver.cu": [],
     "pbf_context.cu": [],
+    "pbf_dynamic.cu": [],
     "pbf_sort_api.cu": [],
     "pbf_sort_noalloc.cu": [],
-    "lustrine_wrapper.cpp": [],
+    # host float math of scene construction and sources as the reference's
+    # (no FMA contraction, which GCC applies by default on aarch64)
+    "lustrine_wrapper.cpp": ["-Xcompiler", "-ffp-contract=off"],
 }
 
 

@@ -25,6 +25,32 @@ int g_num_sand = 0;
 int g_num_solid = 0;
 float g_cell_size = 0.0f;
 
+// Particle sources and sinks (Simulation::source / sink, Lustrine.cpp:745-861,
+// 916-1017), host-side bookkeeping around the device step.
+struct Source {
+    std::vector<float> pattern;  // init_chunk_from_grid positions of the pattern grid
+    float dir[3];                // normalised at creation
+    float freq;
+    int capacity, spawned = 0;
+    float timer = 0.0f;
+    bool state = true;
+};
+struct Sink {
+    std::vector<int> cells;  // ascending cell ids of the box
+    float freq;
+    int despawned = 0;  // never incremented, as in the reference (Lustrine.cpp:812-816)
+    float timer = 0.0f;
+    bool state = true;
+};
+std::vector<Source> g_sources;
+std::vector<Sink> g_sinks;
+float g_total_time = 0.0f;
+int g_remaining = 0;  // Simulation::num_remaining_sand_particles
+float g_radius = 0.0f, g_diameter = 0.0f;
+float g_gravity[3] = {0.0f, 0.0f, 0.0f};
+float g_domain[3] = {0.0f, 0.0f, 0.0f};
+int g_grid[3] = {0, 0, 0};
+
 // init_chunk_from_grid (Lustrine.cpp:676-722).  The chunk holds
 // num_occupied * sub^3 entries; cells skipped by the mask leave (0, 0, 0)
 // entries at the end, as in the reference.
@@ -62,6 +88,75 @@ void release() {
     if (g_ctx) lustrine_pbf_destroy(g_ctx);
     g_ctx = nullptr;
     g_num_sand = g_num_solid = 0;
+    g_sources.clear();
+    g_sinks.clear();
+    g_total_time = 0.0f;
+    g_remaining = 0;
+}
+
+// get_cell_indices (neighbors/Utils.hpp:13-21): clamp to [cell/2, domain -
+// cell/2] (bounds formed in double, as glm::vec3(double) does), divide,
+// truncate.
+void cell_indices(const Vec3& p, int out[3]) {
+    const float v[3] = {p.x, p.y, p.z};
+    for (int a = 0; a < 3; a++) {
+        const float lo = (float)((double)g_cell_size * 0.5);
+        const float hi = (float)((double)g_domain[a] - (double)g_cell_size * 0.5);
+        out[a] = (int)(std::min(std::max(v[a], lo), hi) / g_cell_size);
+    }
+}
+
+// Lustrine::simulate (Lustrine.cpp:730-861): sources spawn before the step,
+// sinks remove after it.
+int simulate_frame(float dt) {
+    const float dt_clamped = 0.016f;  // Lustrine.cpp:745
+    for (Source& src : g_sources) src.timer += dt_clamped;
+    for (Source& src : g_sources) {
+        if (!(src.state && src.spawned < src.capacity && src.timer >= src.freq)) continue;
+        const int num = (int)(src.pattern.size() / 3);
+        if (g_remaining < num) continue;
+        const float freq = src.freq;
+        const float t_last = g_total_time;
+        const float offset = freq - std::fmod(t_last, freq);
+        const float speed = freq > 0.0f ? 1.0f * g_diameter / freq : 1.0f;
+        // j = 0 of the reference's spawn loop: offset along the direction,
+        // velocity direction * speed (+ gravity * 0)
+        float off[3], vel[3];
+        for (int a = 0; a < 3; a++) {
+            const float zero = 0.0f * g_diameter * src.dir[a];
+            off[a] = zero + src.dir[a] * offset;
+            vel[a] = src.dir[a] * speed + g_gravity[a] * (0.0f * freq);
+        }
+        std::vector<float> x((size_t)num * 3), v((size_t)num * 3);
+        for (int k = 0; k < num; k++)
+            for (int a = 0; a < 3; a++) {
+                x[3 * (size_t)k + a] = src.pattern[3 * (size_t)k + a] + off[a];
+                v[3 * (size_t)k + a] = vel[a];
+            }
+        if (num > 0)  // Lustrine.cpp:790: a small perturbation against stacking
+            for (int a = 0; a < 3; a++) v[3 * (size_t)(num / 2) + a] += 0.001f * 1.0f;
+        const int rc = lustrine_pbf_spawn(g_ctx, x.data(), v.data(), num);
+        if (rc) return rc;
+        g_num_sand += num;
+        g_remaining -= num;
+        src.timer = 0.0f;
+        src.spawned += num;
+    }
+    int rc = lustrine_pbf_step(g_ctx, dt);
+    if (rc) return rc;
+    std::vector<int> evict_cells;
+    for (const Sink& sk : g_sinks)
+        if (sk.state && sk.timer >= sk.freq) evict_cells.insert(evict_cells.end(), sk.cells.begin(), sk.cells.end());
+    if (!evict_cells.empty()) {
+        int removed = 0;
+        rc = lustrine_pbf_despawn_cells(g_ctx, evict_cells.data(), (int)evict_cells.size(), &removed);
+        if (rc) return rc;
+        g_num_sand -= removed;
+        g_remaining += removed;
+    }
+    for (Sink& sk : g_sinks) sk.timer += dt;
+    g_total_time += dt_clamped;
+    return LUSTRINE_OK;
 }
 
 void init_common(const SimulationParameters* prm, SimulationData* data, GridWrapper* sand, int num_sand,
@@ -87,7 +182,14 @@ void init_common(const SimulationParameters* prm, SimulationData* data, GridWrap
 
     lustrine_pbf_params p;
     lustrine_pbf_params_reference(&p, prm->X, prm->Y, prm->Z, prm->particleRadius, kernel_radius_scale);
+    // Lustrine.cpp:105-126,237: the allocation holds max(n + ns, X Y Z sub^3)
+    // particles; sources may add num_remaining = total - 1 - ns - n of them
+    // (room for them is reserved, up to 2^22 extra particles)
+    const double guess = (double)prm->X * prm->Y * prm->Z * subdivision * subdivision * subdivision;
+    const long long total = std::max<long long>((long long)n + ns, (long long)guess);
+    const long long room = std::max<long long>(0, std::min<long long>(total - 1 - ns - n, 1LL << 22));
     int rc = lustrine_pbf_create(&p, n, ns, &g_ctx);
+    if (!rc && room > 0) rc = lustrine_pbf_reserve(g_ctx, (int)(n + room));
     if (!rc) rc = lustrine_pbf_upload(g_ctx, xs.data(), nullptr, sol.data());
     if (rc) {
         release();
@@ -97,10 +199,16 @@ void init_common(const SimulationParameters* prm, SimulationData* data, GridWrap
     g_num_sand = n;
     g_num_solid = ns;
     g_cell_size = p.cell_size;
+    g_remaining = (int)room;
+    g_radius = prm->particleRadius;
+    g_diameter = prm->particleDiameter;
+    for (int a = 0; a < 3; a++) {
+        g_gravity[a] = p.gravity[a];
+        g_domain[a] = (float)p.domain[a];
+        g_grid[a] = (int)(g_domain[a] / p.cell_size) + 1;
+    }
 
     // Lustrine.cpp:105-126,208-217: index ranges of the reference's arrays
-    const double guess = (double)prm->X * prm->Y * prm->Z * subdivision * subdivision * subdivision;
-    const long long total = std::max<long long>((long long)n + ns, (long long)guess);
     long long solid_start = total - ns, solid_end = total;
     if (ns == 0) solid_start = solid_end = total - 1;  // Lustrine.cpp:219-222
     data->num_sand_particles = n;
@@ -138,10 +246,88 @@ void init_simulation_extra_parameters(const SimulationParameters* parameters, Si
 void simulate(float dt, bool attract_flag, bool blow_flag) {
     (void)attract_flag;
     (void)blow_flag;
-    g_status = g_ctx ? lustrine_pbf_step(g_ctx, dt) : LUSTRINE_ERR_NO_SIMULATION;
+    g_status = g_ctx ? simulate_frame(dt) : LUSTRINE_ERR_NO_SIMULATION;
 }
 
-void simulate_no_flags(float dt) { g_status = g_ctx ? lustrine_pbf_step(g_ctx, dt) : LUSTRINE_ERR_NO_SIMULATION; }
+void simulate_no_flags(float dt) { g_status = g_ctx ? simulate_frame(dt) : LUSTRINE_ERR_NO_SIMULATION; }
+
+// LustrineWrapper.cpp:679-703 / Lustrine.cpp:916-1017
+int add_particle_source(GridWrapper* pattern, Vec3 direction, float freq, int capacity) {
+    if (!g_ctx) {
+        g_status = LUSTRINE_ERR_NO_SIMULATION;
+        return -1;
+    }
+    if (!pattern) {
+        g_status = LUSTRINE_ERR_ARGS;
+        return -1;
+    }
+    Source src;
+    chunk_positions(*pattern, g_diameter, 1, false, src.pattern);
+    const float len = std::sqrt(direction.x * direction.x + direction.y * direction.y + direction.z * direction.z);
+    src.dir[0] = direction.x / len;
+    src.dir[1] = direction.y / len;
+    src.dir[2] = direction.z / len;
+    src.freq = freq;
+    src.capacity = capacity < 0 ? 0x7fffffff : capacity;
+    g_sources.push_back(src);
+    g_status = LUSTRINE_OK;
+    return (int)g_sources.size() - 1;
+}
+
+int add_particle_sink(Vec3 min_pos, Vec3 max_pos, float frequency) {
+    if (!g_ctx) {
+        g_status = LUSTRINE_ERR_NO_SIMULATION;
+        return -1;
+    }
+    int lo[3], hi[3];
+    cell_indices(min_pos, lo);
+    cell_indices(max_pos, hi);
+    Sink sk;
+    sk.freq = frequency;
+    for (int y = lo[1]; y <= hi[1]; y++)
+        for (int x = lo[0]; x <= hi[0]; x++)
+            for (int z = lo[2]; z <= hi[2]; z++) sk.cells.push_back(y * g_grid[0] * g_grid[2] + x * g_grid[2] + z);
+    std::sort(sk.cells.begin(), sk.cells.end());
+    g_sinks.push_back(sk);
+    g_status = LUSTRINE_OK;
+    return (int)g_sinks.size() - 1;
+}
+
+void set_source_state(int index, int state) {
+    if (index < 0 || index >= (int)g_sources.size()) {
+        g_status = LUSTRINE_ERR_ARGS;
+        return;
+    }
+    g_sources[(size_t)index].state = state != 0;
+    g_status = LUSTRINE_OK;
+}
+
+void set_sink_state(int index, int state) {
+    if (index < 0 || index >= (int)g_sinks.size()) {
+        g_status = LUSTRINE_ERR_ARGS;
+        return;
+    }
+    g_sinks[(size_t)index].state = state != 0;
+    g_status = LUSTRINE_OK;
+}
+
+int get_source_spawned(int index) {
+    if (index < 0 || index >= (int)g_sources.size()) {
+        g_status = LUSTRINE_ERR_ARGS;
+        return 0;
+    }
+    g_status = LUSTRINE_OK;
+    return g_sources[(size_t)index].spawned;
+}
+
+int get_sink_despawned(int index) {
+    if (index < 0 || index >= (int)g_sinks.size()) {
+        g_status = LUSTRINE_ERR_ARGS;
+        return 0;
+    }
+    g_status = LUSTRINE_OK;
+    return g_sinks[(size_t)index].despawned;
+}
 
 void simulation_bind_positions_copy(float* position_ptr) {
     if (!g_ctx) {

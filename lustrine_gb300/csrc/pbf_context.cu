@@ -34,11 +34,6 @@ int bits_for(int values) {
 
 }  // namespace
 
-#define CK(call)                                                     \
-    do {                                                             \
-        cudaError_t e_ = (call);                                     \
-        if (e_ != cudaSuccess) return lgb_cuda_status(e_, #call);    \
-    } while (0)
 
 int lgb_cuda_status(cudaError_t e, const char* what) {
     if (getenv("LUSTRINE_DEBUG")) fprintf(stderr, "lustrine: %s: %s\n", what, cudaGetErrorString(e));
@@ -184,19 +179,46 @@ static int derive(const lustrine_pbf_params& q, int n, int ns, StepParams* sp, C
 }
 
 lustrine_pbf::~lustrine_pbf() {
+    free_buffers();
+    if (stream) cudaStreamDestroy(stream);
+}
+
+void lustrine_pbf::free_buffers() {
     for (int k = 0; k < 2; k++)
         if (graph_exec[k]) cudaGraphExecDestroy(graph_exec[k]);
+    graph_exec[0] = graph_exec[1] = nullptr;
     void* ptrs[] = {x[0], x[1], xs[0], xs[1], v[0], v[1], id[0], id[1], xs_alt, vtmp, key, key_sorted,
                     rank, tmp, perm, count, start, block_sums, tile_sum, solid_near, solid, solid_raw, sstart, nbr, cnt, lam,
                     lam_by_id, rho, status, red, qcount, out3, out3d, iota, solid_id, d_scenes, d_scene_of,
                     d_solid_scene_of, cellk, cell_sorted, solid_cell};
     for (void* q : ptrs)
         if (q) cudaFree(q);
-    if (stream) cudaStreamDestroy(stream);
+    x[0] = x[1] = xs[0] = xs[1] = v[0] = v[1] = nullptr;
+    id[0] = id[1] = nullptr;
+    xs_alt = vtmp = solid = solid_raw = lam_src = nullptr;
+    key = key_sorted = rank = tmp = perm = count = start = block_sums = tile_sum = sstart = nullptr;
+    nbr = cnt = status = qcount = iota = solid_id = d_scene_of = d_solid_scene_of = nullptr;
+    cellk = cell_sorted = solid_cell = nullptr;
+    solid_near = nullptr;
+    lam = lam_by_id = rho = out3 = nullptr;
+    red = out3d = nullptr;
+    d_scenes = nullptr;
 }
 
+int lgb_write_sentinel(lustrine_pbf* s) {
+    // the sentinel particle of the padded neighbour lists, at slot n
+    const float4 far = make_float4(SENTINEL_POS, SENTINEL_POS, SENTINEL_POS, 0.0f);
+    const int n = s->n;
+    for (float4* a : {s->xs[0], s->xs[1], s->xs_alt})
+        CK(cudaMemcpyAsync(a + n, &far, sizeof(float4), cudaMemcpyHostToDevice, s->stream));
+    CK(cudaMemsetAsync(s->vtmp + n, 0, sizeof(float4), s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return LUSTRINE_OK;
+}
+
+// Device buffers for s->cap fluid particles (s->n of them active).
 static int ctx_alloc(lustrine_pbf* s) {
-    const int n = s->n, ns = s->ns, C = s->sp.num_cells, m = n > ns ? n : ns;
+    const int n = s->cap, ns = s->ns, C = s->sp.num_cells, m = n > ns ? n : ns;
     int rc = LUSTRINE_OK;
     for (int k = 0; k < 2 && !rc; k++) {
         rc = rc ? rc : dalloc(&s->x[k], n);
@@ -207,7 +229,7 @@ static int ctx_alloc(lustrine_pbf* s) {
     rc = rc ? rc : dalloc(&s->xs_alt, (size_t)n + 1);
     rc = rc ? rc : dalloc(&s->vtmp, (size_t)n + 1);
     rc = rc ? rc : dalloc(&s->key, m);
-    rc = rc ? rc : dalloc(&s->key_sorted, n);
+    rc = rc ? rc : dalloc(&s->key_sorted, m);  // m: key and key_sorted trade places after a despawn
     rc = rc ? rc : dalloc(&s->rank, m);
     rc = rc ? rc : dalloc(&s->tmp, m);
     rc = rc ? rc : dalloc(&s->perm, m);
@@ -249,12 +271,8 @@ static int ctx_alloc(lustrine_pbf* s) {
         for (int i = 0; i < n; i++) ids[(size_t)i] = i;
         CK(cudaMemcpy(s->iota, ids.data(), (size_t)n * sizeof(int), cudaMemcpyHostToDevice));
     }
-    {  // the sentinel particle of the padded neighbour lists
-        const float4 far = make_float4(SENTINEL_POS, SENTINEL_POS, SENTINEL_POS, 0.0f);
-        for (float4* a : {s->xs[0], s->xs[1], s->xs_alt})
-            CK(cudaMemcpy(a + n, &far, sizeof(float4), cudaMemcpyHostToDevice));
-        CK(cudaMemset(s->vtmp + n, 0, sizeof(float4)));
-    }
+    rc = lgb_write_sentinel(s);
+    if (rc) return rc;
     CK(cudaMemsetAsync(s->lam_by_id, 0, s->lam_by_id_len * sizeof(float), s->stream));
     CK(cudaMemsetAsync(s->lam, 0, (size_t)(n ? n : 1) * sizeof(float), s->stream));
     CK(cudaMemsetAsync(s->rho, 0, (size_t)(n ? n : 1) * sizeof(float), s->stream));
@@ -274,6 +292,7 @@ extern "C" int lustrine_pbf_create(const lustrine_pbf_params* p, int n_fluid, in
     if (!s) return LUSTRINE_ERR_NOMEM;
     s->prm = *p;
     s->n = n_fluid;
+    s->cap = n_fluid;
     s->ns = n_solid;
     int rc = derive(*p, n_fluid, n_solid, &s->sp, &s->cp);
     if (rc) {
@@ -291,6 +310,25 @@ extern "C" int lustrine_pbf_create(const lustrine_pbf_params* p, int n_fluid, in
     }
     *out = s;
     return LUSTRINE_OK;
+}
+
+extern "C" int lustrine_pbf_reserve(lustrine_pbf* s, int capacity) {
+    if (!s || capacity < s->n) return LUSTRINE_ERR_ARGS;
+    if (s->is_batch() || s->have_state) return LUSTRINE_ERR_UNSUPPORTED;
+    if (capacity == s->cap) return LUSTRINE_OK;
+    StepParams sp;
+    CellPack cp;
+    // grid table sized for the capacity (hash buckets follow the particle count)
+    int rc = derive(s->prm, capacity, s->ns, &sp, &cp);
+    if (rc) return rc;
+    sp.n = s->n;
+    CK(cudaStreamSynchronize(s->stream));
+    s->free_buffers();
+    s->sp = sp;
+    s->cp = cp;
+    s->cap = capacity;
+    s->steps_done = 0;
+    return ctx_alloc(s);
 }
 
 // Batch geometry: every scene's grid and box, cells numbered scene after
@@ -359,6 +397,7 @@ extern "C" int lustrine_batch_create(const lustrine_pbf_params* p, int num_scene
         s->prm.domain[a] = m;
     }
     s->n = s->sp.n;
+    s->cap = s->n;
     s->ns = s->sp.ns;
     if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
         delete s;
@@ -420,7 +459,8 @@ extern "C" int lustrine_pbf_set_params(lustrine_pbf* s, const lustrine_pbf_param
         sp.dt = s->sp.dt;
         sp.inv_dt = s->sp.inv_dt;
     } else {
-        rc = derive(*p, s->n, s->ns, &sp, &cp);
+        rc = derive(*p, s->cap, s->ns, &sp, &cp);  // the grid table was sized for the capacity
+        sp.n = s->n;
         sp.dt = s->sp.dt;
         sp.inv_dt = s->sp.inv_dt;
         sp.cell_sorted = s->sp.cell_sorted;
@@ -526,6 +566,7 @@ extern "C" int lustrine_pbf_upload(lustrine_pbf* s, const float* x, const float*
     CK(cudaStreamSynchronize(s->stream));
     s->have_state = true;
     s->lists_valid = false;
+    s->cells_valid = false;
     return LUSTRINE_OK;
 }
 
@@ -541,6 +582,7 @@ extern "C" int lustrine_pbf_upload_device(lustrine_pbf* s, const float* x, const
     CK(cudaStreamSynchronize(s->stream));
     s->have_state = true;
     s->lists_valid = false;
+    s->cells_valid = false;
     return LUSTRINE_OK;
 }
 
@@ -646,6 +688,7 @@ static int enqueue_step(lustrine_pbf* s, cudaStream_t st, StageMarks* mk = nullp
 static void finish_step(lustrine_pbf* s, int c) {
     s->cur = 1 - c;
     s->lists_valid = true;
+    s->cells_valid = true;
     s->steps_done++;
     // PBF: iteration k's lambdas are written into xs[1 - c] for even k and
     // into xs_alt for odd k (the Jacobi ping-pong)
@@ -1002,7 +1045,7 @@ extern "C" int lustrine_pbf_query_cell_count(lustrine_pbf* s, const float min_po
     // an empty range (min above max on an axis) counts nothing, as the
     // reference's loops do
     if (box[0] > box[1] || box[2] > box[3] || box[4] > box[5]) return LUSTRINE_OK;
-    if (!s->lists_valid) return LUSTRINE_OK;  // no step yet: the cell table is empty
+    if (!s->cells_valid) return LUSTRINE_OK;  // no step yet: the cell table is empty
     CK(cudaMemsetAsync(s->qcount, 0, sizeof(int), s->stream));
     const bool solids = include_solid && s->ns > 0;
     launch_query_cells(s->sp, s->cp, box, s->start, solids ? s->sstart : nullptr, s->cell_sorted,

@@ -10,12 +10,20 @@
 
 int lgb_cuda_status(cudaError_t e, const char* what);
 
+#define CK(call)                                                     \
+    do {                                                             \
+        cudaError_t e_ = (call);                                     \
+        if (e_ != cudaSuccess) return lgb_cuda_status(e_, #call);    \
+    } while (0)
+
+
 struct lustrine_pbf {
     lustrine_pbf_params prm{};
     lgb::StepParams sp{};
     lgb::CellPack cp{};
     lgb::Tuning tune{128, 4, 128};
     int n = 0, ns = 0;
+    int cap = 0;  // fluid particles the buffers hold (n <= cap; sources append up to it)
     cudaStream_t stream = nullptr;
 
     // fluid state, two sides: the committed state is on side `cur`; a step
@@ -79,8 +87,13 @@ struct lustrine_pbf {
     bool have_state = false;
     bool use_pdl = true;  // programmatic dependent launch between step kernels
     bool lists_valid = false;
+    bool cells_valid = false;  // start[] / sstart[] bin the current slots (queries, sinks)
 
     ~lustrine_pbf();
+    void free_buffers();
     void invalidate_graphs();
     bool mixed() const;
 };
+
+// Writes the sentinel particle of the padded neighbour lists at slot s->n.
+int lgb_write_sentinel(lustrine_pbf* s);

@@ -236,6 +236,27 @@ class PbfSim:
               "profile_step")
         return {k: (ms[i], cnt[i]) for i, k in enumerate(self.STAGES)}
 
+    def reserve(self, capacity: int):
+        """Room for up to `capacity` fluid particles (before the first upload)."""
+        check(self.lib.lustrine_pbf_reserve(self.h, int(capacity)), "reserve")
+
+    def spawn(self, x, v=None):
+        """Append particles (caller indices n, n+1, ...)."""
+        x = np.ascontiguousarray(x, np.float32).reshape(-1, 3)
+        vv = None if v is None else np.ascontiguousarray(v, np.float32).reshape(-1, 3)
+        check(self.lib.lustrine_pbf_spawn(self.h, _ptr(x), _ptr(vv), len(x)), "spawn")
+        self.n += len(x)
+
+    def despawn_cells(self, cells) -> int:
+        """Remove the particles the last step binned in `cells` (swap-remove
+        semantics of the reference's sinks); returns how many left."""
+        cells = np.ascontiguousarray(cells, np.int32).reshape(-1)
+        out = C.c_int(0)
+        check(self.lib.lustrine_pbf_despawn_cells(self.h, _ptr(cells), len(cells), C.byref(out)),
+              "despawn_cells")
+        self.n -= int(out.value)
+        return int(out.value)
+
     def query_cell_count(self, min_pos, max_pos, include_solid: bool = False) -> int:
         """Particles the last step binned in the cells of the box
         (Lustrine::query_cell_num_particles)."""

@@ -14,7 +14,8 @@ from . import _lib
 from ._lib import Color, GridWrapper, SimulationData, SimulationParameters, Vec3
 
 __all__ = ["SimulationParameters", "SimulationData", "GridWrapper", "Vec3", "Color",
-           "query_cell_num_particles",
+           "query_cell_num_particles", "add_particle_source", "add_particle_sink",
+           "set_source_state", "set_sink_state", "get_source_spawned", "get_sink_despawned",
            "init_grid_box", "init_simulation", "init_simulation_extra_parameters", "simulate",
            "simulate_no_flags", "simulation_bind_positions_copy", "cleanup_simulation",
            "get_num_sand_particles", "get_grid_cell_size", "set_simulate_function",
@@ -105,6 +106,30 @@ def get_grid_cell_size() -> int:
 
 def query_cell_num_particles(min_pos, max_pos, include_solid: bool = False) -> int:
     return int(_lib_().query_cell_num_particles(Vec3(*min_pos), Vec3(*max_pos), bool(include_solid)))
+
+
+def add_particle_source(pattern: GridWrapper, direction, freq: float, capacity: int = -1) -> int:
+    return int(_lib_().add_particle_source(C.byref(pattern), Vec3(*direction), float(freq), int(capacity)))
+
+
+def add_particle_sink(min_pos, max_pos, frequency: float) -> int:
+    return int(_lib_().add_particle_sink(Vec3(*min_pos), Vec3(*max_pos), float(frequency)))
+
+
+def set_source_state(index: int, state: bool):
+    _lib_().set_source_state(int(index), 1 if state else 0)
+
+
+def set_sink_state(index: int, state: bool):
+    _lib_().set_sink_state(int(index), 1 if state else 0)
+
+
+def get_source_spawned(index: int) -> int:
+    return int(_lib_().get_source_spawned(int(index)))
+
+
+def get_sink_despawned(index: int) -> int:
+    return int(_lib_().get_sink_despawned(int(index)))
 
 
 def set_simulate_function(index: int):
