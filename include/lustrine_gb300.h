@@ -285,6 +285,10 @@ LUSTRINE_API int lustrine_pbf_query_cell_count(lustrine_pbf* s, const float min_
 LUSTRINE_API int lustrine_pbf_reserve(lustrine_pbf* s, int capacity);
 LUSTRINE_API int lustrine_pbf_spawn(lustrine_pbf* s, const float* x, const float* v, int m);
 LUSTRINE_API int lustrine_pbf_despawn_cells(lustrine_pbf* s, const int* cells, int ncells, int* removed);
+/* Sets the fluid count to n (<= the capacity) for a caller that keeps the
+ * state on the host and uploads all of it next (lustrine_pbf_upload_state_async);
+ * the particles' contents are undefined until then. */
+LUSTRINE_API int lustrine_pbf_set_count(lustrine_pbf* s, int n);
 /* Device-side error bits since the last call, as a status code (synchronises). */
 LUSTRINE_API int lustrine_pbf_status(lustrine_pbf* s);
 /* The context's cudaStream_t, as void*. */

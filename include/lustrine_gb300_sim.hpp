@@ -24,7 +24,9 @@
 // positions, positions_star, velocities and lambdas back.  The device
 // context of a Simulation is created on its first call (solids are uploaded
 // then: they are static in the fluid step) and kept until
-// lustrine_gb300::release(sim).  Errors are reported by last_status(), the
+// lustrine_gb300::release(sim); when the sand count changes (the reference's
+// sources and sinks run on the host around the step) the context takes the
+// new count, growing its buffers by doubling.  Errors are reported by last_status(), the
 // step itself returning void like the reference's.
 #pragma once
 
@@ -40,7 +42,7 @@ namespace lustrine_gb300 {
 namespace detail {
 struct Entry {
     lustrine_pbf* ctx = nullptr;
-    int n = 0, ns = 0;
+    int n = 0, ns = 0, cap = 0;
 };
 inline std::unordered_map<const void*, Entry>& table() {
     static std::unordered_map<const void*, Entry> t;
@@ -103,14 +105,17 @@ void simulate_fluid(Simulation* sim, float dt) {
     }
     const lustrine_pbf_params p = detail::params_of(sim);
     int rc = LUSTRINE_OK;
-    if (e.ctx && (e.n != n || e.ns != ns)) {  // particles were added or removed
+    if (e.ctx && (e.ns != ns || n > e.cap)) {  // solids changed, or more sand than the buffers hold
         release(sim);
-        e = detail::Entry{};
+        e.ctx = nullptr;
     }
     float* x = reinterpret_cast<float*>(sim->positions) + 3 * (size_t)start;
     float* v = reinterpret_cast<float*>(sim->velocities) + 3 * (size_t)start;
     if (!e.ctx) {
+        // sources add sand between steps (Lustrine.cpp:745-800): room for growth
+        const int cap = n > e.cap ? (e.cap ? (n > 2 * e.cap ? n : 2 * e.cap) : n) : e.cap;
         rc = lustrine_pbf_create(&p, n, ns, &e.ctx);
+        if (!rc && cap > n) rc = lustrine_pbf_reserve(e.ctx, cap);
         const float* solid = ns ? reinterpret_cast<const float*>(sim->positions) + 3 * (size_t)sim->ptr_solid_start
                                 : nullptr;
         if (!rc) rc = lustrine_pbf_upload(e.ctx, x, v, solid);
@@ -121,6 +126,7 @@ void simulate_fluid(Simulation* sim, float dt) {
         }
         e.n = n;
         e.ns = ns;
+        e.cap = cap > n ? cap : n;
         std::lock_guard<std::mutex> lock(detail::table_mutex());
         detail::table()[sim] = e;
     } else {
@@ -132,6 +138,12 @@ void simulate_fluid(Simulation* sim, float dt) {
         cur.use_graph = p.use_graph;
         cur.max_neighbors = p.max_neighbors;
         if (std::memcmp(&cur, &p, sizeof(p)) != 0) rc = lustrine_pbf_set_params(e.ctx, &p);
+        if (!rc && n != e.n) {  // sand added or removed by the host since the last step
+            rc = lustrine_pbf_set_count(e.ctx, n);
+            e.n = n;
+            std::lock_guard<std::mutex> lock(detail::table_mutex());
+            detail::table()[sim] = e;
+        }
         if (!rc) rc = lustrine_pbf_upload_state_async(e.ctx, x, v);
     }
     if (!rc) rc = lustrine_pbf_step(e.ctx, dt);

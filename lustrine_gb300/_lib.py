@@ -138,6 +138,7 @@ SIGNATURES = {
     "lustrine_pbf_reserve": (C.c_int, [_P, C.c_int]),
     "lustrine_pbf_spawn": (C.c_int, [_P, _P, _P, C.c_int]),
     "lustrine_pbf_despawn_cells": (C.c_int, [_P, _P, C.c_int, _IP]),
+    "lustrine_pbf_set_count": (C.c_int, [_P, C.c_int]),
     "lustrine_pbf_status": (C.c_int, [_P]),
     "lustrine_pbf_stream": (C.c_int, [_P, C.POINTER(_P)]),
     "lustrine_pbf_launches_per_step": (C.c_int, [_P]),

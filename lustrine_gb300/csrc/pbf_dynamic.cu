@@ -134,6 +134,20 @@ extern "C" int lustrine_pbf_spawn(lustrine_pbf* s, const float* x, const float* 
     return after_resize(s);
 }
 
+extern "C" int lustrine_pbf_set_count(lustrine_pbf* s, int n) {
+    if (!s || n < 0) return LUSTRINE_ERR_ARGS;
+    if (s->is_batch()) return LUSTRINE_ERR_UNSUPPORTED;
+    if (!s->have_state) return LUSTRINE_ERR_ARGS;
+    if (n > s->cap) return LUSTRINE_ERR_TOO_LARGE;
+    if (n == s->n) return LUSTRINE_OK;
+    if (n > s->n)  // identity labels for the new slots until the caller's state upload
+        CK(cudaMemcpyAsync(s->id[s->cur] + s->n, s->iota + s->n, (size_t)(n - s->n) * sizeof(int),
+                           cudaMemcpyDeviceToDevice, s->stream));
+    s->n = n;
+    s->cells_valid = false;
+    return after_resize(s);
+}
+
 extern "C" int lustrine_pbf_despawn_cells(lustrine_pbf* s, const int* cells, int ncells, int* removed) {
     if (!s || ncells < 0 || (ncells > 0 && !cells)) return LUSTRINE_ERR_ARGS;
     if (removed) *removed = 0;
