@@ -189,7 +189,7 @@ void lustrine_pbf::free_buffers() {
     graph_exec[0] = graph_exec[1] = nullptr;
     void* ptrs[] = {x[0], x[1], xs[0], xs[1], v[0], v[1], id[0], id[1], xs_alt, vtmp, key, key_sorted,
                     rank, tmp, perm, count, start, block_sums, tile_sum, solid_near, solid, solid_raw, sstart, nbr, cnt, lam,
-                    lam_by_id, rho, status, red, qcount, out3, out3d, iota, solid_id, d_scenes, d_scene_of,
+                    lam_by_id, rho, status, red, qcount, out3, out3d, iota, slot_of, solid_id, d_scenes, d_scene_of,
                     d_solid_scene_of, cellk, cell_sorted, solid_cell};
     for (void* q : ptrs)
         if (q) cudaFree(q);
@@ -197,7 +197,7 @@ void lustrine_pbf::free_buffers() {
     id[0] = id[1] = nullptr;
     xs_alt = vtmp = solid = solid_raw = lam_src = nullptr;
     key = key_sorted = rank = tmp = perm = count = start = block_sums = tile_sum = sstart = nullptr;
-    nbr = cnt = status = qcount = iota = solid_id = d_scene_of = d_solid_scene_of = nullptr;
+    nbr = cnt = status = qcount = iota = slot_of = solid_id = d_scene_of = d_solid_scene_of = nullptr;
     cellk = cell_sorted = solid_cell = nullptr;
     solid_near = nullptr;
     lam = lam_by_id = rho = out3 = nullptr;
@@ -254,6 +254,7 @@ static int ctx_alloc(lustrine_pbf* s) {
     rc = rc ? rc : dalloc(&s->out3, (size_t)3 * m);
     rc = rc ? rc : dalloc(&s->out3d, (size_t)3 * n);
     rc = rc ? rc : dalloc(&s->iota, n);
+    rc = rc ? rc : dalloc(&s->slot_of, n);
     rc = rc ? rc : dalloc(&s->solid_id, ns);
     if (ns > 0) {
         rc = rc ? rc : dalloc(&s->solid_near, (size_t)C);
@@ -586,10 +587,30 @@ extern "C" int lustrine_pbf_upload_device(lustrine_pbf* s, const float* x, const
     return LUSTRINE_OK;
 }
 
+// Device address of page-locked host memory the kernels can use directly,
+// or nullptr (pageable memory goes through a staging copy).
+static const void* host_view(const void* p) {
+    if (!p) return nullptr;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 extern "C" int lustrine_pbf_upload_state_async(lustrine_pbf* s, const float* x, const float* v) {
     if (!s || !s->have_state || (!x && s->n > 0)) return LUSTRINE_ERR_ARGS;
     const int n = s->n;
     if (!n) return LUSTRINE_OK;
+    const float* hx = (const float*)host_view(x);
+    const float* hv = (const float*)host_view(v);
+    if (hx && !s->is_batch() && (!v || hv)) {  // read straight from the page-locked buffers
+        const int c = s->cur;
+        launch_pack_state(s->mixed(), s->sp, s->cp, hx, hv, n, s->x[c], s->v[c], s->id[c], s->stream);
+        CK(cudaGetLastError());
+        return LUSTRINE_OK;
+    }
     // Written in caller order into the current side; the next step re-sorts.
     float* sx = (float*)s->out3d;
     CK(cudaMemcpyAsync(sx, x, (size_t)n * 3 * sizeof(float), cudaMemcpyHostToDevice, s->stream));
@@ -955,6 +976,15 @@ extern "C" int lustrine_pbf_download_state_async(lustrine_pbf* s, float* x, floa
     if (!s || !s->have_state) return LUSTRINE_ERR_ARGS;
     const int n = s->n;
     if (!n) return LUSTRINE_OK;
+    float* hx = (float*)host_view(x);
+    float* hv = (float*)host_view(v);
+    if ((!x || hx) && (!v || hv)) {  // write straight into the page-locked buffers
+        const int c = s->cur;
+        launch_unpack_state(s->mixed(), s->sp, s->cp, s->x[c], s->v[c], s->id[c], s->slot_of, n, hx, hv,
+                            s->stream);
+        CK(cudaGetLastError());
+        return LUSTRINE_OK;
+    }
     const size_t b3 = (size_t)n * 3 * sizeof(float);
     unpermute_state(s, x != nullptr, v != nullptr);
     if (x) CK(cudaMemcpyAsync(x, s->out3, b3, cudaMemcpyDeviceToHost, s->stream));

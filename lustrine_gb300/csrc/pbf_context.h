@@ -36,6 +36,7 @@ struct lustrine_pbf {
     float4* xs_alt = nullptr;  // Jacobi ping-pong partner of xs
     float4* vtmp = nullptr;    // velocities before XSPH
     int* iota = nullptr;       // 0..n-1
+    int* slot_of = nullptr;    // slot of every caller index (state download)
 
     // counting sort
     int* key = nullptr;

@@ -98,6 +98,12 @@ void launch_pack_pos(bool mixed, const StepParams& p, const CellPack& cp, const 
 void launch_query_cells(const StepParams& p, const CellPack& cp, const int box[6], const int* fstart,
                         const int* sstart, const int* cell_sorted, const int* solid_cell, int* out,
                         cudaStream_t st);
+// state from / into host-visible memory (page-locked host buffers read and
+// written by the kernels): hv may be nullptr (zero velocities / not written)
+void launch_pack_state(bool mixed, const StepParams& p, const CellPack& cp, const float* hx, const float* hv,
+                       int n, float4* x, float4* v, int* id, cudaStream_t st);
+void launch_unpack_state(bool mixed, const StepParams& p, const CellPack& cp, const float4* x, const float4* v,
+                         const int* id, int* slot_of, int n, float* hx, float* hv, cudaStream_t st);
 void launch_reduce(bool mixed, const StepParams& p, const CellPack& cp, const float4* x,
                    const float4* v, const float* rho, double* out, cudaStream_t st);
 

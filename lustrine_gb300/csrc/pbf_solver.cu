@@ -704,6 +704,22 @@ __global__ void k_unpermute_pos_d(StepParams p, CellPack cp, const float4* __res
     out[3 * (size_t)i + 2] = bz + (double)q.z;
 }
 
+// Caller position into the state representation.  Mixed: the cell is
+// clamped to the cells a clamped position can occupy (the packed field
+// widths); the offset keeps the exact position, so a caller position outside
+// the box stays where it is (it may then lie outside [0, cell)) and the next
+// prediction clamps it like the plain form does.
+template <bool MIXED>
+__device__ __forceinline__ float4 pack_position(const StepParams& p, const CellPack& cp, const Geo& g, float x,
+                                                float y, float z) {
+    if (!MIXED) return make_float4(x, y, z, 0.0f);
+    int cx = min(max((int)floorf(x * p.inv_cell), 0), (int)floorf(g.hix * p.inv_cell));
+    int cy = min(max((int)floorf(y * p.inv_cell), 0), (int)floorf(g.hiy * p.inv_cell));
+    int cz = min(max((int)floorf(z * p.inv_cell), 0), (int)floorf(g.hiz * p.inv_cell));
+    return make_float4(x - (float)cx * p.cell, y - (float)cy * p.cell, z - (float)cz * p.cell,
+                       pack_cell(cp, cx, cy, cz));
+}
+
 // Caller positions (float3, id order) into the state representation, slot = id.
 // scene_of: scene of each packed element in a batch (nullptr for one scene).
 template <bool MIXED>
@@ -711,21 +727,59 @@ __global__ void k_pack_pos(StepParams p, CellPack cp, const float* __restrict__ 
                            const int* __restrict__ scene_of, float4* __restrict__ out) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    float x = in[3 * (size_t)i], y = in[3 * (size_t)i + 1], z = in[3 * (size_t)i + 2];
-    if (!MIXED) {
-        out[i] = make_float4(x, y, z, 0.0f);
-        return;
-    }
-    // The cell is clamped to the cells a clamped position can occupy (the
-    // packed field widths); the offset keeps the exact position, so a caller
-    // position outside the box stays where it is (it may then lie outside
-    // [0, cell)) and the next prediction clamps it like the plain form does.
     const Geo g = (p.scenes && scene_of) ? geo_scene(p, scene_of[i]) : geo_single(p);
-    int cx = min(max((int)floorf(x * p.inv_cell), 0), (int)floorf(g.hix * p.inv_cell));
-    int cy = min(max((int)floorf(y * p.inv_cell), 0), (int)floorf(g.hiy * p.inv_cell));
-    int cz = min(max((int)floorf(z * p.inv_cell), 0), (int)floorf(g.hiz * p.inv_cell));
-    out[i] = make_float4(x - (float)cx * p.cell, y - (float)cy * p.cell, z - (float)cz * p.cell,
-                         pack_cell(cp, cx, cy, cz));
+    out[i] = pack_position<MIXED>(p, cp, g, in[3 * (size_t)i], in[3 * (size_t)i + 1], in[3 * (size_t)i + 2]);
+}
+
+// The state straight from / into page-locked host memory, which the GPU
+// reads and writes over the host link (no staging copy): caller order on the
+// host, slot order on the device.  Upload: slot = caller index.
+template <bool MIXED>
+__global__ void k_pack_state(StepParams p, CellPack cp, const float* __restrict__ hx,
+                             const float* __restrict__ hv, int n, float4* __restrict__ x,
+                             float4* __restrict__ v, int* __restrict__ id) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    x[i] = pack_position<MIXED>(p, cp, geo_single(p), hx[3 * (size_t)i], hx[3 * (size_t)i + 1],
+                                hx[3 * (size_t)i + 2]);
+    v[i] = hv ? make_float4(hv[3 * (size_t)i], hv[3 * (size_t)i + 1], hv[3 * (size_t)i + 2], 0.0f)
+              : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    id[i] = i;
+}
+
+__global__ void k_slot_of(const int* __restrict__ id, int n, int* __restrict__ slot_of) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < n) slot_of[id[s]] = s;
+}
+
+// Download: one thread per caller index gathers its slot, so the host writes
+// are contiguous.
+template <bool MIXED>
+__global__ void k_unpack_state(StepParams p, CellPack cp, const float4* __restrict__ x,
+                               const float4* __restrict__ v, const int* __restrict__ slot_of, int n,
+                               float* __restrict__ hx, float* __restrict__ hv) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int s = slot_of[i];
+    if (hx) {
+        const float4 q = x[s];
+        float a = q.x, b = q.y, c = q.z;
+        if (MIXED) {
+            const int3 cc = unpack_cell(cp, q.w);
+            a += (float)cc.x * p.cell;
+            b += (float)cc.y * p.cell;
+            c += (float)cc.z * p.cell;
+        }
+        hx[3 * (size_t)i] = a;
+        hx[3 * (size_t)i + 1] = b;
+        hx[3 * (size_t)i + 2] = c;
+    }
+    if (hv) {
+        const float4 u = v[s];
+        hv[3 * (size_t)i] = u.x;
+        hv[3 * (size_t)i + 1] = u.y;
+        hv[3 * (size_t)i + 2] = u.z;
+    }
 }
 
 // Particles binned in a box of cells by the last step (the sorted cell table
@@ -967,6 +1021,19 @@ void launch_pack_pos(bool mixed, const StepParams& p, const CellPack& cp, const 
                      const int* scene_of, float4* out, cudaStream_t st) {
     if (n <= 0) return;
     LGB_DISPATCH(mixed, k_pack_pos, blocks_for(n, 256), 256, st, p, cp, in, n, scene_of, out);
+}
+
+void launch_pack_state(bool mixed, const StepParams& p, const CellPack& cp, const float* hx, const float* hv,
+                       int n, float4* x, float4* v, int* id, cudaStream_t st) {
+    if (n <= 0) return;
+    LGB_DISPATCH(mixed, k_pack_state, blocks_for(n, 256), 256, st, p, cp, hx, hv, n, x, v, id);
+}
+
+void launch_unpack_state(bool mixed, const StepParams& p, const CellPack& cp, const float4* x, const float4* v,
+                         const int* id, int* slot_of, int n, float* hx, float* hv, cudaStream_t st) {
+    if (n <= 0) return;
+    launch_k(k_slot_of, blocks_for(n, 256), 256, st, pdl_enabled(), id, n, slot_of);
+    LGB_DISPATCH(mixed, k_unpack_state, blocks_for(n, 256), 256, st, p, cp, x, v, (const int*)slot_of, n, hx, hv);
 }
 
 void launch_reduce(bool mixed, const StepParams& p, const CellPack& cp, const float4* x,

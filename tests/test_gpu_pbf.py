@@ -246,3 +246,46 @@ def test_edge_cases_empty_single_and_no_solids():
     bad.iterations = 0
     with pytest.raises(LustrineError):
         PbfSim(bad, 10, 0)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_state_transfers_page_locked_and_pageable_agree(precision):
+    """upload/download_state_async read and write page-locked host buffers
+    directly from the kernels and stage pageable ones through copies: both
+    give the same states."""
+    torch = pytest.importorskip("torch")
+    from lustrine_gb300 import PbfSim, scenes
+    sc = scenes.config0(seed=29)
+    p = _params(sc, precision=precision)
+    a, b = PbfSim(p, sc.n), PbfSim(p, sc.n)
+    for s in (a, b):
+        s.upload(sc.x)
+        s.step(sc.dt, 2)
+    x_ref, v_ref, _, _ = a.download()
+    px = torch.empty((sc.n, 3), dtype=torch.float32).pin_memory()
+    pv = torch.empty((sc.n, 3), dtype=torch.float32).pin_memory()
+    a.download_state_async(px.data_ptr(), pv.data_ptr())
+    a.synchronize()
+    np.testing.assert_array_equal(px.numpy(), x_ref)
+    np.testing.assert_array_equal(pv.numpy(), v_ref)
+    hx, hv = np.empty_like(x_ref), np.empty_like(v_ref)
+    b.download_state_async(hx.ctypes.data, hv.ctypes.data)
+    b.synchronize()
+    np.testing.assert_array_equal(hx, x_ref)
+    # a new state in: page-locked into a, pageable into b
+    rng = np.random.default_rng(3)
+    nx = (x_ref + rng.uniform(-0.05, 0.05, x_ref.shape)).astype(np.float32)
+    nv = rng.normal(size=v_ref.shape).astype(np.float32)
+    px.numpy()[:] = nx
+    pv.numpy()[:] = nv
+    a.upload_state_async(px.data_ptr(), pv.data_ptr())
+    b.upload_state_async(nx.ctypes.data, nv.ctypes.data)
+    for s in (a, b):
+        s.step(sc.dt)
+    xa, va, _, _ = a.download()
+    xb, vb, _, _ = b.download()
+    np.testing.assert_array_equal(xa, xb)
+    np.testing.assert_array_equal(va, vb)
+    assert a.status() == 0 and b.status() == 0
+    a.close()
+    b.close()
