@@ -249,6 +249,11 @@ LUSTRINE_API int lustrine_pbf_download(lustrine_pbf* s, float* x, float* v, floa
                                        float* density);
 /* Asynchronous x, v download into host buffers (page-locked for overlap). */
 LUSTRINE_API int lustrine_pbf_download_state_async(lustrine_pbf* s, float* x, float* v);
+/* One frame for a host that keeps the state in its own arrays (x, v: 3 floats
+ * per particle, caller order): upload, one step, download into the same
+ * arrays, synchronise.  Page-locked arrays are read and written by the
+ * kernels directly; pageable ones go through staging copies. */
+LUSTRINE_API int lustrine_pbf_step_host(lustrine_pbf* s, float dt, float* x, float* v);
 /* Positions in double (exact for the mixed representation), host, synchronises. */
 LUSTRINE_API int lustrine_pbf_download_positions_f64(lustrine_pbf* s, double* x);
 /* Neighbour lists of the last step in the caller's ids (solids n_fluid + k):

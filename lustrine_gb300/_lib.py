@@ -131,6 +131,7 @@ SIGNATURES = {
     "lustrine_pbf_synchronize": (C.c_int, [_P]),
     "lustrine_pbf_download": (C.c_int, [_P, _P, _P, _P, _P]),
     "lustrine_pbf_download_state_async": (C.c_int, [_P, _P, _P]),
+    "lustrine_pbf_step_host": (C.c_int, [_P, C.c_float, _P, _P]),
     "lustrine_pbf_download_positions_f64": (C.c_int, [_P, _P]),
     "lustrine_pbf_neighbors": (C.c_int, [_P, _P, _P, C.c_int]),
     "lustrine_pbf_reduce": (C.c_int, [_P, _DP]),

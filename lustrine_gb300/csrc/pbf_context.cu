@@ -992,6 +992,16 @@ extern "C" int lustrine_pbf_download_state_async(lustrine_pbf* s, float* x, floa
     return LUSTRINE_OK;
 }
 
+// One frame of a host that keeps the state: upload, step, download, wait.
+extern "C" int lustrine_pbf_step_host(lustrine_pbf* s, float dt, float* x, float* v) {
+    if (!s || !x) return LUSTRINE_ERR_ARGS;
+    int rc = lustrine_pbf_upload_state_async(s, x, v);
+    if (!rc) rc = lustrine_pbf_step(s, dt);
+    if (!rc) rc = lustrine_pbf_download_state_async(s, x, v);
+    if (!rc) CK(cudaStreamSynchronize(s->stream));
+    return rc;
+}
+
 extern "C" int lustrine_pbf_download_positions_f64(lustrine_pbf* s, double* x) {
     if (!s || !s->have_state || !x) return LUSTRINE_ERR_ARGS;
     const int n = s->n;

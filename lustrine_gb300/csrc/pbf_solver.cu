@@ -733,17 +733,62 @@ __global__ void k_pack_pos(StepParams p, CellPack cp, const float* __restrict__ 
 
 // The state straight from / into page-locked host memory, which the GPU
 // reads and writes over the host link (no staging copy): caller order on the
-// host, slot order on the device.  Upload: slot = caller index.
+// host, slot order on the device.  A block moves the 3 x 256 floats of its
+// 256 particles through shared memory, so the host side is read and written
+// as consecutive 16-byte pieces by consecutive threads (the tail of the
+// array, and an array not 16-byte aligned, one float at a time).
+constexpr int HOST_BLOCK = 256;
+
+__device__ __forceinline__ void host_to_smem(const float* __restrict__ h, int n, float* sm) {
+    const int first = blockIdx.x * HOST_BLOCK;
+    const int m = min(HOST_BLOCK, n - first);
+    const size_t base = 3 * (size_t)first;
+    const int nf = 3 * m;
+    if ((reinterpret_cast<size_t>(h) & 15) == 0) {
+        const float4* h4 = reinterpret_cast<const float4*>(h + base);  // base is a multiple of 768 floats
+        for (int t = threadIdx.x; 4 * t + 3 < nf; t += HOST_BLOCK) {
+            const float4 q = h4[t];
+            sm[4 * t] = q.x;
+            sm[4 * t + 1] = q.y;
+            sm[4 * t + 2] = q.z;
+            sm[4 * t + 3] = q.w;
+        }
+        for (int f = (nf & ~3) + threadIdx.x; f < nf; f += HOST_BLOCK) sm[f] = h[base + f];
+    } else {
+        for (int f = threadIdx.x; f < nf; f += HOST_BLOCK) sm[f] = h[base + f];
+    }
+}
+
+__device__ __forceinline__ void smem_to_host(const float* sm, int n, float* __restrict__ h) {
+    const int first = blockIdx.x * HOST_BLOCK;
+    const int m = min(HOST_BLOCK, n - first);
+    const size_t base = 3 * (size_t)first;
+    const int nf = 3 * m;
+    if ((reinterpret_cast<size_t>(h) & 15) == 0) {
+        float4* h4 = reinterpret_cast<float4*>(h + base);
+        for (int t = threadIdx.x; 4 * t + 3 < nf; t += HOST_BLOCK)
+            h4[t] = make_float4(sm[4 * t], sm[4 * t + 1], sm[4 * t + 2], sm[4 * t + 3]);
+        for (int f = (nf & ~3) + threadIdx.x; f < nf; f += HOST_BLOCK) h[base + f] = sm[f];
+    } else {
+        for (int f = threadIdx.x; f < nf; f += HOST_BLOCK) h[base + f] = sm[f];
+    }
+}
+
+// Upload: slot = caller index.
 template <bool MIXED>
-__global__ void k_pack_state(StepParams p, CellPack cp, const float* __restrict__ hx,
-                             const float* __restrict__ hv, int n, float4* __restrict__ x,
-                             float4* __restrict__ v, int* __restrict__ id) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(HOST_BLOCK) k_pack_state(StepParams p, CellPack cp, const float* __restrict__ hx,
+                                                           const float* __restrict__ hv, int n,
+                                                           float4* __restrict__ x, float4* __restrict__ v,
+                                                           int* __restrict__ id) {
+    __shared__ float sx[3 * HOST_BLOCK], sv[3 * HOST_BLOCK];
+    host_to_smem(hx, n, sx);
+    if (hv) host_to_smem(hv, n, sv);
+    __syncthreads();
+    const int i = blockIdx.x * HOST_BLOCK + threadIdx.x;
     if (i >= n) return;
-    x[i] = pack_position<MIXED>(p, cp, geo_single(p), hx[3 * (size_t)i], hx[3 * (size_t)i + 1],
-                                hx[3 * (size_t)i + 2]);
-    v[i] = hv ? make_float4(hv[3 * (size_t)i], hv[3 * (size_t)i + 1], hv[3 * (size_t)i + 2], 0.0f)
-              : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const int t = 3 * threadIdx.x;
+    x[i] = pack_position<MIXED>(p, cp, geo_single(p), sx[t], sx[t + 1], sx[t + 2]);
+    v[i] = hv ? make_float4(sv[t], sv[t + 1], sv[t + 2], 0.0f) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     id[i] = i;
 }
 
@@ -752,16 +797,17 @@ __global__ void k_slot_of(const int* __restrict__ id, int n, int* __restrict__ s
     if (s < n) slot_of[id[s]] = s;
 }
 
-// Download: one thread per caller index gathers its slot, so the host writes
-// are contiguous.
+// Download: one thread per caller index gathers its slot.
 template <bool MIXED>
-__global__ void k_unpack_state(StepParams p, CellPack cp, const float4* __restrict__ x,
-                               const float4* __restrict__ v, const int* __restrict__ slot_of, int n,
-                               float* __restrict__ hx, float* __restrict__ hv) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const int s = slot_of[i];
-    if (hx) {
+__global__ void __launch_bounds__(HOST_BLOCK) k_unpack_state(StepParams p, CellPack cp, const float4* __restrict__ x,
+                                                             const float4* __restrict__ v,
+                                                             const int* __restrict__ slot_of, int n,
+                                                             float* __restrict__ hx, float* __restrict__ hv) {
+    __shared__ float sx[3 * HOST_BLOCK], sv[3 * HOST_BLOCK];
+    const int i = blockIdx.x * HOST_BLOCK + threadIdx.x;
+    if (i < n) {
+        const int s = slot_of[i];
+        const int t = 3 * threadIdx.x;
         const float4 q = x[s];
         float a = q.x, b = q.y, c = q.z;
         if (MIXED) {
@@ -770,16 +816,19 @@ __global__ void k_unpack_state(StepParams p, CellPack cp, const float4* __restri
             b += (float)cc.y * p.cell;
             c += (float)cc.z * p.cell;
         }
-        hx[3 * (size_t)i] = a;
-        hx[3 * (size_t)i + 1] = b;
-        hx[3 * (size_t)i + 2] = c;
+        sx[t] = a;
+        sx[t + 1] = b;
+        sx[t + 2] = c;
+        if (hv) {
+            const float4 u = v[s];
+            sv[t] = u.x;
+            sv[t + 1] = u.y;
+            sv[t + 2] = u.z;
+        }
     }
-    if (hv) {
-        const float4 u = v[s];
-        hv[3 * (size_t)i] = u.x;
-        hv[3 * (size_t)i + 1] = u.y;
-        hv[3 * (size_t)i + 2] = u.z;
-    }
+    __syncthreads();
+    if (hx) smem_to_host(sx, n, hx);
+    if (hv) smem_to_host(sv, n, hv);
 }
 
 // Particles binned in a box of cells by the last step (the sorted cell table
@@ -1026,14 +1075,15 @@ void launch_pack_pos(bool mixed, const StepParams& p, const CellPack& cp, const 
 void launch_pack_state(bool mixed, const StepParams& p, const CellPack& cp, const float* hx, const float* hv,
                        int n, float4* x, float4* v, int* id, cudaStream_t st) {
     if (n <= 0) return;
-    LGB_DISPATCH(mixed, k_pack_state, blocks_for(n, 256), 256, st, p, cp, hx, hv, n, x, v, id);
+    LGB_DISPATCH(mixed, k_pack_state, blocks_for(n, HOST_BLOCK), HOST_BLOCK, st, p, cp, hx, hv, n, x, v, id);
 }
 
 void launch_unpack_state(bool mixed, const StepParams& p, const CellPack& cp, const float4* x, const float4* v,
                          const int* id, int* slot_of, int n, float* hx, float* hv, cudaStream_t st) {
     if (n <= 0) return;
     launch_k(k_slot_of, blocks_for(n, 256), 256, st, pdl_enabled(), id, n, slot_of);
-    LGB_DISPATCH(mixed, k_unpack_state, blocks_for(n, 256), 256, st, p, cp, x, v, (const int*)slot_of, n, hx, hv);
+    LGB_DISPATCH(mixed, k_unpack_state, blocks_for(n, HOST_BLOCK), HOST_BLOCK, st, p, cp, x, v, (const int*)slot_of,
+                 n, hx, hv);
 }
 
 void launch_reduce(bool mixed, const StepParams& p, const CellPack& cp, const float4* x,

@@ -168,6 +168,11 @@ class PbfSim:
               "download")
         return ax, av, al, ad
 
+    def step_host(self, dt: float, x_ptr: int, v_ptr: int | None):
+        """Upload x, v from host memory, step, download into them, wait."""
+        check(self.lib.lustrine_pbf_step_host(self.h, float(dt), C.c_void_p(x_ptr),
+                                              C.c_void_p(v_ptr) if v_ptr else None), "step_host")
+
     def download_state_async(self, x_ptr: int, v_ptr: int | None):
         check(self.lib.lustrine_pbf_download_state_async(self.h, C.c_void_p(x_ptr),
                                                          C.c_void_p(v_ptr) if v_ptr else None),

@@ -286,6 +286,15 @@ def test_state_transfers_page_locked_and_pageable_agree(precision):
     xb, vb, _, _ = b.download()
     np.testing.assert_array_equal(xa, xb)
     np.testing.assert_array_equal(va, vb)
+    # one-call frames: the state stays in the host arrays
+    hx, hv = xb.copy(), vb.copy()
+    px.numpy()[:] = xa
+    pv.numpy()[:] = va
+    for _ in range(3):
+        a.step_host(sc.dt, px.data_ptr(), pv.data_ptr())
+        b.step_host(sc.dt, hx.ctypes.data, hv.ctypes.data)
+    np.testing.assert_array_equal(px.numpy(), hx)
+    np.testing.assert_array_equal(pv.numpy(), hv)
     assert a.status() == 0 and b.status() == 0
     a.close()
     b.close()
