@@ -2,7 +2,7 @@
 statistics.
 
     python -m lustrine_gb300.run_scene --config config2 --steps 5 [--mixed] [--no-graph]
-        [--grid auto|dense|hashed] [--stages]
+        [--grid auto|dense|hashed] [--stages] [--shape block,unroll,list_block]
 
 Used for profiling captures of a single configuration (a fixed, short
 sequence of launches) and as a quick end-to-end check of an installation.
@@ -25,6 +25,8 @@ def main(argv=None):
     ap.add_argument("--max-neighbors", type=int, default=64)
     ap.add_argument("--grid", default="auto", choices=["auto", "dense", "hashed"])
     ap.add_argument("--stages", action="store_true", help="also print per-stage device ms")
+    ap.add_argument("--shape", default=None,
+                    help="launch shape block,unroll,list_block (default: the library's)")
     a = ap.parse_args(argv)
     sc = getattr(scenes, a.config)()
     p = pbf_params(*sc.domain, iterations=sc.iterations, c_xsph=sc.c_xsph,
@@ -33,6 +35,8 @@ def main(argv=None):
                    grid_mode=["auto", "dense", "hashed"].index(a.grid))
     with PbfSim(p, sc.n, sc.ns) as sim:
         sim.upload(sc.x, None, sc.solid if sc.ns else None)
+        if a.shape:
+            sim.set_tuning(*(int(v) for v in a.shape.split(",")))
         t0 = time.perf_counter()
         sim.step(sc.dt, a.steps)
         sim.synchronize()
