@@ -184,10 +184,11 @@ lustrine_pbf::~lustrine_pbf() {
 }
 
 void lustrine_pbf::free_buffers() {
-    for (int k = 0; k < 2; k++)
+    for (int k = 0; k < 8; k++) {
         if (graph_exec[k]) cudaGraphExecDestroy(graph_exec[k]);
-    graph_exec[0] = graph_exec[1] = nullptr;
-    void* ptrs[] = {x[0], x[1], xs[0], xs[1], v[0], v[1], id[0], id[1], xs_alt, vtmp, key, key_sorted,
+        graph_exec[k] = nullptr;
+    }
+    void* ptrs[] = {x[0], x[1], xs[0], xs[1], v[0], v[1], id[0], id[1], xs_alt, xs_pred, vtmp, key, key_sorted,
                     rank, tmp, perm, count, start, block_sums, tile_sum, solid_near, solid, solid_raw, sstart, nbr, cnt, lam,
                     lam_by_id, rho, status, red, qcount, out3, out3d, iota, slot_of, solid_id, d_scenes, d_scene_of,
                     d_solid_scene_of, cellk, cell_sorted, solid_cell};
@@ -195,7 +196,7 @@ void lustrine_pbf::free_buffers() {
         if (q) cudaFree(q);
     x[0] = x[1] = xs[0] = xs[1] = v[0] = v[1] = nullptr;
     id[0] = id[1] = nullptr;
-    xs_alt = vtmp = solid = solid_raw = lam_src = nullptr;
+    xs_alt = xs_pred = vtmp = solid = solid_raw = lam_src = nullptr;
     key = key_sorted = rank = tmp = perm = count = start = block_sums = tile_sum = sstart = nullptr;
     nbr = cnt = status = qcount = iota = slot_of = solid_id = d_scene_of = d_solid_scene_of = nullptr;
     cellk = cell_sorted = solid_cell = nullptr;
@@ -227,6 +228,7 @@ static int ctx_alloc(lustrine_pbf* s) {
         rc = rc ? rc : dalloc(&s->id[k], n);
     }
     rc = rc ? rc : dalloc(&s->xs_alt, (size_t)n + 1);
+    rc = rc ? rc : dalloc(&s->xs_pred, n);
     rc = rc ? rc : dalloc(&s->vtmp, (size_t)n + 1);
     rc = rc ? rc : dalloc(&s->key, m);
     rc = rc ? rc : dalloc(&s->key_sorted, m);  // m: key and key_sorted trade places after a despawn
@@ -491,10 +493,11 @@ extern "C" int lustrine_pbf_counts(const lustrine_pbf* s, int* n_fluid, int* n_s
 }
 
 void lustrine_pbf::invalidate_graphs() {
-    for (int k = 0; k < 2; k++) {
+    for (int k = 0; k < 8; k++) {
         if (graph_exec[k]) cudaGraphExecDestroy(graph_exec[k]);
         graph_exec[k] = nullptr;
     }
+    pred_ready = false;  // whatever invalidates the step may change the prediction too
 }
 
 bool lustrine_pbf::mixed() const { return prm.precision == LUSTRINE_PRECISION_MIXED; }
@@ -504,6 +507,7 @@ static int setup_solids(lustrine_pbf* s) {
     const int ns = s->ns, C = s->sp.num_cells;
     StepParams p = s->sp;
     CK(cudaMemsetAsync(s->count, 0, (size_t)C * sizeof(int), s->stream));
+    s->count_dirty = false;  // zero again after the scan below
     if (ns > 0) {
         if (s->prm.mode == LUSTRINE_MODE_REFERENCE)
             launch_key_ref(p, s->solid_raw, ns, s->key, s->rank, s->count, s->status, s->stream);
@@ -601,6 +605,7 @@ static const void* host_view(const void* p) {
 
 extern "C" int lustrine_pbf_upload_state_async(lustrine_pbf* s, const float* x, const float* v) {
     if (!s || !s->have_state || (!x && s->n > 0)) return LUSTRINE_ERR_ARGS;
+    s->pred_ready = false;
     const int n = s->n;
     if (!n) return LUSTRINE_OK;
     const float* hx = (const float*)host_view(x);
@@ -632,7 +637,11 @@ struct StageMarks {
 };
 
 // One step's launches.  Returns the number of kernels launched.
-static int enqueue_step(lustrine_pbf* s, cudaStream_t st, StageMarks* mk = nullptr) {
+// predict: run the prediction kernel (else the previous step's commit
+// kernel left it in xs_pred, key, rank, count); tail: the commit kernel
+// predicts the next step (PBF mode only).
+static int enqueue_step(lustrine_pbf* s, cudaStream_t st, StageMarks* mk = nullptr, bool predict = true,
+                        bool tail = false) {
     const int c = s->cur, o = 1 - c, n = s->n, C = s->sp.num_cells;
     const StepParams& p = s->sp;
     const bool mixed = s->mixed();
@@ -641,11 +650,15 @@ static int enqueue_step(lustrine_pbf* s, cudaStream_t st, StageMarks* mk = nullp
     // count[] is all zero here: zeroed at allocation and by every scan.
     // Step kernels use programmatic dependent launch.
     set_pdl(s->use_pdl);
-    if (s->prm.mode == LUSTRINE_MODE_REFERENCE)
+    const bool ref = s->prm.mode == LUSTRINE_MODE_REFERENCE;
+    float4* xs_in = ref ? s->xs[c] : s->xs_pred;  // predicted positions, caller of the sort
+    if (ref) {
         launch_predict_ref(p, s->x[c], s->v[c], s->xs[c], s->key, s->rank, s->count, s->status, st);
-    else
-        launch_predict(mixed, p, s->cp, s->x[c], s->v[c], s->xs[c], s->key, s->rank, s->count, s->cellk, st);
-    k += 1;
+        k += 1;
+    } else if (predict) {
+        launch_predict(mixed, p, s->cp, s->x[c], s->v[c], xs_in, s->key, s->rank, s->count, s->cellk, st);
+        k += 1;
+    }
     if (mk) mk->mark(LUSTRINE_STAGE_PREDICT, st);
     if (s->tile_sum) {
         launch_scan_tiles(s->count, C, s->tile_sum, s->start, st);
@@ -658,7 +671,7 @@ static int enqueue_step(lustrine_pbf* s, cudaStream_t st, StageMarks* mk = nullp
     // stable within a cell: by the caller's id in reference mode (the
     // reference's list order), by the previous slot otherwise
     const int* tie = s->prm.mode == LUSTRINE_MODE_REFERENCE ? s->id[c] : nullptr;
-    launch_sort_state(s->key, s->rank, s->start, tie, n, s->tmp, s->x[c], s->xs[c], s->v[c], s->id[c],
+    launch_sort_state(s->key, s->rank, s->start, tie, n, s->tmp, s->x[c], xs_in, s->v[c], s->id[c],
                       s->key_sorted, s->x[o], s->xs[o], s->v[o], s->id[o], p.hash_bits ? s->cellk : nullptr,
                       s->cell_sorted, st);
     k += 2;
@@ -697,7 +710,8 @@ static int enqueue_step(lustrine_pbf* s, cudaStream_t st, StageMarks* mk = nullp
             b = t;
             k += 2;
         }
-        launch_xsph(mixed, tu, p, s->cp, a, s->vtmp, s->nbr, s->cnt, s->key_sorted, s->x[o], s->v[o], st);
+        launch_xsph(mixed, tu, p, s->cp, a, s->vtmp, s->nbr, s->cnt, s->key_sorted, s->x[o], s->v[o],
+                    tail ? s->xs_pred : nullptr, s->key, s->rank, s->count, s->cellk, st);
         k += 1;
         if (mk) mk->mark(LUSTRINE_STAGE_XSPH, st);
     }
@@ -716,7 +730,9 @@ static void finish_step(lustrine_pbf* s, int c) {
     s->lam_src = (s->prm.iterations % 2 == 1) ? s->xs[1 - c] : s->xs_alt;
 }
 
-extern "C" int lustrine_pbf_step(lustrine_pbf* s, float dt) {
+// One step; tail_allowed: the commit kernel may predict the next step (a
+// caller that replaces the state before it, like step_host, says no).
+static int step_impl(lustrine_pbf* s, float dt, bool tail_allowed) {
     if (!s || !s->have_state) return LUSTRINE_ERR_ARGS;
     if (!(dt > 0.0f) || !std::isfinite(dt)) return LUSTRINE_ERR_ARGS;
     if (s->prm.mode == LUSTRINE_MODE_REFERENCE) {
@@ -730,25 +746,38 @@ extern "C" int lustrine_pbf_step(lustrine_pbf* s, float dt) {
         s->invalidate_graphs();
     }
     const int c = s->cur;
+    const bool pbf = s->prm.mode == LUSTRINE_MODE_PBF;
+    // the previous step predicted this one unless something changed since
+    const bool predict = !(pbf && s->pred_ready && s->pred_dt == dt);
+    const bool tail = pbf && tail_allowed;
+    if (predict && s->count_dirty)  // a histogram of a prediction that will not be used
+        CK(cudaMemsetAsync(s->count, 0, (size_t)s->sp.num_cells * sizeof(int), s->stream));
+    s->count_dirty = false;
+    const int gi = c + (predict ? 2 : 0) + (tail ? 4 : 0);
     if (s->prm.use_graph) {
-        if (!s->graph_exec[c]) {
+        if (!s->graph_exec[gi]) {
             cudaGraph_t g = nullptr;
             CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
-            s->launches = enqueue_step(s, s->stream);
+            s->launches = enqueue_step(s, s->stream, nullptr, predict, tail);
             cudaError_t e = cudaStreamEndCapture(s->stream, &g);
             if (e != cudaSuccess) return lgb_cuda_status(e, "cudaStreamEndCapture");
-            e = cudaGraphInstantiate(&s->graph_exec[c], g, 0);
+            e = cudaGraphInstantiate(&s->graph_exec[gi], g, 0);
             cudaGraphDestroy(g);
             if (e != cudaSuccess) return lgb_cuda_status(e, "cudaGraphInstantiate");
         }
-        CK(cudaGraphLaunch(s->graph_exec[c], s->stream));
+        CK(cudaGraphLaunch(s->graph_exec[gi], s->stream));
     } else {
-        s->launches = enqueue_step(s, s->stream);
+        s->launches = enqueue_step(s, s->stream, nullptr, predict, tail);
         CK(cudaGetLastError());
     }
     finish_step(s, c);
+    s->pred_ready = tail;
+    s->pred_dt = dt;
+    s->count_dirty = tail;
     return LUSTRINE_OK;
 }
+
+extern "C" int lustrine_pbf_step(lustrine_pbf* s, float dt) { return step_impl(s, dt, true); }
 
 extern "C" int lustrine_pbf_steps(lustrine_pbf* s, float dt, int count) {
     if (count < 0) return LUSTRINE_ERR_ARGS;
@@ -772,6 +801,9 @@ extern "C" int lustrine_pbf_profile_step(lustrine_pbf* s, float dt, double* stag
         s->sp.inv_dt = 1.0f / dt;
         s->invalidate_graphs();
     }
+    if (s->count_dirty) CK(cudaMemsetAsync(s->count, 0, (size_t)s->sp.num_cells * sizeof(int), s->stream));
+    s->count_dirty = false;
+    s->pred_ready = false;
     StageMarks mk;
     for (int e = 0; e < 64; e++) CK(cudaEventCreate(&mk.ev[e]));
     s->launches = enqueue_step(s, s->stream, &mk);
@@ -840,6 +872,7 @@ static int snapshot_take(lustrine_pbf* s, Snapshot& sn) {
 
 static int snapshot_restore(lustrine_pbf* s, const Snapshot& sn, int side) {
     s->cur = side;
+    s->pred_ready = false;
     CK(cudaMemcpyAsync(s->x[side], sn.x, (size_t)s->n * sizeof(float4), cudaMemcpyDeviceToDevice, s->stream));
     CK(cudaMemcpyAsync(s->v[side], sn.v, (size_t)s->n * sizeof(float4), cudaMemcpyDeviceToDevice, s->stream));
     CK(cudaMemcpyAsync(s->id[side], sn.id, (size_t)s->n * sizeof(int), cudaMemcpyDeviceToDevice, s->stream));
@@ -851,7 +884,9 @@ static int snapshot_restore(lustrine_pbf* s, const Snapshot& sn, int side) {
 static int time_candidate(lustrine_pbf* s, const Snapshot& sn, int side, float dt, int steps, float* ms) {
     int rc = snapshot_restore(s, sn, side);
     if (rc) return rc;
-    for (int k = 0; k < 2; k++)
+    // untimed steps capture the graphs the timed ones replay (both parities,
+    // with and without a prediction of their own)
+    for (int k = 0; k < 3; k++)
         if ((rc = lustrine_pbf_step(s, dt))) return rc;
     if ((rc = snapshot_restore(s, sn, side))) return rc;
     cudaEvent_t e0, e1;
@@ -996,7 +1031,7 @@ extern "C" int lustrine_pbf_download_state_async(lustrine_pbf* s, float* x, floa
 extern "C" int lustrine_pbf_step_host(lustrine_pbf* s, float dt, float* x, float* v) {
     if (!s || !x) return LUSTRINE_ERR_ARGS;
     int rc = lustrine_pbf_upload_state_async(s, x, v);
-    if (!rc) rc = lustrine_pbf_step(s, dt);
+    if (!rc) rc = step_impl(s, dt, false);  // the next frame replaces the state
     if (!rc) rc = lustrine_pbf_download_state_async(s, x, v);
     if (!rc) CK(cudaStreamSynchronize(s->stream));
     return rc;

@@ -34,6 +34,7 @@ struct lustrine_pbf {
     int* id[2] = {nullptr, nullptr};
     int cur = 0;
     float4* xs_alt = nullptr;  // Jacobi ping-pong partner of xs
+    float4* xs_pred = nullptr; // PBF: predicted positions of the next step, in the committed side's order
     float4* vtmp = nullptr;    // velocities before XSPH
     int* iota = nullptr;       // 0..n-1
     int* slot_of = nullptr;    // slot of every caller index (state download)
@@ -82,7 +83,12 @@ struct lustrine_pbf {
     int* d_solid_scene_of = nullptr;
     bool is_batch() const { return !b_nfluid.empty(); }
 
-    cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};
+    // captured steps: parity + 2 * (own prediction) + 4 * (predicts the next step)
+    cudaGraphExec_t graph_exec[8] = {};
+    // PBF: the last step's commit kernel predicted the next step with dt pred_dt
+    bool pred_ready = false;
+    float pred_dt = 0.0f;
+    bool count_dirty = false;  // count[] holds that prediction's histogram
     int launches = 0;
     long long steps_done = 0;
     bool have_state = false;

@@ -274,6 +274,9 @@ extern "C" int lustrine_pbf_despawn_cells(lustrine_pbf* s, const int* cells, int
         k_keep_scatter<<<nb, DYN_THREADS, 0, st>>>(remap, block_count, n, s->x[c], s->v[c], s->id[c],
                                                    s->key_sorted, s->x[o], s->v[o], s->id[o], s->key);
         std::swap(s->key, s->key_sorted);
+        if (s->count_dirty)  // a histogram of the next step's prediction, dropped with it
+            e = cudaMemsetAsync(s->count, 0, (size_t)C * sizeof(int), st);
+        s->count_dirty = false;
         if (end > 0) k_histogram<<<blocks(end), DYN_THREADS, 0, st>>>(s->key_sorted, end, s->count);
         launch_scan(s->count, C, s->block_sums, s->start, st);  // leaves count zero
         e = cudaGetLastError();

@@ -63,7 +63,7 @@ void launch_delta_ref(const StepParams& p, const float4* xs, float4* xs_out, flo
 
 // pbf_solver.cu (PBF; mixed = cell index + offset representation)
 // cellk: packed cell of every particle on a hashed grid (nullptr when dense)
-void launch_predict(bool mixed, const StepParams& p, const CellPack& cp, const float4* x, float4* v,
+void launch_predict(bool mixed, const StepParams& p, const CellPack& cp, const float4* x, const float4* v,
                     float4* xs, int* key, int* rank, int* count, int* cellk, cudaStream_t st);
 void launch_key(bool mixed, const StepParams& p, const CellPack& cp, const float4* pos, int m,
                 int* key, int* rank, int* count, int* cellk, cudaStream_t st);
@@ -82,9 +82,12 @@ void launch_delta(bool mixed, const Tuning& tu, const StepParams& p, const CellP
                   const float4* xs, float4* xs_out, const int* nbr, const int* cnt,
                   const float4* solid, const int* key_sorted, const float4* x, float4* v_out,
                   cudaStream_t st);
+// XSPH and commit; with xs_next (not nullptr) also the next step's
+// prediction from the committed state (as launch_predict with the same dt)
 void launch_xsph(bool mixed, const Tuning& tu, const StepParams& p, const CellPack& cp,
                  const float4* xs, const float4* v_in, const int* nbr, const int* cnt,
-                 const int* key_sorted, float4* x_out, float4* v_out, cudaStream_t st);
+                 const int* key_sorted, float4* x_out, float4* v_out, float4* xs_next, int* key,
+                 int* rank, int* count, int* cellk, cudaStream_t st);
 void launch_unpermute_pos(bool mixed, const StepParams& p, const CellPack& cp, const float4* a,
                           const int* id, int n, float* out, cudaStream_t st);
 void launch_unpermute_pos_d(bool mixed, const StepParams& p, const CellPack& cp, const float4* a,

@@ -117,8 +117,8 @@ __device__ __forceinline__ int3 decode_cell(const Geo& g, int key) {
 __device__ __forceinline__ float clampf(float v, float lo, float hi) { return fminf(fmaxf(v, lo), hi); }
 
 __device__ __forceinline__ int3 plain_cell(const StepParams& p, const Geo& g, float x, float y, float z) {
-    int cx = (int)floorf(x * p.inv_cell), cy = (int)floorf(y * p.inv_cell),
-        cz = (int)floorf(z * p.inv_cell);
+    int cx = (int)floorf(__fmul_rn(x, p.inv_cell)), cy = (int)floorf(__fmul_rn(y, p.inv_cell)),
+        cz = (int)floorf(__fmul_rn(z, p.inv_cell));
     return make_int3(min(max(cx, 0), g.gx - 1), min(max(cy, 0), g.gy - 1), min(max(cz, 0), g.gz - 1));
 }
 
@@ -183,19 +183,19 @@ __device__ __forceinline__ float4 load_entry(int e, const float4* __restrict__ x
 // Mixed: one axis of an (offset, cell) pair renormalised into [0, cell) and
 // clamped to the box [lo, hi].
 __device__ __forceinline__ void renorm_axis(const StepParams& p, float& o, int& c, float lo, float hi) {
-    float k = floorf(o * p.inv_cell);
+    float k = floorf(__fmul_rn(o, p.inv_cell));
     if (k != 0.0f) {
         c += (int)k;
-        o -= k * p.cell;
-        if (o >= p.cell) { o -= p.cell; c += 1; }
-        if (o < 0.0f) { o += p.cell; c -= 1; }
+        o = __fmaf_rn(-k, p.cell, o);
+        if (o >= p.cell) { o = __fsub_rn(o, p.cell); c += 1; }
+        if (o < 0.0f) { o = __fadd_rn(o, p.cell); c -= 1; }
     }
-    float a = (float)c * p.cell + o;
+    float a = __fmaf_rn((float)c, p.cell, o);
     if (a < lo || a > hi) {
         float t = clampf(a, lo, hi);
-        int tc = (int)floorf(t * p.inv_cell);
+        int tc = (int)floorf(__fmul_rn(t, p.inv_cell));
         c = tc;
-        o = t - (float)tc * p.cell;
+        o = __fmaf_rn(-(float)tc, p.cell, t);
     }
 }
 
@@ -225,30 +225,30 @@ __device__ __forceinline__ int cell_key(const StepParams& p, const CellPack& cp,
     return cell_bucket(c, p.hash_bits);
 }
 
-// Prediction with the box clamp, cell key and histogram.
+// Prediction of one particle from its committed state: v' = v + g dt,
+// x* = x + v' dt clamped to the box (mixed: renormalised into [0, cell) of a
+// cell first), its cell key and its rank in the cell histogram.  Explicit
+// fused multiply-adds keep the arithmetic identical wherever it is inlined:
+// the prediction kernel and the commit kernel of the previous step (which
+// predicts the next step when nothing changes in between) agree bit for bit.
 template <bool MIXED>
-__global__ void k_predict(StepParams p, CellPack cp, const float4* __restrict__ x,
-                          float4* __restrict__ v, float4* __restrict__ xs, int* __restrict__ key,
-                          int* __restrict__ rank, int* __restrict__ count, int* __restrict__ cellk) {
-    pdl_wait();
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= p.n) return;
-    float4 vi = v[i];
-    vi.x += p.gxv * p.dt;
-    vi.y += p.gyv * p.dt;
-    vi.z += p.gzv * p.dt;
-    v[i] = vi;
-    const float4 xi = x[i];
-    const Geo g = geo_slot(p, i);
+__device__ __forceinline__ void predict_one(const StepParams& p, const CellPack& cp, const Geo& g, float4 xi,
+                                            float4 vi, int i, float4* __restrict__ xs, int* __restrict__ key,
+                                            int* __restrict__ rank, int* __restrict__ count,
+                                            int* __restrict__ cellk) {
+    vi.x = __fmaf_rn(p.gxv, p.dt, vi.x);
+    vi.y = __fmaf_rn(p.gyv, p.dt, vi.y);
+    vi.z = __fmaf_rn(p.gzv, p.dt, vi.z);
     int3 c;
     float4 s;
     if (!MIXED) {
-        s = make_float4(clampf(xi.x + vi.x * p.dt, g.lox, g.hix), clampf(xi.y + vi.y * p.dt, g.loy, g.hiy),
-                        clampf(xi.z + vi.z * p.dt, g.loz, g.hiz), 0.0f);
+        s = make_float4(clampf(__fmaf_rn(vi.x, p.dt, xi.x), g.lox, g.hix),
+                        clampf(__fmaf_rn(vi.y, p.dt, xi.y), g.loy, g.hiy),
+                        clampf(__fmaf_rn(vi.z, p.dt, xi.z), g.loz, g.hiz), 0.0f);
         c = plain_cell(p, g, s.x, s.y, s.z);
     } else {
         c = unpack_cell(cp, xi.w);
-        float ox = xi.x + vi.x * p.dt, oy = xi.y + vi.y * p.dt, oz = xi.z + vi.z * p.dt;
+        float ox = __fmaf_rn(vi.x, p.dt, xi.x), oy = __fmaf_rn(vi.y, p.dt, xi.y), oz = __fmaf_rn(vi.z, p.dt, xi.z);
         renorm_axis(p, ox, c.x, g.lox, g.hix);
         renorm_axis(p, oy, c.y, g.loy, g.hiy);
         renorm_axis(p, oz, c.z, g.loz, g.hiz);
@@ -258,6 +258,16 @@ __global__ void k_predict(StepParams p, CellPack cp, const float4* __restrict__ 
     const int k = cell_key(p, cp, g, c, cellk, i);
     key[i] = k;
     rank[i] = atomicAdd(&count[k], 1);
+}
+
+template <bool MIXED>
+__global__ void k_predict(StepParams p, CellPack cp, const float4* __restrict__ x,
+                          const float4* __restrict__ v, float4* __restrict__ xs, int* __restrict__ key,
+                          int* __restrict__ rank, int* __restrict__ count, int* __restrict__ cellk) {
+    pdl_wait();
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.n) return;
+    predict_one<MIXED>(p, cp, geo_slot(p, i), x[i], v[i], i, xs, key, rank, count, cellk);
 }
 
 // Cell key and histogram of static particles (solids; scene from solid_scene_of).
@@ -613,12 +623,18 @@ __global__ void __launch_bounds__(B) k_delta(StepParams p, CellPack cp, const fl
 }
 
 // XSPH viscosity (Macklin & Mueller eq. 17) and commit x = x*.
+// With xs_next, also the next step's prediction from the state it commits
+// (into xs_next, key, rank, count, cellk; count is zero here, the step's
+// scan having consumed it).
 template <bool MIXED, int U, int B>
 __global__ void __launch_bounds__(B) k_xsph(StepParams p, CellPack cp, const float4* __restrict__ xs,
                                             const float4* __restrict__ v_in,
                                             const int* __restrict__ nbr, const int* __restrict__ cnt,
                                             const int* __restrict__ key_sorted,
-                                            float4* __restrict__ x_out, float4* __restrict__ v_out) {
+                                            float4* __restrict__ x_out, float4* __restrict__ v_out,
+                                            float4* __restrict__ xs_next, int* __restrict__ key,
+                                            int* __restrict__ rank, int* __restrict__ count,
+                                            int* __restrict__ cellk) {
     pdl_wait();
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= p.n) return;
@@ -655,13 +671,18 @@ __global__ void __launch_bounds__(B) k_xsph(StepParams p, CellPack cp, const flo
     }
     // v += c sum (v_j - v_i) W, W = K6 hd^3
     const float cx = p.c_xsph * p.k6;
-    v_out[s] = make_float4(vi.x + cx * ax, vi.y + cx * ay, vi.z + cx * az, 0.0f);
+    const float4 vc = make_float4(vi.x + cx * ax, vi.y + cx * ay, vi.z + cx * az, 0.0f);
+    v_out[s] = vc;
+    const Geo g = geo_slot(p, s);
+    float4 xc;
     if (!MIXED) {
-        x_out[s] = make_float4(self.x, self.y, self.z, 0.0f);
+        xc = make_float4(self.x, self.y, self.z, 0.0f);
     } else {
-        int3 cs = slot_cell(p, cp, geo_slot(p, s), key_sorted, p.cell_sorted, s);
-        x_out[s] = make_float4(self.x, self.y, self.z, pack_cell(cp, cs.x, cs.y, cs.z));
+        int3 cs = slot_cell(p, cp, g, key_sorted, p.cell_sorted, s);
+        xc = make_float4(self.x, self.y, self.z, pack_cell(cp, cs.x, cs.y, cs.z));
     }
+    x_out[s] = xc;
+    if (xs_next) predict_one<MIXED>(p, cp, g, xc, vc, s, xs_next, key, rank, count, cellk);
 }
 
 // Absolute positions (float3 triples) in the caller's id order.
@@ -953,7 +974,7 @@ static inline int blocks_for(int n, int t) { return (n + t - 1) / t; }
             launch_k(KERNEL<false>, GRID, BLOCK, ST, pdl_enabled(), __VA_ARGS__);     \
     } while (0)
 
-void launch_predict(bool mixed, const StepParams& p, const CellPack& cp, const float4* x, float4* v,
+void launch_predict(bool mixed, const StepParams& p, const CellPack& cp, const float4* x, const float4* v,
                     float4* xs, int* key, int* rank, int* count, int* cellk, cudaStream_t st) {
     if (p.n <= 0) return;
     LGB_DISPATCH(mixed, k_predict, blocks_for(p.n, 256), 256, st, p, cp, x, v, xs, key, rank, count, cellk);
@@ -1049,9 +1070,11 @@ void launch_delta(bool mixed, const Tuning& tu, const StepParams& p, const CellP
 
 void launch_xsph(bool mixed, const Tuning& tu, const StepParams& p, const CellPack& cp,
                  const float4* xs, const float4* v_in, const int* nbr, const int* cnt,
-                 const int* key_sorted, float4* x_out, float4* v_out, cudaStream_t st) {
+                 const int* key_sorted, float4* x_out, float4* v_out, float4* xs_next, int* key,
+                 int* rank, int* count, int* cellk, cudaStream_t st) {
     if (p.n <= 0) return;
-    TUNE_DISPATCH(k_xsph, mixed, tu, p.n, st, p, cp, xs, v_in, nbr, cnt, key_sorted, x_out, v_out);
+    TUNE_DISPATCH(k_xsph, mixed, tu, p.n, st, p, cp, xs, v_in, nbr, cnt, key_sorted, x_out, v_out, xs_next, key,
+                  rank, count, cellk);
 }
 
 void launch_unpermute_pos(bool mixed, const StepParams& p, const CellPack& cp, const float4* a,

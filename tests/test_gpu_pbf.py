@@ -298,3 +298,31 @@ def test_state_transfers_page_locked_and_pageable_agree(precision):
     assert a.status() == 0 and b.status() == 0
     a.close()
     b.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_next_step_prediction_in_commit_kernel_is_exact(precision):
+    """The commit kernel predicts the next step when nothing changes in
+    between; a context made to predict every step itself (re-setting its
+    launch shape drops the prediction) gives the same states bit for bit,
+    also across a change of dt and with static particles."""
+    from lustrine_gb300 import PbfSim
+    sc = _small_solid_scene()
+    p = _params(sc, precision=precision)
+    a, b = PbfSim(p, sc.n, sc.ns), PbfSim(p, sc.n, sc.ns)
+    for s in (a, b):
+        s.upload(sc.x, None, sc.solid)
+    for k in range(7):
+        dt = sc.dt if k < 4 else 0.5 * sc.dt
+        a.step(dt)
+        b.set_tuning(**b.get_tuning())
+        b.step(dt)
+    xa, va, la, ra = a.download(lambdas=True, density=True)
+    xb, vb, lb, rb = b.download(lambdas=True, density=True)
+    np.testing.assert_array_equal(xa, xb)
+    np.testing.assert_array_equal(va, vb)
+    np.testing.assert_array_equal(la, lb)
+    np.testing.assert_array_equal(ra, rb)
+    assert a.status() == 0 and b.status() == 0
+    a.close()
+    b.close()
