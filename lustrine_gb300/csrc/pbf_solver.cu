@@ -132,11 +132,11 @@ __device__ __forceinline__ float axis_shift(float cell, int e, int at) {
 // x_i - x_j of a pair from the two stored positions and the list entry.
 template <bool MIXED>
 __device__ __forceinline__ float3 rel_e(const StepParams& p, float4 a, float4 b, int e) {
-    float3 d = make_float3(a.x - b.x, a.y - b.y, a.z - b.z);
+    float3 d = make_float3(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y), __fsub_rn(a.z, b.z));
     if (MIXED) {
-        d.x += axis_shift(p.cell, e, 25);
-        d.y += axis_shift(p.cell, e, 27);
-        d.z += axis_shift(p.cell, e, 29);
+        d.x = __fadd_rn(d.x, axis_shift(p.cell, e, 25));
+        d.y = __fadd_rn(d.y, axis_shift(p.cell, e, 27));
+        d.z = __fadd_rn(d.z, axis_shift(p.cell, e, 29));
     }
     return d;
 }
@@ -148,31 +148,39 @@ __device__ __forceinline__ float3 rel_e(const StepParams& p, float4 a, float4 b,
 //   s_corr       -k (W(r) / W(dq))^n,        W(r) / W(dq) = (hd / (h^2 - dq^2))^3
 // r and 1/r come from one reciprocal square root of max(r^2, 1e-30): at
 // r = 0 the offset d is 0 and every pair term with it.
-__device__ __forceinline__ float hdiff(const StepParams& p, float r2) { return fmaxf(p.h2 - r2, 0.0f); }
+// The PBF arithmetic is written with explicit roundings (__fmaf_rn and
+// friends): every instantiation of a kernel (precision, static particles,
+// launch shape) and every kernel sharing a helper then computes the same
+// bits, whatever multiply-adds the compiler would otherwise contract.
+__device__ __forceinline__ float dot3e(float x, float y, float z) {
+    return __fmaf_rn(z, z, __fmaf_rn(y, y, __fmul_rn(x, x)));
+}
+
+__device__ __forceinline__ float hdiff(const StepParams& p, float r2) { return fmaxf(__fsub_rn(p.h2, r2), 0.0f); }
 
 __device__ __forceinline__ float inv_r_of(float r2) { return rsqrtf(fmaxf(r2, 1e-30f)); }
 
 __device__ __forceinline__ float spiky_g(const StepParams& p, float r, float inv_r) {
-    const float f = fmaxf(p.h - r, 0.0f);
-    return f * f * inv_r;
+    const float f = fmaxf(__fsub_rn(p.h, r), 0.0f);
+    return __fmul_rn(__fmul_rn(f, f), inv_r);
 }
 
 __device__ __forceinline__ float scorr_hd(const StepParams& p, float hd) {
-    const float x = hd * p.inv_hdq2;
+    const float x = __fmul_rn(hd, p.inv_hdq2);
     float pw;
     if (p.sn_int == 4) {  // (x^3)^4
-        const float x2 = x * x, x4 = x2 * x2;
-        pw = x4 * x4 * x4;
+        const float x2 = __fmul_rn(x, x), x4 = __fmul_rn(x2, x2);
+        pw = __fmul_rn(__fmul_rn(x4, x4), x4);
     } else {
-        const float t = x * x * x;
+        const float t = __fmul_rn(__fmul_rn(x, x), x);
         if (p.sn_int >= 0) {
             pw = 1.0f;
-            for (int e = 0; e < p.sn_int; e++) pw *= t;
+            for (int e = 0; e < p.sn_int; e++) pw = __fmul_rn(pw, t);
         } else {
             pw = powf(t, p.sn);
         }
     }
-    return -p.sk * pw;
+    return __fmul_rn(-p.sk, pw);
 }
 
 __device__ __forceinline__ float4 load_entry(int e, const float4* __restrict__ xs,
@@ -201,10 +209,10 @@ __device__ __forceinline__ void renorm_axis(const StepParams& p, float& o, int& 
 
 // Mixed: clamp an offset in a fixed cell so the absolute position is in [lo, hi].
 __device__ __forceinline__ float clamp_offset(const StepParams& p, float o, int c, float lo, float hi) {
-    float base = (float)c * p.cell;
-    float a = base + o;
-    if (a < lo) return lo - base;
-    if (a > hi) return hi - base;
+    const float base = __fmul_rn((float)c, p.cell);
+    const float a = __fadd_rn(base, o);
+    if (a < lo) return __fsub_rn(lo, base);
+    if (a > hi) return __fsub_rn(hi, base);
     return o;
 }
 
@@ -327,35 +335,35 @@ __device__ __forceinline__ LambdaAcc lambda_init(const StepParams&) {
 template <bool MIXED>
 __device__ __forceinline__ void lambda_accumulate(const StepParams& p, LambdaAcc& a, float3 d,
                                                   bool solid) {
-    const float r2 = dot3(d.x, d.y, d.z);
+    const float r2 = dot3e(d.x, d.y, d.z);
     const float hd = hdiff(p, r2);
-    const float w = hd * hd * hd;
+    const float w = __fmul_rn(__fmul_rn(hd, hd), hd);
     if (MIXED) {
-        float y = w - a.comp;
-        float t = a.wsum + y;
-        a.comp = (t - a.wsum) - y;
+        const float y = __fsub_rn(w, a.comp);
+        const float t = __fadd_rn(a.wsum, y);
+        a.comp = __fsub_rn(__fsub_rn(t, a.wsum), y);
         a.wsum = t;
     } else {
-        a.wsum += w;
+        a.wsum = __fadd_rn(a.wsum, w);
     }
     const float inv_r = inv_r_of(r2);
-    const float g = spiky_g(p, r2 * inv_r, inv_r);
-    if (!solid) a.S += g * g * r2;
-    a.gx += g * d.x;
-    a.gy += g * d.y;
-    a.gz += g * d.z;
+    const float g = spiky_g(p, __fmul_rn(r2, inv_r), inv_r);
+    if (!solid) a.S = __fmaf_rn(__fmul_rn(g, g), r2, a.S);
+    a.gx = __fmaf_rn(g, d.x, a.gx);
+    a.gy = __fmaf_rn(g, d.y, a.gy);
+    a.gz = __fmaf_rn(g, d.z, a.gz);
 }
 
 // rho = m W(0) + m K6 sum hd^3
 __device__ __forceinline__ float density_of(const StepParams& p, const LambdaAcc& a) {
-    return p.self_density + p.k6m * a.wsum;
+    return __fmaf_rn(p.k6m, a.wsum, p.self_density);
 }
 
 // lambda = -(rho / rho0 - 1) / (S + eps), S = (Ks m / rho0)^2 (sum g^2 r^2 + |sum g d|^2)
 __device__ __forceinline__ float lambda_of(const StepParams& p, const LambdaAcc& a) {
-    const float c = p.ks * p.mr;
-    const float S = c * c * (a.S + dot3(a.gx, a.gy, a.gz));
-    return -(density_of(p, a) / p.rho0 - 1.0f) / (S + p.eps);
+    const float c = __fmul_rn(p.ks, p.mr);
+    const float S = __fmul_rn(__fmul_rn(c, c), __fadd_rn(a.S, dot3e(a.gx, a.gy, a.gz)));
+    return __fdiv_rn(-__fsub_rn(__fdiv_rn(density_of(p, a), p.rho0), 1.0f), __fadd_rn(S, p.eps));
 }
 
 // One row (dy, dx) of the stencil: the cells z0..z1 of a row are consecutive
@@ -380,13 +388,13 @@ __device__ __forceinline__ void walk_row(const StepParams& p, const float4& self
         for (int t = b[k]; t < b[k + 1]; t++) {
             if (!SOLID && t == s) continue;
             const float4 q = SOLID ? __ldg(&pos[t]) : pos[t];
-            float3 d = make_float3(self.x - q.x, self.y - q.y, self.z - q.z);
+            float3 d = make_float3(__fsub_rn(self.x, q.x), __fsub_rn(self.y, q.y), __fsub_rn(self.z, q.z));
             if (MIXED) {
-                d.x += sx;
-                d.y += sy;
-                d.z += sz;
+                d.x = __fadd_rn(d.x, sx);
+                d.y = __fadd_rn(d.y, sy);
+                d.z = __fadd_rn(d.z, sz);
             }
-            if (dot3(d.x, d.y, d.z) <= p.h2) {
+            if (dot3e(d.x, d.y, d.z) <= p.h2) {
                 if (c_n < p.max_nbrs) nbr[(size_t)c_n * p.n + s] = entry(t, dx, dy, dz, SOLID);
                 c_n++;
                 lambda_accumulate<MIXED>(p, a, d, SOLID);
@@ -408,13 +416,13 @@ __device__ __forceinline__ void walk_hashed_cell(const StepParams& p, const floa
     for (int t = start[b], e = start[b + 1]; t < e; t++) {
         if ((!SOLID && t == s) || __ldg(&cells[t]) != packed) continue;
         const float4 q = SOLID ? __ldg(&pos[t]) : pos[t];
-        float3 d = make_float3(self.x - q.x, self.y - q.y, self.z - q.z);
+        float3 d = make_float3(__fsub_rn(self.x, q.x), __fsub_rn(self.y, q.y), __fsub_rn(self.z, q.z));
         if (MIXED) {
-            d.x += sx;
-            d.y += sy;
-            d.z += sz;
+            d.x = __fadd_rn(d.x, sx);
+            d.y = __fadd_rn(d.y, sy);
+            d.z = __fadd_rn(d.z, sz);
         }
-        if (dot3(d.x, d.y, d.z) <= p.h2) {
+        if (dot3e(d.x, d.y, d.z) <= p.h2) {
             if (c_n < p.max_nbrs) nbr[(size_t)c_n * p.n + s] = entry(t, dx, dy, dz, SOLID);
             c_n++;
             lambda_accumulate<MIXED>(p, a, d, SOLID);
@@ -501,12 +509,12 @@ __global__ void __launch_bounds__(B) k_lists_lambda(StepParams p, CellPack cp, f
 }
 
 // Walk a particle's list U entries at a time, calling f(entry, position)
-// for each.  The first U entries are loaded together with the count and
+// for each (SOL: the scene has static particles, whose entries read solid).  The first U entries are loaded together with the count and
 // every next chunk's entries while the current chunk's positions are
 // gathered.  The list is padded with sentinel entries to a multiple of U
 // (the list build's pad), and the buffer holds at least 8 rows, so every
 // entry of a chunk below the count is valid and every load in bounds.
-template <int U, class F>
+template <int U, bool SOL, class F>
 __device__ __forceinline__ void for_each_entry(const StepParams& p, const int* __restrict__ col,
                                                const int* __restrict__ cnt, int s,
                                                const float4* __restrict__ xs,
@@ -525,7 +533,7 @@ __device__ __forceinline__ void for_each_entry(const StepParams& p, const int* _
             for (int u = 0; u < U; u++) nx[u] = __ldg(&col[(size_t)(k + U + u) * p.n]);
         }
 #pragma unroll
-        for (int u = 0; u < U; u++) q[u] = load_entry(e[u], xs, solid);
+        for (int u = 0; u < U; u++) q[u] = SOL ? load_entry(e[u], xs, solid) : xs[entry_slot(e[u])];
 #pragma unroll
         for (int u = 0; u < U; u++) f(e[u], q[u]);
     }
@@ -533,19 +541,22 @@ __device__ __forceinline__ void for_each_entry(const StepParams& p, const int* _
 
 // Lambda pass over the lists (iterations after the first); U neighbour
 // gathers in flight per thread.
-template <bool MIXED, int U, int B>
+// F: bit 0 mixed precision, bit 1 the scene has static particles (the
+// solid-free kernels skip the per-entry solid tests).
+template <int F, int U, int B>
 __global__ void __launch_bounds__(B) k_lambda(StepParams p, float4* __restrict__ xs,
                                               const int* __restrict__ nbr, const int* __restrict__ cnt,
                                               const float4* __restrict__ solid,
                                               float* __restrict__ rho) {
+    constexpr bool MIXED = (F & 1) != 0, SOL = (F & 2) != 0;
     pdl_wait();
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= p.n) return;
     const float4 self = xs[s];
     LambdaAcc a = lambda_init(p);
-    for_each_entry<U>(p, nbr + s, cnt, s, xs, solid, [&](int e, float4 q) {
+    for_each_entry<U, SOL>(p, nbr + s, cnt, s, xs, solid, [&](int e, float4 q) {
         float3 d = rel_e<MIXED>(p, self, q, e);
-        lambda_accumulate<MIXED>(p, a, d, entry_solid(e));
+        lambda_accumulate<MIXED>(p, a, d, SOL && entry_solid(e));
     });
     reinterpret_cast<float*>(xs)[4 * (size_t)s + 3] = lambda_of(p, a);
     if (rho) rho[s] = density_of(p, a);
@@ -553,13 +564,14 @@ __global__ void __launch_bounds__(B) k_lambda(StepParams p, float4* __restrict__
 
 // Position correction with s_corr, solid push-out and box clamp (Jacobi).
 // The last iteration also writes v = (x* - x) / dt.
-template <bool MIXED, int U, int B>
+template <int F, int U, int B>
 __global__ void __launch_bounds__(B) k_delta(StepParams p, CellPack cp, const float4* __restrict__ xs,
                                                float4* __restrict__ xs_out, const int* __restrict__ nbr,
                                                const int* __restrict__ cnt,
                                                const float4* __restrict__ solid,
                                                const int* __restrict__ key_sorted,
                                                const float4* __restrict__ x, float4* __restrict__ v_out) {
+    constexpr bool MIXED = (F & 1) != 0, SOL = (F & 2) != 0;
     pdl_wait();
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= p.n) return;
@@ -568,57 +580,57 @@ __global__ void __launch_bounds__(B) k_delta(StepParams p, CellPack cp, const fl
     float px = 0.0f, py = 0.0f, pz = 0.0f;
     float cx = 0.0f, cy = 0.0f, cz = 0.0f;
     int nct = 0;
-    for_each_entry<U>(p, nbr + s, cnt, s, xs, solid, [&](int e, float4 q) {
-        const bool sol = entry_solid(e);
+    for_each_entry<U, SOL>(p, nbr + s, cnt, s, xs, solid, [&](int e, float4 q) {
+        const bool sol = SOL && entry_solid(e);
         float3 d = rel_e<MIXED>(p, self, q, e);
-        const float r2 = dot3(d.x, d.y, d.z);
+        const float r2 = dot3e(d.x, d.y, d.z);
         const float inv_r = inv_r_of(r2);
-        const float r = r2 * inv_r;
+        const float r = __fmul_rn(r2, inv_r);
         const float lj = sol ? li : q.w;
-        const float w = (li + lj + scorr_hd(p, hdiff(p, r2))) * spiky_g(p, r, inv_r);
-        px += w * d.x;
-        py += w * d.y;
-        pz += w * d.z;
+        const float w = __fmul_rn(__fadd_rn(__fadd_rn(li, lj), scorr_hd(p, hdiff(p, r2))), spiky_g(p, r, inv_r));
+        px = __fmaf_rn(w, d.x, px);
+        py = __fmaf_rn(w, d.y, py);
+        pz = __fmaf_rn(w, d.z, pz);
         if (sol && r < p.contact && r2 > 0.0f) {
-            const float t = (p.contact - r) * inv_r;
-            cx += t * d.x;
-            cy += t * d.y;
-            cz += t * d.z;
+            const float t = __fmul_rn(__fsub_rn(p.contact, r), inv_r);
+            cx = __fmaf_rn(t, d.x, cx);
+            cy = __fmaf_rn(t, d.y, cy);
+            cz = __fmaf_rn(t, d.z, cz);
             nct++;
         }
     });
     // dp = (m / rho0) sum (lambda_i + lambda_j + s_corr) dW, dW = -Ks g d
-    const float kd = -p.ks * p.mr;
-    float dx = px * kd, dy = py * kd, dz = pz * kd;
+    const float kd = __fmul_rn(-p.ks, p.mr);
+    float dx = __fmul_rn(px, kd), dy = __fmul_rn(py, kd), dz = __fmul_rn(pz, kd);
     if (nct) {
         const float inv = __frcp_rn((float)nct);
-        dx += cx * inv;
-        dy += cy * inv;
-        dz += cz * inv;
+        dx = __fmaf_rn(cx, inv, dx);
+        dy = __fmaf_rn(cy, inv, dy);
+        dz = __fmaf_rn(cz, inv, dz);
     }
     float4 out;
     int3 cs = make_int3(0, 0, 0);
     const Geo g = geo_slot(p, s);
     if (!MIXED) {
-        out = make_float4(clampf(self.x + dx, g.lox, g.hix), clampf(self.y + dy, g.loy, g.hiy),
-                          clampf(self.z + dz, g.loz, g.hiz), 0.0f);
+        out = make_float4(clampf(__fadd_rn(self.x, dx), g.lox, g.hix), clampf(__fadd_rn(self.y, dy), g.loy, g.hiy),
+                          clampf(__fadd_rn(self.z, dz), g.loz, g.hiz), 0.0f);
     } else {
         cs = slot_cell(p, cp, g, key_sorted, p.cell_sorted, s);
-        out = make_float4(clamp_offset(p, self.x + dx, cs.x, g.lox, g.hix),
-                          clamp_offset(p, self.y + dy, cs.y, g.loy, g.hiy),
-                          clamp_offset(p, self.z + dz, cs.z, g.loz, g.hiz), 0.0f);
+        out = make_float4(clamp_offset(p, __fadd_rn(self.x, dx), cs.x, g.lox, g.hix),
+                          clamp_offset(p, __fadd_rn(self.y, dy), cs.y, g.loy, g.hiy),
+                          clamp_offset(p, __fadd_rn(self.z, dz), cs.z, g.loz, g.hiz), 0.0f);
     }
     xs_out[s] = out;
     if (v_out) {
         const float4 xo = x[s];
-        float3 d = make_float3(out.x - xo.x, out.y - xo.y, out.z - xo.z);
+        float3 d = make_float3(__fsub_rn(out.x, xo.x), __fsub_rn(out.y, xo.y), __fsub_rn(out.z, xo.z));
         if (MIXED) {
             int3 co = unpack_cell(cp, xo.w);
-            d.x += (float)(cs.x - co.x) * p.cell;
-            d.y += (float)(cs.y - co.y) * p.cell;
-            d.z += (float)(cs.z - co.z) * p.cell;
+            d.x = __fmaf_rn((float)(cs.x - co.x), p.cell, d.x);
+            d.y = __fmaf_rn((float)(cs.y - co.y), p.cell, d.y);
+            d.z = __fmaf_rn((float)(cs.z - co.z), p.cell, d.z);
         }
-        v_out[s] = make_float4(d.x * p.inv_dt, d.y * p.inv_dt, d.z * p.inv_dt, 0.0f);
+        v_out[s] = make_float4(__fmul_rn(d.x, p.inv_dt), __fmul_rn(d.y, p.inv_dt), __fmul_rn(d.z, p.inv_dt), 0.0f);
     }
 }
 
@@ -626,7 +638,7 @@ __global__ void __launch_bounds__(B) k_delta(StepParams p, CellPack cp, const fl
 // With xs_next, also the next step's prediction from the state it commits
 // (into xs_next, key, rank, count, cellk; count is zero here, the step's
 // scan having consumed it).
-template <bool MIXED, int U, int B>
+template <int F, int U, int B>
 __global__ void __launch_bounds__(B) k_xsph(StepParams p, CellPack cp, const float4* __restrict__ xs,
                                             const float4* __restrict__ v_in,
                                             const int* __restrict__ nbr, const int* __restrict__ cnt,
@@ -635,6 +647,7 @@ __global__ void __launch_bounds__(B) k_xsph(StepParams p, CellPack cp, const flo
                                             float4* __restrict__ xs_next, int* __restrict__ key,
                                             int* __restrict__ rank, int* __restrict__ count,
                                             int* __restrict__ cellk) {
+    constexpr bool MIXED = (F & 1) != 0, SOL = (F & 2) != 0;
     pdl_wait();
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= p.n) return;
@@ -651,7 +664,7 @@ __global__ void __launch_bounds__(B) k_xsph(StepParams p, CellPack cp, const flo
 #pragma unroll
             for (int u = 0; u < U; u++) {
                 const int t = __ldg(&col[(size_t)(k + u) * p.n]);  // padded list: valid below roundup(c, U)
-                e[u] = entry_solid(t) ? sent : t;  // solids take no part (their term is the sentinel's zero)
+                e[u] = (SOL && entry_solid(t)) ? sent : t;  // solids take no part (the sentinel's zero term)
             }
 #pragma unroll
             for (int u = 0; u < U; u++) {
@@ -661,17 +674,17 @@ __global__ void __launch_bounds__(B) k_xsph(StepParams p, CellPack cp, const flo
 #pragma unroll
             for (int u = 0; u < U; u++) {
                 float3 d = rel_e<MIXED>(p, self, q[u], e[u]);
-                const float hd = hdiff(p, dot3(d.x, d.y, d.z));
-                const float w = hd * hd * hd;
-                ax += (vj[u].x - vi.x) * w;
-                ay += (vj[u].y - vi.y) * w;
-                az += (vj[u].z - vi.z) * w;
+                const float hd = hdiff(p, dot3e(d.x, d.y, d.z));
+                const float w = __fmul_rn(__fmul_rn(hd, hd), hd);
+                ax = __fmaf_rn(__fsub_rn(vj[u].x, vi.x), w, ax);
+                ay = __fmaf_rn(__fsub_rn(vj[u].y, vi.y), w, ay);
+                az = __fmaf_rn(__fsub_rn(vj[u].z, vi.z), w, az);
             }
         }
     }
     // v += c sum (v_j - v_i) W, W = K6 hd^3
-    const float cx = p.c_xsph * p.k6;
-    const float4 vc = make_float4(vi.x + cx * ax, vi.y + cx * ay, vi.z + cx * az, 0.0f);
+    const float cx = __fmul_rn(p.c_xsph, p.k6);
+    const float4 vc = make_float4(__fmaf_rn(cx, ax, vi.x), __fmaf_rn(cx, ay, vi.y), __fmaf_rn(cx, az, vi.z), 0.0f);
     v_out[s] = vc;
     const Geo g = geo_slot(p, s);
     float4 xc;
@@ -992,8 +1005,9 @@ void launch_key(bool mixed, const StepParams& p, const CellPack& cp, const float
     LGB_DISPATCH(mixed, k_key, blocks_for(m, 256), 256, st, p, cp, pos, m, key, rank, count, cellk);
 }
 
-// Kernels templated on (MIXED, U, B) are instantiated for U in {1, 2, 4} and
-// B in {64, 128, 256}; the tuning picks one (TUNE_CASE expands the switch).
+// Kernels templated on (F, U, B) are instantiated for F in {0..3} (mixed,
+// solids), U in {1, 2, 4, 8} and B in {64, 128, 256}; the tuning and the
+// scene pick one (TUNE_DISPATCH expands the switch).
 #define TUNE_LAUNCH(KERNEL, MIX, U_, B_, N, ST, ...)                                            \
     launch_k(KERNEL<MIX, U_, B_>, blocks_for(N, B_), B_, ST, pdl_enabled(), __VA_ARGS__)
 #define TUNE_BLOCKS(KERNEL, MIX, U_, tu, N, ST, ...)                                            \
@@ -1018,10 +1032,12 @@ void launch_key(bool mixed, const StepParams& p, const CellPack& cp, const float
     } while (0)
 #define TUNE_DISPATCH(KERNEL, mixed, tu, N, ST, ...)                                            \
     do {                                                                                        \
-        if (mixed)                                                                              \
-            TUNE_CASE(KERNEL, true, tu, N, ST, __VA_ARGS__);                                    \
-        else                                                                                    \
-            TUNE_CASE(KERNEL, false, tu, N, ST, __VA_ARGS__);                                   \
+        switch ((mixed ? 1 : 0) | (p.ns > 0 ? 2 : 0)) {                                         \
+            case 0: TUNE_CASE(KERNEL, 0, tu, N, ST, __VA_ARGS__); break;                        \
+            case 1: TUNE_CASE(KERNEL, 1, tu, N, ST, __VA_ARGS__); break;                        \
+            case 2: TUNE_CASE(KERNEL, 2, tu, N, ST, __VA_ARGS__); break;                        \
+            default: TUNE_CASE(KERNEL, 3, tu, N, ST, __VA_ARGS__); break;                       \
+        }                                                                                       \
     } while (0)
 
 void launch_lists_lambda(bool mixed, const Tuning& tu, const StepParams& p, const CellPack& cp,
