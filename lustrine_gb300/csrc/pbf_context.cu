@@ -238,8 +238,7 @@ static int ctx_alloc(lustrine_pbf* s) {
     rc = rc ? rc : dalloc(&s->count, C);
     rc = rc ? rc : dalloc(&s->start, (size_t)C + 1);
     rc = rc ? rc : dalloc(&s->block_sums, scan_block_sums_size(C));
-    const bool tiled_scan = cell_scan_tiles(C) <= CELL_SCAN_MAX_TILES;
-    if (tiled_scan) rc = rc ? rc : dalloc(&s->tile_sum, cell_scan_tiles(C));
+    rc = rc ? rc : dalloc(&s->tile_sum, cell_scan_tiles(C));
     rc = rc ? rc : dalloc(&s->solid, ns);
     rc = rc ? rc : dalloc(&s->solid_raw, ns);
     rc = rc ? rc : dalloc(&s->sstart, (size_t)C + 1);
@@ -660,13 +659,8 @@ static int enqueue_step(lustrine_pbf* s, cudaStream_t st, StageMarks* mk = nullp
         k += 1;
     }
     if (mk) mk->mark(LUSTRINE_STAGE_PREDICT, st);
-    if (s->tile_sum) {
-        launch_scan_tiles(s->count, C, s->tile_sum, s->start, st);
-        k += 2;
-    } else {
-        launch_scan(s->count, C, s->block_sums, s->start, st);
-        k += 3;
-    }
+    launch_scan_tiles(s->count, C, s->tile_sum, s->start, st);
+    k += scan_tiles_launches(C);
     if (mk) mk->mark(LUSTRINE_STAGE_SCAN, st);
     // stable within a cell: by the caller's id in reference mode (the
     // reference's list order), by the previous slot otherwise

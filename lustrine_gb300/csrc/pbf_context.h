@@ -48,7 +48,7 @@ struct lustrine_pbf {
     int* count = nullptr;
     int* start = nullptr;
     int* block_sums = nullptr;
-    int* tile_sum = nullptr;  // per-tile totals of the step's scan (nullptr: three-kernel scan)
+    int* tile_sum = nullptr;  // per-tile totals of the step's scan
 
     // static solids, sorted by cell
     float4* solid = nullptr;

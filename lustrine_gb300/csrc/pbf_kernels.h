@@ -11,10 +11,12 @@ namespace lgb {
 // exclusive scan count -> start (C + 1 entries); zeroes count behind it
 void launch_scan(int* count, int C, int* block_sums, int* start, cudaStream_t st);
 int scan_block_sums_size(int C);
-// scan of the step: tile totals, then tiles scanned independently; for
-// cell_scan_tiles(C) <= CELL_SCAN_MAX_TILES (tile_sum: cell_scan_tiles(C) ints)
+// scan of the step: tile totals, then tiles scanned independently (the
+// totals scanned by one block in between past CELL_SCAN_MAX_TILES tiles);
+// tile_sum: cell_scan_tiles(C) ints; scan_tiles_launches: kernels it issues
 int cell_scan_tiles(int C);
 void launch_scan_tiles(int* count, int C, int* tile_sum, int* start, cudaStream_t st);
+int scan_tiles_launches(int C);
 void launch_sort_tail(const int* key, const int* rank, const int* start, const int* tie, int n,
                       int* tmp, int* perm, cudaStream_t st);
 void launch_gather_state(const int* perm, int n, const int* key, const float4* x, const float4* xs,

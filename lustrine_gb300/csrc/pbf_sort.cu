@@ -7,9 +7,10 @@
 //      the returned value as the particle's provisional rank in its cell;
 //   2. exclusive scan of count over all cells: tile totals, then every tile
 //      scanned from the sum of the totals before it (k_tile_sums,
-//      k_scan_tiles), or reduce / scan of the tile sums / down-sweep (grids
-//      of more than CELL_SCAN_MAX_TILES tiles, the standalone sort entry
-//      points); the scan also zeroes count for the next step's histogram;
+//      k_scan_tiles; grids of more than CELL_SCAN_MAX_TILES tiles scan the
+//      totals in one block in between); the standalone sort entry points use
+//      reduce / scan of the tile sums / down-sweep; the scan also zeroes
+//      count for the next step's histogram;
 //   3. scatter of particle indices to start[key] + rank;
 //   4. stabilisation: atomic arrival order is arbitrary, so each slot counts
 //      the members of its cell with a smaller tie key (previous slot, or the
@@ -176,6 +177,9 @@ __global__ void __launch_bounds__(CELL_SCAN_THREADS) k_tile_sums(const int* __re
     }
 }
 
+// SCANNED: tile_sum already holds every tile's exclusive offset (grids of
+// more than CELL_SCAN_MAX_TILES tiles scan the totals in one block first).
+template <bool SCANNED>
 __global__ void __launch_bounds__(CELL_SCAN_THREADS) k_scan_tiles(int* __restrict__ count, int C,
                                                                   const int* __restrict__ tile_sum,
                                                                   int* __restrict__ start) {
@@ -186,12 +190,14 @@ __global__ void __launch_bounds__(CELL_SCAN_THREADS) k_scan_tiles(int* __restric
     int v[CELL_SCAN_ITEMS];
     load_tile_items(count, C, base, v);
     int part = 0;
-    for (int j = threadIdx.x; j < tile; j += CELL_SCAN_THREADS) part += __ldg(&tile_sum[j]);
+    if (!SCANNED)
+        for (int j = threadIdx.x; j < tile; j += CELL_SCAN_THREADS) part += __ldg(&tile_sum[j]);
     int sum = 0;
 #pragma unroll
     for (int k = 0; k < CELL_SCAN_ITEMS; k++) sum += v[k];
     int total, offset;
     block_exclusive_scan<CELL_SCAN_THREADS>(part, &offset);
+    if (SCANNED) offset = __ldg(&tile_sum[tile]);
     int ex = block_exclusive_scan<CELL_SCAN_THREADS>(sum, &total) + offset;
     if (full) {
         int4* s4 = reinterpret_cast<int4*>(start + base);
@@ -323,10 +329,17 @@ int cell_scan_tiles(int C) { return blocks_for(C, CELL_TILE); }
 
 void launch_scan_tiles(int* count, int C, int* tile_sum, int* start, cudaStream_t st) {
     const bool pdl = pdl_enabled();
-    launch_k(k_tile_sums, cell_scan_tiles(C), CELL_SCAN_THREADS, st, pdl, (const int*)count, C, tile_sum);
-    launch_k(k_scan_tiles, cell_scan_tiles(C), CELL_SCAN_THREADS, st, pdl, count, C, (const int*)tile_sum,
-             start);
+    const int tiles = cell_scan_tiles(C);
+    launch_k(k_tile_sums, tiles, CELL_SCAN_THREADS, st, pdl, (const int*)count, C, tile_sum);
+    if (tiles <= CELL_SCAN_MAX_TILES) {
+        launch_k(k_scan_tiles<false>, tiles, CELL_SCAN_THREADS, st, pdl, count, C, (const int*)tile_sum, start);
+    } else {
+        launch_k(k_scan_sums, 1, SUMS_THREADS, st, pdl, tile_sum, tiles);  // in place, exclusive
+        launch_k(k_scan_tiles<true>, tiles, CELL_SCAN_THREADS, st, pdl, count, C, (const int*)tile_sum, start);
+    }
 }
+
+int scan_tiles_launches(int C) { return cell_scan_tiles(C) <= CELL_SCAN_MAX_TILES ? 2 : 3; }
 
 void launch_sort_tail(const int* key, const int* rank, const int* start, const int* tie, int n,
                       int* tmp, int* perm, cudaStream_t st) {

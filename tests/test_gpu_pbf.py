@@ -326,3 +326,26 @@ def test_next_step_prediction_in_commit_kernel_is_exact(precision):
     assert a.status() == 0 and b.status() == 0
     a.close()
     b.close()
+
+
+def test_neighbour_sets_exact_on_a_grid_past_the_single_pass_scan(orc):
+    """A 300 x 200 x 300 box has 18.3 M cells, past the 4,096 tiles (16.7 M
+    cells) whose totals one scan block sums on its own: the tile totals are
+    scanned first.  The lists still equal the oracle's sets."""
+    from lustrine_gb300 import PbfSim, scenes
+    rng = np.random.default_rng(12)
+    x = scenes.jitter(scenes.lattice((16, 12, 16), (140, 90, 140)), 0.05, rng)
+    from lustrine_gb300 import pbf_params
+    p = pbf_params(300, 200, 300, iterations=1)
+    p.gravity[1] = 0.0
+    sim = PbfSim(p, len(x))
+    sim.upload(x)
+    sim.step(1e-6)
+    assert sim.status() == 0
+    cnt, idx = sim.neighbors()
+    q = orc.reference_params(300, 200, 300)
+    ocnt, oidx = orc.compat_neighbors(q, x)
+    for a, b in zip(rows_sets(cnt, idx), rows_sets(ocnt, oidx)):
+        assert np.array_equal(a, b)
+    assert sim.query_cell_count((0, 0, 0), (300, 200, 300)) == len(x)
+    sim.close()
