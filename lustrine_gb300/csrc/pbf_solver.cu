@@ -129,14 +129,26 @@ __device__ __forceinline__ float axis_shift(float cell, int e, int at) {
     return b == 1 ? 0.0f : (b == 0 ? cell : -cell);
 }
 
-// x_i - x_j of a pair from the two stored positions and the list entry.
+// Mixed: the cell shift (c_i - c_j) * cell of every entry code (bits 25-30:
+// the x, y, z codes d + 1), filled per block in shared memory so a pair
+// reads its shift with one load.  All threads of the block call it.
+__device__ __forceinline__ void fill_shift_table(const StepParams& p, float4* tab) {
+    for (int k = threadIdx.x; k < 64; k += blockDim.x)
+        tab[k] = make_float4(axis_shift(p.cell, k << 25, 25), axis_shift(p.cell, k << 25, 27),
+                             axis_shift(p.cell, k << 25, 29), 0.0f);
+    __syncthreads();
+}
+
+// x_i - x_j of a pair from the two stored positions and the list entry
+// (mixed: plus the shift of its cell code from the block's table).
 template <bool MIXED>
-__device__ __forceinline__ float3 rel_e(const StepParams& p, float4 a, float4 b, int e) {
+__device__ __forceinline__ float3 rel_t(float4 a, float4 b, int e, const float4* tab) {
     float3 d = make_float3(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y), __fsub_rn(a.z, b.z));
     if (MIXED) {
-        d.x = __fadd_rn(d.x, axis_shift(p.cell, e, 25));
-        d.y = __fadd_rn(d.y, axis_shift(p.cell, e, 27));
-        d.z = __fadd_rn(d.z, axis_shift(p.cell, e, 29));
+        const float4 t = tab[(e >> 25) & 63];
+        d.x = __fadd_rn(d.x, t.x);
+        d.y = __fadd_rn(d.y, t.y);
+        d.z = __fadd_rn(d.z, t.z);
     }
     return d;
 }
@@ -550,12 +562,14 @@ __global__ void __launch_bounds__(B) k_lambda(StepParams p, float4* __restrict__
                                               float* __restrict__ rho) {
     constexpr bool MIXED = (F & 1) != 0, SOL = (F & 2) != 0;
     pdl_wait();
+    __shared__ float4 shift_tab[MIXED ? 64 : 1];
+    if (MIXED) fill_shift_table(p, shift_tab);
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= p.n) return;
     const float4 self = xs[s];
     LambdaAcc a = lambda_init(p);
     for_each_entry<U, SOL>(p, nbr + s, cnt, s, xs, solid, [&](int e, float4 q) {
-        float3 d = rel_e<MIXED>(p, self, q, e);
+        float3 d = rel_t<MIXED>(self, q, e, shift_tab);
         lambda_accumulate<MIXED>(p, a, d, SOL && entry_solid(e));
     });
     reinterpret_cast<float*>(xs)[4 * (size_t)s + 3] = lambda_of(p, a);
@@ -573,6 +587,8 @@ __global__ void __launch_bounds__(B) k_delta(StepParams p, CellPack cp, const fl
                                                const float4* __restrict__ x, float4* __restrict__ v_out) {
     constexpr bool MIXED = (F & 1) != 0, SOL = (F & 2) != 0;
     pdl_wait();
+    __shared__ float4 shift_tab[MIXED ? 64 : 1];
+    if (MIXED) fill_shift_table(p, shift_tab);
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= p.n) return;
     const float4 self = xs[s];
@@ -582,7 +598,7 @@ __global__ void __launch_bounds__(B) k_delta(StepParams p, CellPack cp, const fl
     int nct = 0;
     for_each_entry<U, SOL>(p, nbr + s, cnt, s, xs, solid, [&](int e, float4 q) {
         const bool sol = SOL && entry_solid(e);
-        float3 d = rel_e<MIXED>(p, self, q, e);
+        float3 d = rel_t<MIXED>(self, q, e, shift_tab);
         const float r2 = dot3e(d.x, d.y, d.z);
         const float inv_r = inv_r_of(r2);
         const float r = __fmul_rn(r2, inv_r);
@@ -649,6 +665,8 @@ __global__ void __launch_bounds__(B) k_xsph(StepParams p, CellPack cp, const flo
                                             int* __restrict__ cellk) {
     constexpr bool MIXED = (F & 1) != 0, SOL = (F & 2) != 0;
     pdl_wait();
+    __shared__ float4 shift_tab[MIXED ? 64 : 1];
+    if (MIXED) fill_shift_table(p, shift_tab);
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= p.n) return;
     const float4 self = xs[s];
@@ -673,7 +691,7 @@ __global__ void __launch_bounds__(B) k_xsph(StepParams p, CellPack cp, const flo
             }
 #pragma unroll
             for (int u = 0; u < U; u++) {
-                float3 d = rel_e<MIXED>(p, self, q[u], e[u]);
+                float3 d = rel_t<MIXED>(self, q[u], e[u], shift_tab);
                 const float hd = hdiff(p, dot3e(d.x, d.y, d.z));
                 const float w = __fmul_rn(__fmul_rn(hd, hd), hd);
                 ax = __fmaf_rn(__fsub_rn(vj[u].x, vi.x), w, ax);
