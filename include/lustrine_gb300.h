@@ -189,7 +189,7 @@ typedef struct lustrine_pbf_params {
     float c_xsph;             /* PBF mode */
     float solid_contact;      /* PBF mode: push-out distance to solid particles */
     int iterations;           /* PBF mode: solver iterations per step */
-    int max_neighbors;        /* neighbour list capacity per particle */
+    int max_neighbors;        /* neighbour list capacity per particle (reference defaults: 512) */
     int clamp_cells;          /* reference mode: clamp cell coordinates to the grid */
     int use_graph;            /* replay each step from a captured CUDA graph */
     int grid_mode;            /* LUSTRINE_GRID_*: dense cell table or hashed cells (PBF mode) */

@@ -64,7 +64,9 @@ extern "C" void lustrine_pbf_params_reference(lustrine_pbf_params* p, int X, int
     p->c_xsph = 0.1f;
     p->solid_contact = 2.0f * particle_radius;
     p->iterations = 1;
-    p->max_neighbors = 96;
+    // the reference's lists are unbounded and grow to 34-150 entries once its
+    // fluid clusters; lists cost memory only (4 B per entry and particle)
+    p->max_neighbors = 512;
     p->clamp_cells = 1;
     p->use_graph = 1;
 }
@@ -101,7 +103,7 @@ static int derive(const lustrine_pbf_params& q, int n, int ns, StepParams* sp, C
     if (q.mode == LUSTRINE_MODE_PBF && (n >= (1 << 25) || ns >= (1 << 25))) return LUSTRINE_ERR_UNSUPPORTED;
     if (hashed) {
         int bits = 10;
-        while ((1LL << bits) < 2 * parts && bits < 30) bits++;
+        while ((1LL << bits) < 4 * parts && bits < 30) bits++;
         p.hash_bits = bits;
         p.num_cells = 1 << bits;
     } else {
