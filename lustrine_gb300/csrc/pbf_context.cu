@@ -667,7 +667,9 @@ static int enqueue_step(lustrine_pbf* s, cudaStream_t st, StageMarks* mk = nullp
     // stable within a cell: by the caller's id in reference mode (the
     // reference's list order), by the previous slot otherwise
     const int* tie = s->prm.mode == LUSTRINE_MODE_REFERENCE ? s->id[c] : nullptr;
-    launch_sort_state(s->key, s->rank, s->start, tie, n, s->tmp, s->x[c], xs_in, s->v[c], s->id[c],
+    // velocities are not carried: the last position pass recomputes them
+    // (v = (x* - x) / dt) before anything reads them
+    launch_sort_state(s->key, s->rank, s->start, tie, n, s->tmp, s->x[c], xs_in, nullptr, s->id[c],
                       s->key_sorted, s->x[o], s->xs[o], s->v[o], s->id[o], p.hash_bits ? s->cellk : nullptr,
                       s->cell_sorted, st);
     k += 2;

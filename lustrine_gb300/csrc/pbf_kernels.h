@@ -40,8 +40,8 @@ CountingSortScratch counting_sort_scratch(int* base, int n, int num_cells);
 void launch_counting_sort(const int* keys, int n, int num_cells, CountingSortScratch w, int* start,
                           int* sorted, cudaStream_t st);
 // index scatter + stabilisation fused with the reorder of the particle state
-// (aux: an optional int per particle carried into the new order, e.g. the
-// packed cells of a hashed grid)
+// (v may be nullptr: not carried; aux: an optional int per particle carried
+// into the new order, e.g. the packed cells of a hashed grid)
 void launch_sort_state(const int* key, const int* rank, const int* start, const int* tie, int n,
                        int* tmp, const float4* x, const float4* xs, const float4* v, const int* id,
                        int* key_out, float4* x_out, float4* xs_out, float4* v_out, int* id_out,

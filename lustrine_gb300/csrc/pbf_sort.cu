@@ -278,7 +278,7 @@ __global__ void k_stabilize_gather(const int* __restrict__ tmp, const int* __res
     key_out[f] = c;
     x_out[f] = x[i];
     xs_out[f] = xs[i];
-    v_out[f] = v[i];
+    if (v) v_out[f] = v[i];
     id_out[f] = id[i];
     if (aux) aux_out[f] = aux[i];
 }
