@@ -330,7 +330,10 @@ LUSTRINE_API int lustrine_pbf_get_tuning(const lustrine_pbf* s, lustrine_pbf_tun
  * unchanged on return.  Reference mode has a single shape (returned as is). */
 LUSTRINE_API int lustrine_pbf_autotune(lustrine_pbf* s, float dt, int steps, lustrine_pbf_tuning* best,
                                        float* best_ms);
-/* Kernel launches one step issues (for launch accounting). */
+/* Kernel launches of the last step (for launch accounting); before the first
+ * step, those of a step that runs its own prediction kernel.  PBF: prediction
+ * (only when the previous step's commit kernel could not predict this one),
+ * 2-3 scan, 2 sort, list build + 2*iterations - 1 solver passes, commit. */
 LUSTRINE_API int lustrine_pbf_launches_per_step(const lustrine_pbf* s);
 
 /* Sorting::counting_sort (src/neighbors/Sorting.cpp:12-34, declared in

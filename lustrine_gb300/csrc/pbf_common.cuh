@@ -97,11 +97,16 @@ __device__ __forceinline__ float dot3(float ax, float ay, float az) {
 // Programmatic dependent launch: a step kernel launched with programmatic
 // stream serialisation may start while its predecessor drains; it waits
 // here, before reading anything the predecessor wrote, until that grid has
-// completed and its writes are visible.  Without the launch attribute this
-// returns at once.
+// completed and its writes are visible.  It then lets its own successor
+// launch: once every block of this grid has passed this point (all of them
+// resident or done), the successor's blocks take the slots this grid's
+// finished blocks free and wait in their own pdl_wait, so the successor's
+// launch and ramp overlap this grid's tail.  Without the launch attribute
+// both return at once.
 __device__ __forceinline__ void pdl_wait() {
 #if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 900
     asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 #endif
 }
 

@@ -756,7 +756,7 @@ static int step_impl(lustrine_pbf* s, float dt, bool tail_allowed) {
         if (!s->graph_exec[gi]) {
             cudaGraph_t g = nullptr;
             CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
-            s->launches = enqueue_step(s, s->stream, nullptr, predict, tail);
+            s->graph_launches[gi] = enqueue_step(s, s->stream, nullptr, predict, tail);
             cudaError_t e = cudaStreamEndCapture(s->stream, &g);
             if (e != cudaSuccess) return lgb_cuda_status(e, "cudaStreamEndCapture");
             e = cudaGraphInstantiate(&s->graph_exec[gi], g, 0);
@@ -764,6 +764,7 @@ static int step_impl(lustrine_pbf* s, float dt, bool tail_allowed) {
             if (e != cudaSuccess) return lgb_cuda_status(e, "cudaGraphInstantiate");
         }
         CK(cudaGraphLaunch(s->graph_exec[gi], s->stream));
+        s->launches = s->graph_launches[gi];
     } else {
         s->launches = enqueue_step(s, s->stream, nullptr, predict, tail);
         CK(cudaGetLastError());
@@ -1151,8 +1152,11 @@ extern "C" int lustrine_pbf_stream(lustrine_pbf* s, void** stream) {
 
 extern "C" int lustrine_pbf_launches_per_step(const lustrine_pbf* s) {
     if (!s) return -1;
-    int iters = s->prm.mode == LUSTRINE_MODE_REFERENCE ? 0 : s->prm.iterations;
-    return s->prm.mode == LUSTRINE_MODE_REFERENCE ? 9 : 7 + 2 * iters;
+    if (s->launches > 0) return s->launches;
+    // before any step: a step that predicts for itself
+    const int scan = scan_tiles_launches(s->sp.num_cells);
+    if (s->prm.mode == LUSTRINE_MODE_REFERENCE) return 1 + scan + 2 + 3;
+    return 1 + scan + 2 + 2 * s->prm.iterations + 1;
 }
 
 extern "C" const char* lustrine_error_string(int code) {

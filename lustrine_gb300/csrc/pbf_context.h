@@ -89,7 +89,8 @@ struct lustrine_pbf {
     bool pred_ready = false;
     float pred_dt = 0.0f;
     bool count_dirty = false;  // count[] holds that prediction's histogram
-    int launches = 0;
+    int launches = 0;             // kernels the last step launched
+    int graph_launches[8] = {};   // kernels in each captured step
     long long steps_done = 0;
     bool have_state = false;
     bool use_pdl = true;  // programmatic dependent launch between step kernels

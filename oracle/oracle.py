@@ -45,11 +45,41 @@ class OrcParams(C.Structure):
     ]
 
 
+class OrcSandControls(C.Structure):
+    """Mirror of ``orc_sand_controls`` in pbf_oracle.h."""
+
+    _fields_ = [
+        ("player_position", C.c_float * 3),
+        ("attract_flag", C.c_int),
+        ("blow_flag", C.c_int),
+        ("prev_attract_flag", C.c_int),
+        ("attract_radius", C.c_float),
+        ("blow_radius", C.c_float),
+        ("attract_coeff", C.c_float),
+        ("blow_coeff", C.c_float),
+        ("particle_diameter", C.c_float),
+    ]
+
+
+def sand_controls(player=(0.0, 0.0, 0.0), attract=False, blow=False, prev_attract=False,
+                  attract_radius=1.5, blow_radius=2.0, attract_coeff=1000.0, blow_coeff=500.0,
+                  diameter=1.0) -> OrcSandControls:
+    """simulate_sand's controls; the radii and coefficients default to the
+    reference's (Simulation.hpp:239-242)."""
+    c = OrcSandControls()
+    c.player_position[:] = [float(a) for a in player]
+    c.attract_flag, c.blow_flag, c.prev_attract_flag = int(attract), int(blow), int(prev_attract)
+    c.attract_radius, c.blow_radius = attract_radius, blow_radius
+    c.attract_coeff, c.blow_coeff = attract_coeff, blow_coeff
+    c.particle_diameter = diameter
+    return c
+
+
 def build(force: bool = False) -> str:
     """Compile the C restatement with the committed Makefile."""
     if force or not os.path.exists(ORC_SO) or os.path.getmtime(ORC_SO) < max(
         os.path.getmtime(os.path.join(HERE, f))
-        for f in ("pbf_oracle.c", "pbf_oracle.h", "pbf_mode_p.inc")
+        for f in ("pbf_oracle.c", "pbf_oracle.h", "pbf_mode_p.inc", "sand_oracle.inc")
     ):
         subprocess.run(["make", "-s", "-C", HERE], check=True)
     return ORC_SO
@@ -103,6 +133,8 @@ def lib():
                                      _opt(_F), _opt(_F), _opt(_I)]
         L.orc_pbf_density_d.argtypes = [P, C.c_int, C.c_int, _D, _opt(_D), _D]
         L.orc_pbf_lambda_d.argtypes = [P, C.c_int, C.c_int, _D, _opt(_D), _opt(_D), _opt(_D)]
+        L.orc_sand_step.argtypes = [P, C.POINTER(OrcSandControls), C.c_float, C.c_int, C.c_int, _F, _F,
+                                    _I, _opt(_F), _opt(_I), _opt(_I), C.c_int]
         _lib = L
     return _lib
 
@@ -197,6 +229,24 @@ def pbf_lambda(p: OrcParams, xs, solid=None):
     return lam, rho
 
 
+def sand_step(p: OrcParams, ctl: OrcSandControls, dt, x, v, attracted=None, solid=None, cap=64):
+    """One call of the reference's sand step.  The state comes back permuted
+    into cell order, as the reference leaves it.  Returns dict with x, v,
+    attracted, nbr_count, nbr_idx (n x cap; itself twice, static k as n + k)."""
+    x = np.array(x, np.float32).reshape(-1)
+    v = np.array(v, np.float32).reshape(-1)
+    n = len(x) // 3
+    att = np.zeros(n, np.int32) if attracted is None else np.array(attracted, np.int32)
+    s, ns = _solid_arg(solid, np.float32)
+    cnt = np.zeros(n, np.int32)
+    idx = np.full(n * cap, -1, np.int32)
+    rc = lib().orc_sand_step(C.byref(p), C.byref(ctl), dt, n, ns, x, v, att, s, cnt, idx, cap)
+    if rc:
+        raise RuntimeError(f"orc_sand_step failed: {rc}")
+    return dict(x=x.reshape(n, 3), v=v.reshape(n, 3), attracted=att, nbr_count=cnt,
+                nbr_idx=idx.reshape(n, cap))
+
+
 # ---------------------------------------------------------------- reference --
 
 class Reference:
@@ -219,6 +269,13 @@ class Reference:
         L.ref_neighbors.argtypes = [_I, _I, C.c_int]
         L.ref_neighbors.restype = C.c_int
         L.ref_counting_sort.argtypes = [_I, _I, C.c_size_t, C.c_size_t, _I]
+        L.ref_set_step_function.argtypes = [C.c_int]
+        L.ref_set_sand_controls.argtypes = [_F, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float,
+                                            C.c_float]
+        L.ref_get_attracted.argtypes = [_I]
+        L.ref_set_attracted.argtypes = [_I]
+        L.ref_get_float.argtypes = [C.c_int]
+        L.ref_get_float.restype = C.c_float
         self.L = L
 
     def init(self, X, Y, Z, block, block_pos, radius=0.5, scale=2.0, solids=()):
@@ -277,3 +334,23 @@ class Reference:
         out = np.zeros(len(keys), np.int32)
         self.L.ref_counting_sort(counts, keys, len(keys), num_cells, out)
         return out
+
+    def set_step_function(self, which):
+        """0: simulate_fluid, 1: simulate_sand."""
+        self.L.ref_set_step_function(which)
+
+    def set_sand_controls(self, ctl: OrcSandControls):
+        self.L.ref_set_sand_controls(np.array(ctl.player_position[:], np.float32), ctl.attract_flag,
+                                     ctl.blow_flag, ctl.attract_radius, ctl.blow_radius,
+                                     ctl.attract_coeff, ctl.blow_coeff)
+
+    def attracted(self):
+        a = np.zeros(self.n, np.int32)
+        self.L.ref_get_attracted(a)
+        return a
+
+    def set_attracted(self, a):
+        self.L.ref_set_attracted(np.ascontiguousarray(a, np.int32))
+
+    def diameter(self):
+        return float(self.L.ref_get_float(0))

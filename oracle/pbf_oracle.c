@@ -472,3 +472,7 @@ int orc_pbf_lambda_d(const orc_params* p, int n, int ns, const double* xs,
 {
     return pbf_lambda_only_d(p, n, ns, xs, solid, lambdas, density);
 }
+
+/* ----------------------------------------------------------------- sand -- */
+
+#include "sand_oracle.inc"

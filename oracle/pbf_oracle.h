@@ -133,6 +133,34 @@ int orc_pbf_density_d(const orc_params* p, int n, int ns, const double* xs,
 int orc_pbf_lambda_d(const orc_params* p, int n, int ns, const double* xs,
                      const double* solid, double* lambdas, double* density);
 
+/* ----------------------------------------------------------------- sand -- */
+
+/* The inputs of simulate_sand that are not in orc_params: the player's
+ * position (BulletPhysicsSimulation::player_position), the attract and blow
+ * flags of this call and of the previous one (the reference keeps the
+ * previous flag in a function static, Simulate.cpp:185), their radii and
+ * coefficients (Simulation.hpp:239-242) and SimulationParameters's
+ * particleDiameter (Lustrine.cpp:544). */
+typedef struct orc_sand_controls {
+    float player_position[3];
+    int attract_flag, blow_flag, prev_attract_flag;
+    float attract_radius, blow_radius, attract_coeff, blow_coeff;
+    float particle_diameter;
+} orc_sand_controls;
+
+/* One call of simulate_sand (Simulate.cpp:156-325) on n sand particles and
+ * ns static particles: integration with attract and blow, the stable
+ * counting sort by cell that permutes x, v and attracted in place
+ * (find_neighbors_uniform_grid_v1, Neighbors.cpp:262-361), 4 Jacobi
+ * contact/friction substeps each followed by the box clamp, the velocity
+ * update.  x, v: 3n floats; attracted: n ints; solid: 3ns floats.
+ * nbr_count / nbr_idx (n * cap, row-major; may be NULL) receive the
+ * reference's lists in its push order, itself included twice, static
+ * particle k as n + k.  Returns ORC_*. */
+int orc_sand_step(const orc_params* p, const orc_sand_controls* ctl, float dt, int n, int ns,
+                  float* x, float* v, int* attracted, const float* solid,
+                  int* nbr_count, int* nbr_idx, int cap);
+
 #ifdef __cplusplus
 }
 #endif

@@ -138,6 +138,41 @@ void ref_get_solids(float* s)
 
 void ref_step(float dt) { Lustrine::simulate(g_sim, dt); }
 
+// 0: simulate_fluid, 1: simulate_sand (the wrapper's set_simulate_function(0))
+void ref_set_step_function(int which)
+{
+    g_sim->simulate_fun = which == 1 ? simulate_sand : simulate_fluid;
+}
+
+// simulate_sand's inputs outside SimulationParameters (Simulation.hpp:230-242,
+// BulletPhysicsSimulation::player_position; the stubbed Bullet step leaves
+// the player where it is set here).  The previous call's attract flag is a
+// function static inside simulate_sand and cannot be set.
+void ref_set_sand_controls(const float* player, int attract_flag, int blow_flag, float attract_radius,
+                           float blow_radius, float attract_coeff, float blow_coeff)
+{
+    g_sim->bullet_physics_simulation.player_position = glm::vec3(player[0], player[1], player[2]);
+    g_sim->attract_flag = attract_flag != 0;
+    g_sim->blow_flag = blow_flag != 0;
+    g_sim->attract_radius = attract_radius;
+    g_sim->blow_radius = blow_radius;
+    g_sim->attract_coeff = attract_coeff;
+    g_sim->blow_coeff = blow_coeff;
+}
+
+void ref_get_attracted(int* out)
+{
+    for (int i = 0; i < g_sim->ptr_sand_end; i++) out[i] = g_sim->attracted[i];
+}
+
+void ref_set_attracted(const int* in)
+{
+    for (int i = 0; i < g_sim->ptr_sand_end; i++) g_sim->attracted[i] = in[i];
+}
+
+// which: 0 particleDiameter, 1 mass
+float ref_get_float(int which) { return which == 0 ? g_sim->particleDiameter : g_sim->mass; }
+
 // Neighbour lists of the last step, solid indices mapped to n + (i - ptr_solid_start).
 int ref_neighbors(int* count, int* idx, int cap)
 {

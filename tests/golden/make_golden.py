@@ -17,6 +17,15 @@ Fixtures (all from the reference binary, never from the restatement):
                       resting on the solid tops) over a seeded
                       24 x 4 x 24 voxel heightmap (1,168 solids) in a
                       24 x 16 x 24 box, same parameters.
+  ref_sand_steps.npz  the same scene stepped five times with simulate_sand
+                      (Simulate.cpp:156-325, the wrapper's
+                      set_simulate_function(0)): no flags; attract twice
+                      with the player at (12, 6, 12); blow with the player
+                      at (11, 5, 11.5); no flags.  Per step the state the
+                      reference leaves (permuted into cell order), the
+                      attracted flags and the neighbour lists (CSR, the
+                      reference's push order, itself included twice), as
+                      x1..x5, v1..v5, att1..att5, nbr_off1.., nbr1..
 """
 from __future__ import annotations
 
@@ -115,6 +124,39 @@ def make_solids(R):
     return n
 
 
+SAND_PLAN = (dict(), dict(attract=True, player=(12.0, 6.0, 12.0)), dict(attract=True, player=(12.0, 6.0, 12.0)),
+             dict(blow=True, player=(11.0, 5.0, 11.5)), dict())
+
+
+def make_sand(R):
+    """Five simulate_sand calls on the solids scene.  simulate_sand keeps the
+    previous call's attract flag in a function static, false at process start:
+    run this once per process."""
+    cells, rng = solid_grid()
+    n = R.init(24, 16, 24, (10, 8, 10), (7, 3, 7), solids=[(cells.shape, (0, 0, 0), cells)])
+    set_phys(R)
+    x0_ref, _, _, _ = R.state()
+    x0 = (x0_ref + rng.uniform(-0.05, 0.05, x0_ref.shape)).astype(np.float32)
+    v0 = np.zeros_like(x0)
+    R.set_state(x0, v0)
+    R.set_step_function(1)
+    dt = np.float32(1.0 / 60.0)
+    out = dict(domain=np.array([24, 16, 24]), x0=x0, v0=v0, solid=R.solids(), dt=dt,
+               diameter=np.float32(R.diameter()),
+               player=np.array([c.get("player", (0.0, 0.0, 0.0)) for c in SAND_PLAN], np.float32),
+               attract=np.array([c.get("attract", False) for c in SAND_PLAN], np.int32),
+               blow=np.array([c.get("blow", False) for c in SAND_PLAN], np.int32))
+    for s, c in enumerate(SAND_PLAN, start=1):
+        R.set_sand_controls(O.sand_controls(diameter=R.diameter(), **c))
+        R.step(dt)
+        x, _, v, _ = R.state()
+        cnt, idx = R.neighbors(cap=96)
+        off, flat = csr(cnt, idx)
+        out.update({f"x{s}": x, f"v{s}": v, f"att{s}": R.attracted(), f"nbr_off{s}": off, f"nbr{s}": flat})
+    np.savez_compressed(os.path.join(HERE, "ref_sand_steps.npz"), **out)
+    return n
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
@@ -126,6 +168,7 @@ def main():
     make_counting_sort(R)
     make_c0(R)
     make_solids(R)
+    make_sand(R)
     R.L.ref_free()
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):

@@ -312,11 +312,15 @@ def test_next_step_prediction_in_commit_kernel_is_exact(precision):
     a, b = PbfSim(p, sc.n, sc.ns), PbfSim(p, sc.n, sc.ns)
     for s in (a, b):
         s.upload(sc.x, None, sc.solid)
+    iters = p.iterations
     for k in range(7):
         dt = sc.dt if k < 4 else 0.5 * sc.dt
         a.step(dt)
+        # the prediction kernel runs after an upload and a change of dt only
+        assert a.launches_per_step() == 2 + 2 + 2 * iters + 1 + (k in (0, 4))
         b.set_tuning(**b.get_tuning())
         b.step(dt)
+        assert b.launches_per_step() == 2 + 2 + 2 * iters + 2
     xa, va, la, ra = a.download(lambdas=True, density=True)
     xb, vb, lb, rb = b.download(lambdas=True, density=True)
     np.testing.assert_array_equal(xa, xb)

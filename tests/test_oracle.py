@@ -126,3 +126,30 @@ def test_pbf_oracle_conserves_mass_and_stays_in_box(orc):
     # density of the FP64 helper equals the step's last lambda pass at the same state
     rho = orc.pbf_density(p, x)
     assert rho.shape == (sc.n,) and (rho > 0).all()
+
+
+def test_sand_step_bit_exact_five_steps(orc):
+    """simulate_sand restated (integration with attract and blow, the stable
+    sort that permutes the state, symmetric lists, 4 contact/friction
+    substeps) equals the reference's five calls bit for bit, lists in the
+    reference's push order."""
+    g = golden("ref_sand_steps.npz")
+    X, Y, Z = (int(a) for a in g["domain"])
+    p = phys_params(orc.reference_params(X, Y, Z))
+    n = len(g["x0"])
+    x, v, att = g["x0"], g["v0"], np.zeros(n, np.int32)
+    prev = False
+    for k in range(len(g["attract"])):
+        s = k + 1
+        ctl = orc.sand_controls(player=g["player"][k], attract=bool(g["attract"][k]), blow=bool(g["blow"][k]),
+                                prev_attract=prev, diameter=float(g["diameter"]))
+        o = orc.sand_step(p, ctl, float(g["dt"]), x, v, att, solid=g["solid"], cap=96)
+        off, flat = g[f"nbr_off{s}"], g[f"nbr{s}"]
+        assert np.array_equal(np.diff(off), o["nbr_count"])
+        assert np.array_equal(np.concatenate([o["nbr_idx"][i, :o["nbr_count"][i]] for i in range(n)]), flat)
+        assert np.array_equal(o["x"], g[f"x{s}"]) and np.array_equal(o["v"], g[f"v{s}"])
+        assert np.array_equal(o["attracted"], g[f"att{s}"])
+        x, v, att = o["x"], o["v"], o["attracted"]
+        prev = bool(g["attract"][k])
+    # the fixture exercises static neighbours and the attract flags
+    assert (g["nbr5"] >= n).sum() > 0 and g["att2"].sum() > 0 and g["att4"].sum() == 0
