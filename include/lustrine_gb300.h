@@ -51,7 +51,10 @@ enum {
 
 enum {
     LUSTRINE_MODE_REFERENCE = 0, /* simulate_fluid semantics (Simulate.cpp:27-115), Jacobi update */
-    LUSTRINE_MODE_PBF = 1        /* PBF: iterations, poly6/spiky, s_corr, solids, box, XSPH */
+    LUSTRINE_MODE_PBF = 1,       /* PBF: iterations, poly6/spiky, s_corr, solids, box, XSPH */
+    LUSTRINE_MODE_SAND = 2       /* simulate_sand semantics (Simulate.cpp:156-325): contact and
+                                    friction substeps; the particles are re-ordered by cell every
+                                    step, as the reference does (Neighbors.cpp:296-300) */
 };
 
 enum {
@@ -330,6 +333,34 @@ LUSTRINE_API int lustrine_pbf_get_tuning(const lustrine_pbf* s, lustrine_pbf_tun
  * unchanged on return.  Reference mode has a single shape (returned as is). */
 LUSTRINE_API int lustrine_pbf_autotune(lustrine_pbf* s, float dt, int steps, lustrine_pbf_tuning* best,
                                        float* best_ms);
+/* Sand mode (LUSTRINE_MODE_SAND) inputs that lustrine_pbf_params does not
+ * hold: the player's position (the reference reads it from its Bullet world,
+ * BulletPhysicsSimulation.hpp:35), the attract and blow flags of the next
+ * steps (Wrapper::simulate's arguments, LustrineWrapper.cpp:342-346), their
+ * radii and coefficients (Simulation.hpp:239-242) and the particle diameter
+ * of the contact constraint (SimulationParameters::particleDiameter).  The
+ * previous step's attract flag, a function static in the reference
+ * (Simulate.cpp:185), is kept per context. */
+typedef struct lustrine_sand_controls {
+    float player_position[3];
+    int attract_flag;
+    int blow_flag;
+    float attract_radius;     /* 1.5 */
+    float blow_radius;        /* 2.0 */
+    float attract_coeff;      /* 1000 */
+    float blow_coeff;         /* 500 */
+    float particle_diameter;  /* 2 * particle_radius unless the caller says otherwise */
+} lustrine_sand_controls;
+
+/* The reference's defaults (player at the origin, no flags). */
+LUSTRINE_API void lustrine_sand_controls_default(lustrine_sand_controls* c, float particle_radius);
+LUSTRINE_API int lustrine_pbf_set_sand_controls(lustrine_pbf* s, const lustrine_sand_controls* c);
+LUSTRINE_API int lustrine_pbf_get_sand_controls(const lustrine_pbf* s, lustrine_sand_controls* c);
+/* Per-particle attract flags of sand mode (Simulation::attracted; 0 after an
+ * upload), n_fluid ints in the current particle order.  Synchronises. */
+LUSTRINE_API int lustrine_pbf_get_attracted(lustrine_pbf* s, int* flags);
+LUSTRINE_API int lustrine_pbf_set_attracted(lustrine_pbf* s, const int* flags);
+
 /* Kernel launches of the last step (for launch accounting); before the first
  * step, those of a step that runs its own prediction kernel.  PBF: prediction
  * (only when the previous step's commit kernel could not predict this one),

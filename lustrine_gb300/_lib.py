@@ -24,7 +24,7 @@ ERRORS = {
     9: "LUSTRINE_ERR_BAD_VALUE",
     10: "LUSTRINE_ERR_TOO_LARGE",
 }
-MODE_REFERENCE, MODE_PBF = 0, 1
+MODE_REFERENCE, MODE_PBF, MODE_SAND = 0, 1, 2
 PRECISION_FP32, PRECISION_MIXED = 0, 1
 
 
@@ -79,6 +79,12 @@ GRID_AUTO, GRID_DENSE, GRID_HASHED = 0, 1, 2
 
 class PbfTuning(C.Structure):
     _fields_ = [("block", C.c_int), ("unroll", C.c_int), ("list_block", C.c_int)]
+
+
+class SandControls(C.Structure):
+    _fields_ = [("player_position", C.c_float * 3), ("attract_flag", C.c_int), ("blow_flag", C.c_int),
+                ("attract_radius", C.c_float), ("blow_radius", C.c_float), ("attract_coeff", C.c_float),
+                ("blow_coeff", C.c_float), ("particle_diameter", C.c_float)]
 
 
 # Every symbol include/lustrine_gb300.h declares, with its ctypes signature.
@@ -143,6 +149,11 @@ SIGNATURES = {
     "lustrine_pbf_status": (C.c_int, [_P]),
     "lustrine_pbf_stream": (C.c_int, [_P, C.POINTER(_P)]),
     "lustrine_pbf_launches_per_step": (C.c_int, [_P]),
+    "lustrine_sand_controls_default": (None, [C.POINTER(SandControls), C.c_float]),
+    "lustrine_pbf_set_sand_controls": (C.c_int, [_P, C.POINTER(SandControls)]),
+    "lustrine_pbf_get_sand_controls": (C.c_int, [_P, C.POINTER(SandControls)]),
+    "lustrine_pbf_get_attracted": (C.c_int, [_P, _P]),
+    "lustrine_pbf_set_attracted": (C.c_int, [_P, _P]),
     "lustrine_pbf_profile_step": (C.c_int, [_P, C.c_float, _DP, _IP, C.c_int]),
     "lustrine_pbf_set_tuning": (C.c_int, [_P, C.POINTER(PbfTuning)]),
     "lustrine_pbf_get_tuning": (C.c_int, [_P, C.POINTER(PbfTuning)]),

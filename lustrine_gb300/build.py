@@ -1,9 +1,9 @@
 """Build the CUDA library liblustrine_gb300.so in-tree for sm_103a.
 
 Each translation unit is compiled by nvcc in parallel and linked into
-lustrine_gb300/_build/liblustrine_gb300.so.  pbf_compat.cu is compiled with
---fmad=false: the reference-semantics step must not contract a * b + c into
-fused multiply-adds (the reference's arithmetic has none).
+lustrine_gb300/_build/liblustrine_gb300.so.  pbf_compat.cu and sand.cu are
+compiled with --fmad=false: the reference-semantics steps must not contract
+a * b + c into fused multiply-adds (the reference's arithmetic has none).
 """
 from __future__ import annotations
 
@@ -26,6 +26,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fvisibility=hi
 UNITS = {
     "pbf_sort.cu": [],
     "pbf_compat.cu": ["--fmad=false"],
+    "sand.cu": ["--fmad=false"],
     "pbf_solver.cu": [],
     "pbf_context.cu": [],
     "pbf_dynamic.cu": [],

@@ -76,6 +76,16 @@ struct StepParams {
     float dt;
 };
 
+// Sand mode: simulate_sand's per-call inputs (Simulate.cpp:156-209).
+struct SandParams {
+    float px, py, pz;                       // player position
+    int attract, blow, prev_attract;        // this call's flags and the previous call's attract flag
+    float attract_radius, blow_radius;
+    float attract_coeff, blow_coeff;
+    float radius, diameter;                 // particleRadius, particleDiameter
+    float w;                                // 1 / mass
+};
+
 // Launch shape of the PBF iteration kernels, chosen per scene by the autotuner.
 struct Tuning {
     int block;       // threads per block of the lambda, delta and XSPH passes (64, 128, 256)

@@ -10,6 +10,7 @@
 // positions from before the pass) instead of the reference's in-place
 // Gauss-Seidel sweep, which has no parallel form.
 #include "pbf_common.cuh"
+#include "pbf_compat.cuh"
 #include "pbf_kernels.h"
 
 namespace lgb {
@@ -66,28 +67,6 @@ __device__ __forceinline__ float resolve_collision(float value, float lo, float 
     if (value <= lo) return eps;
     if (value > hi) return hi - eps;
     return value;
-}
-
-// get_cell_id (Utils.hpp:24-33): truncating division per axis; optional clamp.
-__device__ __forceinline__ int cell_ref(const StepParams& p, float x, float y, float z, int* status) {
-    int cx = (int)(x / p.cell);
-    int cy = (int)(y / p.cell);
-    int cz = (int)(z / p.cell);
-    if (p.clamp_cells) {
-        cx = min(max(cx, 0), p.gx - 1);
-        cy = min(max(cy, 0), p.gy - 1);
-        cz = min(max(cz, 0), p.gz - 1);
-    }
-    long long id = (long long)cy * p.gx * p.gz + (long long)cx * p.gz + cz;
-    if (id < 0 || id >= p.num_cells) {
-        // The reference writes past its cell table here; record it and clamp.
-        cx = min(max(cx, 0), p.gx - 1);
-        cy = min(max(cy, 0), p.gy - 1);
-        cz = min(max(cz, 0), p.gz - 1);
-        id = (long long)cy * p.gx * p.gz + (long long)cx * p.gz + cz;
-        set_status(status, ST_CELL_RANGE);
-    }
-    return (int)id;
 }
 
 // Simulate.cpp:48-51 plus the cell key and histogram of the counting sort.

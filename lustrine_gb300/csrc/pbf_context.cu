@@ -79,7 +79,8 @@ static int derive(const lustrine_pbf_params& q, int n, int ns, StepParams* sp, C
         return LUSTRINE_ERR_ARGS;
     if (q.max_neighbors <= 0 || q.iterations < 1 || q.iterations > 1000) return LUSTRINE_ERR_ARGS;
     if (!(q.s_corr_n >= 0.0f)) return LUSTRINE_ERR_ARGS;  // (W / W(dq))^n with W = 0 at r = h
-    if (q.mode != LUSTRINE_MODE_REFERENCE && q.mode != LUSTRINE_MODE_PBF) return LUSTRINE_ERR_ARGS;
+    if (q.mode != LUSTRINE_MODE_REFERENCE && q.mode != LUSTRINE_MODE_PBF && q.mode != LUSTRINE_MODE_SAND)
+        return LUSTRINE_ERR_ARGS;
     if (q.precision == LUSTRINE_PRECISION_MIXED && q.mode != LUSTRINE_MODE_PBF)
         return LUSTRINE_ERR_UNSUPPORTED;
     StepParams p;
@@ -149,8 +150,8 @@ static int derive(const lustrine_pbf_params& q, int n, int ns, StepParams* sp, C
     p.gyv = q.gravity[1];
     p.gzv = q.gravity[2];
     const float r = q.particle_radius;
-    if (q.mode == LUSTRINE_MODE_REFERENCE) {
-        // Simulate.cpp:35-37,106-108: bounds [r, (int)domain - r]
+    if (q.mode != LUSTRINE_MODE_PBF) {
+        // Simulate.cpp:35-37,106-108 (fluid), 206-208 and 298 (sand): [r, domain - r]
         p.lox = p.loy = p.loz = r;
         p.hix = (float)q.domain[0] - r;
         p.hiy = (float)q.domain[1] - r;
@@ -193,7 +194,7 @@ void lustrine_pbf::free_buffers() {
     void* ptrs[] = {x[0], x[1], xs[0], xs[1], v[0], v[1], id[0], id[1], xs_alt, xs_pred, vtmp, key, key_sorted,
                     rank, tmp, perm, count, start, block_sums, tile_sum, solid_near, solid, solid_raw, sstart, nbr, cnt, lam,
                     lam_by_id, rho, status, red, qcount, out3, out3d, iota, slot_of, solid_id, d_scenes, d_scene_of,
-                    d_solid_scene_of, cellk, cell_sorted, solid_cell};
+                    d_solid_scene_of, cellk, cell_sorted, solid_cell, att[0], att[1]};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     x[0] = x[1] = xs[0] = xs[1] = v[0] = v[1] = nullptr;
@@ -202,6 +203,7 @@ void lustrine_pbf::free_buffers() {
     key = key_sorted = rank = tmp = perm = count = start = block_sums = tile_sum = sstart = nullptr;
     nbr = cnt = status = qcount = iota = slot_of = solid_id = d_scene_of = d_solid_scene_of = nullptr;
     cellk = cell_sorted = solid_cell = nullptr;
+    att[0] = att[1] = nullptr;
     solid_near = nullptr;
     lam = lam_by_id = rho = out3 = nullptr;
     red = out3d = nullptr;
@@ -228,6 +230,7 @@ static int ctx_alloc(lustrine_pbf* s) {
         rc = rc ? rc : dalloc(&s->xs[k], (size_t)n + 1);  // + the sentinel slot n
         rc = rc ? rc : dalloc(&s->v[k], n);
         rc = rc ? rc : dalloc(&s->id[k], n);
+        rc = rc ? rc : dalloc(&s->att[k], n);  // sand mode's attract flags
     }
     rc = rc ? rc : dalloc(&s->xs_alt, (size_t)n + 1);
     rc = rc ? rc : dalloc(&s->xs_pred, n);
@@ -298,6 +301,7 @@ extern "C" int lustrine_pbf_create(const lustrine_pbf_params* p, int n_fluid, in
     s->n = n_fluid;
     s->cap = n_fluid;
     s->ns = n_solid;
+    lustrine_sand_controls_default(&s->sand, p->particle_radius);
     int rc = derive(*p, n_fluid, n_solid, &s->sp, &s->cp);
     if (rc) {
         delete s;
@@ -510,7 +514,7 @@ static int setup_solids(lustrine_pbf* s) {
     CK(cudaMemsetAsync(s->count, 0, (size_t)C * sizeof(int), s->stream));
     s->count_dirty = false;  // zero again after the scan below
     if (ns > 0) {
-        if (s->prm.mode == LUSTRINE_MODE_REFERENCE)
+        if (s->prm.mode != LUSTRINE_MODE_PBF)  // get_cell_id's truncating division
             launch_key_ref(p, s->solid_raw, ns, s->key, s->rank, s->count, s->status, s->stream);
         else
             launch_key(s->mixed(), p, s->cp, s->solid_raw, ns, s->key, s->rank, s->count, s->cellk,
@@ -540,6 +544,7 @@ static int pack_fluid(lustrine_pbf* s, const float* dx, const float* dv) {
     else
         CK(cudaMemsetAsync(s->v[c], 0, (size_t)n * sizeof(float4), s->stream));
     CK(cudaMemcpyAsync(s->id[c], s->iota, (size_t)n * sizeof(int), cudaMemcpyDeviceToDevice, s->stream));
+    CK(cudaMemsetAsync(s->att[c], 0, (size_t)n * sizeof(int), s->stream));
     CK(cudaGetLastError());
     return LUSTRINE_OK;
 }
@@ -637,6 +642,67 @@ struct StageMarks {
     }
 };
 
+// simulate_sand's per-call inputs from the caller's controls.
+static SandParams sand_params(const lustrine_pbf* s) {
+    const lustrine_sand_controls& c = s->sand;
+    SandParams q;
+    std::memset(&q, 0, sizeof(q));
+    q.px = c.player_position[0];
+    q.py = c.player_position[1];
+    q.pz = c.player_position[2];
+    q.attract = c.attract_flag != 0;
+    q.blow = c.blow_flag != 0;
+    q.prev_attract = s->prev_attract;
+    q.attract_radius = c.attract_radius;
+    q.blow_radius = c.blow_radius;
+    q.attract_coeff = c.attract_coeff;
+    q.blow_coeff = c.blow_coeff;
+    q.radius = s->prm.particle_radius;
+    q.diameter = c.particle_diameter;
+    q.w = 1.0f / s->prm.mass;  // Simulate.cpp:185
+    return q;
+}
+
+// Sand step (simulate_sand): integration and cell keys on side c, the stable
+// sort into side o, lists, 4 contact/friction substeps ping-ponging between
+// xs[o] and xs_alt; the last commits x, v and the attract flags back into
+// side c, which the sort has consumed, so the committed side stays c and the
+// particles are in this step's cell order (the reference re-orders its own
+// arrays the same way).  The id arrays stay the identity: a particle's index
+// is its position in that order, as in the reference.
+static int enqueue_sand_step(lustrine_pbf* s, cudaStream_t st, StageMarks* mk) {
+    const int c = s->cur, o = 1 - c, n = s->n, C = s->sp.num_cells;
+    const StepParams& p = s->sp;
+    const SandParams q = sand_params(s);
+    int k = 0;
+    launch_sand_predict(p, q, s->x[c], s->v[c], s->xs[c], s->att[c], s->key, s->rank, s->count, s->status, st);
+    k += 1;
+    if (mk) mk->mark(LUSTRINE_STAGE_PREDICT, st);
+    launch_scan_tiles(s->count, C, s->tile_sum, s->start, st);
+    k += scan_tiles_launches(C);
+    if (mk) mk->mark(LUSTRINE_STAGE_SCAN, st);
+    launch_sort_state(s->key, s->rank, s->start, nullptr, n, s->tmp, s->x[c], s->xs[c], nullptr, nullptr,
+                      s->key_sorted, s->x[o], s->xs[o], nullptr, nullptr, s->att[c], s->att[o], st);
+    k += 2;
+    if (mk) mk->mark(LUSTRINE_STAGE_SORT, st);
+    launch_sand_lists(p, s->xs[o], s->key_sorted, s->start, s->solid, s->sstart, s->nbr, s->cnt, s->status, st);
+    k += 1;
+    if (mk) mk->mark(LUSTRINE_STAGE_LISTS, st);
+    float4* a = s->xs[o];
+    float4* b = s->xs_alt;
+    for (int sub = 0; sub < 4; sub++) {
+        const bool last = sub == 3;
+        launch_sand_substep(p, q, a, b, s->x[o], s->nbr, s->cnt, s->solid, last ? s->x[c] : nullptr,
+                            last ? s->v[c] : nullptr, s->att[o], s->att[c], st);
+        k += 1;
+        if (mk) mk->mark(LUSTRINE_STAGE_DELTA, st);
+        float4* t = a;
+        a = b;
+        b = t;
+    }
+    return k;
+}
+
 // One step's launches.  Returns the number of kernels launched.
 // predict: run the prediction kernel (else the previous step's commit
 // kernel left it in xs_pred, key, rank, count); tail: the commit kernel
@@ -651,6 +717,11 @@ static int enqueue_step(lustrine_pbf* s, cudaStream_t st, StageMarks* mk = nullp
     // count[] is all zero here: zeroed at allocation and by every scan.
     // Step kernels use programmatic dependent launch.
     set_pdl(s->use_pdl);
+    if (s->sand_mode()) {
+        k = enqueue_sand_step(s, st, mk);
+        set_pdl(false);
+        return k;
+    }
     const bool ref = s->prm.mode == LUSTRINE_MODE_REFERENCE;
     float4* xs_in = ref ? s->xs[c] : s->xs_pred;  // predicted positions, caller of the sort
     if (ref) {
@@ -719,7 +790,7 @@ static int enqueue_step(lustrine_pbf* s, cudaStream_t st, StageMarks* mk = nullp
 
 // Host bookkeeping after the launches of a step that started on side c.
 static void finish_step(lustrine_pbf* s, int c) {
-    s->cur = 1 - c;
+    s->cur = s->sand_mode() ? c : 1 - c;  // the sand step commits into the side it started from
     s->lists_valid = true;
     s->cells_valid = true;
     s->steps_done++;
@@ -742,6 +813,14 @@ static int step_impl(lustrine_pbf* s, float dt, bool tail_allowed) {
         s->sp.dt = dt;
         s->sp.inv_dt = 1.0f / dt;
         s->invalidate_graphs();
+    }
+    if (s->sand_mode()) {
+        // the captured sand step holds its controls (flags, player, previous flag)
+        const SandParams q = sand_params(s);
+        if (std::memcmp(&q, &s->sand_captured, sizeof(q)) != 0) {
+            s->invalidate_graphs();
+            s->sand_captured = q;
+        }
     }
     const int c = s->cur;
     const bool pbf = s->prm.mode == LUSTRINE_MODE_PBF;
@@ -773,6 +852,7 @@ static int step_impl(lustrine_pbf* s, float dt, bool tail_allowed) {
     s->pred_ready = tail;
     s->pred_dt = dt;
     s->count_dirty = tail;
+    if (s->sand_mode()) s->prev_attract = s->sand.attract_flag != 0;  // Simulate.cpp:322
     return LUSTRINE_OK;
 }
 
@@ -825,6 +905,7 @@ extern "C" int lustrine_pbf_profile_step(lustrine_pbf* s, float dt, double* stag
     for (int e = 0; e < 64; e++) cudaEventDestroy(mk.ev[e]);
     if (err != cudaSuccess) return lgb_cuda_status(err, "profile_step");
     finish_step(s, s->cur);
+    if (s->sand_mode()) s->prev_attract = s->sand.attract_flag != 0;
     return LUSTRINE_OK;
 }
 
@@ -1061,12 +1142,14 @@ extern "C" int lustrine_pbf_neighbors(lustrine_pbf* s, int* count, int* idx, int
     if (s->ns) CK(cudaMemcpyAsync(sid.data(), s->solid_id, (size_t)s->ns * sizeof(int), cudaMemcpyDeviceToHost, s->stream));
     CK(cudaStreamSynchronize(s->stream));
     int rc = LUSTRINE_OK;
-    const bool ref = s->prm.mode == LUSTRINE_MODE_REFERENCE;
+    // reference-semantics lists: slot t >= 0 or static slot -1 - u; the sand
+    // lists leave the particle itself out (the reference lists it twice)
+    const bool ref = s->prm.mode != LUSTRINE_MODE_PBF;
     for (int k = 0; k < n; k++) {
         const int i = ids[(size_t)k];
         const int c = cnt[(size_t)k];
         // PBF lists leave the particle itself out; it is reported first
-        const int self = ref ? 0 : 1;
+        const int self = s->prm.mode == LUSTRINE_MODE_PBF ? 1 : 0;
         count[i] = c + self;
         if (!idx) continue;
         if (c + self > cap) rc = LUSTRINE_ERR_NBR_OVERFLOW;
@@ -1144,6 +1227,46 @@ extern "C" int lustrine_pbf_status(lustrine_pbf* s) {
     return LUSTRINE_OK;
 }
 
+extern "C" void lustrine_sand_controls_default(lustrine_sand_controls* c, float particle_radius) {
+    if (!c) return;
+    std::memset(c, 0, sizeof(*c));
+    // Simulation.hpp:239-242; the player starts at the origin (BulletPhysicsSimulation.hpp:35)
+    c->attract_radius = 1.5f;
+    c->blow_radius = 2.0f;
+    c->attract_coeff = 1000.0f;
+    c->blow_coeff = 500.0f;
+    c->particle_diameter = 2.0f * particle_radius;
+}
+
+extern "C" int lustrine_pbf_set_sand_controls(lustrine_pbf* s, const lustrine_sand_controls* c) {
+    if (!s || !c || !(c->particle_diameter >= 0.0f)) return LUSTRINE_ERR_ARGS;
+    s->sand = *c;
+    s->sand_controls_set = true;
+    return LUSTRINE_OK;
+}
+
+extern "C" int lustrine_pbf_get_sand_controls(const lustrine_pbf* s, lustrine_sand_controls* c) {
+    if (!s || !c) return LUSTRINE_ERR_ARGS;
+    *c = s->sand;
+    return LUSTRINE_OK;
+}
+
+extern "C" int lustrine_pbf_get_attracted(lustrine_pbf* s, int* flags) {
+    if (!s || (!flags && s->n)) return LUSTRINE_ERR_ARGS;
+    if (!s->n) return LUSTRINE_OK;
+    CK(cudaMemcpyAsync(flags, s->att[s->cur], (size_t)s->n * sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return LUSTRINE_OK;
+}
+
+extern "C" int lustrine_pbf_set_attracted(lustrine_pbf* s, const int* flags) {
+    if (!s || (!flags && s->n)) return LUSTRINE_ERR_ARGS;
+    if (!s->n) return LUSTRINE_OK;
+    CK(cudaMemcpyAsync(s->att[s->cur], flags, (size_t)s->n * sizeof(int), cudaMemcpyHostToDevice, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return LUSTRINE_OK;
+}
+
 extern "C" int lustrine_pbf_stream(lustrine_pbf* s, void** stream) {
     if (!s || !stream) return LUSTRINE_ERR_ARGS;
     *stream = (void*)s->stream;
@@ -1156,6 +1279,7 @@ extern "C" int lustrine_pbf_launches_per_step(const lustrine_pbf* s) {
     // before any step: a step that predicts for itself
     const int scan = scan_tiles_launches(s->sp.num_cells);
     if (s->prm.mode == LUSTRINE_MODE_REFERENCE) return 1 + scan + 2 + 3;
+    if (s->prm.mode == LUSTRINE_MODE_SAND) return 1 + scan + 2 + 1 + 4;
     return 1 + scan + 2 + 2 * s->prm.iterations + 1;
 }
 

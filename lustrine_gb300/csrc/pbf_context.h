@@ -76,6 +76,15 @@ struct lustrine_pbf {
     float* out3 = nullptr;    // 3 * max(n, ns) floats of staging
     double* out3d = nullptr;  // 3 * n doubles of staging
 
+    // sand mode: per-particle attract flags (two sides, carried by the sort),
+    // the caller's controls, the previous step's attract flag and the
+    // controls the captured sand graph was built with
+    int* att[2] = {nullptr, nullptr};
+    lustrine_sand_controls sand{};
+    bool sand_controls_set = false;
+    int prev_attract = 0;
+    lgb::SandParams sand_captured{};
+
     // batch of independent scenes (empty for one scene)
     std::vector<int> b_domains, b_nfluid, b_nsolid;
     lgb::SceneInfo* d_scenes = nullptr;
@@ -101,6 +110,7 @@ struct lustrine_pbf {
     void free_buffers();
     void invalidate_graphs();
     bool mixed() const;
+    bool sand_mode() const { return prm.mode == LUSTRINE_MODE_SAND; }
 };
 
 // Writes the sentinel particle of the padded neighbour lists at slot s->n.

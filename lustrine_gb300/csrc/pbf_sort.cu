@@ -279,7 +279,7 @@ __global__ void k_stabilize_gather(const int* __restrict__ tmp, const int* __res
     x_out[f] = x[i];
     xs_out[f] = xs[i];
     if (v) v_out[f] = v[i];
-    id_out[f] = id[i];
+    if (id) id_out[f] = id[i];
     if (aux) aux_out[f] = aux[i];
 }
 

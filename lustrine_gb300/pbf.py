@@ -16,10 +16,11 @@ import ctypes as C
 import numpy as np
 
 from . import _lib
-from ._lib import (MODE_PBF, MODE_REFERENCE, PRECISION_FP32, PRECISION_MIXED, LustrineError,
+from ._lib import (MODE_PBF, MODE_REFERENCE, MODE_SAND, PRECISION_FP32, PRECISION_MIXED, LustrineError,
                    PbfParams, check)
 
-__all__ = ["PbfSim", "PbfParams", "reference_params", "pbf_params", "MODE_PBF", "MODE_REFERENCE",
+__all__ = ["PbfSim", "PbfParams", "reference_params", "pbf_params", "sand_params", "MODE_PBF",
+           "MODE_REFERENCE", "MODE_SAND",
            "PRECISION_FP32", "PRECISION_MIXED", "LustrineError"]
 
 
@@ -53,6 +54,19 @@ def pbf_params(X, Y, Z, *, radius=0.5, h=1.0, rest_density=1.0, mass=1.0, gravit
     p.max_neighbors = max_neighbors
     p.use_graph = 1 if use_graph else 0
     p.grid_mode = grid_mode
+    return p
+
+
+def sand_params(X, Y, Z, *, radius=0.5, kernel_radius_scale=2.0, mass=1.0, gravity=-9.81,
+                max_neighbors=96, use_graph=True) -> PbfParams:
+    """Sand-mode parameters: simulate_sand semantics (Simulate.cpp:156-325)
+    on init_simulation_extra_parameters' grid (Lustrine.cpp:543-555)."""
+    p = reference_params(X, Y, Z, radius, kernel_radius_scale)
+    p.mode = MODE_SAND
+    p.mass = mass
+    p.gravity[0], p.gravity[1], p.gravity[2] = 0.0, gravity, 0.0
+    p.max_neighbors = max_neighbors
+    p.use_graph = 1 if use_graph else 0
     return p
 
 
@@ -216,6 +230,39 @@ class PbfSim:
         t = _lib.PbfTuning()
         check(self.lib.lustrine_pbf_get_tuning(self.h, C.byref(t)), "get_tuning")
         return {"block": t.block, "unroll": t.unroll, "list_block": t.list_block}
+
+    # sand mode -------------------------------------------------------------
+    def set_sand_controls(self, player=None, attract=None, blow=None, attract_radius=None,
+                          blow_radius=None, attract_coeff=None, blow_coeff=None, diameter=None):
+        """Inputs of the next sand steps (unset arguments keep their value):
+        the player's position, the attract and blow flags, their radii and
+        coefficients, the contact diameter."""
+        c = _lib.SandControls()
+        check(self.lib.lustrine_pbf_get_sand_controls(self.h, C.byref(c)), "get_sand_controls")
+        if player is not None:
+            c.player_position[:] = [float(a) for a in player]
+        if attract is not None:
+            c.attract_flag = int(bool(attract))
+        if blow is not None:
+            c.blow_flag = int(bool(blow))
+        for name, val in (("attract_radius", attract_radius), ("blow_radius", blow_radius),
+                          ("attract_coeff", attract_coeff), ("blow_coeff", blow_coeff),
+                          ("particle_diameter", diameter)):
+            if val is not None:
+                setattr(c, name, float(val))
+        check(self.lib.lustrine_pbf_set_sand_controls(self.h, C.byref(c)), "set_sand_controls")
+
+    def attracted(self) -> np.ndarray:
+        """Sand mode's per-particle attract flags, current particle order."""
+        a = np.zeros(max(self.n, 1), np.int32)
+        check(self.lib.lustrine_pbf_get_attracted(self.h, a.ctypes.data), "get_attracted")
+        return a[: self.n]
+
+    def set_attracted(self, flags):
+        a = np.ascontiguousarray(flags, np.int32).reshape(-1)
+        if a.size != self.n:
+            raise ValueError(f"expected {self.n} flags, got {a.size}")
+        check(self.lib.lustrine_pbf_set_attracted(self.h, a.ctypes.data), "set_attracted")
 
     def set_tuning(self, block: int, unroll: int, list_block: int):
         t = _lib.PbfTuning(block, unroll, list_block)

@@ -1,0 +1,152 @@
+"""Sand mode (simulate_sand, Simulate.cpp:156-325) on the GPU against the
+reference's own five steps (golden fixture) and against the oracle's
+restatement on larger seeded scenes.  Everything is compared bit for bit:
+positions, velocities, attract flags and the neighbour lists in the
+reference's order (the reference also lists each particle twice in its own
+list; the GPU leaves it out and the substeps skip it)."""
+import numpy as np
+import pytest
+
+from conftest import golden, phys_params
+
+pytestmark = pytest.mark.gpu
+
+
+def _params(domain, mass=1.0, gravity=-9.81, max_neighbors=96, use_graph=True):
+    from lustrine_gb300 import sand_params
+    return sand_params(*domain, mass=mass, gravity=gravity, max_neighbors=max_neighbors,
+                       use_graph=use_graph)
+
+
+def _strip_self(cnt, idx):
+    """Reference-order lists without the particle's own entries."""
+    out = []
+    for i in range(len(cnt)):
+        row = idx[i, :cnt[i]]
+        out.append(row[row != i])
+    return out
+
+
+def _gpu_lists(sim):
+    cnt, idx = sim.neighbors()
+    return [idx[i, :cnt[i]] for i in range(len(cnt))]
+
+
+def test_sand_matches_reference_five_steps():
+    """The reference's fixture: no flags, attract twice, blow, no flags."""
+    from lustrine_gb300 import PbfSim
+    g = golden("ref_sand_steps.npz")
+    n, ns = len(g["x0"]), len(g["solid"])
+    sim = PbfSim(_params(tuple(int(a) for a in g["domain"])), n, ns)
+    sim.upload(g["x0"], g["v0"], g["solid"])
+    for k in range(len(g["attract"])):
+        s = k + 1
+        sim.set_sand_controls(player=g["player"][k], attract=bool(g["attract"][k]), blow=bool(g["blow"][k]),
+                              diameter=float(g["diameter"]))
+        sim.step(float(g["dt"]))
+        x, v, _, _ = sim.download()
+        assert np.array_equal(x, g[f"x{s}"]), f"step {s}: x"
+        assert np.array_equal(v, g[f"v{s}"]), f"step {s}: v"
+        assert np.array_equal(sim.attracted(), g[f"att{s}"]), f"step {s}: attracted"
+        off, flat = g[f"nbr_off{s}"], g[f"nbr{s}"]
+        ref = [flat[off[i]:off[i + 1]] for i in range(n)]
+        ref = [r[r != i] for i, r in enumerate(ref)]
+        got = _gpu_lists(sim)
+        assert all(np.array_equal(a, b) for a, b in zip(got, ref)), f"step {s}: lists"
+    assert sim.status() == 0
+    sim.close()
+
+
+def _pile(rng, block, origin, domain):
+    """A jittered block of sand at unit spacing above a seeded heightmap of
+    static particles (voxel centres)."""
+    from lustrine_gb300 import scenes
+    x = scenes.jitter(scenes.lattice(block, origin), 0.05, rng)
+    X, _, Z = domain
+    H = rng.integers(1, 4, size=(X, Z))
+    sx, sz = np.meshgrid(np.arange(X), np.arange(Z), indexing="ij")
+    solid = [np.stack([sx.ravel() + 0.5, np.full(X * Z, y + 0.5), sz.ravel() + 0.5], 1)[H.ravel() > y]
+             for y in range(3)]
+    return x.astype(np.float32), np.concatenate(solid).astype(np.float32)
+
+
+@pytest.mark.parametrize("use_graph", [True, False])
+def test_sand_matches_oracle_with_controls(orc, use_graph):
+    """20,000 sand particles over 1,500+ static ones, six steps with the
+    player attracting, then blowing, then neither: GPU == oracle bit for bit."""
+    from lustrine_gb300 import PbfSim
+    rng = np.random.default_rng(21)
+    domain = (48, 40, 48)
+    x, solid = _pile(rng, (25, 32, 25), (12, 4, 12), domain)
+    n, ns = len(x), len(solid)
+    sim = PbfSim(_params(domain, use_graph=use_graph), n, ns)
+    sim.upload(x, None, solid)
+    p = phys_params(orc.reference_params(*domain))
+    xo, vo, ao = x.copy(), np.zeros_like(x), np.zeros(n, np.int32)
+    plan = [dict(), dict(attract=True, player=(24.0, 20.0, 24.0)), dict(attract=True, player=(26.0, 18.0, 24.0)),
+            dict(blow=True, player=(20.0, 10.0, 20.0)), dict(blow=True, attract=True, player=(30.0, 8.0, 30.0)),
+            dict()]
+    prev = False
+    att_seen = 0
+    for c in plan:
+        ctl = orc.sand_controls(prev_attract=prev, diameter=1.0, **c)
+        sim.set_sand_controls(player=ctl.player_position[:], attract=bool(ctl.attract_flag),
+                              blow=bool(ctl.blow_flag), diameter=1.0)
+        sim.step(1.0 / 60.0)
+        o = orc.sand_step(p, ctl, np.float32(1.0 / 60.0), xo, vo, ao, solid=solid, cap=96)
+        xo, vo, ao = o["x"], o["v"], o["attracted"]
+        att_seen = max(att_seen, int(ao.sum()))
+        prev = bool(c.get("attract", False))
+        x, v, _, _ = sim.download()
+        assert np.array_equal(x, xo) and np.array_equal(v, vo)
+        assert np.array_equal(sim.attracted(), ao)
+        ref = _strip_self(o["nbr_count"], o["nbr_idx"])
+        got = _gpu_lists(sim)
+        assert all(np.array_equal(a, b) for a, b in zip(got, ref))
+    assert att_seen > 0, "the plan must attract some particles"
+    assert sim.status() == 0
+    sim.close()
+
+
+def test_sand_full_size_pile_one_step_exact(orc):
+    """262,144 sand particles (64^3 block) over a 128 x 128 heightmap: one
+    step equal to the oracle, and a second step keeps every particle in the
+    box with finite velocities."""
+    from lustrine_gb300 import PbfSim
+    rng = np.random.default_rng(5)
+    domain = (128, 80, 128)
+    x, solid = _pile(rng, (64, 64, 64), (32, 4, 32), domain)
+    n, ns = len(x), len(solid)
+    sim = PbfSim(_params(domain), n, ns)
+    sim.upload(x, None, solid)
+    sim.step(1.0 / 60.0)
+    p = phys_params(orc.reference_params(*domain))
+    o = orc.sand_step(p, orc.sand_controls(diameter=1.0), np.float32(1.0 / 60.0), x, np.zeros_like(x), None,
+                      solid=solid, cap=96)
+    xg, vg, _, _ = sim.download()
+    assert np.array_equal(xg, o["x"]) and np.array_equal(vg, o["v"])
+    sim.step(1.0 / 60.0)
+    xg, vg, _, _ = sim.download()
+    assert np.isfinite(vg).all()
+    assert (xg >= 0.5).all() and (xg[:, 0] <= 127.5).all() and (xg[:, 1] <= 79.5).all()
+    assert sim.status() == 0
+    sim.close()
+
+
+def test_sand_without_static_particles_and_empty():
+    from lustrine_gb300 import PbfSim
+    rng = np.random.default_rng(3)
+    from lustrine_gb300 import scenes
+    x = scenes.jitter(scenes.lattice((8, 8, 8), (4, 0, 4)), 0.05, rng)
+    sim = PbfSim(_params((16, 16, 16)), len(x), 0)
+    sim.upload(x)
+    sim.step(1.0 / 60.0, 3)
+    xg, vg, _, _ = sim.download()
+    assert np.isfinite(xg).all() and sim.status() == 0
+    assert sim.launches_per_step() == 10
+    sim.close()
+    empty = PbfSim(_params((8, 8, 8)), 0, 0)
+    empty.upload(np.zeros((0, 3), np.float32))
+    empty.step(1.0 / 60.0)
+    assert empty.status() == 0
+    empty.close()
