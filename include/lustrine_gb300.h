@@ -159,11 +159,14 @@ LUSTRINE_API int get_sink_despawned(int index);
 /* LustrineWrapper.hpp:184 / LustrineWrapper.cpp:288-291: particles in the
  * cells of the box [min, max] after the last step (lustrine_pbf_query_cell_count). */
 LUSTRINE_API int query_cell_num_particles(Vec3 min, Vec3 max, bool include_solid);
-/* LustrineWrapper.cpp:666-677.  0 and 1 select the reference's sand solvers,
- * which this library does not provide (LUSTRINE_ERR_UNSUPPORTED, step
- * unchanged); 2 selects the fluid step with reference semantics; 3 the PBF
- * step. */
+/* LustrineWrapper.cpp:666-677.  0 selects simulate_sand (also the step after
+ * init, Lustrine.cpp:72,312); 1, the reference's simulate_sand_v3, is not
+ * provided (LUSTRINE_ERR_UNSUPPORTED, step unchanged); 2 selects the fluid
+ * step with reference semantics; 3 the PBF step. */
 LUSTRINE_API void set_simulate_function(int index);
+/* The player's position read by the sand step's attract and blow
+ * (the reference takes it from its Bullet world; new entry point). */
+LUSTRINE_API void lustrine_set_player_position(Vec3 position);
 
 /* Outcome of the last layer-1 call (LUSTRINE_OK or an error code). */
 LUSTRINE_API int lustrine_last_status(void);

@@ -110,6 +110,7 @@ SIGNATURES = {
     "get_num_sand_particles": (C.c_int, []),
     "get_grid_cell_size": (C.c_int, []),
     "set_simulate_function": (None, [C.c_int]),
+    "lustrine_set_player_position": (None, [Vec3]),
     "query_cell_num_particles": (C.c_int, [Vec3, Vec3, C.c_bool]),
     "add_particle_source": (C.c_int, [C.POINTER(GridWrapper), Vec3, C.c_float, C.c_int]),
     "add_particle_sink": (C.c_int, [Vec3, Vec3, C.c_float]),

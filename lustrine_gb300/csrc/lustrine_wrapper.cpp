@@ -182,6 +182,8 @@ void init_common(const SimulationParameters* prm, SimulationData* data, GridWrap
 
     lustrine_pbf_params p;
     lustrine_pbf_params_reference(&p, prm->X, prm->Y, prm->Z, prm->particleRadius, kernel_radius_scale);
+    // the step after init is simulate_sand (Lustrine.cpp:72,312)
+    p.mode = LUSTRINE_MODE_SAND;
     // Lustrine.cpp:105-126,237: the allocation holds max(n + ns, X Y Z sub^3)
     // particles; sources may add num_remaining = total - 1 - ns - n of them
     // (room for them is reserved, up to 2^22 extra particles)
@@ -190,6 +192,12 @@ void init_common(const SimulationParameters* prm, SimulationData* data, GridWrap
     const long long room = std::max<long long>(0, std::min<long long>(total - 1 - ns - n, 1LL << 22));
     int rc = lustrine_pbf_create(&p, n, ns, &g_ctx);
     if (!rc && room > 0) rc = lustrine_pbf_reserve(g_ctx, (int)(n + room));
+    if (!rc) {  // simulate_sand's contact distance is the caller's particleDiameter
+        lustrine_sand_controls c;
+        lustrine_sand_controls_default(&c, prm->particleRadius);
+        c.particle_diameter = prm->particleDiameter;
+        rc = lustrine_pbf_set_sand_controls(g_ctx, &c);
+    }
     if (!rc) rc = lustrine_pbf_upload(g_ctx, xs.data(), nullptr, sol.data());
     if (rc) {
         release();
@@ -243,13 +251,37 @@ void init_simulation_extra_parameters(const SimulationParameters* parameters, Si
                 kernel_radius_scale, false);
 }
 
+// LustrineWrapper.cpp:342-346: the flags stay set for later simulate_no_flags
+// calls; the sand step reads them (the fluid steps do not)
 void simulate(float dt, bool attract_flag, bool blow_flag) {
-    (void)attract_flag;
-    (void)blow_flag;
-    g_status = g_ctx ? simulate_frame(dt) : LUSTRINE_ERR_NO_SIMULATION;
+    if (!g_ctx) {
+        g_status = LUSTRINE_ERR_NO_SIMULATION;
+        return;
+    }
+    lustrine_sand_controls c;
+    lustrine_pbf_get_sand_controls(g_ctx, &c);
+    c.attract_flag = attract_flag ? 1 : 0;
+    c.blow_flag = blow_flag ? 1 : 0;
+    g_status = lustrine_pbf_set_sand_controls(g_ctx, &c);
+    if (!g_status) g_status = simulate_frame(dt);
 }
 
 void simulate_no_flags(float dt) { g_status = g_ctx ? simulate_frame(dt) : LUSTRINE_ERR_NO_SIMULATION; }
+
+// The player's position for the sand step's attract and blow (the reference
+// reads it from its Bullet world, which is not part of this library).
+void lustrine_set_player_position(Vec3 position) {
+    if (!g_ctx) {
+        g_status = LUSTRINE_ERR_NO_SIMULATION;
+        return;
+    }
+    lustrine_sand_controls c;
+    lustrine_pbf_get_sand_controls(g_ctx, &c);
+    c.player_position[0] = position.x;
+    c.player_position[1] = position.y;
+    c.player_position[2] = position.z;
+    g_status = lustrine_pbf_set_sand_controls(g_ctx, &c);
+}
 
 // LustrineWrapper.cpp:679-703 / Lustrine.cpp:916-1017
 int add_particle_source(GridWrapper* pattern, Vec3 direction, float freq, int capacity) {
@@ -395,18 +427,20 @@ void set_simulate_function(int index) {
         g_status = LUSTRINE_ERR_NO_SIMULATION;
         return;
     }
-    if (index == 0 || index == 1) {
-        // simulate_sand / simulate_sand_v3 (LustrineWrapper.cpp:668-673) are not built here
+    if (index == 1) {
+        // simulate_sand_v3 (LustrineWrapper.cpp:671-673), an in-place
+        // Gauss-Seidel sweep over cell pairs, is not built here
         g_status = LUSTRINE_ERR_UNSUPPORTED;
         return;
     }
-    if (index != 2 && index != 3) {
+    if (index != 0 && index != 2 && index != 3) {
         g_status = LUSTRINE_ERR_ARGS;  // LustrineWrapper.cpp:674-675
         return;
     }
     lustrine_pbf_params p;
     lustrine_pbf_get_params(g_ctx, &p);
-    p.mode = index == 2 ? LUSTRINE_MODE_REFERENCE : LUSTRINE_MODE_PBF;
+    // 0: simulate_sand (LustrineWrapper.cpp:668-670); 2, 3: the fluid steps
+    p.mode = index == 0 ? LUSTRINE_MODE_SAND : index == 2 ? LUSTRINE_MODE_REFERENCE : LUSTRINE_MODE_PBF;
     g_status = lustrine_pbf_set_params(g_ctx, &p);
 }
 

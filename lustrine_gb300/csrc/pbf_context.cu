@@ -668,8 +668,8 @@ static SandParams sand_params(const lustrine_pbf* s) {
 // xs[o] and xs_alt; the last commits x, v and the attract flags back into
 // side c, which the sort has consumed, so the committed side stays c and the
 // particles are in this step's cell order (the reference re-orders its own
-// arrays the same way).  The id arrays stay the identity: a particle's index
-// is its position in that order, as in the reference.
+// arrays the same way).  The commit makes id[c] the identity: a particle's
+// index is its position in that order, as in the reference.
 static int enqueue_sand_step(lustrine_pbf* s, cudaStream_t st, StageMarks* mk) {
     const int c = s->cur, o = 1 - c, n = s->n, C = s->sp.num_cells;
     const StepParams& p = s->sp;
@@ -681,7 +681,10 @@ static int enqueue_sand_step(lustrine_pbf* s, cudaStream_t st, StageMarks* mk) {
     launch_scan_tiles(s->count, C, s->tile_sum, s->start, st);
     k += scan_tiles_launches(C);
     if (mk) mk->mark(LUSTRINE_STAGE_SCAN, st);
-    launch_sort_state(s->key, s->rank, s->start, nullptr, n, s->tmp, s->x[c], s->xs[c], nullptr, nullptr,
+    // stable by the particle's index (its slot after a sand step; a caller
+    // index after sources or sinks changed the order), as the reference's
+    // counting sort is (Sorting.cpp:29-32)
+    launch_sort_state(s->key, s->rank, s->start, s->id[c], n, s->tmp, s->x[c], s->xs[c], nullptr, nullptr,
                       s->key_sorted, s->x[o], s->xs[o], nullptr, nullptr, s->att[c], s->att[o], st);
     k += 2;
     if (mk) mk->mark(LUSTRINE_STAGE_SORT, st);
@@ -693,7 +696,7 @@ static int enqueue_sand_step(lustrine_pbf* s, cudaStream_t st, StageMarks* mk) {
     for (int sub = 0; sub < 4; sub++) {
         const bool last = sub == 3;
         launch_sand_substep(p, q, a, b, s->x[o], s->nbr, s->cnt, s->solid, last ? s->x[c] : nullptr,
-                            last ? s->v[c] : nullptr, s->att[o], s->att[c], st);
+                            last ? s->v[c] : nullptr, s->att[o], s->att[c], s->id[c], st);
         k += 1;
         if (mk) mk->mark(LUSTRINE_STAGE_DELTA, st);
         float4* t = a;

@@ -70,7 +70,8 @@ __global__ void __launch_bounds__(DYN_THREADS) k_keep_count(const int* __restric
 __global__ void __launch_bounds__(DYN_THREADS) k_keep_scatter(
     const int* __restrict__ remap, const int* __restrict__ block_offset, int n, const float4* __restrict__ x,
     const float4* __restrict__ v, const int* __restrict__ id, const int* __restrict__ key,
-    float4* __restrict__ x_out, float4* __restrict__ v_out, int* __restrict__ id_out, int* __restrict__ key_out) {
+    const int* __restrict__ att, float4* __restrict__ x_out, float4* __restrict__ v_out, int* __restrict__ id_out,
+    int* __restrict__ key_out, int* __restrict__ att_out) {
     __shared__ int warp_count[DYN_THREADS / 32];
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     const int nid = s < n ? remap[id[s]] : -1;
@@ -87,6 +88,7 @@ __global__ void __launch_bounds__(DYN_THREADS) k_keep_scatter(
     v_out[d] = v[s];
     id_out[d] = nid;
     key_out[d] = key[s];
+    att_out[d] = att[s];  // sand mode's attract flag travels with its particle
 }
 
 __global__ void k_histogram(const int* __restrict__ key, int n, int* __restrict__ count) {
@@ -129,6 +131,8 @@ extern "C" int lustrine_pbf_spawn(lustrine_pbf* s, const float* x, const float* 
         CK(cudaMemsetAsync(s->v[c] + n, 0, (size_t)m * sizeof(float4), s->stream));
     }
     CK(cudaMemcpyAsync(s->id[c] + n, s->iota + n, (size_t)m * sizeof(int), cudaMemcpyDeviceToDevice, s->stream));
+    // sand mode: spawned particles start unattracted
+    CK(cudaMemsetAsync(s->att[c] + n, 0, (size_t)m * sizeof(int), s->stream));
     CK(cudaGetLastError());
     s->n = n + m;
     return after_resize(s);
@@ -140,9 +144,11 @@ extern "C" int lustrine_pbf_set_count(lustrine_pbf* s, int n) {
     if (!s->have_state) return LUSTRINE_ERR_ARGS;
     if (n > s->cap) return LUSTRINE_ERR_TOO_LARGE;
     if (n == s->n) return LUSTRINE_OK;
-    if (n > s->n)  // identity labels for the new slots until the caller's state upload
+    if (n > s->n) {  // identity labels for the new slots until the caller's state upload
         CK(cudaMemcpyAsync(s->id[s->cur] + s->n, s->iota + s->n, (size_t)(n - s->n) * sizeof(int),
                            cudaMemcpyDeviceToDevice, s->stream));
+        CK(cudaMemsetAsync(s->att[s->cur] + s->n, 0, (size_t)(n - s->n) * sizeof(int), s->stream));
+    }
     s->n = n;
     s->cells_valid = false;
     return after_resize(s);
@@ -272,7 +278,8 @@ extern "C" int lustrine_pbf_despawn_cells(lustrine_pbf* s, const int* cells, int
     e = cudaMemcpyAsync(block_count, bc.data(), (size_t)nb * sizeof(int), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) {
         k_keep_scatter<<<nb, DYN_THREADS, 0, st>>>(remap, block_count, n, s->x[c], s->v[c], s->id[c],
-                                                   s->key_sorted, s->x[o], s->v[o], s->id[o], s->key);
+                                                   s->key_sorted, s->att[c], s->x[o], s->v[o], s->id[o], s->key,
+                                                   s->att[o]);
         std::swap(s->key, s->key_sorted);
         if (s->count_dirty)  // a histogram of the next step's prediction, dropped with it
             e = cudaMemsetAsync(s->count, 0, (size_t)C * sizeof(int), st);

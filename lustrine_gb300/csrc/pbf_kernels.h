@@ -69,11 +69,12 @@ void launch_sand_predict(const StepParams& p, const SandParams& q, const float4*
 void launch_sand_lists(const StepParams& p, const float4* xs, const int* key, const int* fstart,
                        const float4* solid, const int* sstart, int* nbr, int* cnt, int* status,
                        cudaStream_t st);
-// x_commit == nullptr: write star_out; otherwise commit x, v and the flags
+// x_commit == nullptr: write star_out; otherwise commit x, v, the flags and
+// the identity index of every slot
 void launch_sand_substep(const StepParams& p, const SandParams& q, const float4* tmp_in, float4* star_out,
                          const float4* xpre, const int* nbr, const int* cnt, const float4* solid,
                          float4* x_commit, float4* v_commit, const int* att_in, int* att_commit,
-                         cudaStream_t st);
+                         int* id_commit, cudaStream_t st);
 
 // pbf_solver.cu (PBF; mixed = cell index + offset representation)
 // cellk: packed cell of every particle on a hashed grid (nullptr when dense)

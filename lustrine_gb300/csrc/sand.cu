@@ -219,14 +219,16 @@ __device__ __forceinline__ void sand_pair(const StepParams& p, const SandParams&
 // One contact/friction substep (Simulate.cpp:221-303): every particle reads
 // positions_tmp (tmp_in) and the pre-step positions (xpre), writes its new
 // clamped position.  The last substep commits instead: x = x*,
-// v = (x* - x) / dt (Simulate.cpp:309-313) and the attract flags, into the
-// side the step started from (whose contents the sort already consumed).
+// v = (x* - x) / dt (Simulate.cpp:309-313), the attract flags and the
+// particle's index -- its slot in this step's cell order, as the reference
+// re-orders its arrays -- into the side the step started from (whose
+// contents the sort already consumed).
 __global__ void k_sand_substep(StepParams p, SandParams q, const float4* __restrict__ tmp_in,
                                float4* __restrict__ star_out, const float4* __restrict__ xpre,
                                const int* __restrict__ nbr, const int* __restrict__ cnt,
                                const float4* __restrict__ solid, float4* __restrict__ x_commit,
                                float4* __restrict__ v_commit, const int* __restrict__ att_in,
-                               int* __restrict__ att_commit) {
+                               int* __restrict__ att_commit, int* __restrict__ id_commit) {
     pdl_wait();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
@@ -249,6 +251,7 @@ __global__ void k_sand_substep(StepParams p, SandParams q, const float4* __restr
     x_commit[i] = s;
     v_commit[i] = make_float4((s.x - xi.x) / p.dt, (s.y - xi.y) / p.dt, (s.z - xi.z) / p.dt, 0.0f);
     att_commit[i] = att_in[i];
+    id_commit[i] = i;
 }
 
 // ------------------------------------------------------------------ launch --
@@ -273,10 +276,10 @@ void launch_sand_lists(const StepParams& p, const float4* xs, const int* key, co
 void launch_sand_substep(const StepParams& p, const SandParams& q, const float4* tmp_in, float4* star_out,
                          const float4* xpre, const int* nbr, const int* cnt, const float4* solid,
                          float4* x_commit, float4* v_commit, const int* att_in, int* att_commit,
-                         cudaStream_t st) {
+                         int* id_commit, cudaStream_t st) {
     if (p.n <= 0) return;
     launch_k(k_sand_substep, blocks_for(p.n, 128), 128, st, pdl_enabled(), p, q, tmp_in, star_out, xpre, nbr,
-             cnt, solid, x_commit, v_commit, att_in, att_commit);
+             cnt, solid, x_commit, v_commit, att_in, att_commit, id_commit);
 }
 
 }  // namespace lgb

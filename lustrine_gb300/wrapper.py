@@ -18,7 +18,7 @@ __all__ = ["SimulationParameters", "SimulationData", "GridWrapper", "Vec3", "Col
            "set_source_state", "set_sink_state", "get_source_spawned", "get_sink_despawned",
            "init_grid_box", "init_simulation", "init_simulation_extra_parameters", "simulate",
            "simulate_no_flags", "simulation_bind_positions_copy", "cleanup_simulation",
-           "get_num_sand_particles", "get_grid_cell_size", "set_simulate_function",
+           "get_num_sand_particles", "get_grid_cell_size", "set_simulate_function", "set_player_position",
            "last_status", "free_grid"]
 
 
@@ -133,7 +133,14 @@ def get_sink_despawned(index: int) -> int:
 
 
 def set_simulate_function(index: int):
+    """0: simulate_sand (the step after init), 2: the fluid step with the
+    reference's semantics, 3: the PBF step."""
     _lib_().set_simulate_function(index)
+
+
+def set_player_position(position):
+    """The player's position for the sand step's attract and blow."""
+    _lib_().lustrine_set_player_position(Vec3(*[float(a) for a in position]))
 
 
 def last_status() -> int:

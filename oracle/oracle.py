@@ -134,7 +134,7 @@ def lib():
         L.orc_pbf_density_d.argtypes = [P, C.c_int, C.c_int, _D, _opt(_D), _D]
         L.orc_pbf_lambda_d.argtypes = [P, C.c_int, C.c_int, _D, _opt(_D), _opt(_D), _opt(_D)]
         L.orc_sand_step.argtypes = [P, C.POINTER(OrcSandControls), C.c_float, C.c_int, C.c_int, _F, _F,
-                                    _I, _opt(_F), _opt(_I), _opt(_I), C.c_int]
+                                    _I, _opt(_F), _opt(_I), _opt(_I), C.c_int, _opt(_F)]
         _lib = L
     return _lib
 
@@ -232,7 +232,8 @@ def pbf_lambda(p: OrcParams, xs, solid=None):
 def sand_step(p: OrcParams, ctl: OrcSandControls, dt, x, v, attracted=None, solid=None, cap=64):
     """One call of the reference's sand step.  The state comes back permuted
     into cell order, as the reference leaves it.  Returns dict with x, v,
-    attracted, nbr_count, nbr_idx (n x cap; itself twice, static k as n + k)."""
+    attracted, nbr_count, nbr_idx (n x cap; itself twice, static k as n + k)
+    and xs (the predicted positions the step binned, sorted order)."""
     x = np.array(x, np.float32).reshape(-1)
     v = np.array(v, np.float32).reshape(-1)
     n = len(x) // 3
@@ -240,11 +241,12 @@ def sand_step(p: OrcParams, ctl: OrcSandControls, dt, x, v, attracted=None, soli
     s, ns = _solid_arg(solid, np.float32)
     cnt = np.zeros(n, np.int32)
     idx = np.full(n * cap, -1, np.int32)
-    rc = lib().orc_sand_step(C.byref(p), C.byref(ctl), dt, n, ns, x, v, att, s, cnt, idx, cap)
+    xs = np.zeros(3 * max(n, 1), np.float32)
+    rc = lib().orc_sand_step(C.byref(p), C.byref(ctl), dt, n, ns, x, v, att, s, cnt, idx, cap, xs)
     if rc:
         raise RuntimeError(f"orc_sand_step failed: {rc}")
     return dict(x=x.reshape(n, 3), v=v.reshape(n, 3), attracted=att, nbr_count=cnt,
-                nbr_idx=idx.reshape(n, cap))
+                nbr_idx=idx.reshape(n, cap), xs=xs[: 3 * n].reshape(n, 3))
 
 
 # ---------------------------------------------------------------- reference --

@@ -156,10 +156,12 @@ typedef struct orc_sand_controls {
  * update.  x, v: 3n floats; attracted: n ints; solid: 3ns floats.
  * nbr_count / nbr_idx (n * cap, row-major; may be NULL) receive the
  * reference's lists in its push order, itself included twice, static
- * particle k as n + k.  Returns ORC_*. */
+ * particle k as n + k.  xs_sorted (3n floats, may be NULL) receives the
+ * predicted positions in the sorted order, the positions the step binned
+ * (the cells its sinks read).  Returns ORC_*. */
 int orc_sand_step(const orc_params* p, const orc_sand_controls* ctl, float dt, int n, int ns,
                   float* x, float* v, int* attracted, const float* solid,
-                  int* nbr_count, int* nbr_idx, int cap);
+                  int* nbr_count, int* nbr_idx, int cap, float* xs_sorted);
 
 #ifdef __cplusplus
 }

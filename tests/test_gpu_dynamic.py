@@ -121,6 +121,8 @@ def test_wrapper_sources_and_sinks_match_a_restatement():
     try:
         W.init_simulation_extra_parameters(prm, [sand], [floor], 1, 2.0)
         assert W.last_status() == 0
+        W.set_simulate_function(2)  # the fluid step (simulate_sand follows init)
+        assert W.last_status() == 0
         n0 = W.get_num_sand_particles()
         src = W.add_particle_source(pattern, (0.0, -1.0, 0.0), 0.03, 12)
         snk = W.add_particle_sink((7, 5, 7), (10, 7.5, 10), 0.0)  # the block's lower corner

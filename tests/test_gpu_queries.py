@@ -134,6 +134,8 @@ def test_wrapper_entry_points_drive_reference_mode(orc):
     try:
         data = W.init_simulation_extra_parameters(prm, [sand], [floor], 1, 2.0)
         assert W.last_status() == 0
+        W.set_simulate_function(2)  # the fluid step (simulate_sand follows init)
+        assert W.last_status() == 0
         n = W.get_num_sand_particles()
         assert n == data.num_sand_particles == 6 * 5 * 6 and data.num_solid_particles == 400
         x0 = W.simulation_bind_positions_copy()

@@ -150,3 +150,99 @@ def test_sand_without_static_particles_and_empty():
     empty.step(1.0 / 60.0)
     assert empty.status() == 0
     empty.close()
+
+
+def test_wrapper_runs_simulate_sand_after_init(orc):
+    """The reference's C entry points: init_simulation_extra_parameters leaves
+    simulate_sand selected (Lustrine.cpp:312); simulate(dt, attract, blow)
+    passes its flags, simulate_no_flags keeps them; positions come back in
+    the reference's order (re-sorted by cell every step)."""
+    from lustrine_gb300 import wrapper as W
+    from lustrine_gb300._lib import SimulationParameters
+    from test_gpu_queries import _box_solid_positions
+    prm = SimulationParameters(20, 20, 20, 0.5, 1.0)
+    sand = W.init_grid_box(prm, 6, 5, 6, (5.0, 3.0, 5.0), type_=1)
+    floor = W.init_grid_box(prm, 20, 1, 20, (0.0, 0.0, 0.0), type_=0)
+    try:
+        W.init_simulation_extra_parameters(prm, [sand], [floor], 1, 2.0)
+        assert W.last_status() == 0
+        x = W.simulation_bind_positions_copy()
+        solid = _box_solid_positions(20, 1, 20, (0.0, 0.0, 0.0), 1.0)
+        p = orc.reference_params(20, 20, 20, 0.5, 2.0)  # mass 5, gravity -10 (Simulation.hpp:157-171)
+        v, att = np.zeros_like(x), np.zeros(len(x), np.int32)
+        W.set_player_position((8.0, 5.0, 8.0))
+        prev, seen = False, 0
+        for flags in ((False, False), (True, False), None, (False, True), (False, False)):
+            if flags is None:  # the previous call's flags stay
+                W.simulate_no_flags(1 / 60)
+                flags = last
+            else:
+                W.simulate(1 / 60, *flags)
+            assert W.last_status() == 0
+            ctl = orc.sand_controls(player=(8.0, 5.0, 8.0), attract=flags[0], blow=flags[1], prev_attract=prev,
+                                    diameter=1.0)
+            o = orc.sand_step(p, ctl, np.float32(1 / 60), x, v, att, solid=solid, cap=96)
+            x, v, att = o["x"], o["v"], o["attracted"]
+            prev, last = flags[0], flags
+            seen = max(seen, int(att.sum()))
+            assert np.array_equal(W.simulation_bind_positions_copy(), x)
+        assert seen > 0, "the player must attract some particles"
+        W.set_simulate_function(1)  # simulate_sand_v3 is not provided
+        assert W.last_status() != 0
+        W.set_simulate_function(0)
+        assert W.last_status() == 0
+    finally:
+        W.cleanup_simulation()
+        W.free_grid(sand)
+        W.free_grid(floor)
+
+
+def test_sand_sources_and_sinks_match_oracle(orc):
+    """Spawned blocks and a sink on the sand step: the context's spawn,
+    step and cell despawn against the oracle's step with the reference's
+    spawn (append) and swap-remove eviction (Lustrine.cpp:768-834) of the
+    sand particles the step binned in the sink cells."""
+    from lustrine_gb300 import PbfSim, scenes
+    rng = np.random.default_rng(8)
+    domain = (24, 24, 24)
+    x, solid = _pile(rng, (6, 6, 6), (9, 4, 9), domain)
+    n0 = len(x)
+    sim = PbfSim(_params(domain), n0, len(solid))
+    sim.reserve(n0 + 64)
+    sim.upload(x, None, solid)
+    p = phys_params(orc.reference_params(*domain))
+    g = [int(a) for a in p.grid]
+    sink = np.array([y * g[0] * g[2] + xx * g[2] + z for y in range(3, 6) for xx in range(8, 12)
+                     for z in range(8, 12)], np.int32)
+    pat = scenes.lattice((2, 1, 2), (11.0, 16.0, 11.0)).astype(np.float32)
+    xo, vo, ao = x.copy(), np.zeros_like(x), np.zeros(n0, np.int32)
+    ctl = orc.sand_controls(diameter=1.0)
+    dt = np.float32(1 / 60)
+    for frame in range(10):
+        if frame % 3 == 1:
+            vs = np.tile(np.array([0.0, -2.0, 0.0], np.float32), (len(pat), 1))
+            sim.spawn(pat, vs)
+            xo, vo = np.concatenate([xo, pat]), np.concatenate([vo, vs])
+            ao = np.concatenate([ao, np.zeros(len(pat), np.int32)])
+        sim.step(float(dt))
+        o = orc.sand_step(p, ctl, dt, xo, vo, ao, solid=solid, cap=96)
+        xo, vo, ao = o["x"].copy(), o["v"].copy(), o["attracted"].copy()
+        if frame % 2 == 0:
+            removed = sim.despawn_cells(sink)
+            keys = ((np.trunc(o["xs"][:, 1] / p.cell_size).astype(np.int64) * g[0] * g[2])
+                    + np.trunc(o["xs"][:, 0] / p.cell_size).astype(np.int64) * g[2]
+                    + np.trunc(o["xs"][:, 2] / p.cell_size).astype(np.int64))
+            evict = [i for c in sink for i in np.nonzero(keys == c)[0]]
+            end = len(xo)
+            for e in evict:  # Lustrine.cpp:824-832
+                xo[e], vo[e], ao[e] = xo[end - 1], vo[end - 1], ao[end - 1]
+                end -= 1
+            xo, vo, ao = xo[:end], vo[:end], ao[:end]
+            assert removed == len(evict)
+        xg, vg, _, _ = sim.download()
+        assert len(xg) == len(xo)
+        assert np.array_equal(xg, xo) and np.array_equal(vg, vo)
+        assert np.array_equal(sim.attracted(), ao)
+    assert sim.n < n0 + 3 * len(pat)  # the sink removed particles
+    assert sim.status() == 0
+    sim.close()
