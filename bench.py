@@ -202,6 +202,24 @@ def cpu_reference_rate(scene, budget_s, min_steps=3):
     return scene.n / t, len(times), t
 
 
+def cpu_sand_rate(scene, x, v, reps=3):
+    """The reference's sand step restated by the oracle (single thread) on the
+    given state: median time of `reps` steps from it.  Particle-substeps/s."""
+    from oracle import oracle as O
+    O.build()
+    p = O.reference_params(*scene.domain)
+    p.mass = 1.0
+    p.gravity[1] = -9.81
+    ctl = O.sand_controls(diameter=1.0)
+    times = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        O.sand_step(p, ctl, np.float32(scene.dt), x, v, None, solid=scene.solid, cap=96)
+        times.append(time.perf_counter() - t0)
+    t = statistics.median(times)
+    return scene.n * 4 / t, t
+
+
 def run_reference(args, world, rank):
     if rank != 0:
         return
@@ -413,6 +431,7 @@ def run_variants(args, flush):
                                "launch_shape": sim.tuned["tuning"],
                                "stage_ms": {a: round(b[0], 4) for a, b in prof.items()}}
     sim.close()
+    out["sand_config1_262k"] = run_sand(k, flush)
     out["config3_batched_vs_plain"] = run_config3(max(3, min(args.steps, 10)), flush)
     # 4,194,304 particles in a 4096 x 256 x 4096 box: 4.3e9 cells, so the
     # grid is hashed (2^23 buckets); mixed precision is the mode the box needs
@@ -427,6 +446,36 @@ def run_variants(args, flush):
                      "max_density_error": sim.reduce()["max_density_error"],
                      "stage_ms": {a: round(b[0], 4) for a, b in prof.items()}}
         sim.close()
+    return out
+
+
+def run_sand(steps, flush):
+    """simulate_sand on the GPU (sand mode: integration, stable cell sort,
+    symmetric lists, 4 contact/friction substeps) on config 1's scene with the
+    64^3 block as sand over the heightmap's static particles.  Rate in
+    particle-substeps/s from CUDA-event step times (L2 flushed before each),
+    and the oracle's restatement of the reference's sand step timed on one
+    host core from the same state."""
+    import torch
+    from lustrine_gb300 import PbfSim, sand_params, scenes
+    sc = scenes.config1()
+    sim = PbfSim(sand_params(*sc.domain), sc.n, sc.ns)
+    sim.upload(sc.x, None, sc.solid)
+    sim.step(sc.dt, 5)
+    sim.synchronize()
+    ext = torch.cuda.ExternalStream(sim.stream())
+    ms = time_steps(sim, sc.dt, steps, flush, ext)
+    prof = profile_stages(sim, sc.dt, reps=2)
+    x, v, _, _ = sim.download()
+    out = {"value": sc.n * 4 / (np.median(ms) * 1e-3), "unit": "particle-substeps/s",
+           "ms_per_step": float(np.median(ms)), "status": sim.status(),
+           "launches_per_step": sim.launches_per_step(), "sand_particles": sc.n, "static_particles": sc.ns,
+           "stage_ms": {a: round(b[0], 4) for a, b in prof.items() if b[1]}}
+    sim.close()
+    rate, t = cpu_sand_rate(sc, x, v)
+    out["cpu_baseline"] = {"value": rate, "unit": "particle-substeps/s", "cores": 1, "kind": "port",
+                           "ms_per_step": t * 1e3,
+                           "sample": "median of 3 single steps of the full scene from the GPU's state"}
     return out
 
 

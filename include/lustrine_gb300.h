@@ -267,7 +267,7 @@ LUSTRINE_API int lustrine_pbf_download_positions_f64(lustrine_pbf* s, double* x)
 LUSTRINE_API int lustrine_pbf_neighbors(lustrine_pbf* s, int* count, int* idx, int cap);
 /* FP64 reductions on the device: [0] mass, [1..3] momentum, [4] kinetic
  * energy, [5..7] centre of mass, [8] max |rho / rho0 - 1| of the last lambda
- * pass.  Synchronises. */
+ * pass (0 in sand mode, which computes no density).  Synchronises. */
 LUSTRINE_API int lustrine_pbf_reduce(lustrine_pbf* s, double out[9]);
 /* Particles the last step binned in the grid cells of the box [min_pos,
  * max_pos] (Lustrine::query_cell_num_particles, Lustrine.cpp:864-914: corners

@@ -1171,7 +1171,9 @@ extern "C" int lustrine_pbf_neighbors(lustrine_pbf* s, int* count, int* idx, int
 extern "C" int lustrine_pbf_reduce(lustrine_pbf* s, double out[9]) {
     if (!s || !s->have_state || !out) return LUSTRINE_ERR_ARGS;
     const int c = s->cur;
-    launch_reduce(s->mixed(), s->sp, s->cp, s->x[c], s->v[c], s->steps_done ? s->rho : nullptr, s->red,
+    // densities exist after a fluid step (the sand step computes none)
+    const bool dens = s->steps_done && !s->sand_mode();
+    launch_reduce(s->mixed(), s->sp, s->cp, s->x[c], s->v[c], dens ? s->rho : nullptr, s->red,
                   s->stream);
     CK(cudaMemcpyAsync(out, s->red, 9 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
     CK(cudaStreamSynchronize(s->stream));

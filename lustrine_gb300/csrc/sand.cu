@@ -117,10 +117,10 @@ __global__ void k_sand_lists(StepParams p, const float4* __restrict__ xs, const 
     const int xlo = xx - 1 < 0 ? 0 : -1, xhi = xx + 1 >= p.gx ? 0 : 1;
     const int zlo = zz - 1 < 0 ? 0 : -1, zhi = zz + 1 >= p.gz ? 0 : 1;
     int c_n = 0;
-    // sand below i that found i
-    for (int y = ylo; y <= yhi; y++)
-        for (int x = xlo; x <= xhi; x++)
-            for (int z = zlo; z <= zhi; z++) {
+    // sand below i that found i: cells up to its own (later cells hold later slots)
+    for (int y = ylo; y <= 0; y++)
+        for (int x = (y < 0 ? xlo : max(xlo, -1)); x <= (y < 0 ? xhi : 0); x++)
+            for (int z = zlo; z <= ((y < 0 || x < 0) ? zhi : 0); z++) {
                 const int c = (yy + y) * slab + (xx + x) * p.gz + (zz + z);
                 const int e = min(fstart[c + 1], i);
                 for (int t = fstart[c]; t < e; t++) {
@@ -131,7 +131,7 @@ __global__ void k_sand_lists(StepParams p, const float4* __restrict__ xs, const 
                     }
                 }
             }
-    // its own walk: static particles, then sand above i
+    // its own walk: static particles, then sand above i (cells from its own on)
     for (int y = ylo; y <= yhi; y++)
         for (int x = xlo; x <= xhi; x++)
             for (int z = zlo; z <= zhi; z++) {
@@ -143,6 +143,7 @@ __global__ void k_sand_lists(StepParams p, const float4* __restrict__ xs, const 
                         c_n++;
                     }
                 }
+                if (c < id) continue;
                 for (int t = max(fstart[c], i + 1), e = fstart[c + 1]; t < e; t++) {
                     const float4 o = xs[t];
                     if (sdot(self.x - o.x, self.y - o.y, self.z - o.z) <= p.h2) {

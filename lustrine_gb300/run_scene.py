@@ -2,7 +2,10 @@
 statistics.
 
     python -m lustrine_gb300.run_scene --config config2 --steps 5 [--mixed] [--no-graph]
-        [--grid auto|dense|hashed] [--stages] [--shape block,unroll,list_block]
+        [--grid auto|dense|hashed] [--stages] [--shape block,unroll,list_block] [--sand]
+
+--sand steps the scene's particles with simulate_sand's semantics (sand mode)
+instead of the PBF step.
 
 Used for profiling captures of a single configuration (a fixed, short
 sequence of launches) and as a quick end-to-end check of an installation.
@@ -13,7 +16,7 @@ import argparse
 import json
 import time
 
-from . import PRECISION_FP32, PRECISION_MIXED, PbfSim, pbf_params, scenes
+from . import PRECISION_FP32, PRECISION_MIXED, PbfSim, pbf_params, sand_params, scenes
 
 
 def main(argv=None):
@@ -27,12 +30,16 @@ def main(argv=None):
     ap.add_argument("--stages", action="store_true", help="also print per-stage device ms")
     ap.add_argument("--shape", default=None,
                     help="launch shape block,unroll,list_block (default: the library's)")
+    ap.add_argument("--sand", action="store_true", help="the sand step (simulate_sand semantics)")
     a = ap.parse_args(argv)
     sc = getattr(scenes, a.config)()
-    p = pbf_params(*sc.domain, iterations=sc.iterations, c_xsph=sc.c_xsph,
-                   precision=PRECISION_MIXED if a.mixed else PRECISION_FP32,
-                   max_neighbors=a.max_neighbors, use_graph=not a.no_graph,
-                   grid_mode=["auto", "dense", "hashed"].index(a.grid))
+    if a.sand:
+        p = sand_params(*sc.domain, max_neighbors=max(a.max_neighbors, 96), use_graph=not a.no_graph)
+    else:
+        p = pbf_params(*sc.domain, iterations=sc.iterations, c_xsph=sc.c_xsph,
+                       precision=PRECISION_MIXED if a.mixed else PRECISION_FP32,
+                       max_neighbors=a.max_neighbors, use_graph=not a.no_graph,
+                       grid_mode=["auto", "dense", "hashed"].index(a.grid))
     with PbfSim(p, sc.n, sc.ns) as sim:
         sim.upload(sc.x, None, sc.solid if sc.ns else None)
         if a.shape:
@@ -42,7 +49,7 @@ def main(argv=None):
         sim.synchronize()
         wall = time.perf_counter() - t0
         r = sim.reduce()
-        out = {"config": sc.name, "n": sc.n, "ns": sc.ns, "steps": a.steps,
+        out = {"config": sc.name + ("_sand" if a.sand else ""), "n": sc.n, "ns": sc.ns, "steps": a.steps,
                "wall_ms_per_step": wall / max(a.steps, 1) * 1e3, "status": sim.status(),
                "kinetic": r["kinetic"], "com": r["com"], "max_density_error": r["max_density_error"]}
         if a.stages:  # mean of 10 profiled steps
