@@ -1,5 +1,5 @@
-// lustrine_gb300_sim.hpp -- the GB300 fluid step behind the reference's C++
-// step hook.
+// lustrine_gb300_sim.hpp -- the GB300 fluid and sand steps behind the
+// reference's C++ step hook.
 //
 // The reference steps a Simulation through a function pointer,
 // Simulation::simulate_fun (src/Simulation.hpp:22,137), called by
@@ -28,6 +28,15 @@
 // sources and sinks run on the host around the step) the context takes the
 // new count, growing its buffers by doubling.  Errors are reported by last_status(), the
 // step itself returning void like the reference's.
+//
+// lustrine_gb300::simulate_sand<Simulation> stands for Lustrine::simulate_sand
+// (src/Simulate.cpp:156-325), the step init_simulation_extra_parameters selects
+// (src/Lustrine.cpp:312).  Besides positions and velocities it uploads the
+// attract flags (Simulation::attracted) and reads the attract/blow flags, radii,
+// coefficients, particleDiameter and the player's position
+// (bullet_physics_simulation.player_position); it writes back positions,
+// positions_star, velocities and attracted in the order the step leaves them
+// (re-sorted by cell, as the reference's step re-orders its arrays).
 #pragma once
 
 #include <cstring>
@@ -43,6 +52,7 @@ namespace detail {
 struct Entry {
     lustrine_pbf* ctx = nullptr;
     int n = 0, ns = 0, cap = 0;
+    bool prev_attract = false;  // simulate_sand's previous attract flag (a re-created context forgets it)
 };
 inline std::unordered_map<const void*, Entry>& table() {
     static std::unordered_map<const void*, Entry> t;
@@ -77,6 +87,60 @@ lustrine_pbf_params params_of(const Simulation* sim) {
     p.mode = LUSTRINE_MODE_REFERENCE;
     return p;
 }
+
+// The device context of sim for mode p, holding the sand range's x and v
+// (created on the first call, re-created when the solids change or the sand
+// outgrows it, re-parameterised and re-counted otherwise).  Returns a status.
+template <class Simulation>
+int acquire(Simulation* sim, const lustrine_pbf_params& p, int n, int ns, float* x, float* v, Entry* out) {
+    Entry e;
+    {
+        std::lock_guard<std::mutex> lock(table_mutex());
+        e = table()[sim];
+    }
+    int rc = LUSTRINE_OK;
+    if (e.ctx && (e.ns != ns || n > e.cap)) {  // solids changed, or more sand than the buffers hold
+        std::lock_guard<std::mutex> lock(table_mutex());
+        lustrine_pbf_destroy(e.ctx);
+        e.ctx = nullptr;
+    }
+    if (!e.ctx) {
+        // sources add sand between steps (Lustrine.cpp:745-800): room for growth
+        const int cap = n > e.cap ? (e.cap ? (n > 2 * e.cap ? n : 2 * e.cap) : n) : e.cap;
+        rc = lustrine_pbf_create(&p, n, ns, &e.ctx);
+        if (!rc && cap > n) rc = lustrine_pbf_reserve(e.ctx, cap);
+        const float* solid = ns ? reinterpret_cast<const float*>(sim->positions) + 3 * (size_t)sim->ptr_solid_start
+                                : nullptr;
+        if (!rc) rc = lustrine_pbf_upload(e.ctx, x, v, solid);
+        if (rc) {
+            if (e.ctx) lustrine_pbf_destroy(e.ctx);
+            std::lock_guard<std::mutex> lock(table_mutex());
+            table().erase(sim);
+            return rc;
+        }
+        e.n = n;
+        e.ns = ns;
+        e.cap = cap > n ? cap : n;
+    } else {
+        // the game may change parameters between steps (ImGui sliders do,
+        // experiments/fluid/fluid.cpp:176-189); unchanged ones keep the
+        // captured step graphs
+        lustrine_pbf_params cur;
+        lustrine_pbf_get_params(e.ctx, &cur);
+        cur.use_graph = p.use_graph;
+        cur.max_neighbors = p.max_neighbors;
+        if (std::memcmp(&cur, &p, sizeof(p)) != 0) rc = lustrine_pbf_set_params(e.ctx, &p);
+        if (!rc && n != e.n) {  // sand added or removed by the host since the last step
+            rc = lustrine_pbf_set_count(e.ctx, n);
+            e.n = n;
+        }
+        if (!rc) rc = lustrine_pbf_upload_state_async(e.ctx, x, v);
+    }
+    std::lock_guard<std::mutex> lock(table_mutex());
+    table()[sim] = e;
+    *out = e;
+    return rc;
+}
 }  // namespace detail
 
 // Outcome of the last simulate_fluid call on this thread.
@@ -98,54 +162,10 @@ void simulate_fluid(Simulation* sim, float dt) {
     const int start = sim->ptr_sand_start, end = sim->ptr_sand_end;
     const int n = end > start ? end - start : 0;
     const int ns = sim->ptr_solid_end > sim->ptr_solid_start ? sim->ptr_solid_end - sim->ptr_solid_start : 0;
-    detail::Entry e;
-    {
-        std::lock_guard<std::mutex> lock(detail::table_mutex());
-        e = detail::table()[sim];
-    }
-    const lustrine_pbf_params p = detail::params_of(sim);
-    int rc = LUSTRINE_OK;
-    if (e.ctx && (e.ns != ns || n > e.cap)) {  // solids changed, or more sand than the buffers hold
-        release(sim);
-        e.ctx = nullptr;
-    }
     float* x = reinterpret_cast<float*>(sim->positions) + 3 * (size_t)start;
     float* v = reinterpret_cast<float*>(sim->velocities) + 3 * (size_t)start;
-    if (!e.ctx) {
-        // sources add sand between steps (Lustrine.cpp:745-800): room for growth
-        const int cap = n > e.cap ? (e.cap ? (n > 2 * e.cap ? n : 2 * e.cap) : n) : e.cap;
-        rc = lustrine_pbf_create(&p, n, ns, &e.ctx);
-        if (!rc && cap > n) rc = lustrine_pbf_reserve(e.ctx, cap);
-        const float* solid = ns ? reinterpret_cast<const float*>(sim->positions) + 3 * (size_t)sim->ptr_solid_start
-                                : nullptr;
-        if (!rc) rc = lustrine_pbf_upload(e.ctx, x, v, solid);
-        if (rc) {
-            if (e.ctx) lustrine_pbf_destroy(e.ctx);
-            detail::status() = rc;
-            return;
-        }
-        e.n = n;
-        e.ns = ns;
-        e.cap = cap > n ? cap : n;
-        std::lock_guard<std::mutex> lock(detail::table_mutex());
-        detail::table()[sim] = e;
-    } else {
-        // the game may change parameters between steps (ImGui sliders do,
-        // experiments/fluid/fluid.cpp:176-189); unchanged ones keep the
-        // captured step graphs
-        lustrine_pbf_params cur;
-        lustrine_pbf_get_params(e.ctx, &cur);
-        cur.use_graph = p.use_graph;
-        cur.max_neighbors = p.max_neighbors;
-        if (std::memcmp(&cur, &p, sizeof(p)) != 0) rc = lustrine_pbf_set_params(e.ctx, &p);
-        if (!rc && n != e.n) {  // sand added or removed by the host since the last step
-            rc = lustrine_pbf_set_count(e.ctx, n);
-            e.n = n;
-            std::lock_guard<std::mutex> lock(detail::table_mutex());
-            detail::table()[sim] = e;
-        }
-        if (!rc) rc = lustrine_pbf_upload_state_async(e.ctx, x, v);
-    }
+    detail::Entry e;
+    int rc = detail::acquire(sim, detail::params_of(sim), n, ns, x, v, &e);
     if (!rc) rc = lustrine_pbf_step(e.ctx, dt);
     std::vector<float> lam((size_t)n);
     if (!rc) rc = lustrine_pbf_download(e.ctx, x, v, n ? lam.data() : nullptr, nullptr);
@@ -155,6 +175,51 @@ void simulate_fluid(Simulation* sim, float dt) {
         std::memcpy(reinterpret_cast<float*>(sim->positions_star) + 3 * (size_t)start, x,
                     sizeof(float) * 3 * (size_t)n);
         for (int i = 0; i < n && (size_t)(start + i) < sim->lambdas.size(); i++) sim->lambdas[start + i] = lam[i];
+    }
+    detail::status() = rc;
+}
+
+template <class Simulation>
+void simulate_sand(Simulation* sim, float dt) {
+    const int start = sim->ptr_sand_start, end = sim->ptr_sand_end;
+    const int n = end > start ? end - start : 0;
+    const int ns = sim->ptr_solid_end > sim->ptr_solid_start ? sim->ptr_solid_end - sim->ptr_solid_start : 0;
+    float* x = reinterpret_cast<float*>(sim->positions) + 3 * (size_t)start;
+    float* v = reinterpret_cast<float*>(sim->velocities) + 3 * (size_t)start;
+    lustrine_pbf_params p = detail::params_of(sim);
+    p.mode = LUSTRINE_MODE_SAND;
+    p.max_neighbors = 96;
+    detail::Entry e;
+    int rc = detail::acquire(sim, p, n, ns, x, v, &e);
+    if (!rc) {  // Simulate.cpp:183-209 inputs
+        lustrine_sand_controls c;
+        lustrine_sand_controls_default(&c, sim->particleRadius);
+        const auto& pl = sim->bullet_physics_simulation.player_position;
+        c.player_position[0] = pl.x;
+        c.player_position[1] = pl.y;
+        c.player_position[2] = pl.z;
+        c.attract_flag = sim->attract_flag ? 1 : 0;
+        c.blow_flag = sim->blow_flag ? 1 : 0;
+        c.attract_radius = sim->attract_radius;
+        c.blow_radius = sim->blow_radius;
+        c.attract_coeff = sim->attract_coeff;
+        c.blow_coeff = sim->blow_coeff;
+        c.particle_diameter = sim->particleDiameter;
+        rc = lustrine_pbf_set_sand_controls(e.ctx, &c);
+    }
+    // Simulate.cpp:188-190: the flags drop when attraction stops
+    if (!rc && e.prev_attract && !sim->attract_flag)
+        for (int i = 0; i < n; i++) sim->attracted[start + i] = 0;
+    if (!rc && n) rc = lustrine_pbf_set_attracted(e.ctx, sim->attracted + start);
+    if (!rc) rc = lustrine_pbf_step(e.ctx, dt);
+    if (!rc) rc = lustrine_pbf_download(e.ctx, x, v, nullptr, nullptr);
+    if (!rc && n) rc = lustrine_pbf_get_attracted(e.ctx, sim->attracted + start);
+    if (!rc) {
+        sim->time_step = dt;  // Simulate.cpp:170
+        std::memcpy(reinterpret_cast<float*>(sim->positions_star) + 3 * (size_t)start, x,
+                    sizeof(float) * 3 * (size_t)n);
+        std::lock_guard<std::mutex> lock(detail::table_mutex());
+        detail::table()[sim].prev_attract = sim->attract_flag;
     }
     detail::status() = rc;
 }

@@ -4,6 +4,9 @@
 // change ptr_sand_end on the host), writing every step's input and output
 // state to a file:
 //   repeated: int n, int ns, float x_in[3n], v_in[3n], solid[3ns], x_out[3n], v_out[3n]
+// With a second argument "sand" it runs simulate_sand, the player attracting
+// in steps 1-2 and blowing in step 3, and each record adds the attract flags
+// before (int att_in[n]) and after (int att_out[n]) the step.
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -12,9 +15,13 @@
 struct vec3 {
     float x, y, z;
 };
+struct Bullet {
+    vec3 player_position{0, 0, 0};
+};
 struct Sim {
     void (*simulate_fun)(Sim*, float) = nullptr;
-    float particleRadius = 0.5f, kernelRadius = 1.0f, kernelFactor = 0.5f, cell_size = 1.0f;
+    float particleRadius = 0.5f, particleDiameter = 1.0f, kernelRadius = 1.0f, kernelFactor = 0.5f,
+          cell_size = 1.0f;
     float domainX = 24, domainY = 24, domainZ = 24;
     float rest_density = 24, mass = 5;
     vec3 gravity{0, -10, 0};
@@ -24,6 +31,10 @@ struct Sim {
     vec3* positions = nullptr;
     vec3* positions_star = nullptr;
     int ptr_sand_start = 0, ptr_sand_end = 0, ptr_solid_start = 0, ptr_solid_end = 0;
+    Bullet bullet_physics_simulation;
+    bool attract_flag = false, blow_flag = false;
+    int* attracted = nullptr;
+    float attract_radius = 1.5f, blow_radius = 2.0f, attract_coeff = 1000.0f, blow_coeff = 500.0f;
 };
 
 #include "lustrine_gb300_sim.hpp"
@@ -46,9 +57,13 @@ static void add_block(Sim& s, int X, int Y, int Z, float ox, float oy, float oz)
 
 int main(int argc, char** argv) {
     if (argc < 2) return 2;
+    const bool sand = argc > 2 && std::strcmp(argv[2], "sand") == 0;
     const int total = 4096, ns = 24 * 24;
     std::vector<vec3> pos(total), pstar(total), vel(total);
+    std::vector<int> att(total, 0);
     Sim s;
+    s.attracted = att.data();
+    s.bullet_physics_simulation.player_position = vec3{10.0f, 8.0f, 10.0f};
     s.positions = pos.data();
     s.positions_star = pstar.data();
     s.velocities = vel.data();
@@ -58,7 +73,7 @@ int main(int argc, char** argv) {
     for (int x = 0; x < 24; x++)
         for (int z = 0; z < 24; z++) pos[(size_t)(total - ns + x * 24 + z)] = vec3{x + 0.5f, 0.5f, z + 0.5f};
     add_block(s, 8, 8, 8, 6, 4, 6);
-    s.simulate_fun = lustrine_gb300::simulate_fluid<Sim>;
+    s.simulate_fun = sand ? lustrine_gb300::simulate_sand<Sim> : lustrine_gb300::simulate_fluid<Sim>;
     FILE* f = std::fopen(argv[1], "wb");
     if (!f) return 2;
     // step; step; +10 (grows past 512); step; -30 (set_count); step; +600 (grows again); step
@@ -72,6 +87,9 @@ int main(int argc, char** argv) {
         std::fwrite(pos.data(), sizeof(vec3), (size_t)n, f);
         std::fwrite(vel.data(), sizeof(vec3), (size_t)n, f);
         std::fwrite(pos.data() + (total - ns), sizeof(vec3), (size_t)ns, f);
+        s.attract_flag = k == 1 || k == 2;
+        s.blow_flag = k == 3;
+        if (sand) std::fwrite(att.data(), sizeof(int), (size_t)n, f);
         s.simulate_fun(&s, 1.0f / 60.0f);
         if (lustrine_gb300::last_status() != LUSTRINE_OK) {
             std::fprintf(stderr, "step %d: status %d\n", k, lustrine_gb300::last_status());
@@ -79,6 +97,7 @@ int main(int argc, char** argv) {
         }
         std::fwrite(pos.data(), sizeof(vec3), (size_t)n, f);
         std::fwrite(vel.data(), sizeof(vec3), (size_t)n, f);
+        if (sand) std::fwrite(att.data(), sizeof(int), (size_t)n, f);
     }
     std::fclose(f);
     lustrine_gb300::release(&s);
