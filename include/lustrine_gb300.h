@@ -173,7 +173,23 @@ LUSTRINE_API int lustrine_last_status(void);
 /* The context behind the layer-1 simulation (NULL before init_simulation). */
 struct lustrine_pbf;
 LUSTRINE_API struct lustrine_pbf* lustrine_global_context(void);
-/* Frees what init_grid_box allocated in grid. */
+/* LustrineWrapper.cpp:146-151 with VoxelLoader.cpp:48-99: the first model of
+ * the MagicaVoxel file at path (the first one with a voxel) as a SOLID grid at
+ * position, in the grid order x -> y -> z: cells hold the voxels' colour
+ * indices (0: empty), colors the palette colours / 255 (float division),
+ * has_one_color_per_cell set, color zero (the reference leaves it unset).
+ * A file without an RGBA palette chunk or with an index map (IMAP) gives the
+ * grid with zero colours and LUSTRINE_ERR_UNSUPPORTED; a missing file or one
+ * with no voxel, LUSTRINE_ERR_ARGS and the grid untouched. */
+LUSTRINE_API void init_grid_magikavoxel(GridWrapper* grid, const char* path, Vec3 position);
+/* LustrineWrapper.cpp:537-624: the same model with cells 1 for occupied
+ * voxels, colors the palette colours / 255 divided in double, the given type;
+ * position and color are left as the caller set them.  path holds pathlen wide
+ * characters, each narrowed to one byte as the reference does.  (The
+ * reference allocates the cells with sizeof(bool) per cell and overruns them;
+ * here they are int arrays of num_grid_cells.) */
+LUSTRINE_API void create_grid(GridWrapper* grid, const wchar_t* path, int type, int pathlen);
+/* Frees what init_grid_box, init_grid_magikavoxel and create_grid allocated in grid. */
 LUSTRINE_API void lustrine_free_grid(GridWrapper* grid);
 
 /* --------------------------------------------------- layer 2: context API */

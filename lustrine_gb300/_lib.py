@@ -121,6 +121,8 @@ SIGNATURES = {
     "lustrine_last_status": (C.c_int, []),
     "lustrine_global_context": (_P, []),
     "lustrine_free_grid": (None, [C.POINTER(GridWrapper)]),
+    "init_grid_magikavoxel": (None, [C.POINTER(GridWrapper), C.c_char_p, Vec3]),
+    "create_grid": (None, [C.POINTER(GridWrapper), C.c_wchar_p, C.c_int, C.c_int]),
     # layer 2: context API
     "lustrine_pbf_params_reference": (None, [C.POINTER(PbfParams), C.c_int, C.c_int, C.c_int,
                                              C.c_float, C.c_float]),

@@ -35,6 +35,7 @@ UNITS = {
     # host float math of scene construction and sources as the reference's
     # (no FMA contraction, which GCC applies by default on aarch64)
     "lustrine_wrapper.cpp": ["-Xcompiler", "-ffp-contract=off"],
+    "vox.cpp": [],
 }
 
 

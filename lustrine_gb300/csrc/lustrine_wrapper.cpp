@@ -13,9 +13,11 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <string>
 #include <vector>
 
 #include "lustrine_gb300.h"
+#include "vox.h"
 
 namespace {
 
@@ -397,6 +399,78 @@ void init_grid_box(const SimulationParameters* parameters, GridWrapper* grid, in
     grid->num_occupied_grid_cells = cells;
     grid->type = type;
     g_status = LUSTRINE_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// The model as a grid in the reference's grid order (x -> y -> z,
+// VoxelLoader.cpp:69-97): occupied cells hold the colour index (index_cells)
+// or 1, colours are the palette colour / 255 in float (float_colors, glm's
+// vec4 /= 255.0) or in double (LustrineWrapper.cpp:608-611).
+void vox_to_grid(const lgb::VoxModel& m, bool index_cells, bool float_colors, GridWrapper* grid) {
+    const int X = m.sx, Y = m.sy, Z = m.sz;
+    const int cells = X * Y * Z;
+    grid->cells = new int[cells > 0 ? cells : 1]();
+    grid->colors = new Color[cells > 0 ? cells : 1]();
+    grid->has_one_color_per_cell = true;
+    grid->X = X;
+    grid->Y = Y;
+    grid->Z = Z;
+    grid->num_grid_cells = cells;
+    int occupied = 0;
+    for (int x = 0; x < X; x++)
+        for (int y = 0; y < Y; y++)
+            for (int z = 0; z < Z; z++) {
+                const int c = m.voxels[(size_t)x + (size_t)y * X + (size_t)z * X * Y];
+                if (c == 0) continue;
+                const int g = (x * Y * Z) + (y * Z) + z;
+                const uint8_t* rgba = m.rgba[(c + 255) & 255];  // colour index c names entry c - 1
+                grid->cells[g] = index_cells ? c : 1;
+                float col[4];
+                for (int a = 0; a < 4; a++)
+                    col[a] = float_colors ? (float)rgba[a] / 255.0f : (float)((double)rgba[a] / 255.0);
+                grid->colors[g] = Color{col[0], col[1], col[2], col[3]};
+                occupied++;
+            }
+    grid->num_occupied_grid_cells = occupied;
+}
+
+}  // namespace
+
+extern "C" {
+
+void init_grid_magikavoxel(GridWrapper* grid, const char* path, Vec3 position) {
+    lgb::VoxModel m;
+    const int rc = grid && path ? lgb::vox_read_file(path, &m) : LUSTRINE_ERR_ARGS;
+    if (!grid || m.voxels.empty()) {
+        g_status = rc ? rc : LUSTRINE_ERR_ARGS;
+        return;
+    }
+    vox_to_grid(m, true, true, grid);
+    grid->type = 0;  // MaterialType SOLID (Simulation.hpp:28-31)
+    grid->position = position;
+    grid->color = Color{0.0f, 0.0f, 0.0f, 0.0f};
+    g_status = rc;
+}
+
+void create_grid(GridWrapper* grid, const wchar_t* path, int type, int pathlen) {
+    if (!grid || !path || pathlen < 0) {
+        g_status = LUSTRINE_ERR_ARGS;
+        return;
+    }
+    std::string narrow((size_t)pathlen, '\0');
+    for (int i = 0; i < pathlen; i++) narrow[(size_t)i] = (char)path[i];  // LustrineWrapper.cpp:540-545
+    lgb::VoxModel m;
+    const int rc = lgb::vox_read_file(narrow.c_str(), &m);
+    if (m.voxels.empty()) {
+        g_status = rc ? rc : LUSTRINE_ERR_ARGS;
+        return;
+    }
+    vox_to_grid(m, false, false, grid);
+    grid->type = type;
+    g_status = rc;
 }
 
 void lustrine_free_grid(GridWrapper* grid) {

@@ -7,6 +7,7 @@ reference, each one's outcome is available from last_status().
 from __future__ import annotations
 
 import ctypes as C
+import os
 
 import numpy as np
 
@@ -19,6 +20,7 @@ __all__ = ["SimulationParameters", "SimulationData", "GridWrapper", "Vec3", "Col
            "init_grid_box", "init_simulation", "init_simulation_extra_parameters", "simulate",
            "simulate_no_flags", "simulation_bind_positions_copy", "cleanup_simulation",
            "get_num_sand_particles", "get_grid_cell_size", "set_simulate_function", "set_player_position",
+           "init_grid_magikavoxel", "create_grid", "grid_arrays",
            "last_status", "free_grid"]
 
 
@@ -48,6 +50,34 @@ def grid_from_cells(cells: np.ndarray, position, type_=0, color=(1, 1, 1, 1)):
     g.num_occupied_grid_cells = int((cells != 0).sum())
     g.type = type_
     return g, cells
+
+
+def init_grid_magikavoxel(path: str, position=(0.0, 0.0, 0.0)) -> GridWrapper:
+    """The first model of a MagicaVoxel file as a SOLID grid (cells hold
+    colour indices).  Free with free_grid."""
+    g = GridWrapper()
+    _lib_().init_grid_magikavoxel(C.byref(g), os.fsencode(path), Vec3(*[float(a) for a in position]))
+    return g
+
+
+def create_grid(path: str, type_=0) -> GridWrapper:
+    """The same model through the wrapper's create_grid (cells 1, colours in
+    double).  Free with free_grid."""
+    g = GridWrapper()
+    _lib_().create_grid(C.byref(g), str(path), int(type_), len(str(path)))
+    return g
+
+
+def grid_arrays(g: GridWrapper):
+    """(cells[X, Y, Z] int32, colors[X, Y, Z, 4] float32) copies of a grid."""
+    n = g.X * g.Y * g.Z
+    cells = np.ctypeslib.as_array(g.cells, shape=(n,)).copy().reshape(g.X, g.Y, g.Z) if n else np.zeros((0,))
+    if g.colors and n:
+        colors = np.ctypeslib.as_array(C.cast(g.colors, C.POINTER(C.c_float)), shape=(4 * n,)).copy()
+        colors = colors.reshape(g.X, g.Y, g.Z, 4)
+    else:
+        colors = None
+    return cells, colors
 
 
 def free_grid(g: GridWrapper):

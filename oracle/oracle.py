@@ -278,6 +278,8 @@ class Reference:
         L.ref_set_attracted.argtypes = [_I]
         L.ref_get_float.argtypes = [C.c_int]
         L.ref_get_float.restype = C.c_float
+        L.ref_load_vox.argtypes = [C.c_char_p, _I, _I, _F, C.c_int]
+        L.ref_load_vox.restype = C.c_int
         self.L = L
 
     def init(self, X, Y, Z, block, block_pos, radius=0.5, scale=2.0, solids=()):
@@ -356,3 +358,15 @@ class Reference:
 
     def diameter(self):
         return float(self.L.ref_get_float(0))
+
+    def load_vox(self, path, cap=1 << 24):
+        """init_grid_from_magika_voxel: (cells[X, Y, Z], colors[X, Y, Z, 4], occupied)."""
+        dims = np.zeros(3, np.int32)
+        cells = np.zeros(cap, np.int32)
+        colors = np.zeros(4 * cap, np.float32)
+        occ = self.L.ref_load_vox(os.fsencode(str(path)), dims, cells, colors, cap)
+        if occ < 0:
+            raise RuntimeError("voxel grid larger than cap")
+        X, Y, Z = (int(a) for a in dims)
+        n = X * Y * Z
+        return cells[:n].reshape(X, Y, Z), colors[:4 * n].reshape(X, Y, Z, 4), occ

@@ -170,6 +170,24 @@ void ref_set_attracted(const int* in)
     for (int i = 0; i < g_sim->ptr_sand_end; i++) g_sim->attracted[i] = in[i];
 }
 
+// Lustrine::init_grid_from_magika_voxel (VoxelLoader.cpp:48-99): dims[3]
+// (X, Y, Z), cells[X*Y*Z], colors[4*X*Y*Z] in the grid's x -> y -> z order.
+// Returns the occupied cell count, or -1 when the grid exceeds cap cells.
+int ref_load_vox(const char* path, int* dims, int* cells, float* colors, int cap)
+{
+    Grid g;
+    init_grid_from_magika_voxel(&g, path, glm::vec3(0.0f), SOLID);
+    dims[0] = g.X;
+    dims[1] = g.Y;
+    dims[2] = g.Z;
+    if (g.num_grid_cells > cap) return -1;
+    for (int i = 0; i < g.num_grid_cells; i++) {
+        cells[i] = g.cells[(size_t)i];
+        for (int a = 0; a < 4; a++) colors[4 * i + a] = g.colors[(size_t)i][a];
+    }
+    return g.num_occupied_grid_cells;
+}
+
 // which: 0 particleDiameter, 1 mass
 float ref_get_float(int which) { return which == 0 ? g_sim->particleDiameter : g_sim->mass; }
 

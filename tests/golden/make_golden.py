@@ -26,12 +26,19 @@ Fixtures (all from the reference binary, never from the restatement):
                       attracted flags and the neighbour lists (CSR, the
                       reference's push order, itself included twice), as
                       x1..x5, v1..v5, att1..att5, nbr_off1.., nbr1..
+  vox/*.vox, vox_ref.npz  small MagicaVoxel files written here from the
+                      published chunk format (SIZE, XYZI, RGBA, PACK; an empty
+                      first model; a voxel listed twice; colour index 255),
+                      and what the reference's loader init_grid_from_magika_voxel
+                      (VoxelLoader.cpp:48-99) makes of each: cells, colours,
+                      occupied count; with the palettes written.
 """
 from __future__ import annotations
 
 import argparse
 import ctypes
 import os
+import struct
 import sys
 
 import numpy as np
@@ -157,6 +164,50 @@ def make_sand(R):
     return n
 
 
+def _vox_chunk(cid, content=b"", children=b""):
+    return cid + struct.pack("<II", len(content), len(children)) + content + children
+
+
+def write_vox(path, models, rgba, version=150, extra=b""):
+    """A MagicaVoxel file: models = [((X, Y, Z), [(x, y, z, colour), ...]), ...]."""
+    kids = extra
+    for size, vox in models:
+        kids += _vox_chunk(b"SIZE", struct.pack("<III", *size))
+        kids += _vox_chunk(b"XYZI", struct.pack("<I", len(vox)) + b"".join(bytes(v) for v in vox))
+    kids += _vox_chunk(b"RGBA", np.ascontiguousarray(rgba, np.uint8).tobytes())
+    with open(path, "wb") as f:
+        f.write(b"VOX " + struct.pack("<I", version) + _vox_chunk(b"MAIN", b"", kids))
+
+
+def make_vox(R):
+    rng = np.random.default_rng(11)
+    d = os.path.join(HERE, "vox")
+    os.makedirs(d, exist_ok=True)
+    files = {}
+    # a 5 x 4 x 6 model, ~40 % occupied, colours 1..255
+    pal = rng.integers(0, 256, size=(256, 4), dtype=np.uint8)
+    vox = [(x, y, z, int(rng.integers(1, 256))) for x in range(5) for y in range(4) for z in range(6)
+           if rng.random() < 0.4]
+    files["box.vox"] = (pal, [((5, 4, 6), vox)], 150, b"")
+    # an empty first model (skipped), a PACK chunk, version 200
+    pal2 = rng.integers(0, 256, size=(256, 4), dtype=np.uint8)
+    vox2 = [(x, y, z, 1 + (x + 2 * y + 3 * z) % 7) for x in range(4) for y in range(2) for z in range(3)
+            if (x + y + z) % 2 == 0]
+    files["empty_first.vox"] = (pal2, [((3, 3, 3), []), ((4, 2, 3), vox2)], 200,
+                                _vox_chunk(b"PACK", struct.pack("<I", 2)))
+    # a voxel listed twice (the later colour stays), colour index 255, a second model ignored
+    vox3 = [(0, 0, 0, 3), (1, 2, 1, 255), (0, 0, 0, 9), (2, 0, 1, 1)]
+    files["dup.vox"] = (pal, [((3, 3, 2), vox3), ((2, 2, 2), [(1, 1, 1, 5)])], 150, b"")
+    out = {}
+    for name, (p, models, version, extra) in files.items():
+        path = os.path.join(d, name)
+        write_vox(path, models, p, version, extra)
+        cells, colors, occ = R.load_vox(path)
+        key = name[:-4]
+        out.update({f"{key}_cells": cells, f"{key}_colors": colors, f"{key}_occupied": occ, f"{key}_rgba": p})
+    np.savez_compressed(os.path.join(HERE, "vox_ref.npz"), **out)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
@@ -169,6 +220,7 @@ def main():
     make_c0(R)
     make_solids(R)
     make_sand(R)
+    make_vox(R)
     R.L.ref_free()
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):

@@ -246,3 +246,37 @@ def test_sand_sources_and_sinks_match_oracle(orc):
     assert sim.n < n0 + 3 * len(pat)  # the sink removed particles
     assert sim.status() == 0
     sim.close()
+
+
+def test_wrapper_sand_on_a_vox_floor(orc):
+    """A MagicaVoxel model (tests/golden/vox/box.vox) as the static grid of a
+    wrapper simulation: its occupied cells become the static particles
+    (init_chunk_from_grid order, stored from the end backwards) and the sand
+    step over them equals the oracle's."""
+    import os
+    from conftest import GOLDEN
+    from lustrine_gb300 import wrapper as W
+    from lustrine_gb300._lib import SimulationParameters
+    prm = SimulationParameters(20, 20, 20, 0.5, 1.0)
+    floor = W.init_grid_magikavoxel(os.path.join(GOLDEN, "vox", "box.vox"), (6.0, 0.0, 6.0))
+    sand = W.init_grid_box(prm, 4, 4, 4, (6.0, 4.0, 6.0), type_=1)
+    try:
+        cells, _ = W.grid_arrays(floor)
+        W.init_simulation_extra_parameters(prm, [sand], [floor], 1, 2.0)
+        assert W.last_status() == 0
+        solid = np.array([(x + 6.5, y + 0.5, z + 6.5) for x in range(cells.shape[0]) for y in range(cells.shape[1])
+                          for z in range(cells.shape[2]) if cells[x, y, z] != 0], np.float32)[::-1]
+        x = W.simulation_bind_positions_copy()
+        v, att = np.zeros_like(x), np.zeros(len(x), np.int32)
+        p = orc.reference_params(20, 20, 20, 0.5, 2.0)
+        for _ in range(6):
+            W.simulate(1 / 60, False, False)
+            assert W.last_status() == 0
+            o = orc.sand_step(p, orc.sand_controls(diameter=1.0), np.float32(1 / 60), x, v, att, solid=solid, cap=96)
+            x, v, att = o["x"], o["v"], o["attracted"]
+            assert np.array_equal(W.simulation_bind_positions_copy(), x)
+        assert (o["nbr_idx"] >= len(x)).any(), "the sand must reach the voxel floor"
+    finally:
+        W.cleanup_simulation()
+        W.free_grid(floor)
+        W.free_grid(sand)
