@@ -266,12 +266,15 @@ static int ctx_alloc(lustrine_pbf* s) {
         rc = rc ? rc : dalloc(&s->solid_near, (size_t)C);
         s->sp.solid_near = s->solid_near;
     }
-    if (s->sp.hash_bits) {  // hashed grid: packed cells, unsorted and sorted
+    // packed cells, unsorted and sorted: the hashed grid tells cells sharing a
+    // bucket apart by them; mixed precision reads a slot's cell from them
+    // (shifts and masks, where the dense key would need two integer divisions)
+    if (s->sp.hash_bits || s->prm.precision == LUSTRINE_PRECISION_MIXED) {
         rc = rc ? rc : dalloc(&s->cellk, m);
         rc = rc ? rc : dalloc(&s->cell_sorted, n);
-        rc = rc ? rc : dalloc(&s->solid_cell, ns);
         s->sp.cell_sorted = s->cell_sorted;
     }
+    if (s->sp.hash_bits) rc = rc ? rc : dalloc(&s->solid_cell, ns);
     if (rc) return rc;
     if (n) {
         std::vector<int> ids((size_t)n);
@@ -744,7 +747,7 @@ static int enqueue_step(lustrine_pbf* s, cudaStream_t st, StageMarks* mk = nullp
     // velocities are not carried: the last position pass recomputes them
     // (v = (x* - x) / dt) before anything reads them
     launch_sort_state(s->key, s->rank, s->start, tie, n, s->tmp, s->x[c], xs_in, nullptr, s->id[c],
-                      s->key_sorted, s->x[o], s->xs[o], s->v[o], s->id[o], p.hash_bits ? s->cellk : nullptr,
+                      s->key_sorted, s->x[o], s->xs[o], s->v[o], s->id[o], s->cell_sorted ? s->cellk : nullptr,
                       s->cell_sorted, st);
     k += 2;
     if (mk) mk->mark(LUSTRINE_STAGE_SORT, st);

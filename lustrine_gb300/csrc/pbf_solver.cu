@@ -234,11 +234,15 @@ __device__ __forceinline__ unsigned pack_bits(const CellPack& cp, int3 c) {
     return (unsigned)c.x | ((unsigned)c.y << cp.by_shift) | ((unsigned)c.z << cp.bz_shift);
 }
 
-// Sort key of a cell: its dense id, or its hash bucket (the packed cell then
-// goes to cellk so the neighbour walk can tell cells sharing a bucket apart).
+// Sort key of a cell: its dense id, or its hash bucket.  The packed cell goes
+// to cellk (when given): the hashed walk tells cells sharing a bucket apart by
+// it, and mixed precision reads a slot's cell from it.
 __device__ __forceinline__ int cell_key(const StepParams& p, const CellPack& cp, const Geo& g, int3 c,
                                         int* cellk, int i) {
-    if (!p.hash_bits) return linear_cell(g, c);
+    if (!p.hash_bits) {
+        if (cellk) cellk[i] = (int)pack_bits(cp, c);
+        return linear_cell(g, c);
+    }
     // a static particle outside the box joins the last packable cell
     c = make_int3(min(c.x, (int)cp.mx), min(c.y, (int)cp.my), min(c.z, (int)cp.mz));
     cellk[i] = (int)pack_bits(cp, c);
@@ -442,12 +446,12 @@ __device__ __forceinline__ void walk_hashed_cell(const StepParams& p, const floa
     }
 }
 
-// Cell of fluid slot s in the current step: from its packed cell on a
-// hashed grid, from its dense key otherwise.
+// Cell of fluid slot s in the current step: from its packed cell where the
+// sort carried one (hashed grid, mixed precision), else from its dense key.
 __device__ __forceinline__ int3 slot_cell(const StepParams& p, const CellPack& cp, const Geo& g,
                                           const int* __restrict__ key_sorted,
                                           const int* __restrict__ cell_sorted, int s) {
-    if (p.hash_bits) {
+    if (cell_sorted) {
         const unsigned u = (unsigned)__ldg(&cell_sorted[s]);
         return make_int3((int)(u & cp.mx), (int)((u >> cp.by_shift) & cp.my), (int)((u >> cp.bz_shift) & cp.mz));
     }
