@@ -243,7 +243,7 @@ static int ctx_alloc(lustrine_pbf* s) {
     rc = rc ? rc : dalloc(&s->count, C);
     rc = rc ? rc : dalloc(&s->start, (size_t)C + 1);
     rc = rc ? rc : dalloc(&s->block_sums, scan_block_sums_size(C));
-    rc = rc ? rc : dalloc(&s->tile_sum, cell_scan_tiles(C));
+    rc = rc ? rc : dalloc(&s->tile_sum, 2 * (size_t)cell_scan_tiles(C));
     rc = rc ? rc : dalloc(&s->solid, ns);
     rc = rc ? rc : dalloc(&s->solid_raw, ns);
     rc = rc ? rc : dalloc(&s->sstart, (size_t)C + 1);
@@ -506,6 +506,20 @@ void lustrine_pbf::invalidate_graphs() {
         graph_exec[k] = nullptr;
     }
     pred_ready = false;  // whatever invalidates the step may change the prediction too
+    tiles_dirty = true;
+}
+
+// The tile totals a step of parity c scans (the other half is zeroed by that
+// scan for the prediction of the following step).
+static int* tiles_of(lustrine_pbf* s, int parity) {
+    return s->tile_sum + (size_t)parity * cell_scan_tiles(s->sp.num_cells);
+}
+
+// Zero both halves of the tile totals (after a prediction was dropped).
+static int clear_tiles(lustrine_pbf* s) {
+    CK(cudaMemsetAsync(s->tile_sum, 0, 2 * (size_t)cell_scan_tiles(s->sp.num_cells) * sizeof(int), s->stream));
+    s->tiles_dirty = false;
+    return LUSTRINE_OK;
 }
 
 bool lustrine_pbf::mixed() const { return prm.precision == LUSTRINE_PRECISION_MIXED; }
@@ -681,7 +695,7 @@ static int enqueue_sand_step(lustrine_pbf* s, cudaStream_t st, StageMarks* mk) {
     launch_sand_predict(p, q, s->x[c], s->v[c], s->xs[c], s->att[c], s->key, s->rank, s->count, s->status, st);
     k += 1;
     if (mk) mk->mark(LUSTRINE_STAGE_PREDICT, st);
-    launch_scan_tiles(s->count, C, s->tile_sum, s->start, st);
+    launch_scan_tiles(s->count, C, tiles_of(s, c), s->start, st, false, tiles_of(s, o));
     k += scan_tiles_launches(C);
     if (mk) mk->mark(LUSTRINE_STAGE_SCAN, st);
     // stable by the particle's index (its slot after a sand step; a caller
@@ -734,12 +748,15 @@ static int enqueue_step(lustrine_pbf* s, cudaStream_t st, StageMarks* mk = nullp
         launch_predict_ref(p, s->x[c], s->v[c], s->xs[c], s->key, s->rank, s->count, s->status, st);
         k += 1;
     } else if (predict) {
-        launch_predict(mixed, p, s->cp, s->x[c], s->v[c], xs_in, s->key, s->rank, s->count, s->cellk, st);
+        launch_predict(mixed, p, s->cp, s->x[c], s->v[c], xs_in, s->key, s->rank, s->count, s->cellk,
+                       tiles_of(s, c), st);
         k += 1;
     }
     if (mk) mk->mark(LUSTRINE_STAGE_PREDICT, st);
-    launch_scan_tiles(s->count, C, s->tile_sum, s->start, st);
-    k += scan_tiles_launches(C);
+    // PBF: the prediction (this step's or the previous commit kernel's)
+    // counted the tile totals; the scan zeroes the other half for the next
+    launch_scan_tiles(s->count, C, tiles_of(s, c), s->start, st, !ref, tiles_of(s, o));
+    k += scan_tiles_launches(C, !ref);
     if (mk) mk->mark(LUSTRINE_STAGE_SCAN, st);
     // stable within a cell: by the caller's id in reference mode (the
     // reference's list order), by the previous slot otherwise
@@ -786,7 +803,8 @@ static int enqueue_step(lustrine_pbf* s, cudaStream_t st, StageMarks* mk = nullp
             k += 2;
         }
         launch_xsph(mixed, tu, p, s->cp, a, s->vtmp, s->nbr, s->cnt, s->key_sorted, s->x[o], s->v[o],
-                    tail ? s->xs_pred : nullptr, s->key, s->rank, s->count, s->cellk, st);
+                    tail ? s->xs_pred : nullptr, s->key, s->rank, s->count, s->cellk,
+                    tail ? tiles_of(s, o) : nullptr, st);
         k += 1;
         if (mk) mk->mark(LUSTRINE_STAGE_XSPH, st);
     }
@@ -835,6 +853,10 @@ static int step_impl(lustrine_pbf* s, float dt, bool tail_allowed) {
     const bool tail = pbf && tail_allowed;
     if (predict && s->count_dirty)  // a histogram of a prediction that will not be used
         CK(cudaMemsetAsync(s->count, 0, (size_t)s->sp.num_cells * sizeof(int), s->stream));
+    if (predict && (s->count_dirty || s->tiles_dirty)) {  // and its tile totals
+        int rc = clear_tiles(s);
+        if (rc) return rc;
+    }
     s->count_dirty = false;
     const int gi = c + (predict ? 2 : 0) + (tail ? 4 : 0);
     if (s->prm.use_graph) {
@@ -889,6 +911,8 @@ extern "C" int lustrine_pbf_profile_step(lustrine_pbf* s, float dt, double* stag
     if (s->count_dirty) CK(cudaMemsetAsync(s->count, 0, (size_t)s->sp.num_cells * sizeof(int), s->stream));
     s->count_dirty = false;
     s->pred_ready = false;
+    int trc = clear_tiles(s);
+    if (trc) return trc;
     StageMarks mk;
     for (int e = 0; e < 64; e++) CK(cudaEventCreate(&mk.ev[e]));
     s->launches = enqueue_step(s, s->stream, &mk);
@@ -1288,7 +1312,7 @@ extern "C" int lustrine_pbf_launches_per_step(const lustrine_pbf* s) {
     const int scan = scan_tiles_launches(s->sp.num_cells);
     if (s->prm.mode == LUSTRINE_MODE_REFERENCE) return 1 + scan + 2 + 3;
     if (s->prm.mode == LUSTRINE_MODE_SAND) return 1 + scan + 2 + 1 + 4;
-    return 1 + scan + 2 + 2 * s->prm.iterations + 1;
+    return 1 + scan_tiles_launches(s->sp.num_cells, true) + 2 + 2 * s->prm.iterations + 1;
 }
 
 extern "C" const char* lustrine_error_string(int code) {

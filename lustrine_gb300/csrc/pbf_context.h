@@ -48,7 +48,7 @@ struct lustrine_pbf {
     int* count = nullptr;
     int* start = nullptr;
     int* block_sums = nullptr;
-    int* tile_sum = nullptr;  // per-tile totals of the step's scan
+    int* tile_sum = nullptr;  // per-tile totals of the step's scan, two halves (step parity)
 
     // static solids, sorted by cell
     float4* solid = nullptr;
@@ -98,6 +98,7 @@ struct lustrine_pbf {
     bool pred_ready = false;
     float pred_dt = 0.0f;
     bool count_dirty = false;  // count[] holds that prediction's histogram
+    bool tiles_dirty = true;   // tile totals may hold counts of a dropped prediction
     int launches = 0;             // kernels the last step launched
     int graph_launches[8] = {};   // kernels in each captured step
     long long steps_done = 0;

@@ -13,10 +13,14 @@ void launch_scan(int* count, int C, int* block_sums, int* start, cudaStream_t st
 int scan_block_sums_size(int C);
 // scan of the step: tile totals, then tiles scanned independently (the
 // totals scanned by one block in between past CELL_SCAN_MAX_TILES tiles);
-// tile_sum: cell_scan_tiles(C) ints; scan_tiles_launches: kernels it issues
+// tile_sum: cell_scan_tiles(C) ints.  counted: the prediction already
+// counted the tile totals into tile_sum (no totals pass); tile_zero (may be
+// null): the other totals buffer, zeroed for the next prediction.
+// scan_tiles_launches: kernels it issues.
 int cell_scan_tiles(int C);
-void launch_scan_tiles(int* count, int C, int* tile_sum, int* start, cudaStream_t st);
-int scan_tiles_launches(int C);
+void launch_scan_tiles(int* count, int C, int* tile_sum, int* start, cudaStream_t st, bool counted = false,
+                       int* tile_zero = nullptr);
+int scan_tiles_launches(int C, bool counted = false);
 void launch_sort_tail(const int* key, const int* rank, const int* start, const int* tie, int n,
                       int* tmp, int* perm, cudaStream_t st);
 void launch_gather_state(const int* perm, int n, const int* key, const float4* x, const float4* xs,
@@ -78,8 +82,10 @@ void launch_sand_substep(const StepParams& p, const SandParams& q, const float4*
 
 // pbf_solver.cu (PBF; mixed = cell index + offset representation)
 // cellk: packed cell of every particle on a hashed grid (nullptr when dense)
+// tile_count (may be null): per-tile totals of the step's cell scan, counted
+// as the histogram is (one atomic per tile a warp touches)
 void launch_predict(bool mixed, const StepParams& p, const CellPack& cp, const float4* x, const float4* v,
-                    float4* xs, int* key, int* rank, int* count, int* cellk, cudaStream_t st);
+                    float4* xs, int* key, int* rank, int* count, int* cellk, int* tile_count, cudaStream_t st);
 void launch_key(bool mixed, const StepParams& p, const CellPack& cp, const float4* pos, int m,
                 int* key, int* rank, int* count, int* cellk, cudaStream_t st);
 // near[key] = 1 for every cell (bucket) within one cell of a static particle
@@ -102,7 +108,7 @@ void launch_delta(bool mixed, const Tuning& tu, const StepParams& p, const CellP
 void launch_xsph(bool mixed, const Tuning& tu, const StepParams& p, const CellPack& cp,
                  const float4* xs, const float4* v_in, const int* nbr, const int* cnt,
                  const int* key_sorted, float4* x_out, float4* v_out, float4* xs_next, int* key,
-                 int* rank, int* count, int* cellk, cudaStream_t st);
+                 int* rank, int* count, int* cellk, int* tile_count, cudaStream_t st);
 void launch_unpermute_pos(bool mixed, const StepParams& p, const CellPack& cp, const float4* a,
                           const int* id, int n, float* out, cudaStream_t st);
 void launch_unpermute_pos_d(bool mixed, const StepParams& p, const CellPack& cp, const float4* a,

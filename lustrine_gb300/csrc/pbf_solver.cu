@@ -255,11 +255,14 @@ __device__ __forceinline__ int cell_key(const StepParams& p, const CellPack& cp,
 // fused multiply-adds keep the arithmetic identical wherever it is inlined:
 // the prediction kernel and the commit kernel of the previous step (which
 // predicts the next step when nothing changes in between) agree bit for bit.
+// tile_count (may be null): the cell scan's per-tile totals, counted here
+// with one atomic per tile a warp's particles fall in (slots are in cell
+// order, so a warp's keys share a tile of CELL_TILE cells nearly always).
 template <bool MIXED>
 __device__ __forceinline__ void predict_one(const StepParams& p, const CellPack& cp, const Geo& g, float4 xi,
                                             float4 vi, int i, float4* __restrict__ xs, int* __restrict__ key,
                                             int* __restrict__ rank, int* __restrict__ count,
-                                            int* __restrict__ cellk) {
+                                            int* __restrict__ cellk, int* __restrict__ tile_count) {
     vi.x = __fmaf_rn(p.gxv, p.dt, vi.x);
     vi.y = __fmaf_rn(p.gyv, p.dt, vi.y);
     vi.z = __fmaf_rn(p.gzv, p.dt, vi.z);
@@ -282,16 +285,22 @@ __device__ __forceinline__ void predict_one(const StepParams& p, const CellPack&
     const int k = cell_key(p, cp, g, c, cellk, i);
     key[i] = k;
     rank[i] = atomicAdd(&count[k], 1);
+    if (tile_count) {
+        const int tile = k >> CELL_TILE_SHIFT;
+        const unsigned peers = __match_any_sync(__activemask(), tile);
+        if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&tile_count[tile], __popc(peers));
+    }
 }
 
 template <bool MIXED>
 __global__ void k_predict(StepParams p, CellPack cp, const float4* __restrict__ x,
                           const float4* __restrict__ v, float4* __restrict__ xs, int* __restrict__ key,
-                          int* __restrict__ rank, int* __restrict__ count, int* __restrict__ cellk) {
+                          int* __restrict__ rank, int* __restrict__ count, int* __restrict__ cellk,
+                          int* __restrict__ tile_count) {
     pdl_wait();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
-    predict_one<MIXED>(p, cp, geo_slot(p, i), x[i], v[i], i, xs, key, rank, count, cellk);
+    predict_one<MIXED>(p, cp, geo_slot(p, i), x[i], v[i], i, xs, key, rank, count, cellk, tile_count);
 }
 
 // Cell key and histogram of static particles (solids; scene from solid_scene_of).
@@ -473,7 +482,9 @@ __global__ void __launch_bounds__(B) k_lists_lambda(StepParams p, CellPack cp, f
     if (s >= p.n) return;
     const float4 self = xs[s];
     const Geo g = geo_slot(p, s);
-    const int3 c = slot_cell(p, cp, g, key_sorted, cell_sorted, s);
+    // fp32 on a dense grid: the cell the prediction keyed this position by
+    const int3 c = (MIXED || HASHED) ? slot_cell(p, cp, g, key_sorted, cell_sorted, s)
+                                     : plain_cell(p, g, self.x, self.y, self.z);
     LambdaAcc a = lambda_init(p);
     int c_n = 0;
     const int slab = g.gx * g.gz;
@@ -666,7 +677,7 @@ __global__ void __launch_bounds__(B) k_xsph(StepParams p, CellPack cp, const flo
                                             float4* __restrict__ x_out, float4* __restrict__ v_out,
                                             float4* __restrict__ xs_next, int* __restrict__ key,
                                             int* __restrict__ rank, int* __restrict__ count,
-                                            int* __restrict__ cellk) {
+                                            int* __restrict__ cellk, int* __restrict__ tile_count) {
     constexpr bool MIXED = (F & 1) != 0, SOL = (F & 2) != 0;
     pdl_wait();
     __shared__ float4 shift_tab[MIXED ? 64 : 1];
@@ -717,7 +728,7 @@ __global__ void __launch_bounds__(B) k_xsph(StepParams p, CellPack cp, const flo
         xc = make_float4(self.x, self.y, self.z, pack_cell(cp, cs.x, cs.y, cs.z));
     }
     x_out[s] = xc;
-    if (xs_next) predict_one<MIXED>(p, cp, g, xc, vc, s, xs_next, key, rank, count, cellk);
+    if (xs_next) predict_one<MIXED>(p, cp, g, xc, vc, s, xs_next, key, rank, count, cellk, tile_count);
 }
 
 // Absolute positions (float3 triples) in the caller's id order.
@@ -1010,9 +1021,10 @@ static inline int blocks_for(int n, int t) { return (n + t - 1) / t; }
     } while (0)
 
 void launch_predict(bool mixed, const StepParams& p, const CellPack& cp, const float4* x, const float4* v,
-                    float4* xs, int* key, int* rank, int* count, int* cellk, cudaStream_t st) {
+                    float4* xs, int* key, int* rank, int* count, int* cellk, int* tile_count, cudaStream_t st) {
     if (p.n <= 0) return;
-    LGB_DISPATCH(mixed, k_predict, blocks_for(p.n, 256), 256, st, p, cp, x, v, xs, key, rank, count, cellk);
+    LGB_DISPATCH(mixed, k_predict, blocks_for(p.n, 256), 256, st, p, cp, x, v, xs, key, rank, count, cellk,
+                 tile_count);
 }
 
 void launch_mark_solid_near(bool mixed, const StepParams& p, const CellPack& cp, const float4* pos, int m,
@@ -1109,10 +1121,10 @@ void launch_delta(bool mixed, const Tuning& tu, const StepParams& p, const CellP
 void launch_xsph(bool mixed, const Tuning& tu, const StepParams& p, const CellPack& cp,
                  const float4* xs, const float4* v_in, const int* nbr, const int* cnt,
                  const int* key_sorted, float4* x_out, float4* v_out, float4* xs_next, int* key,
-                 int* rank, int* count, int* cellk, cudaStream_t st) {
+                 int* rank, int* count, int* cellk, int* tile_count, cudaStream_t st) {
     if (p.n <= 0) return;
     TUNE_DISPATCH(k_xsph, mixed, tu, p.n, st, p, cp, xs, v_in, nbr, cnt, key_sorted, x_out, v_out, xs_next, key,
-                  rank, count, cellk);
+                  rank, count, cellk, tile_count);
 }
 
 void launch_unpermute_pos(bool mixed, const StepParams& p, const CellPack& cp, const float4* a,

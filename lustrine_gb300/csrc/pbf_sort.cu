@@ -179,12 +179,16 @@ __global__ void __launch_bounds__(CELL_SCAN_THREADS) k_tile_sums(const int* __re
 
 // SCANNED: tile_sum already holds every tile's exclusive offset (grids of
 // more than CELL_SCAN_MAX_TILES tiles scan the totals in one block first).
+// tile_zero (may be null): per-tile totals that the next prediction will
+// count into, zeroed here (one entry per tile).
 template <bool SCANNED>
 __global__ void __launch_bounds__(CELL_SCAN_THREADS) k_scan_tiles(int* __restrict__ count, int C,
                                                                   const int* __restrict__ tile_sum,
-                                                                  int* __restrict__ start) {
+                                                                  int* __restrict__ start,
+                                                                  int* __restrict__ tile_zero) {
     pdl_wait();
     const int tile = blockIdx.x;
+    if (tile_zero && threadIdx.x == 0) tile_zero[tile] = 0;
     const long long base = (long long)tile * CELL_TILE + (long long)threadIdx.x * CELL_SCAN_ITEMS;
     const bool full = base + CELL_SCAN_ITEMS <= C;
     int v[CELL_SCAN_ITEMS];
@@ -327,19 +331,24 @@ int scan_block_sums_size(int C) { return blocks_for(C, SCAN_TILE) + 1; }
 
 int cell_scan_tiles(int C) { return blocks_for(C, CELL_TILE); }
 
-void launch_scan_tiles(int* count, int C, int* tile_sum, int* start, cudaStream_t st) {
+void launch_scan_tiles(int* count, int C, int* tile_sum, int* start, cudaStream_t st, bool counted,
+                       int* tile_zero) {
     const bool pdl = pdl_enabled();
     const int tiles = cell_scan_tiles(C);
-    launch_k(k_tile_sums, tiles, CELL_SCAN_THREADS, st, pdl, (const int*)count, C, tile_sum);
+    if (!counted) launch_k(k_tile_sums, tiles, CELL_SCAN_THREADS, st, pdl, (const int*)count, C, tile_sum);
     if (tiles <= CELL_SCAN_MAX_TILES) {
-        launch_k(k_scan_tiles<false>, tiles, CELL_SCAN_THREADS, st, pdl, count, C, (const int*)tile_sum, start);
+        launch_k(k_scan_tiles<false>, tiles, CELL_SCAN_THREADS, st, pdl, count, C, (const int*)tile_sum, start,
+                 tile_zero);
     } else {
         launch_k(k_scan_sums, 1, SUMS_THREADS, st, pdl, tile_sum, tiles);  // in place, exclusive
-        launch_k(k_scan_tiles<true>, tiles, CELL_SCAN_THREADS, st, pdl, count, C, (const int*)tile_sum, start);
+        launch_k(k_scan_tiles<true>, tiles, CELL_SCAN_THREADS, st, pdl, count, C, (const int*)tile_sum, start,
+                 tile_zero);
     }
 }
 
-int scan_tiles_launches(int C) { return cell_scan_tiles(C) <= CELL_SCAN_MAX_TILES ? 2 : 3; }
+int scan_tiles_launches(int C, bool counted) {
+    return (cell_scan_tiles(C) <= CELL_SCAN_MAX_TILES ? 1 : 2) + (counted ? 0 : 1);
+}
 
 void launch_sort_tail(const int* key, const int* rank, const int* start, const int* tie, int n,
                       int* tmp, int* perm, cudaStream_t st) {

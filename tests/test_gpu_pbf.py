@@ -316,11 +316,12 @@ def test_next_step_prediction_in_commit_kernel_is_exact(precision):
     for k in range(7):
         dt = sc.dt if k < 4 else 0.5 * sc.dt
         a.step(dt)
-        # the prediction kernel runs after an upload and a change of dt only
-        assert a.launches_per_step() == 2 + 2 + 2 * iters + 1 + (k in (0, 4))
+        # the prediction kernel runs after an upload and a change of dt only;
+        # scan 1 (tile totals counted by the prediction), sort 2, passes, commit
+        assert a.launches_per_step() == 1 + 2 + 2 * iters + 1 + (k in (0, 4))
         b.set_tuning(**b.get_tuning())
         b.step(dt)
-        assert b.launches_per_step() == 2 + 2 + 2 * iters + 2
+        assert b.launches_per_step() == 1 + 2 + 2 * iters + 2
     xa, va, la, ra = a.download(lambdas=True, density=True)
     xb, vb, lb, rb = b.download(lambdas=True, density=True)
     np.testing.assert_array_equal(xa, xb)
