@@ -553,6 +553,7 @@ static int setup_solids(lustrine_pbf* s) {
 // into the state representation; slot k holds particle k.
 static int pack_fluid(lustrine_pbf* s, const float* dx, const float* dv) {
     const int n = s->n, c = s->cur;
+    s->slot_of_valid = false;
     if (!n) return LUSTRINE_OK;
     // caller order = slot order here; in a batch, particles come scene by scene
     launch_pack_pos(s->mixed(), s->sp, s->cp, dx, n, s->sp.scene_of, s->x[c], s->stream);
@@ -629,6 +630,7 @@ static const void* host_view(const void* p) {
 extern "C" int lustrine_pbf_upload_state_async(lustrine_pbf* s, const float* x, const float* v) {
     if (!s || !s->have_state || (!x && s->n > 0)) return LUSTRINE_ERR_ARGS;
     s->pred_ready = false;
+    s->slot_of_valid = false;
     const int n = s->n;
     if (!n) return LUSTRINE_OK;
     const float* hx = (const float*)host_view(x);
@@ -702,7 +704,7 @@ static int enqueue_sand_step(lustrine_pbf* s, cudaStream_t st, StageMarks* mk) {
     // index after sources or sinks changed the order), as the reference's
     // counting sort is (Sorting.cpp:29-32)
     launch_sort_state(s->key, s->rank, s->start, s->id[c], n, s->tmp, s->x[c], s->xs[c], nullptr, nullptr,
-                      s->key_sorted, s->x[o], s->xs[o], nullptr, nullptr, s->att[c], s->att[o], st);
+                      s->key_sorted, s->x[o], s->xs[o], nullptr, nullptr, s->att[c], s->att[o], nullptr, st);
     k += 2;
     if (mk) mk->mark(LUSTRINE_STAGE_SORT, st);
     launch_sand_lists(p, s->xs[o], s->key_sorted, s->start, s->solid, s->sstart, s->nbr, s->cnt, s->status, st);
@@ -765,7 +767,7 @@ static int enqueue_step(lustrine_pbf* s, cudaStream_t st, StageMarks* mk = nullp
     // (v = (x* - x) / dt) before anything reads them
     launch_sort_state(s->key, s->rank, s->start, tie, n, s->tmp, s->x[c], xs_in, nullptr, s->id[c],
                       s->key_sorted, s->x[o], s->xs[o], s->v[o], s->id[o], s->cell_sorted ? s->cellk : nullptr,
-                      s->cell_sorted, st);
+                      s->cell_sorted, s->slot_of, st);
     k += 2;
     if (mk) mk->mark(LUSTRINE_STAGE_SORT, st);
     if (s->prm.mode == LUSTRINE_MODE_REFERENCE) {
@@ -815,6 +817,7 @@ static int enqueue_step(lustrine_pbf* s, cudaStream_t st, StageMarks* mk = nullp
 // Host bookkeeping after the launches of a step that started on side c.
 static void finish_step(lustrine_pbf* s, int c) {
     s->cur = s->sand_mode() ? c : 1 - c;  // the sand step commits into the side it started from
+    s->slot_of_valid = !s->sand_mode();   // the fluid steps' sort recorded every particle's slot
     s->lists_valid = true;
     s->cells_valid = true;
     s->steps_done++;
@@ -1125,8 +1128,9 @@ extern "C" int lustrine_pbf_download_state_async(lustrine_pbf* s, float* x, floa
     float* hv = (float*)host_view(v);
     if ((!x || hx) && (!v || hv)) {  // write straight into the page-locked buffers
         const int c = s->cur;
-        launch_unpack_state(s->mixed(), s->sp, s->cp, s->x[c], s->v[c], s->id[c], s->slot_of, n, hx, hv,
-                            s->stream);
+        launch_unpack_state(s->mixed(), s->sp, s->cp, s->x[c], s->v[c], s->id[c], s->slot_of, s->slot_of_valid, n,
+                            hx, hv, s->stream);
+        s->slot_of_valid = true;
         CK(cudaGetLastError());
         return LUSTRINE_OK;
     }
@@ -1140,6 +1144,35 @@ extern "C" int lustrine_pbf_download_state_async(lustrine_pbf* s, float* x, floa
 // One frame of a host that keeps the state: upload, step, download, wait.
 extern "C" int lustrine_pbf_step_host(lustrine_pbf* s, float dt, float* x, float* v) {
     if (!s || !x) return LUSTRINE_ERR_ARGS;
+    const float* hx = (const float*)host_view(x);
+    const float* hv = (const float*)host_view(v);
+    if (s->prm.mode == LUSTRINE_MODE_PBF && !s->is_batch() && s->have_state && s->n > 0 && hx && (!v || hv) &&
+        dt > 0.0f && std::isfinite(dt)) {
+        // page-locked arrays: the upload is fused with the step's prediction,
+        // the rest of the step runs from that prediction, and the download
+        // reads the slots the sort recorded
+        if (s->sp.dt != dt) {
+            s->sp.dt = dt;
+            s->sp.inv_dt = 1.0f / dt;
+            s->invalidate_graphs();
+        }
+        if (s->count_dirty) CK(cudaMemsetAsync(s->count, 0, (size_t)s->sp.num_cells * sizeof(int), s->stream));
+        if (s->count_dirty || s->tiles_dirty) {
+            int rc = clear_tiles(s);
+            if (rc) return rc;
+        }
+        s->count_dirty = false;
+        const int c = s->cur;
+        launch_pack_predict(s->mixed(), s->sp, s->cp, hx, hv, s->n, s->x[c], s->id[c], s->xs_pred, s->key, s->rank,
+                            s->count, s->cellk, tiles_of(s, c), s->stream);
+        CK(cudaGetLastError());
+        s->pred_ready = true;
+        s->pred_dt = dt;
+        int rc = step_impl(s, dt, false);
+        if (!rc) rc = lustrine_pbf_download_state_async(s, x, v);
+        if (!rc) CK(cudaStreamSynchronize(s->stream));
+        return rc;
+    }
     int rc = lustrine_pbf_upload_state_async(s, x, v);
     if (!rc) rc = step_impl(s, dt, false);  // the next frame replaces the state
     if (!rc) rc = lustrine_pbf_download_state_async(s, x, v);

@@ -38,6 +38,7 @@ struct lustrine_pbf {
     float4* vtmp = nullptr;    // velocities before XSPH
     int* iota = nullptr;       // 0..n-1
     int* slot_of = nullptr;    // slot of every caller index (state download)
+    bool slot_of_valid = false;  // written by the last sort of the committed side
 
     // counting sort
     int* key = nullptr;

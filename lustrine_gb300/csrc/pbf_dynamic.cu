@@ -102,6 +102,7 @@ __global__ void k_histogram(const int* __restrict__ key, int n, int* __restrict_
 int after_resize(lustrine_pbf* s) {
     s->sp.n = s->n;
     s->invalidate_graphs();
+    s->slot_of_valid = false;
     s->lists_valid = false;
     s->lam_src = nullptr;
     if (s->n) {

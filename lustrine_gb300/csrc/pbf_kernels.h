@@ -49,7 +49,7 @@ void launch_counting_sort(const int* keys, int n, int num_cells, CountingSortScr
 void launch_sort_state(const int* key, const int* rank, const int* start, const int* tie, int n,
                        int* tmp, const float4* x, const float4* xs, const float4* v, const int* id,
                        int* key_out, float4* x_out, float4* xs_out, float4* v_out, int* id_out,
-                       const int* aux, int* aux_out, cudaStream_t st);
+                       const int* aux, int* aux_out, int* slot_of, cudaStream_t st);
 void launch_gather_int(const int* perm, int n, const int* src, int* dst, cudaStream_t st);
 
 // pbf_compat.cu (reference semantics, no FMA contraction)
@@ -126,8 +126,15 @@ void launch_query_cells(const StepParams& p, const CellPack& cp, const int box[6
 // written by the kernels): hv may be nullptr (zero velocities / not written)
 void launch_pack_state(bool mixed, const StepParams& p, const CellPack& cp, const float* hx, const float* hv,
                        int n, float4* x, float4* v, int* id, cudaStream_t st);
+// slot_of_valid: slot_of already maps every caller index to its slot (the
+// last sort wrote it); otherwise it is rebuilt from id first
 void launch_unpack_state(bool mixed, const StepParams& p, const CellPack& cp, const float4* x, const float4* v,
-                         const int* id, int* slot_of, int n, float* hx, float* hv, cudaStream_t st);
+                         const int* id, int* slot_of, bool slot_of_valid, int n, float* hx, float* hv,
+                         cudaStream_t st);
+// a host frame's upload fused with the step's prediction (slot = caller index)
+void launch_pack_predict(bool mixed, const StepParams& p, const CellPack& cp, const float* hx, const float* hv,
+                         int n, float4* x, int* id, float4* xs, int* key, int* rank, int* count, int* cellk,
+                         int* tile_count, cudaStream_t st);
 void launch_reduce(bool mixed, const StepParams& p, const CellPack& cp, const float4* x,
                    const float4* v, const float* rho, double* out, cudaStream_t st);
 

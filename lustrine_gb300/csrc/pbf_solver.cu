@@ -859,6 +859,32 @@ __global__ void __launch_bounds__(HOST_BLOCK) k_pack_state(StepParams p, CellPac
     id[i] = i;
 }
 
+// Upload fused with the step's prediction (a host frame: the state comes in
+// from page-locked memory and is stepped at once): slot = caller index, x
+// packed into the state, v used by the prediction only (the step recomputes
+// it), then predict_one as k_predict does on the same values.
+template <bool MIXED>
+__global__ void __launch_bounds__(HOST_BLOCK) k_pack_predict(StepParams p, CellPack cp, const float* __restrict__ hx,
+                                                             const float* __restrict__ hv, int n,
+                                                             float4* __restrict__ x, int* __restrict__ id,
+                                                             float4* __restrict__ xs, int* __restrict__ key,
+                                                             int* __restrict__ rank, int* __restrict__ count,
+                                                             int* __restrict__ cellk, int* __restrict__ tile_count) {
+    __shared__ float sx[3 * HOST_BLOCK], sv[3 * HOST_BLOCK];
+    host_to_smem(hx, n, sx);
+    if (hv) host_to_smem(hv, n, sv);
+    __syncthreads();
+    const int i = blockIdx.x * HOST_BLOCK + threadIdx.x;
+    if (i >= n) return;
+    const int t = 3 * threadIdx.x;
+    const Geo g = geo_single(p);
+    const float4 xi = pack_position<MIXED>(p, cp, g, sx[t], sx[t + 1], sx[t + 2]);
+    const float4 vi = hv ? make_float4(sv[t], sv[t + 1], sv[t + 2], 0.0f) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    x[i] = xi;
+    id[i] = i;
+    predict_one<MIXED>(p, cp, g, xi, vi, i, xs, key, rank, count, cellk, tile_count);
+}
+
 __global__ void k_slot_of(const int* __restrict__ id, int n, int* __restrict__ slot_of) {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s < n) slot_of[id[s]] = s;
@@ -1151,10 +1177,19 @@ void launch_pack_state(bool mixed, const StepParams& p, const CellPack& cp, cons
     LGB_DISPATCH(mixed, k_pack_state, blocks_for(n, HOST_BLOCK), HOST_BLOCK, st, p, cp, hx, hv, n, x, v, id);
 }
 
-void launch_unpack_state(bool mixed, const StepParams& p, const CellPack& cp, const float4* x, const float4* v,
-                         const int* id, int* slot_of, int n, float* hx, float* hv, cudaStream_t st) {
+void launch_pack_predict(bool mixed, const StepParams& p, const CellPack& cp, const float* hx, const float* hv,
+                         int n, float4* x, int* id, float4* xs, int* key, int* rank, int* count, int* cellk,
+                         int* tile_count, cudaStream_t st) {
     if (n <= 0) return;
-    launch_k(k_slot_of, blocks_for(n, 256), 256, st, pdl_enabled(), id, n, slot_of);
+    LGB_DISPATCH(mixed, k_pack_predict, blocks_for(n, HOST_BLOCK), HOST_BLOCK, st, p, cp, hx, hv, n, x, id, xs,
+                 key, rank, count, cellk, tile_count);
+}
+
+void launch_unpack_state(bool mixed, const StepParams& p, const CellPack& cp, const float4* x, const float4* v,
+                         const int* id, int* slot_of, bool slot_of_valid, int n, float* hx, float* hv,
+                         cudaStream_t st) {
+    if (n <= 0) return;
+    if (!slot_of_valid) launch_k(k_slot_of, blocks_for(n, 256), 256, st, pdl_enabled(), id, n, slot_of);
     LGB_DISPATCH(mixed, k_unpack_state, blocks_for(n, HOST_BLOCK), HOST_BLOCK, st, p, cp, x, v, (const int*)slot_of,
                  n, hx, hv);
 }

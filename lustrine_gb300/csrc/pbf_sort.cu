@@ -264,7 +264,7 @@ __global__ void k_stabilize_gather(const int* __restrict__ tmp, const int* __res
                                    int* __restrict__ key_out, float4* __restrict__ x_out,
                                    float4* __restrict__ xs_out, float4* __restrict__ v_out,
                                    int* __restrict__ id_out, const int* __restrict__ aux,
-                                   int* __restrict__ aux_out) {
+                                   int* __restrict__ aux_out, int* __restrict__ slot_of) {
     pdl_wait();
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
@@ -285,6 +285,7 @@ __global__ void k_stabilize_gather(const int* __restrict__ tmp, const int* __res
     if (v) v_out[f] = v[i];
     if (id) id_out[f] = id[i];
     if (aux) aux_out[f] = aux[i];
+    if (slot_of) slot_of[id[i]] = f;  // the caller index's new slot (state downloads)
 }
 
 __global__ void k_gather_int(const int* __restrict__ perm, int n, const int* __restrict__ src,
@@ -360,12 +361,12 @@ void launch_sort_tail(const int* key, const int* rank, const int* start, const i
 void launch_sort_state(const int* key, const int* rank, const int* start, const int* tie, int n,
                        int* tmp, const float4* x, const float4* xs, const float4* v, const int* id,
                        int* key_out, float4* x_out, float4* xs_out, float4* v_out, int* id_out,
-                       const int* aux, int* aux_out, cudaStream_t st) {
+                       const int* aux, int* aux_out, int* slot_of, cudaStream_t st) {
     if (n <= 0) return;
     const bool pdl = pdl_enabled();
     launch_k(k_scatter_index, blocks_for(n, 256), 256, st, pdl, key, rank, start, n, tmp);
     launch_k(k_stabilize_gather, blocks_for(n, 256), 256, st, pdl, (const int*)tmp, key, start, tie, n,
-             x, xs, v, id, key_out, x_out, xs_out, v_out, id_out, aux, aux_out);
+             x, xs, v, id, key_out, x_out, xs_out, v_out, id_out, aux, aux_out, slot_of);
 }
 
 void launch_gather_solid(const int* perm, int n, const float4* src, float4* dst, cudaStream_t st) {

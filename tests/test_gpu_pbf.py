@@ -295,6 +295,15 @@ def test_state_transfers_page_locked_and_pageable_agree(precision):
         b.step_host(sc.dt, hx.ctypes.data, hv.ctypes.data)
     np.testing.assert_array_equal(px.numpy(), hx)
     np.testing.assert_array_equal(pv.numpy(), hv)
+    # device-resident steps after host frames: the page-locked download reads
+    # the slots the last sort recorded, the pageable one unpermutes by id
+    for s in (a, b):
+        s.step(sc.dt, 2)
+    a.download_state_async(px.data_ptr(), pv.data_ptr())
+    a.synchronize()
+    xb, vb, _, _ = b.download()
+    np.testing.assert_array_equal(px.numpy(), xb)
+    np.testing.assert_array_equal(pv.numpy(), vb)
     assert a.status() == 0 and b.status() == 0
     a.close()
     b.close()
