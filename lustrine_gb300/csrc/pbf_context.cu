@@ -994,6 +994,10 @@ static int snapshot_restore(lustrine_pbf* s, const Snapshot& sn, int side) {
 
 // Milliseconds per step of `steps` graph-replayed steps from the snapshot
 // with the current tuning (two untimed steps capture both parities' graphs).
+// Milliseconds per step of the current launch shape: the median over three
+// timings of `steps` graph-replayed steps, each from the snapshot (one
+// timing is at the mercy of clock and scheduling noise; the shapes differ by
+// a few per cent).
 static int time_candidate(lustrine_pbf* s, const Snapshot& sn, int side, float dt, int steps, float* ms) {
     int rc = snapshot_restore(s, sn, side);
     if (rc) return rc;
@@ -1001,21 +1005,25 @@ static int time_candidate(lustrine_pbf* s, const Snapshot& sn, int side, float d
     // with and without a prediction of their own)
     for (int k = 0; k < 3; k++)
         if ((rc = lustrine_pbf_step(s, dt))) return rc;
-    if ((rc = snapshot_restore(s, sn, side))) return rc;
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
-    cudaEventRecord(e0, s->stream);
-    for (int k = 0; k < steps && !rc; k++) rc = lustrine_pbf_step(s, dt);
-    cudaEventRecord(e1, s->stream);
-    cudaError_t e = cudaEventSynchronize(e1);
-    float t = 0.0f;
-    if (e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
+    float t[3] = {0.0f, 0.0f, 0.0f};
+    cudaError_t e = cudaSuccess;
+    for (int r = 0; r < 3 && !rc && e == cudaSuccess; r++) {
+        if ((rc = snapshot_restore(s, sn, side))) break;
+        cudaEventRecord(e0, s->stream);
+        for (int k = 0; k < steps && !rc; k++) rc = lustrine_pbf_step(s, dt);
+        cudaEventRecord(e1, s->stream);
+        e = cudaEventSynchronize(e1);
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&t[r], e0, e1);
+    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (rc) return rc;
     if (e != cudaSuccess) return lgb_cuda_status(e, "autotune timing");
-    *ms = t / (float)steps;
+    std::sort(t, t + 3);
+    *ms = t[1] / (float)steps;
     return LUSTRINE_OK;
 }
 
