@@ -431,6 +431,7 @@ def run_variants(args, flush):
                                "launch_shape": sim.tuned["tuning"],
                                "stage_ms": {a: round(b[0], 4) for a, b in prof.items()}}
     sim.close()
+    out["reference_semantics_config1"] = run_reference_semantics(k, flush)
     out["sand_config1_262k"] = run_sand(k, flush)
     out["config3_batched_vs_plain"] = run_config3(max(3, min(args.steps, 10)), flush)
     # 4,194,304 particles in a 4096 x 256 x 4096 box: 4.3e9 cells, so the
@@ -446,6 +447,30 @@ def run_variants(args, flush):
                      "max_density_error": sim.reduce()["max_density_error"],
                      "stage_ms": {a: round(b[0], 4) for a, b in prof.items()}}
         sim.close()
+    return out
+
+
+def run_reference_semantics(steps, flush):
+    """The reference's fluid step semantics on the GPU (mode R: one lambda
+    and one position pass, cubic kernel, Jacobi update) on config 1's scene:
+    the same work per particle-iteration as the CPU reference arm."""
+    import torch
+    from lustrine_gb300 import PbfSim, reference_params, scenes
+    sc = scenes.config1()
+    p = reference_params(*sc.domain)
+    p.rest_density, p.mass, p.relaxation_epsilon = 1.0, 1.0, 10.0
+    p.gravity[1] = -9.81
+    p.s_corr_dq, p.s_corr_k, p.s_corr_n = 0.2, 0.1, 4.0
+    p.clamp_cells = 1
+    sim = PbfSim(p, sc.n, sc.ns)
+    sim.upload(sc.x, None, sc.solid)
+    sim.step(sc.dt, 3)
+    sim.synchronize()
+    ext = torch.cuda.ExternalStream(sim.stream())
+    ms = time_steps(sim, sc.dt, steps, flush, ext)
+    out = {"value": sc.n / (np.median(ms) * 1e-3), "unit": UNIT, "ms_per_step": float(np.median(ms)),
+           "status": sim.status(), "launches_per_step": sim.launches_per_step(), "solver_iterations": 1}
+    sim.close()
     return out
 
 

@@ -33,9 +33,9 @@ __device__ __forceinline__ float W_ref(const StepParams& p, float r) {
     return result;
 }
 
-// cubic_kernel_grad (Kernels.cpp:26-41)
-__device__ __forceinline__ float3 gradW_ref(const StepParams& p, float rx, float ry, float rz) {
-    float len = sqrtf((rx * rx + ry * ry) + rz * rz);
+// cubic_kernel_grad (Kernels.cpp:26-41); len = glm::length(r), which the
+// callers already hold (the same expression, so the same bits)
+__device__ __forceinline__ float3 gradW_ref(const StepParams& p, float rx, float ry, float rz, float len) {
     float rl = len * p.kfac;
     float q = rl / p.h;
     float3 out = make_float3(0.0f, 0.0f, 0.0f);
@@ -73,6 +73,7 @@ __device__ __forceinline__ float resolve_collision(float value, float lo, float 
 __global__ void k_predict_ref(StepParams p, const float4* __restrict__ x, float4* __restrict__ v,
                               float4* __restrict__ xs, int* __restrict__ key,
                               int* __restrict__ rank, int* __restrict__ count, int* status) {
+    pdl_wait();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
     float4 xi = x[i], vi = v[i];
@@ -90,6 +91,7 @@ __global__ void k_predict_ref(StepParams p, const float4* __restrict__ x, float4
 
 __global__ void k_key_ref(StepParams p, const float4* __restrict__ pos, int m, int* __restrict__ key,
                           int* __restrict__ rank, int* __restrict__ count, int* status) {
+    pdl_wait();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m) return;
     float4 s = pos[i];
@@ -106,6 +108,7 @@ __global__ void k_lists_ref(StepParams p, const float4* __restrict__ xs, const i
                             const int* __restrict__ fstart, const float4* __restrict__ solid,
                             const int* __restrict__ sstart, int* __restrict__ nbr,
                             int* __restrict__ cnt, int* status) {
+    pdl_wait();
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= p.n) return;
     const float4 self = xs[s];
@@ -150,36 +153,40 @@ __device__ __forceinline__ float4 nbr_pos(int j, const float4* __restrict__ xs,
 }
 
 // Simulate.cpp:58-88; lambdas are stored by the caller's particle id because
-// the position pass indexes them by list position (Simulate.cpp:97).
+// the position pass indexes them by list position (Simulate.cpp:97).  The
+// reference's two loops over the list (density, then gradients) run as one:
+// each sum still takes its terms in list order, so the bits are the same,
+// with one gather per neighbour instead of two.
 __global__ void k_lambda_ref(StepParams p, const float4* __restrict__ xs, const int* __restrict__ id,
                              const int* __restrict__ nbr, const int* __restrict__ cnt,
                              const float4* __restrict__ solid, float* __restrict__ lam_by_id,
                              float* __restrict__ rho) {
+    pdl_wait();
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= p.n) return;
     const float4 self = xs[s];
     const int c = cnt[s];
     float density = 0.0f;
-    for (int k = 0; k < c; k++) {
-        float4 o = nbr_pos(nbr[(size_t)k * p.n + s], xs, solid);
-        float ix = self.x - o.x, iy = self.y - o.y, iz = self.z - o.z;
-        float len = sqrtf((ix * ix + iy * iy) + iz * iz);
-        density += p.mass * W_ref(p, len);
-    }
-    density += p.mass * W_ref(p, 0.0f);
-    float constraint = (float)((double)(density / p.rho0) - 1.0);
     float gsum = 0.0f;
     float gcx = 0.0f, gcy = 0.0f, gcz = 0.0f;
     const float coef = -(p.mass / p.rho0);
+    int e_next = c > 0 ? __ldg(&nbr[s]) : 0;
     for (int k = 0; k < c; k++) {
-        float4 o = nbr_pos(nbr[(size_t)k * p.n + s], xs, solid);
-        float3 g = gradW_ref(p, self.x - o.x, self.y - o.y, self.z - o.z);
+        const int e = e_next;
+        if (k + 1 < c) e_next = __ldg(&nbr[(size_t)(k + 1) * p.n + s]);  // next entry while this one is used
+        float4 o = nbr_pos(e, xs, solid);
+        float ix = self.x - o.x, iy = self.y - o.y, iz = self.z - o.z;
+        float len = sqrtf((ix * ix + iy * iy) + iz * iz);
+        density += p.mass * W_ref(p, len);
+        float3 g = gradW_ref(p, ix, iy, iz, len);
         float nx = coef * g.x, ny = coef * g.y, nz = coef * g.z;
         gsum += (nx * nx + ny * ny) + nz * nz;
         gcx -= nx;
         gcy -= ny;
         gcz -= nz;
     }
+    density += p.mass * W_ref(p, 0.0f);
+    float constraint = (float)((double)(density / p.rho0) - 1.0);
     gsum += (gcx * gcx + gcy * gcy) + gcz * gcz;
     float lam = 0.0f;
     if (gsum > 0.0f) lam = (-constraint) / (gsum + p.eps);
@@ -193,6 +200,7 @@ __global__ void k_delta_ref(StepParams p, const float4* __restrict__ xs, float4*
                             const int* __restrict__ id, const int* __restrict__ nbr,
                             const int* __restrict__ cnt, const float4* __restrict__ solid,
                             const float* __restrict__ lam_by_id) {
+    pdl_wait();
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= p.n) return;
     const float4 self = xs[s];
@@ -200,12 +208,15 @@ __global__ void k_delta_ref(StepParams p, const float4* __restrict__ xs, float4*
     const float w_dq = W_ref(p, p.dq);
     const int c = cnt[s];
     float px = 0.0f, py = 0.0f, pz = 0.0f;
+    int e_next = c > 0 ? __ldg(&nbr[s]) : 0;
     for (int k = 0; k < c; k++) {
-        float4 o = nbr_pos(nbr[(size_t)k * p.n + s], xs, solid);
+        const int e = e_next;
+        if (k + 1 < c) e_next = __ldg(&nbr[(size_t)(k + 1) * p.n + s]);
+        float4 o = nbr_pos(e, xs, solid);
         float ix = self.x - o.x, iy = self.y - o.y, iz = self.z - o.z;
         float len = sqrtf((ix * ix + iy * iy) + iz * iz);
         float sc = scorr_ref(p, len, w_dq);
-        float3 g = gradW_ref(p, ix, iy, iz);
+        float3 g = gradW_ref(p, ix, iy, iz, len);
         float w = (li + lam_by_id[k]) + sc;
         px += w * g.x;
         py += w * g.y;
@@ -232,36 +243,37 @@ static inline int blocks_for(int n, int t) { return (n + t - 1) / t; }
 void launch_predict_ref(const StepParams& p, const float4* x, float4* v, float4* xs, int* key,
                         int* rank, int* count, int* status, cudaStream_t st) {
     if (p.n <= 0) return;
-    k_predict_ref<<<blocks_for(p.n, 256), 256, 0, st>>>(p, x, v, xs, key, rank, count, status);
+    launch_k(k_predict_ref, blocks_for(p.n, 256), 256, st, pdl_enabled(), p, x, v, xs, key, rank, count, status);
 }
 
 void launch_key_ref(const StepParams& p, const float4* pos, int m, int* key, int* rank, int* count,
                     int* status, cudaStream_t st) {
     if (m <= 0) return;
-    k_key_ref<<<blocks_for(m, 256), 256, 0, st>>>(p, pos, m, key, rank, count, status);
+    launch_k(k_key_ref, blocks_for(m, 256), 256, st, pdl_enabled(), p, pos, m, key, rank, count, status);
 }
 
 void launch_lists_ref(const StepParams& p, const float4* xs, const int* key, const int* fstart,
                       const float4* solid, const int* sstart, int* nbr, int* cnt, int* status,
                       cudaStream_t st) {
     if (p.n <= 0) return;
-    k_lists_ref<<<blocks_for(p.n, 128), 128, 0, st>>>(p, xs, key, fstart, solid, sstart, nbr, cnt,
-                                                       status);
+    launch_k(k_lists_ref, blocks_for(p.n, 128), 128, st, pdl_enabled(), p, xs, key, fstart, solid, sstart, nbr,
+             cnt, status);
 }
 
 void launch_lambda_ref(const StepParams& p, const float4* xs, const int* id, const int* nbr,
                        const int* cnt, const float4* solid, float* lam_by_id, float* rho,
                        cudaStream_t st) {
     if (p.n <= 0) return;
-    k_lambda_ref<<<blocks_for(p.n, 128), 128, 0, st>>>(p, xs, id, nbr, cnt, solid, lam_by_id, rho);
+    launch_k(k_lambda_ref, blocks_for(p.n, 128), 128, st, pdl_enabled(), p, xs, id, nbr, cnt, solid, lam_by_id,
+             rho);
 }
 
 void launch_delta_ref(const StepParams& p, const float4* xs, float4* xs_out, float4* x, float4* v,
                       const int* id, const int* nbr, const int* cnt, const float4* solid,
                       const float* lam_by_id, cudaStream_t st) {
     if (p.n <= 0) return;
-    k_delta_ref<<<blocks_for(p.n, 128), 128, 0, st>>>(p, xs, xs_out, x, v, id, nbr, cnt, solid,
-                                                       lam_by_id);
+    launch_k(k_delta_ref, blocks_for(p.n, 128), 128, st, pdl_enabled(), p, xs, xs_out, x, v, id, nbr, cnt, solid,
+             lam_by_id);
 }
 
 }  // namespace lgb
