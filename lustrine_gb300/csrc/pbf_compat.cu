@@ -116,14 +116,25 @@ __global__ void k_lists_ref(StepParams p, const float4* __restrict__ xs, const i
     const int slab = p.gx * p.gz;
     const int yy = id / slab, xx = (id % slab) / p.gz, zz = id % p.gz;
     int c_n = 0;
+    // a row's cells z-1 .. z+1 are consecutive ids: their fluid and solid
+    // ranges come from four loads of each table; the cells are still walked
+    // one by one, fluid before solids, as the reference lists them
+    const int z0 = max(zz - 1, 0), z1 = min(zz + 1, p.gz - 1);
     for (int y = -1; y <= 1; y++)
-        for (int x = -1; x <= 1; x++)
-            for (int z = -1; z <= 1; z++) {
-                if (xx + x < 0 || xx + x >= p.gx || yy + y < 0 || yy + y >= p.gy || zz + z < 0 ||
-                    zz + z >= p.gz)
-                    continue;
-                const int c = (yy + y) * slab + (xx + x) * p.gz + (zz + z);
-                for (int t = fstart[c], e = fstart[c + 1]; t < e; t++) {
+        for (int x = -1; x <= 1; x++) {
+            if (xx + x < 0 || xx + x >= p.gx || yy + y < 0 || yy + y >= p.gy) continue;
+            const int row = (yy + y) * slab + (xx + x) * p.gz;
+            int fb[4], sb[4];
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const bool in = z0 + k <= z1 + 1;
+                fb[k] = in ? __ldg(&fstart[row + z0 + k]) : 0;
+                sb[k] = in ? __ldg(&sstart[row + z0 + k]) : 0;
+            }
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                if (z0 + k > z1) break;
+                for (int t = fb[k]; t < fb[k + 1]; t++) {
                     float4 o = xs[t];
                     float dx = self.x - o.x, dy = self.y - o.y, dz = self.z - o.z;
                     if ((dx * dx + dy * dy) + dz * dz <= p.h2) {
@@ -131,8 +142,8 @@ __global__ void k_lists_ref(StepParams p, const float4* __restrict__ xs, const i
                         c_n++;
                     }
                 }
-                for (int t = sstart[c], e = sstart[c + 1]; t < e; t++) {
-                    float4 o = solid[t];
+                for (int t = sb[k]; t < sb[k + 1]; t++) {
+                    float4 o = __ldg(&solid[t]);
                     float dx = self.x - o.x, dy = self.y - o.y, dz = self.z - o.z;
                     if ((dx * dx + dy * dy) + dz * dz <= p.h2) {
                         if (c_n < p.max_nbrs) nbr[(size_t)c_n * p.n + s] = -1 - t;
@@ -140,6 +151,7 @@ __global__ void k_lists_ref(StepParams p, const float4* __restrict__ xs, const i
                     }
                 }
             }
+        }
     if (c_n > p.max_nbrs) {
         set_status(status, ST_NBR_OVERFLOW);
         c_n = p.max_nbrs;
