@@ -242,7 +242,9 @@ LUSTRINE_API int lustrine_pbf_destroy(lustrine_pbf* s);
  * scenes with one launch per stage. */
 LUSTRINE_API int lustrine_batch_create(const lustrine_pbf_params* p, int num_scenes, const int* domains,
                                        const int* n_fluid, const int* n_solid, lustrine_pbf** out);
-/* Change parameters (same mode/precision/domain/max_neighbors as at create). */
+/* Change parameters (same precision, domain, cell size, grid mode and
+ * max_neighbors as at create; the mode may change -- entering sand mode
+ * from another mode clears the attract flags). */
 LUSTRINE_API int lustrine_pbf_set_params(lustrine_pbf* s, const lustrine_pbf_params* p);
 LUSTRINE_API int lustrine_pbf_get_params(const lustrine_pbf* s, lustrine_pbf_params* p);
 LUSTRINE_API int lustrine_pbf_counts(const lustrine_pbf* s, int* n_fluid, int* n_solid);

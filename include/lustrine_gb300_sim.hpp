@@ -127,9 +127,10 @@ int acquire(Simulation* sim, const lustrine_pbf_params& p, int n, int ns, float*
         // captured step graphs
         lustrine_pbf_params cur;
         lustrine_pbf_get_params(e.ctx, &cur);
-        cur.use_graph = p.use_graph;
-        cur.max_neighbors = p.max_neighbors;
-        if (std::memcmp(&cur, &p, sizeof(p)) != 0) rc = lustrine_pbf_set_params(e.ctx, &p);
+        lustrine_pbf_params want = p;
+        want.use_graph = cur.use_graph;
+        want.max_neighbors = cur.max_neighbors;  // the list capacity is fixed at creation
+        if (std::memcmp(&cur, &want, sizeof(want)) != 0) rc = lustrine_pbf_set_params(e.ctx, &want);
         if (!rc && n != e.n) {  // sand added or removed by the host since the last step
             rc = lustrine_pbf_set_count(e.ctx, n);
             e.n = n;

@@ -480,6 +480,10 @@ extern "C" int lustrine_pbf_set_params(lustrine_pbf* s, const lustrine_pbf_param
     if (rc) return rc;
     // the grid's table (dense cells or hash buckets) was sized at creation
     if (sp.hash_bits != s->sp.hash_bits || sp.num_cells != s->sp.num_cells) return LUSTRINE_ERR_UNSUPPORTED;
+    // the fluid steps re-sort the particles without the sand mode's attract
+    // flags: entering sand mode from another mode starts them cleared
+    if (p->mode == LUSTRINE_MODE_SAND && s->prm.mode != LUSTRINE_MODE_SAND && s->n > 0)
+        CK(cudaMemsetAsync(s->att[s->cur], 0, (size_t)s->n * sizeof(int), s->stream));
     s->prm = *p;
     s->sp = sp;
     s->cp = cp;

@@ -280,3 +280,28 @@ def test_wrapper_sand_on_a_vox_floor(orc):
         W.cleanup_simulation()
         W.free_grid(floor)
         W.free_grid(sand)
+
+
+def test_mode_switch_into_sand_clears_attract_flags():
+    """The fluid steps re-sort particles without the sand flags: switching
+    from a fluid step back to sand starts with cleared flags, and the
+    context keeps stepping in every mode it is switched to."""
+    from lustrine_gb300 import MODE_PBF, MODE_REFERENCE, MODE_SAND, PbfSim, scenes
+    rng = np.random.default_rng(9)
+    x = scenes.jitter(scenes.lattice((8, 8, 8), (4, 2, 4)), 0.05, rng)
+    p = _params((16, 16, 16))
+    sim = PbfSim(p, len(x), 0)
+    sim.upload(x)
+    sim.set_attracted(np.ones(len(x), np.int32))
+    sim.step(1 / 60)
+    assert sim.attracted().sum() == len(x)  # no attraction in play: the flags stay
+    for mode in (MODE_REFERENCE, MODE_PBF, MODE_SAND):
+        q = sim.params
+        q.mode = mode
+        if mode == MODE_PBF:
+            q.iterations = 2
+        sim.set_params(q)
+        sim.step(1 / 60, 2)
+        assert sim.status() == 0
+    assert sim.attracted().sum() == 0
+    sim.close()
