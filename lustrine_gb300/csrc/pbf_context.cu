@@ -183,6 +183,9 @@ static int derive(const lustrine_pbf_params& q, int n, int ns, StepParams* sp, C
 
 lustrine_pbf::~lustrine_pbf() {
     free_buffers();
+    if (fork_ev) cudaEventDestroy(fork_ev);
+    if (join_ev) cudaEventDestroy(join_ev);
+    if (side) cudaStreamDestroy(side);
     if (stream) cudaStreamDestroy(stream);
 }
 
@@ -190,6 +193,10 @@ void lustrine_pbf::free_buffers() {
     for (int k = 0; k < 8; k++) {
         if (graph_exec[k]) cudaGraphExecDestroy(graph_exec[k]);
         graph_exec[k] = nullptr;
+    }
+    for (int k = 0; k < 2; k++) {
+        if (host_graph[k]) cudaGraphExecDestroy(host_graph[k]);
+        host_graph[k] = nullptr;
     }
     void* ptrs[] = {x[0], x[1], xs[0], xs[1], v[0], v[1], id[0], id[1], xs_alt, xs_pred, vtmp, key, key_sorted,
                     rank, tmp, perm, count, start, block_sums, tile_sum, solid_near, solid, solid_raw, sstart, nbr, cnt, lam,
@@ -509,6 +516,10 @@ void lustrine_pbf::invalidate_graphs() {
         if (graph_exec[k]) cudaGraphExecDestroy(graph_exec[k]);
         graph_exec[k] = nullptr;
     }
+    for (int k = 0; k < 2; k++) {
+        if (host_graph[k]) cudaGraphExecDestroy(host_graph[k]);
+        host_graph[k] = nullptr;
+    }
     pred_ready = false;  // whatever invalidates the step may change the prediction too
     tiles_dirty = true;
 }
@@ -729,12 +740,21 @@ static int enqueue_sand_step(lustrine_pbf* s, cudaStream_t st, StageMarks* mk) {
     return k;
 }
 
+// A page-locked host frame's download, split around the commit kernel: the
+// positions it commits are the last position pass's output, so they go to
+// the host on the side stream while XSPH runs; the velocities follow XSPH.
+struct HostFrame {
+    float* hx;
+    float* hv;
+};
+
 // One step's launches.  Returns the number of kernels launched.
 // predict: run the prediction kernel (else the previous step's commit
 // kernel left it in xs_pred, key, rank, count); tail: the commit kernel
-// predicts the next step (PBF mode only).
+// predicts the next step (PBF mode only); hf: download into page-locked host
+// buffers within the step (PBF fp32 only).
 static int enqueue_step(lustrine_pbf* s, cudaStream_t st, StageMarks* mk = nullptr, bool predict = true,
-                        bool tail = false) {
+                        bool tail = false, const HostFrame* hf = nullptr) {
     const int c = s->cur, o = 1 - c, n = s->n, C = s->sp.num_cells;
     const StepParams& p = s->sp;
     const bool mixed = s->mixed();
@@ -808,10 +828,26 @@ static int enqueue_step(lustrine_pbf* s, cudaStream_t st, StageMarks* mk = nullp
             b = t;
             k += 2;
         }
+        if (hf) {  // positions out on the side stream (slots recorded by this step's sort)
+            cudaEventRecord(s->fork_ev, st);
+            cudaStreamWaitEvent(s->side, s->fork_ev, 0);
+            launch_unpack_state(false, p, s->cp, a, nullptr, s->id[o], s->slot_of, true, n, hf->hx, nullptr,
+                                s->side);
+            k += 1;
+        }
         launch_xsph(mixed, tu, p, s->cp, a, s->vtmp, s->nbr, s->cnt, s->key_sorted, s->x[o], s->v[o],
                     tail ? s->xs_pred : nullptr, s->key, s->rank, s->count, s->cellk,
                     tail ? tiles_of(s, o) : nullptr, st);
         k += 1;
+        if (hf) {
+            if (hf->hv) {
+                launch_unpack_state(false, p, s->cp, nullptr, s->v[o], s->id[o], s->slot_of, true, n, nullptr,
+                                    hf->hv, st);
+                k += 1;
+            }
+            cudaEventRecord(s->join_ev, s->side);
+            cudaStreamWaitEvent(st, s->join_ev, 0);
+        }
         if (mk) mk->mark(LUSTRINE_STAGE_XSPH, st);
     }
     set_pdl(false);
@@ -1175,6 +1211,42 @@ extern "C" int lustrine_pbf_step_host(lustrine_pbf* s, float dt, float* x, float
         }
         s->count_dirty = false;
         const int c = s->cur;
+        if (!s->mixed() && s->prm.use_graph) {
+            // the whole frame as one graph for this buffer pair: upload fused
+            // with the prediction, the step, the positions downloaded while
+            // the commit kernel runs, then the velocities
+            if (!s->side) {
+                CK(cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking));
+                CK(cudaEventCreateWithFlags(&s->fork_ev, cudaEventDisableTiming));
+                CK(cudaEventCreateWithFlags(&s->join_ev, cudaEventDisableTiming));
+            }
+            if (!s->host_graph[c] || s->host_graph_ptr[c][0] != hx || s->host_graph_ptr[c][1] != hv) {
+                if (s->host_graph[c]) cudaGraphExecDestroy(s->host_graph[c]);
+                s->host_graph[c] = nullptr;
+                cudaGraph_t g = nullptr;
+                CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+                launch_pack_predict(false, s->sp, s->cp, hx, hv, s->n, s->x[c], s->id[c], s->xs_pred, s->key,
+                                    s->rank, s->count, s->cellk, tiles_of(s, c), s->stream);
+                const HostFrame hf{const_cast<float*>(hx), const_cast<float*>(hv)};
+                const int k = 1 + enqueue_step(s, s->stream, nullptr, false, false, &hf);
+                cudaError_t e = cudaStreamEndCapture(s->stream, &g);
+                if (e != cudaSuccess) return lgb_cuda_status(e, "cudaStreamEndCapture (host frame)");
+                e = cudaGraphInstantiate(&s->host_graph[c], g, 0);
+                cudaGraphDestroy(g);
+                if (e != cudaSuccess) return lgb_cuda_status(e, "cudaGraphInstantiate (host frame)");
+                s->host_graph_ptr[c][0] = hx;
+                s->host_graph_ptr[c][1] = hv;
+                s->host_graph_launches[c] = k;
+            }
+            CK(cudaGraphLaunch(s->host_graph[c], s->stream));
+            s->launches = s->host_graph_launches[c];
+            finish_step(s, c);
+            s->pred_ready = false;
+            s->pred_dt = dt;
+            s->count_dirty = false;
+            CK(cudaStreamSynchronize(s->stream));
+            return LUSTRINE_OK;
+        }
         launch_pack_predict(s->mixed(), s->sp, s->cp, hx, hv, s->n, s->x[c], s->id[c], s->xs_pred, s->key, s->rank,
                             s->count, s->cellk, tiles_of(s, c), s->stream);
         CK(cudaGetLastError());

@@ -108,6 +108,15 @@ struct lustrine_pbf {
     bool lists_valid = false;
     bool cells_valid = false;  // start[] / sstart[] bin the current slots (queries, sinks)
 
+    // page-locked host frames (lustrine_pbf_step_host, fp32): one graph per
+    // step parity for the caller's last buffer pair, with the positions
+    // downloaded on a side stream while the commit kernel runs
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+    cudaGraphExec_t host_graph[2] = {nullptr, nullptr};
+    const void* host_graph_ptr[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+    int host_graph_launches[2] = {0, 0};
+
     ~lustrine_pbf();
     void free_buffers();
     void invalidate_graphs();

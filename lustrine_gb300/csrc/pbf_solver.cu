@@ -886,6 +886,7 @@ __global__ void __launch_bounds__(HOST_BLOCK) k_pack_predict(StepParams p, CellP
 }
 
 __global__ void k_slot_of(const int* __restrict__ id, int n, int* __restrict__ slot_of) {
+    pdl_wait();
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s < n) slot_of[id[s]] = s;
 }
@@ -896,22 +897,25 @@ __global__ void __launch_bounds__(HOST_BLOCK) k_unpack_state(StepParams p, CellP
                                                              const float4* __restrict__ v,
                                                              const int* __restrict__ slot_of, int n,
                                                              float* __restrict__ hx, float* __restrict__ hv) {
+    pdl_wait();
     __shared__ float sx[3 * HOST_BLOCK], sv[3 * HOST_BLOCK];
     const int i = blockIdx.x * HOST_BLOCK + threadIdx.x;
     if (i < n) {
         const int s = slot_of[i];
         const int t = 3 * threadIdx.x;
-        const float4 q = x[s];
-        float a = q.x, b = q.y, c = q.z;
-        if (MIXED) {
-            const int3 cc = unpack_cell(cp, q.w);
-            a += (float)cc.x * p.cell;
-            b += (float)cc.y * p.cell;
-            c += (float)cc.z * p.cell;
+        if (hx) {
+            const float4 q = x[s];
+            float a = q.x, b = q.y, c = q.z;
+            if (MIXED) {
+                const int3 cc = unpack_cell(cp, q.w);
+                a += (float)cc.x * p.cell;
+                b += (float)cc.y * p.cell;
+                c += (float)cc.z * p.cell;
+            }
+            sx[t] = a;
+            sx[t + 1] = b;
+            sx[t + 2] = c;
         }
-        sx[t] = a;
-        sx[t + 1] = b;
-        sx[t + 2] = c;
         if (hv) {
             const float4 u = v[s];
             sv[t] = u.x;
