@@ -392,38 +392,36 @@ __device__ __forceinline__ float lambda_of(const StepParams& p, const LambdaAcc&
 }
 
 // One row (dy, dx) of the stencil: the cells z0..z1 of a row are consecutive
-// ids, so their particles form one slot range; the cell bounds are loaded
-// once per row and give each candidate's dz.
+// ids, so their particles form one slot range, walked in one loop (a warp
+// then runs as many rounds as its fullest row, not the sum over the three
+// cells of its fullest cell); a candidate's dz follows from the cell bounds,
+// loaded once per row.  The candidates come in the same order as cell by cell.
 template <bool MIXED, bool SOLID>
 __device__ __forceinline__ void walk_row(const StepParams& p, const float4& self, int s,
                                          const float4* __restrict__ pos, const int* __restrict__ start,
                                          int row, int zc, int gz, int dx, int dy, LambdaAcc& a, int& c_n,
                                          int* __restrict__ nbr) {
     const int z0 = max(zc - 1, 0), z1 = min(zc + 1, gz - 1);
-    int b[4];
-#pragma unroll
-    for (int k = 0; k < 4; k++) b[k] = (z0 + k <= z1 + 1) ? start[row + z0 + k] : 0;
+    const int b0 = start[row + z0];
+    const int b1 = start[row + z0 + 1];
+    const int b2 = (z0 + 1 <= z1) ? start[row + z0 + 2] : b1;
+    const int b3 = (z0 + 2 <= z1) ? start[row + z0 + 3] : b2;
+    const int dz0 = z0 - zc;
     const float sx = -(float)dx * p.cell, sy = -(float)dy * p.cell;
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-        const int z = z0 + k;
-        if (z > z1) break;
-        const int dz = z - zc;
-        const float sz = -(float)dz * p.cell;
-        for (int t = b[k]; t < b[k + 1]; t++) {
-            if (!SOLID && t == s) continue;
-            const float4 q = SOLID ? __ldg(&pos[t]) : pos[t];
-            float3 d = make_float3(__fsub_rn(self.x, q.x), __fsub_rn(self.y, q.y), __fsub_rn(self.z, q.z));
-            if (MIXED) {
-                d.x = __fadd_rn(d.x, sx);
-                d.y = __fadd_rn(d.y, sy);
-                d.z = __fadd_rn(d.z, sz);
-            }
-            if (dot3e(d.x, d.y, d.z) <= p.h2) {
-                if (c_n < p.max_nbrs) nbr[(size_t)c_n * p.n + s] = entry(t, dx, dy, dz, SOLID);
-                c_n++;
-                lambda_accumulate<MIXED>(p, a, d, SOLID);
-            }
+    for (int t = b0; t < b3; t++) {
+        if (!SOLID && t == s) continue;
+        const int dz = dz0 + (t >= b1) + (t >= b2);
+        const float4 q = SOLID ? __ldg(&pos[t]) : pos[t];
+        float3 d = make_float3(__fsub_rn(self.x, q.x), __fsub_rn(self.y, q.y), __fsub_rn(self.z, q.z));
+        if (MIXED) {
+            d.x = __fadd_rn(d.x, sx);
+            d.y = __fadd_rn(d.y, sy);
+            d.z = __fadd_rn(d.z, -(float)dz * p.cell);
+        }
+        if (dot3e(d.x, d.y, d.z) <= p.h2) {
+            if (c_n < p.max_nbrs) nbr[(size_t)c_n * p.n + s] = entry(t, dx, dy, dz, SOLID);
+            c_n++;
+            lambda_accumulate<MIXED>(p, a, d, SOLID);
         }
     }
 }
