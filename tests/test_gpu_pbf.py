@@ -187,29 +187,47 @@ def test_graph_and_direct_launches_are_identical():
     assert np.array_equal(res[0][0], res[1][0]) and np.array_equal(res[0][1], res[1][1])
 
 
-def test_rollout_statistics_vs_fp64_oracle(orc):
-    """40 steps of the 10k dam break: kinetic energy, centre of mass and max
-    density error track the FP64 oracle run from the same state."""
+@pytest.mark.parametrize("epsilon,steps", [(10.0, 100), (30.0, 200)])
+def test_rollout_statistics_vs_fp64_oracle(orc, epsilon, steps):
+    """The 10k dam break stepped on the GPU against the FP64 oracle run from
+    the same state: kinetic energy, centre of mass and max density error every
+    20 steps.  The flow is chaotic, so the band is set by the oracle itself:
+    the GPU must stay as close to the FP64 run as a second FP64 run started
+    from positions perturbed by 1e-6 relative (about 16 fp32 ulps) stays, or
+    within a floor of 2 % (energy), 0.02 (centre of mass, box of 40) and 3 %
+    (density error).  Config 0's own parameters (epsilon 10) over its 100
+    steps; 200 steps at epsilon 30: with h equal to the particle spacing a
+    lone particle's density is W(0) = 1.567 rest densities, so every
+    constraint pushes outwards and at epsilon 10 the FP64 run itself gains
+    energy without bound after about 110 steps."""
     from lustrine_gb300 import PbfSim, scenes
     sc = scenes.config0(seed=25)
-    p = _params(sc)
+    p = _params(sc, relaxation_epsilon=epsilon, max_neighbors=128)
     q = _oracle_params(orc, p)
     sim = PbfSim(p, sc.n)
     sim.upload(sc.x)
-    x, v = sc.x.astype(np.float64), np.zeros((sc.n, 3))
-    for s in range(40):
+    rng = np.random.default_rng(7)
+    xa = sc.x.astype(np.float64)
+    xb = xa * (1.0 + 1e-6 * rng.uniform(-1.0, 1.0, xa.shape))
+    va, vb = np.zeros((sc.n, 3)), np.zeros((sc.n, 3))
+
+    def stats(x, v, rho):
+        return 0.5 * q.mass * (v ** 2).sum(), x.mean(0), np.abs(rho / q.rest_density - 1).max()
+
+    for s in range(steps):
         sim.step(sc.dt)
-        o = orc.pbf_step(q, sc.dt, x, v)
-        x, v = o["x"], o["v"]
-        if s % 10 == 9:
+        oa = orc.pbf_step(q, sc.dt, xa, va)
+        ob = orc.pbf_step(q, sc.dt, xb, vb)
+        xa, va, xb, vb = oa["x"], oa["v"], ob["x"], ob["v"]
+        if s % 20 == 19:
             r = sim.reduce()
-            ke64 = 0.5 * q.mass * (v ** 2).sum()
-            com64 = x.mean(0)
+            assert sim.status() == 0, s
             assert abs(r["mass"] - sc.n * q.mass) < 1e-6
-            assert abs(r["kinetic"] - ke64) <= 0.02 * ke64 + 1e-6
-            assert np.abs(np.array(r["com"]) - com64).max() <= 0.02
-            err64 = np.abs(o["density"] / q.rest_density - 1).max()
-            assert abs(r["max_density_error"] - err64) <= 0.02 * err64
+            ke_a, com_a, err_a = stats(xa, va, oa["density"])
+            ke_b, com_b, err_b = stats(xb, vb, ob["density"])
+            assert abs(r["kinetic"] - ke_a) <= max(3 * abs(ke_b - ke_a), 0.02 * ke_a), s
+            assert np.abs(np.array(r["com"]) - com_a).max() <= max(3 * np.abs(com_b - com_a).max(), 0.02), s
+            assert abs(r["max_density_error"] - err_a) <= max(3 * abs(err_b - err_a), 0.03 * err_a), s
     xg = sim.positions()
     assert (xg >= 0.5 - 1e-5).all() and (xg <= 39.5 + 1e-5).all()
     sim.close()

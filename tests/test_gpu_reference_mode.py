@@ -156,3 +156,64 @@ def test_reference_mode_rollout_statistics(orc):
             assert np.abs(com_g - com_a).max() <= max(3 * np.abs(com_b - com_a).max(), 0.05)
     assert sim.status() in (0, 5)  # cell clamp may be reported
     sim.close()
+
+
+def test_reference_mode_200_step_rollout_in_the_oracle_ensemble(orc):
+    """200 steps of a 1,200-particle block (10 x 12 x 10 in a 20^3 box) under
+    the reference's step.  Its dynamics collapse the block into one cluster
+    within ~60 steps (kinetic energy swings over four decades; every particle
+    ends with hundreds of neighbours), so single trajectories diverge
+    completely: the GPU run is compared as one more member of an ensemble of
+    five oracle runs whose starts differ by one ulp in 1 % of the particles.
+    Over steps 100-199 its mean log10 kinetic energy and its mean largest
+    neighbour count must lie within the ensemble's range widened by two of
+    the ensemble's standard deviations, and it must conserve the particles
+    inside the box."""
+    from lustrine_gb300 import scenes
+    rng = np.random.default_rng(12)
+    x0 = scenes.jitter(scenes.lattice((10, 12, 10), (5, 0, 5)), 0.05, rng)
+    n, dt = len(x0), 1 / 60
+    p = phys_params(orc.reference_params(20, 20, 20))
+    p.jacobi = 1
+    p.clamp_cells = 1
+
+    def late_stats(step):
+        ke, nb = [], []
+        for s in range(200):
+            x, v, cnt = step()
+            if s >= 100:
+                ke.append(np.log10(0.5 * (np.asarray(v, np.float64) ** 2).sum() + 1.0))
+                nb.append(cnt.max())
+        return np.mean(ke), np.mean(nb), x
+
+    ens = []
+    for k in range(5):
+        x = x0.copy()
+        if k:
+            sel = np.random.default_rng(100 + k).random(n) < 0.01
+            x[sel] = np.nextafter(x[sel], np.float32(np.inf))
+        st = dict(x=x, v=np.zeros_like(x), lambdas=None)
+
+        def ostep(st=st):
+            o = orc.compat_step(p, dt, st["x"], st["v"], lambdas=st["lambdas"], cap=n)
+            st.update(x=o["x"], v=o["v"], lambdas=o["lambdas"])
+            return o["x"], o["v"], o["nbr_count"]
+        ens.append(late_stats(ostep)[:2])
+    ens = np.array(ens)
+
+    sim = _sim((20, 20, 20), n, max_neighbors=n)
+    sim.upload(x0, None)
+
+    def gstep():
+        sim.step(dt)
+        x, v, _, _ = sim.download()
+        cnt, _ = sim.neighbors(cap=n)
+        return x, v, cnt
+    ke_g, nb_g, xg = late_stats(gstep)
+    assert sim.status() in (0, 5)  # cell clamp may be reported
+    sim.close()
+    for val, col in ((ke_g, ens[:, 0]), (nb_g, ens[:, 1])):
+        lo, hi, sd = col.min(), col.max(), col.std()
+        assert lo - 2 * sd <= val <= hi + 2 * sd, (val, col)
+    assert np.isfinite(xg).all() and len(xg) == n
+    assert (xg >= 0.0).all() and (xg <= 20.0).all()
