@@ -5,7 +5,7 @@ C ABI, include/lustrine_gb300.h); this package is its Python host side.
 """
 from ._lib import LustrineError, load
 from .pbf import (MODE_PBF, MODE_REFERENCE, MODE_SAND, PRECISION_FP32, PRECISION_MIXED, PbfParams, PbfSim,
-                  pbf_params, reference_params, sand_params)
+                  pbf_params, reference_params, rest_lattice_mass, sand_params)
 
-__all__ = ["LustrineError", "load", "PbfSim", "PbfParams", "pbf_params", "reference_params", "sand_params",
+__all__ = ["LustrineError", "load", "PbfSim", "PbfParams", "pbf_params", "reference_params", "rest_lattice_mass", "sand_params",
            "MODE_PBF", "MODE_REFERENCE", "MODE_SAND", "PRECISION_FP32", "PRECISION_MIXED"]

@@ -12,6 +12,7 @@ order given to upload (the reference's storage order of solids).
 from __future__ import annotations
 
 import ctypes as C
+import math
 
 import numpy as np
 
@@ -33,16 +34,39 @@ def reference_params(X, Y, Z, radius=0.5, kernel_radius_scale=2.0) -> PbfParams:
     return p
 
 
-def pbf_params(X, Y, Z, *, radius=0.5, h=1.0, rest_density=1.0, mass=1.0, gravity=-9.81,
+def rest_lattice_mass(rest_density: float, h: float, spacing: float) -> float:
+    """The particle mass whose poly6 density (support h) on a cubic lattice
+    of the given spacing equals rest_density: rest_density / sum of W over the
+    lattice sites closer than h, W(r) = 315 / (64 pi h^9) (h^2 - r^2)^3.  At
+    spacing h the neighbours sit where W vanishes and the sum is W(0) alone:
+    m = rest_density * 64 pi h^3 / 315 (0.638 at h = 1)."""
+    k = int(h // spacing) + 1
+    s = 0.0
+    for i in range(-k, k + 1):
+        for j in range(-k, k + 1):
+            for l in range(-k, k + 1):
+                r2 = (i * i + j * j + l * l) * spacing * spacing
+                if r2 < h * h:
+                    s += (h * h - r2) ** 3
+    return rest_density / (315.0 / (64.0 * math.pi * h ** 9) * s)
+
+
+def pbf_params(X, Y, Z, *, radius=0.5, h=1.0, rest_density=1.0, mass=None, gravity=-9.81,
                iterations=4, s_corr_k=0.1, s_corr_n=4.0, s_corr_dq_frac=0.2, c_xsph=0.01,
                epsilon=10.0, precision=PRECISION_FP32, max_neighbors=64, use_graph=True,
                grid_mode=0) -> PbfParams:
-    """PBF-mode parameters of the benchmark scenes (dam breaks at unit spacing)."""
+    """PBF-mode parameters of the benchmark scenes (dam breaks at unit spacing).
+
+    mass defaults to rest_lattice_mass(rest_density, h, 2 radius): the
+    particles' rest lattice is then at the rest density.  A unit mass at rest
+    density 1 and h equal to the spacing would put every particle at 1.567
+    rest densities on its own, every constraint pushing outwards at rest:
+    such a dam break gains energy without bound after about 110 steps."""
     p = reference_params(X, Y, Z, radius, h / radius)
     p.mode = MODE_PBF
     p.precision = precision
     p.rest_density = rest_density
-    p.mass = mass
+    p.mass = rest_lattice_mass(rest_density, h, 2.0 * radius) if mass is None else mass
     p.gravity[0], p.gravity[1], p.gravity[2] = 0.0, gravity, 0.0
     p.relaxation_epsilon = epsilon
     p.iterations = iterations

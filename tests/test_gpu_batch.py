@@ -87,12 +87,14 @@ def test_batch_config3_shapes_run():
     conserves mass (FP64 reduction)."""
     from lustrine_gb300 import PbfSim, pbf_params, scenes
     scs = scenes.config3(num=64)
-    b = PbfSim.batch(pbf_params(8, 8, 8, iterations=4), [sc.domain for sc in scs], [sc.n for sc in scs])
+    p = pbf_params(8, 8, 8, iterations=4)
+    b = PbfSim.batch(p, [sc.domain for sc in scs], [sc.n for sc in scs])
     b.upload(np.concatenate([sc.x for sc in scs]))
     b.step(1 / 60, 3)
     assert b.status() == 0
     r = b.reduce()
-    assert abs(r["mass"] - sum(sc.n for sc in scs)) < 1e-6
+    total = sum(sc.n for sc in scs) * p.mass
+    assert abs(r["mass"] - total) <= 1e-12 * total
     x = b.positions()
     off = 0
     for sc in scs:

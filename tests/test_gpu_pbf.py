@@ -187,48 +187,50 @@ def test_graph_and_direct_launches_are_identical():
     assert np.array_equal(res[0][0], res[1][0]) and np.array_equal(res[0][1], res[1][1])
 
 
-@pytest.mark.parametrize("epsilon,steps", [(10.0, 100), (30.0, 200)])
-def test_rollout_statistics_vs_fp64_oracle(orc, epsilon, steps):
-    """The 10k dam break stepped on the GPU against the FP64 oracle run from
-    the same state: kinetic energy, centre of mass and max density error every
-    20 steps.  The flow is chaotic, so the band is set by the oracle itself:
-    the GPU must stay as close to the FP64 run as a second FP64 run started
-    from positions perturbed by 1e-6 relative (about 16 fp32 ulps) stays, or
-    within a floor of 2 % (energy), 0.02 (centre of mass, box of 40) and 3 %
-    (density error).  Config 0's own parameters (epsilon 10) over its 100
-    steps; 200 steps at epsilon 30: with h equal to the particle spacing a
-    lone particle's density is W(0) = 1.567 rest densities, so every
-    constraint pushes outwards and at epsilon 10 the FP64 run itself gains
-    energy without bound after about 110 steps."""
+def test_rollout_statistics_vs_fp64_oracle(orc):
+    """Config 0's 100 steps of the 10k dam break (collapse and splash) on the
+    GPU against the FP64 oracle.  (1) Every step from the GPU's own state: the
+    GPU's next positions and velocities against one FP64 step from the same
+    state, within 2e-5 of the box size (per second for velocities) -- the
+    chaos-free check.  (2) The free trajectories every 20 steps: kinetic
+    energy, centre of mass and max density error within twice the largest
+    deviation of three FP64 runs started from positions perturbed by 1e-6,
+    1e-5 and 1e-4 relative, or within a floor of 2 % (energy), 0.02 (centre of
+    mass, box of 40) and 3 % (density error): the flow is chaotic and the max
+    density error an extreme over 10,000 particles."""
     from lustrine_gb300 import PbfSim, scenes
     sc = scenes.config0(seed=25)
-    p = _params(sc, relaxation_epsilon=epsilon, max_neighbors=128)
+    p = _params(sc, max_neighbors=128)
     q = _oracle_params(orc, p)
+    L = max(sc.domain)
     sim = PbfSim(p, sc.n)
     sim.upload(sc.x)
     rng = np.random.default_rng(7)
-    xa = sc.x.astype(np.float64)
-    xb = xa * (1.0 + 1e-6 * rng.uniform(-1.0, 1.0, xa.shape))
-    va, vb = np.zeros((sc.n, 3)), np.zeros((sc.n, 3))
+    x0 = sc.x.astype(np.float64)
+    pert = rng.uniform(-1.0, 1.0, x0.shape)
+    runs = [(x0 * (1.0 + e * pert), np.zeros_like(x0)) for e in (0.0, 1e-6, 1e-5, 1e-4)]
+    xg, vg = sc.x, np.zeros_like(sc.x)
 
     def stats(x, v, rho):
-        return 0.5 * q.mass * (v ** 2).sum(), x.mean(0), np.abs(rho / q.rest_density - 1).max()
+        return np.array([0.5 * q.mass * (v ** 2).sum(), *x.mean(0), np.abs(rho / q.rest_density - 1).max()])
 
-    for s in range(steps):
+    for s in range(100):
+        one = orc.pbf_step(q, sc.dt, xg, vg)
         sim.step(sc.dt)
-        oa = orc.pbf_step(q, sc.dt, xa, va)
-        ob = orc.pbf_step(q, sc.dt, xb, vb)
-        xa, va, xb, vb = oa["x"], oa["v"], ob["x"], ob["v"]
+        xg, vg, _, _ = sim.download()
+        assert np.abs(xg - one["x"]).max() <= 2e-5 * L, s
+        assert np.abs(vg - one["v"]).max() <= 2e-5 * L / sc.dt, s
+        outs = [orc.pbf_step(q, sc.dt, x, v) for x, v in runs]
+        runs = [(o["x"], o["v"]) for o in outs]
         if s % 20 == 19:
             r = sim.reduce()
             assert sim.status() == 0, s
             assert abs(r["mass"] - sc.n * q.mass) < 1e-6
-            ke_a, com_a, err_a = stats(xa, va, oa["density"])
-            ke_b, com_b, err_b = stats(xb, vb, ob["density"])
-            assert abs(r["kinetic"] - ke_a) <= max(3 * abs(ke_b - ke_a), 0.02 * ke_a), s
-            assert np.abs(np.array(r["com"]) - com_a).max() <= max(3 * np.abs(com_b - com_a).max(), 0.02), s
-            assert abs(r["max_density_error"] - err_a) <= max(3 * abs(err_b - err_a), 0.03 * err_a), s
-    xg = sim.positions()
+            st = [stats(o["x"], o["v"], o["density"]) for o in outs]
+            a, spread = st[0], np.max([np.abs(b - st[0]) for b in st[1:]], axis=0)
+            g = np.array([r["kinetic"], *r["com"], r["max_density_error"]])
+            band = np.maximum(2 * spread, [0.02 * a[0], 0.02, 0.02, 0.02, 0.03 * a[4]])
+            assert (np.abs(g - a) <= band).all(), (s, g, a, band)
     assert (xg >= 0.5 - 1e-5).all() and (xg <= 39.5 + 1e-5).all()
     sim.close()
 

@@ -62,3 +62,19 @@ def test_scenes_match_config_shapes():
     assert len(counts) == 512 and counts.min() >= 1024 and counts.max() <= 65536
     s = scenes.batched_scene(1500, np.random.default_rng(0))
     assert s.n == 1500 and (s.x.max(0) < np.array(s.domain)).all()
+
+
+def test_rest_lattice_mass_puts_the_rest_lattice_at_rest_density():
+    """The PBF scenes' default mass: the poly6 density of the rest lattice
+    equals the rest density, for h at the spacing and beyond it."""
+    from lustrine_gb300 import pbf_params, rest_lattice_mass
+    for rho0, h, spacing in ((1.0, 1.0, 1.0), (1.0, 2.0, 1.0), (24.0, 1.5, 0.5)):
+        m = rest_lattice_mass(rho0, h, spacing)
+        k = np.arange(-6, 7)
+        r2 = (k[:, None, None] ** 2 + k[None, :, None] ** 2 + k[None, None, :] ** 2) * spacing ** 2
+        hd = np.clip(h * h - r2, 0.0, None)
+        rho = m * 315.0 / (64.0 * np.pi * h ** 9) * (hd ** 3).sum()
+        assert abs(rho - rho0) <= 1e-12 * rho0
+    assert abs(rest_lattice_mass(1.0, 1.0, 1.0) - 64.0 * np.pi / 315.0) < 1e-15
+    assert abs(pbf_params(40, 40, 40).mass - np.float32(64.0 * np.pi / 315.0)) == 0
+    assert pbf_params(40, 40, 40, mass=1.0).mass == 1.0
