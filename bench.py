@@ -508,7 +508,8 @@ def run_config3(steps, flush):
     """512 independent scenes (log-uniform 1,024-65,536 particles): the batched
     step (one launch per stage for all scenes, fp32 and mixed precision)
     against the plain step applied scene by scene (one context and stream per
-    scene).  Wall-clock time per step of all scenes, device synchronised,
+    scene), both with the scenes' steps overlapping on the GPU and one after
+    another.  Wall-clock time per step of all scenes, device synchronised,
     L2 flushed before each step; the equal-error condition (batched mixed
     density within 1e-4 of FP64) is asserted by tests/test_gpu_batch.py."""
     import torch
@@ -555,10 +556,22 @@ def run_config3(steps, flush):
     t = wall(step_each)
     out["plain_per_scene"] = {"value": total * 4 / t, "ms_per_step": t * 1e3,
                               "status": max(s.status() for s in sims),
-                              "launches_per_step": sum(s.launches_per_step() for s in sims)}
+                              "launches_per_step": sum(s.launches_per_step() for s in sims),
+                              "overlap": "each scene's context on its own stream: the scenes' steps overlap"}
+
+    def step_each_serial():
+        for s in sims:
+            s.step(dt)
+            s.synchronize()
+
+    t = wall(step_each_serial)
+    out["plain_serial"] = {"value": total * 4 / t, "ms_per_step": t * 1e3,
+                           "status": max(s.status() for s in sims),
+                           "overlap": "none: each scene's step completes before the next is issued"}
     for s in sims:
         s.close()
     out["batched_mixed_over_plain"] = out["batched_mixed"]["value"] / out["plain_per_scene"]["value"]
+    out["batched_mixed_over_plain_serial"] = out["batched_mixed"]["value"] / out["plain_serial"]["value"]
     return out
 
 
