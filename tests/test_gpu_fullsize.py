@@ -101,3 +101,73 @@ def test_config4_full_mixed_step_blob_vs_fp64_oracle(orc):
     rho_ref = orc.pbf_density(q, o["x"])
     rho = orc.pbf_density(q, mine)
     assert np.abs(rho - rho_ref).max() <= 1e-4 * np.abs(rho_ref).max()
+
+
+@pytest.mark.parametrize("mixed", [False, True])
+def test_config3_full_batch_step_vs_fp64_oracle(orc, mixed):
+    """All 512 scenes of config 3 in one batched step: status, FP64 mass,
+    every scene inside its box, and its smallest, median and largest scenes
+    against the oracle stepping each alone."""
+    from lustrine_gb300 import PRECISION_FP32, PRECISION_MIXED, PbfSim, pbf_params, scenes
+    scs = scenes.config3()
+    assert len(scs) == 512
+    p = pbf_params(8, 8, 8, iterations=4, precision=PRECISION_MIXED if mixed else PRECISION_FP32)
+    with PbfSim.batch(p, [sc.domain for sc in scs], [sc.n for sc in scs]) as b:
+        b.upload(np.concatenate([sc.x for sc in scs]))
+        b.step(scs[0].dt)
+        assert b.status() == 0
+        x, v, _, _ = b.download()
+        r = b.reduce()
+    total = sum(sc.n for sc in scs)
+    assert abs(r["mass"] - total * p.mass) <= 1e-9 * total * p.mass
+    off = np.concatenate([[0], np.cumsum([sc.n for sc in scs])])
+    for k, sc in enumerate(scs):
+        xs = x[off[k]:off[k + 1]]
+        assert (xs >= 0.5 - 1e-4).all() and (xs <= np.array(sc.domain) - 0.5 + 1e-4).all(), k
+    order = np.argsort([sc.n for sc in scs])
+    for k in (order[0], order[len(order) // 2], order[-1]):
+        sc = scs[k]
+        q = _oracle_params(orc, p, sc.domain)
+        o = orc.pbf_step(q, sc.dt, sc.x, np.zeros_like(sc.x))
+        L = max(sc.domain)
+        assert np.abs(x[off[k]:off[k + 1]] - o["x"]).max() <= 2e-5 * L, k
+        assert np.abs(v[off[k]:off[k + 1]] - o["v"]).max() <= 2e-5 * L / sc.dt, k
+
+
+def test_config1_reference_semantics_full_step_vs_oracle(orc):
+    """Config 1 (262,144 fluid + 50,000 static particles) under the
+    reference's own step (mode R: its cubic kernel, double self density,
+    lambda by list position, 0.01 floor snap, one pass) against the oracle's
+    restatement of that step, pinned to the compiled reference: neighbour
+    counts equal, lambdas, positions and velocities within 1e-5 relative
+    (per particle, normwise), and bitwise equal for all but a few particles
+    (the reference's powf misrounds ~0.07 % of the s_corr powers, which the
+    GPU evaluates exactly)."""
+    from conftest import phys_params
+    from lustrine_gb300 import PbfSim, reference_params, scenes
+    sc = scenes.config1()
+    p = phys_params(reference_params(*sc.domain))
+    p.max_neighbors = 64
+    with PbfSim(p, sc.n, sc.ns) as sim:
+        sim.upload(sc.x, None, sc.solid)
+        sim.step(sc.dt)
+        assert sim.status() == 0
+        x, v, lam, _ = sim.download(lambdas=True)
+        cnt, _ = sim.neighbors(cap=16)
+    q = phys_params(orc.reference_params(*sc.domain))
+    q.jacobi = 1
+    o = orc.compat_step(q, sc.dt, sc.x, np.zeros_like(sc.x), solid=sc.solid, cap=64)
+    assert np.array_equal(cnt, o["nbr_count"])
+
+    def rel(a, b):
+        a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+        nb = np.linalg.norm(b.reshape(len(b), -1), axis=1)
+        floor = 1e-3 * np.sqrt(np.mean(nb ** 2))
+        return np.linalg.norm((a - b).reshape(len(b), -1), axis=1) / np.maximum(nb, floor)
+
+    assert rel(x, o["x"]).max() <= 1e-5
+    assert rel(v, o["v"]).max() <= 1e-5
+    lo = o["lambdas"][:sc.n]
+    assert np.all(np.abs(lam - lo) <= 1e-5 * np.maximum(np.abs(lo), 1e-3 * np.abs(lo).max()))
+    same = np.mean(np.all(x == o["x"], axis=1) & np.all(v == o["v"], axis=1))
+    assert same >= 0.99, same
