@@ -433,6 +433,7 @@ def run_variants(args, flush):
     sim.close()
     out["reference_semantics_config1"] = run_reference_semantics(k, flush)
     out["sand_config1_262k"] = run_sand(k, flush)
+    out["sources_sinks_config1"] = run_sources_sinks(max(k, 10))
     out["config3_batched_vs_plain"] = run_config3(max(3, min(args.steps, 10)), flush)
     # 4,194,304 particles in a 4096 x 256 x 4096 box: 4.3e9 cells, so the
     # grid is hashed (2^23 buckets); mixed precision is the mode the box needs
@@ -501,6 +502,56 @@ def run_sand(steps, flush):
     out["cpu_baseline"] = {"value": rate, "unit": "particle-substeps/s", "cores": 1, "kind": "port",
                            "ms_per_step": t * 1e3,
                            "sample": "median of 3 single steps of the full scene from the GPU's state"}
+    return out
+
+
+def run_sources_sinks(frames):
+    """Particles entering and leaving config 1's scene on the device: each
+    frame spawns a 16 x 16 sheet of particles (a source), steps, and removes
+    the particles binned in 16 x 16 floor cells (a sink, the reference's
+    swap-remove order); the count the sink returns ends each frame on the
+    host.  Wall-clock milliseconds per frame against the same frames without
+    source and sink, and the cell-count query (Lustrine::query_cell_num_particles)
+    over the whole box and over a 16^3 region, per call."""
+    from lustrine_gb300 import PbfSim, pbf_params, scenes
+    sc = scenes.config1()
+    p = pbf_params(*sc.domain, iterations=sc.iterations, c_xsph=sc.c_xsph)
+    sheet = scenes.lattice((16, 1, 16), (104, 40, 40))
+    gx, gz = sc.domain[0] + 1, sc.domain[2] + 1
+    # floor cells beside the block (x 20-35, z 64-79), where the dam break spreads
+    sink = np.array([0 * gx * gz + x * gz + z for x in range(20, 36) for z in range(64, 80)], np.int32)
+    out = {"spawned_per_frame": len(sheet), "sink_cells": len(sink), "frames": frames}
+    for name, dynamic in (("plain", False), ("sources_sinks", True)):
+        sim = PbfSim(p, sc.n, sc.ns)
+        sim.reserve(sc.n + len(sheet) * (frames + 5))
+        sim.upload(sc.x, None, sc.solid)
+        sim.step(sc.dt, 3)
+        sim.synchronize()
+        ts, removed = [], 0
+        for _ in range(frames):
+            t0 = time.perf_counter()
+            if dynamic:
+                sim.spawn(sheet)
+            sim.step(sc.dt)
+            if dynamic:
+                removed += sim.despawn_cells(sink)
+            else:
+                sim.synchronize()
+            ts.append(time.perf_counter() - t0)
+        out[name + "_ms_per_frame"] = float(np.median(ts) * 1e3)
+        if dynamic:
+            out["removed_total"] = removed
+            out["particles_after"] = sim.n
+            out["status"] = sim.status()
+            for label, lo, hi in (("query_whole_box_us", (0, 0, 0), sc.domain),
+                                  ("query_16cube_us", (40, 8, 40), (56, 24, 56))):
+                q = []
+                for _ in range(20):
+                    t0 = time.perf_counter()
+                    sim.query_cell_count(lo, hi)
+                    q.append(time.perf_counter() - t0)
+                out[label] = float(np.median(q) * 1e6)
+        sim.close()
     return out
 
 

@@ -522,6 +522,7 @@ void lustrine_pbf::invalidate_graphs() {
     }
     pred_ready = false;  // whatever invalidates the step may change the prediction too
     tiles_dirty = true;
+    graphs_fresh = true;
 }
 
 // The tile totals a step of parity c scans (the other half is zeroed by that
@@ -902,7 +903,10 @@ static int step_impl(lustrine_pbf* s, float dt, bool tail_allowed) {
     }
     s->count_dirty = false;
     const int gi = c + (predict ? 2 : 0) + (tail ? 4 : 0);
-    if (s->prm.use_graph) {
+    // right after an invalidation, launch directly (see graphs_fresh)
+    const bool use_graph = s->prm.use_graph && !(s->graphs_fresh && !s->graph_exec[gi]);
+    s->graphs_fresh = false;
+    if (use_graph) {
         if (!s->graph_exec[gi]) {
             cudaGraph_t g = nullptr;
             CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));

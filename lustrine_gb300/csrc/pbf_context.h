@@ -102,6 +102,10 @@ struct lustrine_pbf {
     bool tiles_dirty = true;   // tile totals may hold counts of a dropped prediction
     int launches = 0;             // kernels the last step launched
     int graph_launches[8] = {};   // kernels in each captured step
+    // the step graphs were dropped since the last step: the next step runs its
+    // kernels directly and only a step after it captures, so a scene whose
+    // particle count or controls change every frame pays no capture
+    bool graphs_fresh = true;
     long long steps_done = 0;
     bool have_state = false;
     bool use_pdl = true;  // programmatic dependent launch between step kernels
