@@ -340,11 +340,14 @@ LUSTRINE_API int lustrine_pbf_profile_step(lustrine_pbf* s, float dt, double* st
                                            int* stage_launches, int num_stages);
 /* Launch shape of the PBF iteration kernels (lambda, delta-p, XSPH) and of
  * the neighbour-list build.  block and list_block: 64, 128 or 256 threads;
- * unroll: neighbour gathers in flight per thread, 1, 2, 4 or 8. */
+ * unroll: neighbour gathers in flight per thread of the lambda and delta-p
+ * passes, 1, 2, 4 or 8; xsph_unroll: the same for the XSPH pass (0 in
+ * lustrine_pbf_set_tuning: as unroll). */
 typedef struct lustrine_pbf_tuning {
     int block;
     int unroll;
     int list_block;
+    int xsph_unroll;
 } lustrine_pbf_tuning;
 LUSTRINE_API int lustrine_pbf_set_tuning(lustrine_pbf* s, const lustrine_pbf_tuning* t);
 LUSTRINE_API int lustrine_pbf_get_tuning(const lustrine_pbf* s, lustrine_pbf_tuning* t);

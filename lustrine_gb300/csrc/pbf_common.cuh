@@ -88,9 +88,10 @@ struct SandParams {
 
 // Launch shape of the PBF iteration kernels, chosen per scene by the autotuner.
 struct Tuning {
-    int block;       // threads per block of the lambda, delta and XSPH passes (64, 128, 256)
-    int unroll;      // neighbour gathers in flight per thread (1, 2, 4)
-    int list_block;  // threads per block of the list build (64, 128, 256)
+    int block;        // threads per block of the lambda, delta and XSPH passes (64, 128, 256)
+    int unroll;       // neighbour gathers in flight per thread of the lambda and delta passes (1, 2, 4, 8)
+    int list_block;   // threads per block of the list build (64, 128, 256)
+    int xsph_unroll;  // neighbour gathers in flight per thread of the XSPH pass (1, 2, 4, 8)
 };
 
 // Mixed precision: a cell's integer coordinates packed into 32 bits,

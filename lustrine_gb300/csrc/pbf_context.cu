@@ -989,9 +989,10 @@ extern "C" int lustrine_pbf_profile_step(lustrine_pbf* s, float dt, double* stag
 extern "C" int lustrine_pbf_set_tuning(lustrine_pbf* s, const lustrine_pbf_tuning* t) {
     if (!s || !t) return LUSTRINE_ERR_ARGS;
     auto ok = [](int b) { return b == 64 || b == 128 || b == 256; };
-    if (!ok(t->block) || !ok(t->list_block) || (t->unroll != 1 && t->unroll != 2 && t->unroll != 4 && t->unroll != 8))
-        return LUSTRINE_ERR_ARGS;
-    s->tune = Tuning{t->block, t->unroll, t->list_block};
+    auto ok_u = [](int u) { return u == 1 || u == 2 || u == 4 || u == 8; };
+    const int xu = t->xsph_unroll ? t->xsph_unroll : t->unroll;  // 0: as the other passes
+    if (!ok(t->block) || !ok(t->list_block) || !ok_u(t->unroll) || !ok_u(xu)) return LUSTRINE_ERR_ARGS;
+    s->tune = Tuning{t->block, t->unroll, t->list_block, xu};
     s->invalidate_graphs();
     return LUSTRINE_OK;
 }
@@ -1001,6 +1002,7 @@ extern "C" int lustrine_pbf_get_tuning(const lustrine_pbf* s, lustrine_pbf_tunin
     t->block = s->tune.block;
     t->unroll = s->tune.unroll;
     t->list_block = s->tune.list_block;
+    t->xsph_unroll = s->tune.xsph_unroll;
     return LUSTRINE_OK;
 }
 
@@ -1046,7 +1048,8 @@ static int time_candidate(lustrine_pbf* s, const Snapshot& sn, int side, float d
     int rc = snapshot_restore(s, sn, side);
     if (rc) return rc;
     // untimed steps capture the graphs the timed ones replay (both parities,
-    // with and without a prediction of their own)
+    // with and without a prediction of their own), the first one included
+    s->graphs_fresh = false;
     for (int k = 0; k < 3; k++)
         if ((rc = lustrine_pbf_step(s, dt))) return rc;
     cudaEvent_t e0, e1;
@@ -1092,7 +1095,7 @@ extern "C" int lustrine_pbf_autotune(lustrine_pbf* s, float dt, int steps, lustr
     // the iteration kernels' shape first, then the list build's block size
     for (int bi = 0; bi < 3 && !rc; bi++)
         for (int ui = 0; ui < 4 && !rc; ui++) {
-            s->tune = Tuning{blocks[bi], unrolls[ui], keep.list_block};
+            s->tune = Tuning{blocks[bi], unrolls[ui], keep.list_block, unrolls[ui]};
             s->invalidate_graphs();
             float ms = 0.0f;
             rc = time_candidate(s, sn, side, dt, steps, &ms);
@@ -1102,7 +1105,19 @@ extern "C" int lustrine_pbf_autotune(lustrine_pbf* s, float dt, int steps, lustr
             }
         }
     for (int bi = 0; bi < 3 && !rc; bi++) {
-        s->tune = Tuning{top.block, top.unroll, blocks[bi]};
+        s->tune = Tuning{top.block, top.unroll, blocks[bi], top.xsph_unroll};
+        s->invalidate_graphs();
+        float ms = 0.0f;
+        rc = time_candidate(s, sn, side, dt, steps, &ms);
+        if (!rc && ms < top_ms) {
+            top_ms = ms;
+            top = s->tune;
+        }
+    }
+    // then the XSPH pass's gathers in flight (it gains from more than the others)
+    for (int ui = 0; ui < 4 && !rc; ui++) {
+        if (unrolls[ui] == top.xsph_unroll) continue;
+        s->tune = Tuning{top.block, top.unroll, top.list_block, unrolls[ui]};
         s->invalidate_graphs();
         float ms = 0.0f;
         rc = time_candidate(s, sn, side, dt, steps, &ms);

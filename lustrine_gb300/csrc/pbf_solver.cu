@@ -1111,8 +1111,9 @@ void launch_lists_lambda(bool mixed, const Tuning& tu, const StepParams& p, cons
                          int* cnt, float* rho, int* status, cudaStream_t st) {
     if (p.n <= 0) return;
     const int B = tu.list_block <= 64 ? 64 : (tu.list_block <= 128 ? 128 : 256);
-    StepParams pp = p;  // lists padded for the chunk of the passes that read them
-    pp.pad = tu.unroll >= 8 ? 8 : (tu.unroll >= 4 ? 4 : (tu.unroll >= 2 ? 2 : 1));
+    StepParams pp = p;  // lists padded for the largest chunk of the passes that read them
+    const int u = tu.unroll > tu.xsph_unroll ? tu.unroll : tu.xsph_unroll;
+    pp.pad = u >= 8 ? 8 : (u >= 4 ? 4 : (u >= 2 ? 2 : 1));
     const bool pdl = pdl_enabled();
 #define LGB_LISTS_H(MIX, H, BB)                                                                 \
     launch_k(k_lists_lambda<MIX, H, BB>, blocks_for(p.n, BB), BB, st, pdl, pp, cp, xs, key_sorted, \
@@ -1154,7 +1155,9 @@ void launch_xsph(bool mixed, const Tuning& tu, const StepParams& p, const CellPa
                  const int* key_sorted, float4* x_out, float4* v_out, float4* xs_next, int* key,
                  int* rank, int* count, int* cellk, int* tile_count, cudaStream_t st) {
     if (p.n <= 0) return;
-    TUNE_DISPATCH(k_xsph, mixed, tu, p.n, st, p, cp, xs, v_in, nbr, cnt, key_sorted, x_out, v_out, xs_next, key,
+    Tuning tx = tu;  // the XSPH pass has its own gathers in flight
+    tx.unroll = tu.xsph_unroll;
+    TUNE_DISPATCH(k_xsph, mixed, tx, p.n, st, p, cp, xs, v_in, nbr, cnt, key_sorted, x_out, v_out, xs_next, key,
                   rank, count, cellk, tile_count);
 }
 

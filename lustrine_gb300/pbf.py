@@ -253,7 +253,7 @@ class PbfSim:
     def get_tuning(self) -> dict:
         t = _lib.PbfTuning()
         check(self.lib.lustrine_pbf_get_tuning(self.h, C.byref(t)), "get_tuning")
-        return {"block": t.block, "unroll": t.unroll, "list_block": t.list_block}
+        return {"block": t.block, "unroll": t.unroll, "list_block": t.list_block, "xsph_unroll": t.xsph_unroll}
 
     # sand mode -------------------------------------------------------------
     def set_sand_controls(self, player=None, attract=None, blow=None, attract_radius=None,
@@ -288,8 +288,8 @@ class PbfSim:
             raise ValueError(f"expected {self.n} flags, got {a.size}")
         check(self.lib.lustrine_pbf_set_attracted(self.h, a.ctypes.data), "set_attracted")
 
-    def set_tuning(self, block: int, unroll: int, list_block: int):
-        t = _lib.PbfTuning(block, unroll, list_block)
+    def set_tuning(self, block: int, unroll: int, list_block: int, xsph_unroll: int = 0):
+        t = _lib.PbfTuning(block, unroll, list_block, xsph_unroll)
         check(self.lib.lustrine_pbf_set_tuning(self.h, C.byref(t)), "set_tuning")
 
     def autotune(self, dt: float, steps: int = 3) -> tuple[dict, float]:
@@ -299,7 +299,8 @@ class PbfSim:
         ms = C.c_float()
         check(self.lib.lustrine_pbf_autotune(self.h, float(dt), int(steps), C.byref(t), C.byref(ms)),
               "autotune")
-        return {"block": t.block, "unroll": t.unroll, "list_block": t.list_block}, float(ms.value)
+        return ({"block": t.block, "unroll": t.unroll, "list_block": t.list_block, "xsph_unroll": t.xsph_unroll},
+                float(ms.value))
 
     STAGES = ("predict", "scan", "sort", "lists", "lambda", "delta", "xsph")
 

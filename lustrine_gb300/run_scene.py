@@ -2,7 +2,7 @@
 statistics.
 
     python -m lustrine_gb300.run_scene --config config2 --steps 5 [--mixed] [--no-graph]
-        [--grid auto|dense|hashed] [--stages] [--shape block,unroll,list_block] [--sand]
+        [--grid auto|dense|hashed] [--stages] [--shape block,unroll,list_block[,xsph_unroll]] [--sand]
 
 --sand steps the scene's particles with simulate_sand's semantics (sand mode)
 instead of the PBF step.
@@ -29,7 +29,7 @@ def main(argv=None):
     ap.add_argument("--grid", default="auto", choices=["auto", "dense", "hashed"])
     ap.add_argument("--stages", action="store_true", help="also print per-stage device ms")
     ap.add_argument("--shape", default=None,
-                    help="launch shape block,unroll,list_block (default: the library's)")
+                    help="launch shape block,unroll,list_block[,xsph_unroll] (default: the library's)")
     ap.add_argument("--sand", action="store_true", help="the sand step (simulate_sand semantics)")
     a = ap.parse_args(argv)
     sc = getattr(scenes, a.config)()
