@@ -396,10 +396,28 @@ def run_e2e(sim, sc, args, ext):
         # buffers and waits: the host holds the step's result
         sim.step_host(sc.dt, x.data_ptr(), v.data_ptr())
     dt_wall = (time.perf_counter() - t0) / steps
+    # the reference wrapper's frame (simulate, then simulation_bind_positions_copy):
+    # the state stays on the device, the positions come to the host every step
+    sim.synchronize()
+    for _ in range(2):
+        sim.step(sc.dt)
+        sim.download_state_async(x.data_ptr(), None)
+        sim.synchronize()
+    t1 = time.perf_counter()
+    for _ in range(steps):
+        sim.step(sc.dt)
+        sim.download_state_async(x.data_ptr(), None)
+        sim.synchronize()
+    frame = (time.perf_counter() - t1) / steps
     return {"value": n * sim.params.iterations / dt_wall, "unit": UNIT,
             "h2d_bytes_per_step": 2 * 12 * n, "d2h_bytes_per_step": 2 * 12 * n,
             "ms_per_step": dt_wall * 1e3,
-            "path": "lustrine_pbf_step_host (page-locked host buffers, read and written by the kernels)"}
+            "path": "lustrine_pbf_step_host (page-locked host buffers, read and written by the kernels)",
+            "positions_out_frame": {"value": n * sim.params.iterations / frame, "ms_per_step": frame * 1e3,
+                                    "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 12 * n,
+                                    "path": "state resident on the device, positions to page-locked host "
+                                            "memory every step (the reference wrapper's simulate + "
+                                            "simulation_bind_positions_copy frame)"}}
 
 
 def run_variants(args, flush):
