@@ -78,3 +78,20 @@ def test_rest_lattice_mass_puts_the_rest_lattice_at_rest_density():
     assert abs(rest_lattice_mass(1.0, 1.0, 1.0) - 64.0 * np.pi / 315.0) < 1e-15
     assert abs(pbf_params(40, 40, 40).mass - np.float32(64.0 * np.pi / 315.0)) == 0
     assert pbf_params(40, 40, 40, mass=1.0).mass == 1.0
+
+
+def _header_struct_fields(name):
+    text = open(os.path.join(ROOT, "include", "lustrine_gb300.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    body = re.search(r"typedef struct " + name + r"\s*\{(.*?)\}\s*" + name + ";", text, re.S).group(1)
+    return [re.findall(r"(\w+)\s*(?:\[\d+\])?\s*;", d)[0] for d in body.split(";") if d.strip()
+            for d in [d + ";"]]
+
+
+def test_ctypes_structs_follow_the_header():
+    """The Python host side's ctypes structs list the header's fields in the
+    header's order (the launch shape, the sand controls)."""
+    from lustrine_gb300._lib import PbfTuning, SandControls
+    for cls, name in ((PbfTuning, "lustrine_pbf_tuning"), (SandControls, "lustrine_sand_controls")):
+        assert [f[0] for f in cls._fields_] == _header_struct_fields(name), name
+    assert C.sizeof(PbfTuning) == 16
