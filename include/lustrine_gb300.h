@@ -46,7 +46,8 @@ enum {
     LUSTRINE_ERR_NO_SIMULATION = 7,  /* wrapper call before init_simulation */
     LUSTRINE_ERR_TIMEOUT = 8,        /* a bounded device wait gave up */
     LUSTRINE_ERR_BAD_VALUE = 9,      /* non-finite particle state */
-    LUSTRINE_ERR_TOO_LARGE = 10      /* input larger than a fixed-scratch entry point's limit */
+    LUSTRINE_ERR_TOO_LARGE = 10      /* input larger than a fixed limit (a no-allocation entry
+                                        point's scratch, or a context's reserved capacity) */
 };
 
 enum {
@@ -105,8 +106,9 @@ typedef struct GridWrapper {
 
 /* LustrineWrapper.hpp:86-94 / LustrineWrapper.cpp:165-221.  Builds the scene
  * with the reference's init_simulation layout (kernel radius 3.1 r, solid
- * cells whose value is 1 masked out, Lustrine.cpp:188,253) and selects the
- * GPU fluid step in reference mode. */
+ * cells whose value is 1 masked out, Lustrine.cpp:188,253).  The step after
+ * init is the sand step (simulate_sand, as the reference's init selects,
+ * Lustrine.cpp:72,312); set_simulate_function(2) or (3) selects a fluid step. */
 LUSTRINE_API void init_simulation(const SimulationParameters* parameters, SimulationData* data,
                                   GridWrapper* sand_grids, int num_sand_grids,
                                   GridWrapper* solid_grids, int num_solid_grids, int subdivision);
@@ -118,12 +120,18 @@ LUSTRINE_API void init_simulation_extra_parameters(const SimulationParameters* p
                                                    int num_sand_grids, GridWrapper* solid_grids,
                                                    int num_solid_grids, int subdivision,
                                                    float kernel_radius_scale, int with_credits);
-/* LustrineWrapper.cpp:343-351: one step of the selected fluid step.  The
- * attract/blow flags drive the sand solver only and are ignored. */
+/* LustrineWrapper.cpp:343-351: one frame of the selected step (sources, the
+ * step, sinks, as Lustrine::simulate).  The attract/blow flags are kept for
+ * later simulate_no_flags calls; the sand step reads them (attract towards and
+ * blow away from the player, Simulate.cpp:187-209), the fluid steps do not. */
 LUSTRINE_API void simulate(float dt, bool attract_flag, bool blow_flag);
 LUSTRINE_API void simulate_no_flags(float dt);
-/* LustrineWrapper.cpp:377-379: copies 3 * num_sand_particles floats (particle
- * positions in the order init_simulation created them).  Synchronises. */
+/* LustrineWrapper.cpp:377-379: copies 3 * num_sand_particles floats of
+ * particle positions.  Order: after a sand step, the order of that step's cell
+ * sort (the reference's sand step re-orders its particle arrays by cell every
+ * step, Neighbors.cpp:296-300, and returns them in that order); after a fluid
+ * step, the order init_simulation created them in (sources append).
+ * Synchronises. */
 LUSTRINE_API void simulation_bind_positions_copy(float* position_ptr);
 /* LustrineWrapper.cpp:353-375 */
 LUSTRINE_API void cleanup_simulation(void);
@@ -167,6 +175,63 @@ LUSTRINE_API void set_simulate_function(int index);
 /* The player's position read by the sand step's attract and blow
  * (the reference takes it from its Bullet world; new entry point). */
 LUSTRINE_API void lustrine_set_player_position(Vec3 position);
+/* LustrineWrapper.hpp:158 / LustrineWrapper.cpp:505-511: radii and
+ * coefficients of the sand step's attract and blow forces (defaults 1.5, 2,
+ * 1000, 500, Simulation.hpp), kept until the next call. */
+LUSTRINE_API void set_attract_blow_parameters(float attract_radius, float blow_radius,
+                                              float attract_coeff, float blow_coeff);
+
+/* LustrineWrapper.hpp:76-79 */
+typedef struct BindingString {
+    int64_t length;
+    char* data;
+} BindingString;
+/* LustrineWrapper.hpp:120-121 / LustrineWrapper.cpp:381-393.  read_vox_scene
+ * (a .vox scene graph as JSON for the game; no particle data) is not built:
+ * it returns an empty string (length 0, data NULL) and records
+ * LUSTRINE_ERR_UNSUPPORTED.  free_string releases a string's data. */
+LUSTRINE_API void read_vox_scene(BindingString* data, const uint8_t* buffer, int64_t size);
+LUSTRINE_API void free_string(BindingString* data);
+/* LustrineWrapper.hpp:187-188 / LustrineWrapper.cpp:713-719: allocate and
+ * release a 10^9-byte host block (the reference's allocator probe);
+ * LUSTRINE_ERR_NOMEM when the allocation fails. */
+LUSTRINE_API void test_allocate_1gb(void);
+LUSTRINE_API void test_deallocate_1gb(void);
+/* The Bullet rigid-body world and the player (LustrineWrapper.hpp:132-157,
+ * 173-182): not part of this library (they never change particle state, the
+ * fluid and sand steps take the player's position as an input instead).  Each
+ * records LUSTRINE_ERR_UNSUPPORTED and returns zero (check_collisions sets
+ * *size to 0), so a binding that declares them loads and runs. */
+LUSTRINE_API Vec3 get_gravity(void);
+LUSTRINE_API void set_gravity(Vec3 new_gravity);
+LUSTRINE_API int add_box(Vec3 position, bool is_dynamic, Vec3 half_dimensions);
+LUSTRINE_API int add_capsule(Vec3 position, float radius, float height);
+LUSTRINE_API int add_detector_block(Vec3 position, Vec3 half_dims);
+LUSTRINE_API int check_collision(int body1, int body2);
+LUSTRINE_API int do_collide(int body);
+LUSTRINE_API int do_collide_except_for(int body, int exception_id);
+LUSTRINE_API void check_collisions(int body, int* indices, int* size);
+LUSTRINE_API int get_num_bodies(void);
+LUSTRINE_API void apply_impulse(int body, Vec3 impulse, Vec3 relative_pos);
+LUSTRINE_API Vec3 get_position(int body);
+LUSTRINE_API Vec3 get_velocity(int body);
+LUSTRINE_API void set_velocity(int body, Vec3 velocity);
+LUSTRINE_API void set_position(int body, Vec3 position);
+LUSTRINE_API void add_velocity(int body, Vec3 velocity);
+LUSTRINE_API void set_body_no_rotation(int body);
+LUSTRINE_API void set_body_frixion(int body, float frixion);
+LUSTRINE_API float get_body_frixion(int body);
+LUSTRINE_API void set_body_damping(int body, float linear, float angular);
+LUSTRINE_API float get_body_damping(int body);
+LUSTRINE_API void set_player_id(int id);
+LUSTRINE_API void set_player_box_scale(Vec3 scale);
+LUSTRINE_API int is_grounded(int id);
+LUSTRINE_API void set_body_gravity(int id, Vec3 gravity);
+LUSTRINE_API void set_body_no_collision_response(int id);
+LUSTRINE_API int collide_with_player(int id);
+LUSTRINE_API void enable_particles_bounding_boxes(void);
+LUSTRINE_API void disable_particles_bounding_boxes(void);
+LUSTRINE_API void set_player_particles_bounding_spheres_radius_placement(float radius);
 
 /* Outcome of the last layer-1 call (LUSTRINE_OK or an error code). */
 LUSTRINE_API int lustrine_last_status(void);
@@ -413,8 +478,9 @@ LUSTRINE_API int lustrine_counting_sort(int* counts, const int* keys, size_t num
  * until the process exits.  Limits: num_positions <= LUSTRINE_NOALLOC_MAX_KEYS
  * and num_cells <= LUSTRINE_NOALLOC_MAX_CELLS, else LUSTRINE_ERR_TOO_LARGE.
  * The first call on a device looks up the array's device address (make it
- * before any stream capture).  All calls share the array: calls that overlap
- * on the GPU race.  Same arguments, results and synchronisation as
+ * before any stream capture) and keeps it for that device's context: do not
+ * call this entry point again in a process after cudaDeviceReset of that
+ * device.  All calls share the array: calls that overlap on the GPU race.  Same arguments, results and synchronisation as
  * lustrine_counting_sort. */
 #define LUSTRINE_NOALLOC_MAX_KEYS (1 << 20)
 #define LUSTRINE_NOALLOC_MAX_CELLS (1 << 20)

@@ -62,6 +62,10 @@ class GridWrapper(C.Structure):
                 ("num_occupied_grid_cells", C.c_int), ("type", C.c_int)]
 
 
+class BindingString(C.Structure):
+    _fields_ = [("length", C.c_int64), ("data", C.c_char_p)]
+
+
 class PbfParams(C.Structure):
     _fields_ = [("mode", C.c_int), ("precision", C.c_int), ("domain", C.c_int * 3),
                 ("particle_radius", C.c_float), ("kernel_radius", C.c_float),
@@ -123,6 +127,42 @@ SIGNATURES = {
     "lustrine_free_grid": (None, [C.POINTER(GridWrapper)]),
     "init_grid_magikavoxel": (None, [C.POINTER(GridWrapper), C.c_char_p, Vec3]),
     "create_grid": (None, [C.POINTER(GridWrapper), C.c_wchar_p, C.c_int, C.c_int]),
+    "set_attract_blow_parameters": (None, [C.c_float, C.c_float, C.c_float, C.c_float]),
+    "read_vox_scene": (None, [C.POINTER(BindingString), _P, C.c_int64]),
+    "free_string": (None, [C.POINTER(BindingString)]),
+    "test_allocate_1gb": (None, []),
+    "test_deallocate_1gb": (None, []),
+    # the Bullet world and the player: not built (each records LUSTRINE_ERR_UNSUPPORTED)
+    "get_gravity": (Vec3, []),
+    "set_gravity": (None, [Vec3]),
+    "add_box": (C.c_int, [Vec3, C.c_bool, Vec3]),
+    "add_capsule": (C.c_int, [Vec3, C.c_float, C.c_float]),
+    "add_detector_block": (C.c_int, [Vec3, Vec3]),
+    "check_collision": (C.c_int, [C.c_int, C.c_int]),
+    "do_collide": (C.c_int, [C.c_int]),
+    "do_collide_except_for": (C.c_int, [C.c_int, C.c_int]),
+    "check_collisions": (None, [C.c_int, _IP, _IP]),
+    "get_num_bodies": (C.c_int, []),
+    "apply_impulse": (None, [C.c_int, Vec3, Vec3]),
+    "get_position": (Vec3, [C.c_int]),
+    "get_velocity": (Vec3, [C.c_int]),
+    "set_velocity": (None, [C.c_int, Vec3]),
+    "set_position": (None, [C.c_int, Vec3]),
+    "add_velocity": (None, [C.c_int, Vec3]),
+    "set_body_no_rotation": (None, [C.c_int]),
+    "set_body_frixion": (None, [C.c_int, C.c_float]),
+    "get_body_frixion": (C.c_float, [C.c_int]),
+    "set_body_damping": (None, [C.c_int, C.c_float, C.c_float]),
+    "get_body_damping": (C.c_float, [C.c_int]),
+    "set_player_id": (None, [C.c_int]),
+    "set_player_box_scale": (None, [Vec3]),
+    "is_grounded": (C.c_int, [C.c_int]),
+    "set_body_gravity": (None, [C.c_int, Vec3]),
+    "set_body_no_collision_response": (None, [C.c_int]),
+    "collide_with_player": (C.c_int, [C.c_int]),
+    "enable_particles_bounding_boxes": (None, []),
+    "disable_particles_bounding_boxes": (None, []),
+    "set_player_particles_bounding_spheres_radius_placement": (None, [C.c_float]),
     # layer 2: context API
     "lustrine_pbf_params_reference": (None, [C.POINTER(PbfParams), C.c_int, C.c_int, C.c_int,
                                              C.c_float, C.c_float]),

@@ -13,6 +13,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <new>
 #include <string>
 #include <vector>
 
@@ -517,6 +518,112 @@ void set_simulate_function(int index) {
     p.mode = index == 0 ? LUSTRINE_MODE_SAND : index == 2 ? LUSTRINE_MODE_REFERENCE : LUSTRINE_MODE_PBF;
     g_status = lustrine_pbf_set_params(g_ctx, &p);
 }
+
+// LustrineWrapper.cpp:505-511: radii and coefficients of the sand step's
+// attract and blow forces (Simulate.cpp:187-209), kept by the context until
+// the next call
+void set_attract_blow_parameters(float attract_radius, float blow_radius, float attract_coeff,
+                                 float blow_coeff) {
+    if (!g_ctx) {
+        g_status = LUSTRINE_ERR_NO_SIMULATION;
+        return;
+    }
+    lustrine_sand_controls c;
+    lustrine_pbf_get_sand_controls(g_ctx, &c);
+    c.attract_radius = attract_radius;
+    c.blow_radius = blow_radius;
+    c.attract_coeff = attract_coeff;
+    c.blow_coeff = blow_coeff;
+    g_status = lustrine_pbf_set_sand_controls(g_ctx, &c);
+}
+
+// LustrineWrapper.cpp:381-393.  The scene graph of a .vox file as JSON is
+// not produced (it carries no particle data): the string comes back empty.
+void read_vox_scene(BindingString* data, const uint8_t* buffer, int64_t size) {
+    (void)buffer;
+    (void)size;
+    if (data) {
+        data->length = 0;
+        data->data = nullptr;
+    }
+    g_status = LUSTRINE_ERR_UNSUPPORTED;
+}
+
+void free_string(BindingString* data) {
+    if (data) {
+        delete[] data->data;
+        data->length = 0;
+        data->data = nullptr;
+    }
+    g_status = LUSTRINE_OK;
+}
+
+// LustrineWrapper.cpp:713-719: a host allocation of 10^9 bytes held until
+// test_deallocate_1gb (the reference's probe of the host allocator).
+static char* g_test_block = nullptr;
+
+void test_allocate_1gb(void) {
+    if (!g_test_block) g_test_block = new (std::nothrow) char[1000000000];
+    g_status = g_test_block ? LUSTRINE_OK : LUSTRINE_ERR_NOMEM;
+}
+
+void test_deallocate_1gb(void) {
+    delete[] g_test_block;
+    g_test_block = nullptr;
+    g_status = LUSTRINE_OK;
+}
+
+// The Bullet rigid-body world and the player (LustrineWrapper.hpp:132-157,
+// 173-182) are not part of this library: every call records
+// LUSTRINE_ERR_UNSUPPORTED and returns zero values, so a binding that
+// declares them loads and runs.
+static Vec3 unsupported_vec3() {
+    g_status = LUSTRINE_ERR_UNSUPPORTED;
+    return Vec3{0.0f, 0.0f, 0.0f};
+}
+static int unsupported_int() {
+    g_status = LUSTRINE_ERR_UNSUPPORTED;
+    return 0;
+}
+static float unsupported_float() {
+    g_status = LUSTRINE_ERR_UNSUPPORTED;
+    return 0.0f;
+}
+
+Vec3 get_gravity(void) { return unsupported_vec3(); }
+void set_gravity(Vec3) { unsupported_int(); }
+int add_box(Vec3, bool, Vec3) { return unsupported_int(); }
+int add_capsule(Vec3, float, float) { return unsupported_int(); }
+int add_detector_block(Vec3, Vec3) { return unsupported_int(); }
+int check_collision(int, int) { return unsupported_int(); }
+int do_collide(int) { return unsupported_int(); }
+int do_collide_except_for(int, int) { return unsupported_int(); }
+void check_collisions(int, int* indices, int* size) {
+    (void)indices;
+    if (size) *size = 0;
+    unsupported_int();
+}
+int get_num_bodies(void) { return unsupported_int(); }
+void apply_impulse(int, Vec3, Vec3) { unsupported_int(); }
+Vec3 get_position(int) { return unsupported_vec3(); }
+Vec3 get_velocity(int) { return unsupported_vec3(); }
+void set_velocity(int, Vec3) { unsupported_int(); }
+void set_position(int, Vec3) { unsupported_int(); }
+void add_velocity(int, Vec3) { unsupported_int(); }
+void set_body_no_rotation(int) { unsupported_int(); }
+void set_body_frixion(int, float) { unsupported_int(); }
+float get_body_frixion(int) { return unsupported_float(); }
+void set_body_damping(int, float, float) { unsupported_int(); }
+float get_body_damping(int) { return unsupported_float(); }
+void set_player_id(int) { unsupported_int(); }
+void set_player_box_scale(Vec3) { unsupported_int(); }
+int is_grounded(int) { return unsupported_int(); }
+void set_body_gravity(int, Vec3) { unsupported_int(); }
+void set_body_no_collision_response(int) { unsupported_int(); }
+int collide_with_player(int) { return unsupported_int(); }
+void enable_particles_bounding_boxes(void) { unsupported_int(); }
+void disable_particles_bounding_boxes(void) { unsupported_int(); }
+void set_player_particles_bounding_spheres_radius_placement(float) { unsupported_int(); }
 
 int lustrine_last_status(void) { return g_status; }
 

@@ -8,6 +8,17 @@
 namespace lgb {
 
 // pbf_sort.cu
+// Scan of the standalone sort entry points: tiles of SCAN_TILE cells, one
+// block each (reduce / scan of the tile sums / down-sweep).
+constexpr int SCAN_THREADS = 256;
+constexpr int SCAN_ITEMS = 8;
+constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+constexpr size_t scan_block_sums_ints(size_t C) { return (C + SCAN_TILE - 1) / SCAN_TILE + 1; }
+// Scratch of the standalone counting sort: count[C], the scan's tile sums,
+// key[n], rank[n] (also the big cells' merge space), tmp[n], status.
+constexpr size_t counting_sort_scratch_ints_for(size_t n, size_t C) {
+    return C + scan_block_sums_ints(C) + 3 * n + 1;
+}
 // exclusive scan count -> start (C + 1 entries); zeroes count behind it
 void launch_scan(int* count, int C, int* block_sums, int* start, cudaStream_t st);
 int scan_block_sums_size(int C);
@@ -21,7 +32,8 @@ int cell_scan_tiles(int C);
 void launch_scan_tiles(int* count, int C, int* tile_sum, int* start, cudaStream_t st, bool counted = false,
                        int* tile_zero = nullptr);
 int scan_tiles_launches(int C, bool counted = false);
-void launch_sort_tail(const int* key, const int* rank, const int* start, const int* tie, int n,
+// rank doubles as merge space for cells of more than a few dozen particles
+void launch_sort_tail(const int* key, int* rank, const int* start, const int* tie, int n,
                       int* tmp, int* perm, cudaStream_t st);
 void launch_gather_state(const int* perm, int n, const int* key, const float4* x, const float4* xs,
                          const float4* v, const int* id, int* key_out, float4* x_out,
@@ -46,7 +58,7 @@ void launch_counting_sort(const int* keys, int n, int num_cells, CountingSortScr
 // index scatter + stabilisation fused with the reorder of the particle state
 // (v may be nullptr: not carried; aux: an optional int per particle carried
 // into the new order, e.g. the packed cells of a hashed grid)
-void launch_sort_state(const int* key, const int* rank, const int* start, const int* tie, int n,
+void launch_sort_state(const int* key, int* rank, const int* start, const int* tie, int n,
                        int* tmp, const float4* x, const float4* xs, const float4* v, const int* id,
                        int* key_out, float4* x_out, float4* xs_out, float4* v_out, int* id_out,
                        const int* aux, int* aux_out, int* slot_of, cudaStream_t st);

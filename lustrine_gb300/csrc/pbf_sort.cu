@@ -12,11 +12,16 @@
 //      reduce / scan of the tile sums / down-sweep; the scan also zeroes
 //      count for the next step's histogram;
 //   3. scatter of particle indices to start[key] + rank;
-//   4. stabilisation: atomic arrival order is arbitrary, so each slot counts
-//      the members of its cell with a smaller tie key (previous slot, or the
-//      caller's id in compat mode) and moves to that rank -- the result is
-//      the stable order of the reference's counting sort -- and the particle
-//      state is gathered into that slot in the same kernel.
+//   4. stabilisation: atomic arrival order is arbitrary, so every cell's
+//      members are put in the order of a tie key (previous slot, or the
+//      caller's id in compat mode) -- the result is the stable order of the
+//      reference's counting sort -- and the particle state is gathered into
+//      the final slot in the same kernel.  A member of a cell of at most
+//      SMALL_CELL particles counts the members with a smaller tie key (O(k)
+//      per particle); a larger cell is sorted by the block holding its first
+//      slot: a bitonic sort in shared memory up to SORT_CAP members, beyond
+//      that sorted runs of SORT_CAP merged pairwise through the rank array
+//      (free once the scatter has read it) -- O(k log k) for a cell of k.
 #include "pbf_common.cuh"
 #include "pbf_kernels.h"
 
@@ -27,10 +32,6 @@ thread_local bool t_pdl = false;
 }
 void set_pdl(bool on) { t_pdl = on; }
 bool pdl_enabled() { return t_pdl; }
-
-constexpr int SCAN_THREADS = 256;
-constexpr int SCAN_ITEMS = 8;
-constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
 
 __device__ __forceinline__ int warp_inclusive_scan(int v) {
     const int lane = threadIdx.x & 31;
@@ -237,55 +238,174 @@ __global__ void k_scatter_index(const int* __restrict__ key, const int* __restri
     if (i < n) tmp[start[key[i]] + rank[i]] = i;
 }
 
-__global__ void k_stabilize(const int* __restrict__ tmp, const int* __restrict__ key,
-                            const int* __restrict__ start, const int* __restrict__ tie, int n,
-                            int* __restrict__ perm) {
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= n) return;
-    const int i = tmp[s];
-    const int c = key[i];
-    const int a = start[c], b = start[c + 1];
-    const int mine = tie ? tie[i] : i;
-    int r = 0;
-    for (int t = a; t < b; t++) {
-        int o = tmp[t];
-        int ot = tie ? tie[o] : o;
-        r += ot < mine;
+// ------------------------------------------------------- stabilisation --
+
+constexpr int STAB_THREADS = 256;
+constexpr int SMALL_CELL = 32;   // cells up to this size: O(k) rank per member
+constexpr int SORT_CAP = 2048;   // members a block sorts in shared memory at once
+constexpr int MAX_BIG_PER_BLOCK = STAB_THREADS / (SMALL_CELL + 1) + 1;
+
+__device__ __forceinline__ int tie_of(const int* __restrict__ tie, int e) { return tie ? tie[e] : e; }
+
+// Bitonic sort of N (a power of two <= SORT_CAP) (tie, element) pairs in
+// shared memory, ascending by tie (ties are distinct; pads carry INT_MAX).
+__device__ __forceinline__ void bitonic_sort_smem(int* kk, int* vv, int N) {
+    for (int size = 2; size <= N; size <<= 1) {
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            for (int t = threadIdx.x; t < N / 2; t += blockDim.x) {
+                const int lo = 2 * stride * (t / stride) + (t % stride);
+                const int hi = lo + stride;
+                const bool up = (lo & size) == 0;
+                const int a = kk[lo], b = kk[hi];
+                if ((a > b) == up) {
+                    kk[lo] = b;
+                    kk[hi] = a;
+                    const int x = vv[lo];
+                    vv[lo] = vv[hi];
+                    vv[hi] = x;
+                }
+            }
+            __syncthreads();
+        }
     }
-    perm[a + r] = i;
+}
+
+// Number of elements of run A (length la) that precede output position q of
+// the merge of A and B (length lb), both ascending by tie; A first on equal
+// ties (ties are distinct, so that never happens).
+__device__ __forceinline__ int merge_split(const int* __restrict__ A, int la, const int* __restrict__ B,
+                                           int lb, int q, const int* __restrict__ tie) {
+    int lo = max(0, q - lb), hi = min(q, la);
+    while (lo < hi) {
+        const int m = (lo + hi) >> 1;  // m elements of A and q - m of B before q?
+        if (tie_of(tie, A[m]) < tie_of(tie, B[q - m - 1]))
+            lo = m + 1;
+        else
+            hi = m;
+    }
+    return lo;
+}
+
+// Sorts the k members of the cell at slots [a, a + k) of buf (element ids in
+// arrival order) by tie; returns the buffer (buf or aux) holding the sorted
+// members at [a, a + k).  All threads of the block call it.
+__device__ int* sort_cell(int* __restrict__ buf, int* __restrict__ aux, int a, int k,
+                          const int* __restrict__ tie, int* kk, int* vv) {
+    // runs of SORT_CAP sorted in shared memory, written back in place
+    for (int c0 = 0; c0 < k; c0 += SORT_CAP) {
+        const int m = min(SORT_CAP, k - c0);
+        int N = 64;
+        while (N < m) N <<= 1;
+        for (int t = threadIdx.x; t < N; t += blockDim.x) {
+            const int e = t < m ? buf[a + c0 + t] : -1;
+            kk[t] = t < m ? tie_of(tie, e) : 0x7fffffff;
+            vv[t] = e;
+        }
+        __syncthreads();
+        bitonic_sort_smem(kk, vv, N);
+        for (int t = threadIdx.x; t < m; t += blockDim.x) buf[a + c0 + t] = vv[t];
+        __syncthreads();
+    }
+    // pairwise merges of sorted runs, ping-ponging between buf and aux; each
+    // thread merges one contiguous stretch of the output from its split
+    int* src = buf;
+    int* dst = aux;
+    for (int w = SORT_CAP; w < k; w <<= 1) {
+        for (int lo = 0; lo < k; lo += 2 * w) {
+            const int la = min(w, k - lo), lb = max(0, min(w, k - lo - w));
+            const int len = la + lb;
+            const int* A = src + a + lo;
+            const int* B = A + la;
+            int* O = dst + a + lo;
+            const int per = (len + blockDim.x - 1) / blockDim.x;
+            const int q0 = min(len, (int)threadIdx.x * per), q1 = min(len, q0 + per);
+            if (q0 < q1) {
+                int i = merge_split(A, la, B, lb, q0, tie), j = q0 - i;
+                for (int q = q0; q < q1; q++) {
+                    const bool takeA = j >= lb || (i < la && tie_of(tie, A[i]) < tie_of(tie, B[j]));
+                    O[q] = takeA ? A[i++] : B[j++];
+                }
+            }
+        }
+        __syncthreads();
+        int* t = src;
+        src = dst;
+        dst = t;
+    }
+    return src;
+}
+
+// Final slot of the member at slot s of a small cell (k <= SMALL_CELL):
+// a + the number of members with a smaller tie.
+__device__ __forceinline__ int small_rank(const int* __restrict__ tmp, const int* __restrict__ tie, int a, int b,
+                                          int mine) {
+    int r = 0;
+    for (int t = a; t < b; t++) r += tie_of(tie, tmp[t]) < mine;
+    return r;
+}
+
+// The stabilisation of one block of slots.  emit(f, i): element i goes to
+// slot f.  Small cells are placed per slot; every big cell whose first slot
+// is in this block's range is sorted by the whole block (the other blocks
+// skip its members).
+template <class Emit>
+__device__ __forceinline__ void stabilize_block(int* __restrict__ tmp, int* __restrict__ aux,
+                                                const int* __restrict__ key, const int* __restrict__ start,
+                                                const int* __restrict__ tie, int n, Emit&& emit) {
+    __shared__ int kk[SORT_CAP], vv[SORT_CAP];
+    __shared__ int big_a[MAX_BIG_PER_BLOCK], big_k[MAX_BIG_PER_BLOCK];
+    __shared__ int num_big;
+    if (threadIdx.x == 0) num_big = 0;
+    __syncthreads();
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < n) {
+        const int i = tmp[s];
+        const int c = key[i];
+        const int a = start[c], b = start[c + 1];
+        if (b - a <= SMALL_CELL) {
+            emit(a + small_rank(tmp, tie, a, b, tie_of(tie, i)), i);
+        } else if (s == a) {
+            const int q = atomicAdd(&num_big, 1);
+            big_a[q] = a;
+            big_k[q] = b - a;
+        }
+    }
+    __syncthreads();
+    for (int q = 0; q < num_big; q++) {
+        const int a = big_a[q], k = big_k[q];
+        const int* sorted = sort_cell(tmp, aux, a, k, tie, kk, vv);
+        for (int p = threadIdx.x; p < k; p += blockDim.x) emit(a + p, sorted[a + p]);
+        __syncthreads();
+    }
+}
+
+// Standalone sort: perm[final slot] = element.  aux: n ints of merge space.
+__global__ void __launch_bounds__(STAB_THREADS) k_stabilize(int* __restrict__ tmp, int* __restrict__ aux,
+                                                            const int* __restrict__ key,
+                                                            const int* __restrict__ start,
+                                                            const int* __restrict__ tie, int n,
+                                                            int* __restrict__ perm) {
+    stabilize_block(tmp, aux, key, start, tie, n, [&](int f, int i) { perm[f] = i; });
 }
 
 // Stabilisation fused with the reorder: the slot found for particle i
 // receives its state directly (no permutation array round trip).
-__global__ void k_stabilize_gather(const int* __restrict__ tmp, const int* __restrict__ key,
-                                   const int* __restrict__ start, const int* __restrict__ tie, int n,
-                                   const float4* __restrict__ x, const float4* __restrict__ xs,
-                                   const float4* __restrict__ v, const int* __restrict__ id,
-                                   int* __restrict__ key_out, float4* __restrict__ x_out,
-                                   float4* __restrict__ xs_out, float4* __restrict__ v_out,
-                                   int* __restrict__ id_out, const int* __restrict__ aux,
-                                   int* __restrict__ aux_out, int* __restrict__ slot_of) {
+__global__ void __launch_bounds__(STAB_THREADS) k_stabilize_gather(
+    int* __restrict__ tmp, int* __restrict__ aux, const int* __restrict__ key, const int* __restrict__ start,
+    const int* __restrict__ tie, int n, const float4* __restrict__ x, const float4* __restrict__ xs,
+    const float4* __restrict__ v, const int* __restrict__ id, int* __restrict__ key_out,
+    float4* __restrict__ x_out, float4* __restrict__ xs_out, float4* __restrict__ v_out, int* __restrict__ id_out,
+    const int* __restrict__ aux_in, int* __restrict__ aux_out, int* __restrict__ slot_of) {
     pdl_wait();
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= n) return;
-    const int i = tmp[s];
-    const int c = key[i];
-    const int a = start[c], b = start[c + 1];
-    const int mine = tie ? tie[i] : i;
-    int r = 0;
-    for (int t = a; t < b; t++) {
-        int o = tmp[t];
-        int ot = tie ? tie[o] : o;
-        r += ot < mine;
-    }
-    const int f = a + r;
-    key_out[f] = c;
-    x_out[f] = x[i];
-    xs_out[f] = xs[i];
-    if (v) v_out[f] = v[i];
-    if (id) id_out[f] = id[i];
-    if (aux) aux_out[f] = aux[i];
-    if (slot_of) slot_of[id[i]] = f;  // the caller index's new slot (state downloads)
+    stabilize_block(tmp, aux, key, start, tie, n, [&](int f, int i) {
+        key_out[f] = key[i];
+        x_out[f] = x[i];
+        xs_out[f] = xs[i];
+        if (v) v_out[f] = v[i];
+        if (id) id_out[f] = id[i];
+        if (aux_in) aux_out[f] = aux_in[i];
+        if (slot_of) slot_of[id[i]] = f;  // the caller index's new slot (state downloads)
+    });
 }
 
 __global__ void k_gather_int(const int* __restrict__ perm, int n, const int* __restrict__ src,
@@ -328,7 +448,7 @@ void launch_scan(int* count, int C, int* block_sums, int* start, cudaStream_t st
     launch_k(k_scan_down, nb, SCAN_THREADS, st, pdl, count, C, (const int*)block_sums, start);
 }
 
-int scan_block_sums_size(int C) { return blocks_for(C, SCAN_TILE) + 1; }
+int scan_block_sums_size(int C) { return scan_block_sums_ints(C); }
 
 int cell_scan_tiles(int C) { return blocks_for(C, CELL_TILE); }
 
@@ -351,22 +471,23 @@ int scan_tiles_launches(int C, bool counted) {
     return (cell_scan_tiles(C) <= CELL_SCAN_MAX_TILES ? 1 : 2) + (counted ? 0 : 1);
 }
 
-void launch_sort_tail(const int* key, const int* rank, const int* start, const int* tie, int n,
+void launch_sort_tail(const int* key, int* rank, const int* start, const int* tie, int n,
                       int* tmp, int* perm, cudaStream_t st) {
     if (n <= 0) return;
     k_scatter_index<<<blocks_for(n, 256), 256, 0, st>>>(key, rank, start, n, tmp);
-    k_stabilize<<<blocks_for(n, 256), 256, 0, st>>>(tmp, key, start, tie, n, perm);
+    k_stabilize<<<blocks_for(n, STAB_THREADS), STAB_THREADS, 0, st>>>(tmp, rank, key, start, tie, n, perm);
 }
 
-void launch_sort_state(const int* key, const int* rank, const int* start, const int* tie, int n,
+void launch_sort_state(const int* key, int* rank, const int* start, const int* tie, int n,
                        int* tmp, const float4* x, const float4* xs, const float4* v, const int* id,
                        int* key_out, float4* x_out, float4* xs_out, float4* v_out, int* id_out,
                        const int* aux, int* aux_out, int* slot_of, cudaStream_t st) {
     if (n <= 0) return;
     const bool pdl = pdl_enabled();
-    launch_k(k_scatter_index, blocks_for(n, 256), 256, st, pdl, key, rank, start, n, tmp);
-    launch_k(k_stabilize_gather, blocks_for(n, 256), 256, st, pdl, (const int*)tmp, key, start, tie, n,
-             x, xs, v, id, key_out, x_out, xs_out, v_out, id_out, aux, aux_out, slot_of);
+    launch_k(k_scatter_index, blocks_for(n, 256), 256, st, pdl, key, (const int*)rank, start, n, tmp);
+    // the rank array, read by the scatter only, is the big cells' merge space
+    launch_k(k_stabilize_gather, blocks_for(n, STAB_THREADS), STAB_THREADS, st, pdl, tmp, rank, key, start, tie,
+             n, x, xs, v, id, key_out, x_out, xs_out, v_out, id_out, aux, aux_out, slot_of);
 }
 
 void launch_gather_solid(const int* perm, int n, const float4* src, float4* dst, cudaStream_t st) {
@@ -387,10 +508,7 @@ void launch_counting_sort(const int* keys, int n, int num_cells, CountingSortScr
     launch_sort_tail(w.key, w.rank, start, nullptr, n, w.tmp, sorted, st);
 }
 
-size_t counting_sort_scratch_ints(int n, int num_cells) {
-    // count[num_cells], block sums, key[n], rank[n], tmp[n], status
-    return (size_t)num_cells + (size_t)scan_block_sums_size(num_cells) + 3 * (size_t)n + 1;
-}
+size_t counting_sort_scratch_ints(int n, int num_cells) { return counting_sort_scratch_ints_for(n, num_cells); }
 
 CountingSortScratch counting_sort_scratch(int* base, int n, int num_cells) {
     CountingSortScratch w;

@@ -20,11 +20,13 @@ static int sort_args_ok(const int* counts, const int* keys, size_t n, size_t num
 static int sort_with_scratch(int* counts, const int* keys, int n, int num_cells, int* sorted,
                              int* scratch, cudaStream_t st) {
     CountingSortScratch w = counting_sort_scratch(scratch, n, num_cells);
-    cudaMemsetAsync(w.count, 0, (size_t)num_cells * sizeof(int), st);
-    cudaMemsetAsync(w.status, 0, sizeof(int), st);
+    // the histogram and the status word start at zero
+    cudaError_t e = cudaMemsetAsync(w.count, 0, (size_t)num_cells * sizeof(int), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(w.status, 0, sizeof(int), st);
+    if (e != cudaSuccess) return lgb_cuda_status(e, "cudaMemsetAsync");
     launch_counting_sort(keys, n, num_cells, w, counts, sorted, st);
     int bad = 0;
-    cudaError_t e = cudaMemcpyAsync(&bad, w.status, sizeof(int), cudaMemcpyDeviceToHost, st);
+    e = cudaMemcpyAsync(&bad, w.status, sizeof(int), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return lgb_cuda_status(e, "counting_sort");
     return bad ? LUSTRINE_ERR_ARGS : LUSTRINE_OK;

@@ -14,7 +14,10 @@
 // Host code may not use the array's name as a device address (on the host it
 // names a host-side stand-in), so the first call on each device looks up its
 // device address with cudaGetSymbolAddress while that device is current and
-// keeps it; make that first call before any stream capture.  Every call
+// keeps it; make that first call before any stream capture.  The kept
+// address belongs to the device's context: after cudaDeviceReset (which
+// unloads the library's device image) it is stale, so this entry point must
+// not be called again in that process after a reset of the device.  Every call
 // shares the array and leaves its contents behind: the parts that must start
 // at zero are cleared on each call, and calls whose work overlaps on the GPU
 // (different streams or host threads) race on it.
@@ -28,10 +31,10 @@ using namespace lgb;
 
 namespace {
 
-// count[cells] + tile sums + key, rank, tmp[keys] + status, at the maxima
-constexpr size_t kScratchInts = (size_t)LUSTRINE_NOALLOC_MAX_CELLS +
-                                ((size_t)LUSTRINE_NOALLOC_MAX_CELLS + 2047) / 2048 + 1 +
-                                3 * (size_t)LUSTRINE_NOALLOC_MAX_KEYS + 1;
+// the sort's scratch (count[cells] + scan tile sums + key, rank, tmp[keys] +
+// status) at the maxima, sized by the same layout function the sort uses
+constexpr size_t kScratchInts =
+    counting_sort_scratch_ints_for((size_t)LUSTRINE_NOALLOC_MAX_KEYS, (size_t)LUSTRINE_NOALLOC_MAX_CELLS);
 static_assert(kScratchInts * sizeof(int) <= LUSTRINE_NOALLOC_SCRATCH_BYTES,
               "scratch array larger than the documented size");
 
@@ -65,6 +68,9 @@ extern "C" int lustrine_counting_sort_noalloc(int* counts, const int* keys, size
     if (!counts || num_cells < 1 || (num_positions > 0 && (!keys || !sorted_indices)))
         return LUSTRINE_ERR_ARGS;
     if (num_positions > (size_t)LUSTRINE_NOALLOC_MAX_KEYS || num_cells > (size_t)LUSTRINE_NOALLOC_MAX_CELLS)
+        return LUSTRINE_ERR_TOO_LARGE;
+    if (counting_sort_scratch_ints((int)num_positions, (int)num_cells) * sizeof(int) >
+        (size_t)LUSTRINE_NOALLOC_SCRATCH_BYTES)
         return LUSTRINE_ERR_TOO_LARGE;
     int* scratch = nullptr;
     int rc = scratch_for_current_device(&scratch);

@@ -85,10 +85,19 @@ def build(force: bool = False) -> str:
     return ORC_SO
 
 
-def build_ref(ref_root: str = "/root/reference") -> str | None:
-    """Compile the reference's fluid path from the reference tree (present only
-    where the reference is mounted).  Returns the library path or None."""
-    if not os.path.isdir(os.path.join(ref_root, "src")):
+def reference_dir() -> str | None:
+    """The reference tree named by LUSTRINE_REFERENCE_DIR, or None when the
+    variable is unset or names no tree with a src/ folder."""
+    d = os.environ.get("LUSTRINE_REFERENCE_DIR")
+    return d if d and os.path.isdir(os.path.join(d, "src")) else None
+
+
+def build_ref(ref_root: str | None = None) -> str | None:
+    """Compile the reference's fluid path from the reference tree (ref_root,
+    else LUSTRINE_REFERENCE_DIR).  Returns the library path, or the one built
+    earlier, or None."""
+    ref_root = ref_root or reference_dir()
+    if not ref_root or not os.path.isdir(os.path.join(ref_root, "src")):
         return REF_SO if os.path.exists(REF_SO) else None
     subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={ref_root}"], check=True)
     return REF_SO

@@ -14,6 +14,12 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (runs the CUDA kernels)")
 
 
+# The reference tree, for the CPU tests that read or compile it (named by
+# LUSTRINE_REFERENCE_DIR; those tests skip when it is unset).
+REF = os.environ.get("LUSTRINE_REFERENCE_DIR") or ""
+HAVE_REF = bool(REF) and os.path.isdir(os.path.join(REF, "src"))
+
+
 def golden(name):
     return dict(np.load(os.path.join(GOLDEN, name)))
 

@@ -1,7 +1,7 @@
 """Write the golden fixtures under tests/golden/ by running the reference's own
 code, compiled from the reference tree by `make -C oracle ref`.
 
-    python tests/golden/make_golden.py [--ref /root/reference]
+    python tests/golden/make_golden.py [--ref <reference tree>]   (default: $LUSTRINE_REFERENCE_DIR)
 
 Fixtures (all from the reference binary, never from the restatement):
   counting_sort.npz   Sorting::counting_sort on the unit test's input
@@ -26,6 +26,9 @@ Fixtures (all from the reference binary, never from the restatement):
                       attracted flags and the neighbour lists (CSR, the
                       reference's push order, itself included twice), as
                       x1..x5, v1..v5, att1..att5, nbr_off1.., nbr1..
+  wrapper_symbols.txt  the names of every extern "C" entry point the
+                      reference's wrapper header declares
+                      (src/LustrineWrapper.hpp), one per line.
   vox/*.vox, vox_ref.npz  small MagicaVoxel files written here from the
                       published chunk format (SIZE, XYZI, RGBA, PACK; an empty
                       first model; a voxel listed twice; colour index 255),
@@ -208,10 +211,32 @@ def make_vox(R):
     np.savez_compressed(os.path.join(HERE, "vox_ref.npz"), **out)
 
 
+def make_wrapper_symbols(ref_root):
+    """The reference wrapper's extern "C" names, read from its header (lines
+    commented out with // are skipped)."""
+    import re
+    names = []
+    for line in open(os.path.join(ref_root, "src", "LustrineWrapper.hpp")):
+        code = line.split("//", 1)[0]
+        m = re.search(r'extern\s+"C"\s+\w+\s+[\w:<>\s\*]+?\b(\w+)\s*\(', code)
+        if m:
+            names.append(m.group(1))
+    with open(os.path.join(HERE, "wrapper_symbols.txt"), "w") as f:
+        f.write("\n".join(names) + "\n")
+    return names
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("LUSTRINE_REFERENCE_DIR"))
+    ap.add_argument("--symbols-only", action="store_true",
+                    help="write wrapper_symbols.txt only (no reference build)")
     a = ap.parse_args()
+    if not a.ref or not os.path.isdir(os.path.join(a.ref, "src")):
+        raise SystemExit("the reference tree is not available (--ref or LUSTRINE_REFERENCE_DIR); fixtures are committed")
+    make_wrapper_symbols(a.ref)
+    if a.symbols_only:
+        return
     path = O.build_ref(a.ref)
     if not path:
         raise SystemExit("the reference tree is not available; fixtures are committed")

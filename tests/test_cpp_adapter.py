@@ -8,9 +8,7 @@ import subprocess
 
 import pytest
 
-from conftest import ROOT
-
-REF = "/root/reference"
+from conftest import HAVE_REF, REF, ROOT
 
 
 def _compile(tmp_path, extra):
@@ -30,7 +28,7 @@ def test_adapter_compiles_with_simulation_fields(tmp_path):
     _compile(tmp_path, [])
 
 
-@pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "src")), reason="reference tree not mounted")
+@pytest.mark.skipif(not HAVE_REF, reason="LUSTRINE_REFERENCE_DIR not set")
 def test_adapter_compiles_against_reference_simulation(tmp_path):
     shim = os.path.join(ROOT, "oracle", "ref_shim")
     _compile(tmp_path, ["-DWITH_REFERENCE", "-DPLATFORM_UNIX", "-w", "-I", shim, "-I", f"{REF}/src",

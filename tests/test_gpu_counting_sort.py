@@ -45,3 +45,34 @@ def test_counting_sort_empty_and_bad_keys():
     assert len(perm) == 0 and np.array_equal(counts, np.zeros(6, np.int32))
     with pytest.raises(LustrineError):
         _sort(np.array([0, 5, 1], np.int32), 5)
+
+
+@pytest.mark.parametrize("case", ["all_equal_65536", "thresholds", "merge_passes", "mixed_sizes"])
+def test_counting_sort_skewed_keys_stable(case):
+    """Skewed key distributions: the members of a cell of more than 32 keys
+    are ordered by a block-wide sort (bitonic in shared memory up to 2,048,
+    merged runs beyond), so a cell of k keys costs O(k log k), not O(k^2)."""
+    rng = np.random.default_rng(7)
+    if case == "all_equal_65536":
+        keys, cells = np.zeros(65536, np.int32), 3
+    elif case == "thresholds":
+        # cells of exactly 32, 33, 2048 and 2049 members, interleaved
+        sizes = {0: 32, 1: 33, 2: 2048, 3: 2049, 4: 1}
+        keys = np.concatenate([np.full(k, c, np.int32) for c, k in sizes.items()])
+        keys = keys[rng.permutation(len(keys))]
+        cells = 5
+    elif case == "merge_passes":
+        # one cell of 20,000 keys (runs of 2,048 merged over four passes) among uniform keys
+        keys = np.concatenate([np.full(20_000, 11, np.int32), rng.integers(0, 64, 5000).astype(np.int32)])
+        keys = keys[rng.permutation(len(keys))]
+        cells = 64
+    else:
+        # log-uniform cell sizes up to 5,000 over 200 cells
+        sizes = np.exp(rng.uniform(0, np.log(5000), 200)).astype(int) + 1
+        keys = np.repeat(np.arange(200, dtype=np.int32), sizes)
+        keys = keys[rng.permutation(len(keys))]
+        cells = 200
+    counts, perm = _sort(keys, cells)
+    assert np.array_equal(perm, np.argsort(keys, kind="stable"))
+    hist = np.bincount(keys, minlength=cells)
+    assert counts[-1] == len(keys) and np.array_equal(counts[:-1], np.cumsum(hist) - hist)

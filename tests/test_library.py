@@ -4,6 +4,7 @@ reference's layouts.  No compute call is made here."""
 import ctypes as C
 import os
 import re
+import subprocess
 
 import numpy as np
 
@@ -25,6 +26,50 @@ def test_library_builds_and_exports_every_declared_symbol():
     assert not missing, missing
     # the Python binding covers the same set
     assert set(declared) <= set(_lib.SIGNATURES), set(declared) - set(_lib.SIGNATURES)
+
+
+def _exported_symbols():
+    from lustrine_gb300 import _lib
+    _lib.load()
+    out = subprocess.run(["nm", "-D", "--defined-only", _lib.library_path()], capture_output=True,
+                         text=True, check=True).stdout
+    return {ln.split()[-1] for ln in out.splitlines() if ln.strip()}
+
+
+def test_library_exports_every_reference_wrapper_symbol():
+    """nm -D of the library is a superset of the extern "C" names the
+    reference's wrapper header declares (tests/golden/wrapper_symbols.txt,
+    written from src/LustrineWrapper.hpp by make_golden.py), so a binding
+    built for the reference's library finds every entry point here."""
+    ref = [ln.strip() for ln in open(os.path.join(ROOT, "tests", "golden", "wrapper_symbols.txt")) if ln.strip()]
+    assert len(ref) == 54
+    missing = sorted(set(ref) - _exported_symbols())
+    assert not missing, missing
+    assert set(ref) <= set(_declared_symbols())
+
+
+def test_unbuilt_wrapper_entry_points_record_unsupported():
+    """The Bullet/player entry points and read_vox_scene answer with zeros and
+    record LUSTRINE_ERR_UNSUPPORTED (no GPU involved); set_attract_blow_parameters
+    before init records LUSTRINE_ERR_NO_SIMULATION."""
+    from lustrine_gb300 import _lib
+    lib = _lib.load()
+    v = lib.get_gravity()
+    assert (v.x, v.y, v.z) == (0.0, 0.0, 0.0) and lib.lustrine_last_status() == 6
+    assert lib.add_box(_lib.Vec3(1, 2, 3), True, _lib.Vec3(1, 1, 1)) == 0 and lib.lustrine_last_status() == 6
+    assert lib.get_body_frixion(0) == 0.0 and lib.lustrine_last_status() == 6
+    idx = np.full(4, 7, np.int32)
+    size = np.full(1, 5, np.int32)
+    lib.check_collisions(0, idx.ctypes.data_as(C.POINTER(C.c_int)), size.ctypes.data_as(C.POINTER(C.c_int)))
+    assert size[0] == 0 and lib.lustrine_last_status() == 6
+    s = _lib.BindingString(3, b"abc")
+    lib.read_vox_scene(C.byref(s), None, 0)
+    assert s.length == 0 and not s.data and lib.lustrine_last_status() == 6
+    lib.free_string(C.byref(s))
+    assert lib.lustrine_last_status() == 0
+    lib.cleanup_simulation()
+    lib.set_attract_blow_parameters(1.0, 2.0, 3.0, 4.0)
+    assert lib.lustrine_last_status() == 7
 
 
 def test_struct_layouts_match_reference_abi():

@@ -9,9 +9,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, golden
-
-REF = "/root/reference"
+from conftest import GOLDEN, HAVE_REF, REF, golden
 FILES = ("box", "empty_first", "dup")
 
 
@@ -94,7 +92,7 @@ def test_vox_errors(tmp_path):
     assert isinstance(GridWrapper(), GridWrapper) and W is not None
 
 
-@pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "src")), reason="reference tree not mounted")
+@pytest.mark.skipif(not HAVE_REF, reason="LUSTRINE_REFERENCE_DIR not set")
 def test_reference_assets_load_like_the_reference(orc):
     path = orc.build_ref(REF)
     R = orc.Reference(path)
