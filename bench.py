@@ -1,25 +1,39 @@
-"""Benchmark of the GB300 PBF step: particle-solver-iterations per second.
+"""Benchmark of the GB300 PBF step: particle-solver-iterations per second,
+batched mixed precision against the plain step, at equal error.
 
-Workload (one line of JSON on rank 0): the voxel-solid dam break -- 262,144
-fluid particles (64^3 jittered lattice) and ~50k static solid particles from
-a seeded 64 x 64 heightmap in a 128 x 64 x 128 box, h = 1, 4 solver
-iterations, dt = 1/60, PBF step (poly6 / spiky, s_corr, box and solid
-collision, XSPH).  A "step" is one full step (prediction, counting sort,
-neighbour lists, 4 x (lambda, delta-p), XSPH and commit).
+Workload (one line of JSON on rank 0): 512 independent dam-break scenes with
+particle counts log-uniform in [1,024, 65,536] (seeded; 7,546,040 particles),
+each a jittered block at unit spacing in a box of side 2 ceil(n^(1/3)) and
+height ceil(n^(1/3)) + 2, h = 1, 4 solver iterations, dt = 1/60, PBF step
+(poly6 / spiky, s_corr, box collision, XSPH).  A "step" is one full step of
+every scene (prediction, counting sort, neighbour lists, 4 x (lambda,
+delta-p), XSPH and commit).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-value     sum over ranks of fluid particles x iterations / device time per
-          step (CUDA events on the library's stream, max over ranks); L2 is
-          flushed (a 256 MiB write) before every timed step.
-e2e       the same metric through the C ABI with the state in page-locked
-          host memory: every step uploads x and v, steps, downloads x and v.
+value     particles x iterations of all scenes / device time per step of the
+          batched mixed-precision context (one launch per stage for all
+          scenes, the step one CUDA graph; CUDA events on the library's
+          stream, max over ranks); L2 flushed (a 256 MiB write) before every
+          timed step (the working set, ~1 GB, is larger than L2 anyway).
+plain     the plain step on the same scenes: one fp32 context per scene, each
+          on its own stream so the scenes' steps overlap; wall clock per step
+          of all scenes, and the batched context timed the same way; ratio.
+fp64_error  both arms against the FP64 oracle, one step from the same state,
+          on the smallest, median and largest scenes: max relative density
+          error and max position error (units of h).
+e2e       the batched step through the C ABI with the state in page-locked
+          host memory (upload x and v, step, download x and v, every step).
 roofline  the step's dominant kernel, from a live per-stage CUDA-event
-          profile: algorithmic bytes per launch / average launch time.
-cpu_baseline  the oracle's restatement of the reference step (one solver
-          iteration, single thread) on the same scene, on this host.
-Multi-GPU: every rank steps its own replica (the scene does not shard; no
-collective on the data path), scaling "weak".
+          profile: algorithmic bytes per launch / average launch time; and
+          the whole step's algorithmic bytes per particle-iteration.
+cpu_baseline  the reference step (the oracle's restatement, one solver
+          iteration) over every scene in sequence, scenes spread over all
+          host cores (independent scenes; the reference step itself is
+          single-threaded).
+Multi-GPU (weak scaling): 512 scenes per rank, the 512 N scenes of the same
+distribution sharded by scene (longest first to the least-loaded rank); no
+collective on the data path.
 """
 from __future__ import annotations
 
@@ -39,7 +53,9 @@ if ROOT not in sys.path:
 
 METRIC = "PBF particle-solver-iters/s"
 UNIT = "particle-iters/s"
-WORKLOAD = "config1_voxel_solids_262k"
+WORKLOAD = "config3_batched_512_scenes"
+NUM_SCENES = 512
+ITERS = 4
 
 # Algorithmic bytes per particle per launch of each stage: compulsory fp32
 # state traffic (positions 12 B, lambda 4 B; neighbour gathers counted as
@@ -178,6 +194,110 @@ def barrier(world):
 
 
 # --------------------------------------------------------------- CPU legs --
+# The oracle (oracle/) runs only here: the CPU baseline (the reference step as
+# the oracle restates it) and, as the checker, the FP64 step that the GPU
+# results are compared with.
+
+def ref_semantics_params(O, domain):
+    """Oracle parameters of the reference step (simulate_fluid) on a scene:
+    the reference's defaults with the configs' physics."""
+    p = O.reference_params(*domain)
+    p.rest_density, p.mass, p.relaxation_epsilon = 1.0, 1.0, 10.0
+    p.gravity[1] = -9.81
+    p.s_corr_dq, p.s_corr_k, p.s_corr_n = 0.2, 0.1, 4.0
+    p.clamp_cells = 1
+    return p
+
+
+_WORKER = {}
+
+
+def _cpu_worker_init(root, num_scenes):
+    """Pool worker: the oracle library and the config-3 scenes, built once."""
+    if root not in sys.path:
+        sys.path.insert(0, root)
+    from lustrine_gb300 import scenes
+    from oracle import oracle as O
+    _WORKER["O"] = O
+    _WORKER["scenes"] = scenes.config3(num=num_scenes)
+
+
+def _cpu_worker_steps(indices):
+    """Steps the given scenes once each from their initial state with the
+    reference step (one solver iteration); returns (particles, seconds)."""
+    O = _WORKER["O"]
+    scs = _WORKER["scenes"]
+    parts, secs = 0, 0.0
+    for i in indices:
+        sc = scs[i]
+        p = ref_semantics_params(O, sc.domain)
+        t0 = time.perf_counter()
+        O.compat_step(p, sc.dt, sc.x, np.zeros_like(sc.x))
+        secs += time.perf_counter() - t0
+        parts += sc.n
+    return parts, secs
+
+
+class CpuScenes:
+    """The reference step over config-3 scenes on every host core: a pool of
+    worker processes (started with spawn, so it is safe beside a CUDA
+    context), each stepping whole scenes (independent units)."""
+
+    def __init__(self, num_scenes, workers=None):
+        import multiprocessing as mp
+        from oracle import oracle as O
+        O.build()  # once, before the workers load it
+        self.workers = workers or os.cpu_count() or 1
+        self.pool = mp.get_context("spawn").Pool(self.workers, initializer=_cpu_worker_init,
+                                                  initargs=(ROOT, num_scenes))
+
+    def step(self, indices, counts):
+        """One step of the given scenes, spread over the workers (largest
+        scenes first, dealt round-robin); wall seconds and particles."""
+        order = sorted(indices, key=lambda i: -counts[i])
+        chunks = [order[w::self.workers] for w in range(self.workers)]
+        chunks = [c for c in chunks if c]
+        t0 = time.perf_counter()
+        res = self.pool.map(_cpu_worker_steps, chunks, chunksize=1)
+        wall = time.perf_counter() - t0
+        return wall, sum(r[0] for r in res)
+
+    def close(self):
+        self.pool.close()
+        self.pool.join()
+
+
+def oracle_pbf_params(O, p, domain):
+    """Oracle parameters of the PBF step with the GPU context's parameters."""
+    q = O.reference_params(*domain, p.particle_radius, p.kernel_radius / p.particle_radius)
+    for f in ("rest_density", "mass", "relaxation_epsilon", "s_corr_dq", "s_corr_k", "s_corr_n",
+              "c_xsph", "solid_contact", "iterations"):
+        setattr(q, f, getattr(p, f))
+    for a in range(3):
+        q.gravity[a] = p.gravity[a]
+    return q
+
+
+def fp64_errors(p, checks):
+    """The checker: the FP64 oracle step from each check's state, and each
+    GPU result's max relative density error and max position error against
+    it.  checks: [(scene, x0, v0, {arm: (x, rho)})]."""
+    from oracle import oracle as O
+    O.build()
+    out = {}
+    for sc, x0, v0, arms in checks:
+        q = oracle_pbf_params(O, p, sc.domain)
+        o = O.pbf_step(q, sc.dt, x0, v0)
+        rho64 = np.asarray(o["density"], np.float64)
+        for arm, (x, rho) in arms.items():
+            d = out.setdefault(arm, {"max_rel_density_error": 0.0, "max_position_error": 0.0, "scenes": []})
+            de = float(np.max(np.abs(np.asarray(rho, np.float64) - rho64) / np.abs(rho64)))
+            pe = float(np.max(np.abs(np.asarray(x, np.float64) - o["x"])))
+            d["max_rel_density_error"] = max(d["max_rel_density_error"], de)
+            d["max_position_error"] = max(d["max_position_error"], pe)
+            d["scenes"].append({"particles": sc.n, "rel_density_error": de, "position_error": pe})
+    return out
+
 
 def cpu_reference_rate(scene, budget_s, min_steps=3):
     """The reference step restated by the oracle (one solver iteration, single
@@ -221,26 +341,38 @@ def cpu_sand_rate(scene, x, v, reps=3):
 
 
 def run_reference(args, world, rank):
+    """The reference arm: the reference's fluid step (the oracle's restatement
+    of simulate_fluid, bit-exact with the compiled reference; one solver
+    iteration) over the same 512 scenes, scenes spread over every host core.
+    One step = every scene stepped once from its initial state (a snapshot,
+    so every step costs the same)."""
     if rank != 0:
         return
     from lustrine_gb300 import scenes
-    sc = scenes.config1()
-    rates = []
+    counts = [int(c) for c in scenes.batched_counts(NUM_SCENES)]
+    cpu = CpuScenes(NUM_SCENES)
+    idx = list(range(NUM_SCENES))
     for _ in range(args.warmup):
-        cpu_reference_rate(sc, 0.0, min_steps=1)
+        cpu.step(idx, counts)
+    walls = []
+    parts = 0
     for _ in range(args.steps):
-        r, _, _ = cpu_reference_rate(sc, 0.0, min_steps=1)
-        rates.append(r)
-    value = statistics.median(rates)
+        w, parts = cpu.step(idx, counts)
+        walls.append(w)
+    cpu.close()
+    wall = statistics.median(walls)
+    value = parts / wall
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": sc.n / value * 1e3,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": wall * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded jittered lattice + seeded heightmap solids)",
-        "config": {"workload": WORKLOAD, "fluid_particles": sc.n, "solid_particles": sc.ns,
-                   "solver_iterations": 1, "semantics": "reference simulate_fluid, one pass"},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port",
-                         "sample": f"{args.steps} single steps of the full scene from one snapshot"},
+        "data": "synthetic (seeded jittered dam-break blocks, log-uniform scene sizes)",
+        "config": {"workload": WORKLOAD, "scenes": NUM_SCENES, "fluid_particles": parts,
+                   "solver_iterations": 1, "semantics": "reference simulate_fluid, one pass per step",
+                   "parallelism": f"{cpu.workers} host processes, whole scenes each"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cpu.workers, "kind": "port",
+                         "sample": f"all {NUM_SCENES} scenes per step, median of {args.steps} steps, "
+                                   f"each scene from its initial state"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -293,71 +425,163 @@ def run_scene(sc, params, steps, warmup, flush):
     return sim, ext, ms, st
 
 
+def batch_context(scs, precision, dt, warmup):
+    """A batched context over the scenes, stepped `warmup` times after the
+    autotuner chose its launch shape (timed from that state)."""
+    from lustrine_gb300 import PbfSim, pbf_params, tuning
+    b = PbfSim.batch(pbf_params(8, 8, 8, iterations=ITERS, precision=precision), [sc.domain for sc in scs],
+                     [sc.n for sc in scs])
+    b.upload(np.concatenate([sc.x for sc in scs]))
+    b.step(dt, 3)
+    b.tuned = tuning.tune(b, dt, steps=2, cache=None)
+    b.step(dt, warmup)
+    b.synchronize()
+    return b
+
+
+def wall_per_step(step_all, steps, flush):
+    """Median wall-clock seconds of step_all() with the device synchronised on
+    both sides (L2 flushed before each)."""
+    import torch
+    ts = []
+    for _ in range(steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        step_all()
+        torch.cuda.synchronize()
+        ts.append(time.perf_counter() - t0)
+    return statistics.median(ts)
+
+
 def run_ours(args, world, rank, local):
     import torch
-    from lustrine_gb300 import PRECISION_MIXED, pbf_params, scenes
+    from lustrine_gb300 import PRECISION_MIXED, PbfSim, pbf_params, scenes, sharding
     torch.cuda.set_device(local)
-    sc = scenes.config1()
-    params = pbf_params(*sc.domain, iterations=sc.iterations, c_xsph=sc.c_xsph)
+    allsc = scenes.config3(num=NUM_SCENES * world)
+    counts = [sc.n for sc in allsc]
+    mine = sharding.my_scenes(counts, world, rank)
+    scs = [allsc[i] for i in mine]
+    n_local, n_total = sum(sc.n for sc in scs), sum(counts)
+    dt = scs[0].dt
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     clocks = ClockSampler()
     clocks.start()  # runs through the warm-up: the timed region is milliseconds long
 
-    sim, ext, _, _ = run_scene(sc, params, 1, args.warmup, flush)  # warm-up, graph capture
+    b = batch_context(scs, PRECISION_MIXED, dt, args.warmup)
+    ext = torch.cuda.ExternalStream(b.stream())
+    x_keep = torch.empty((n_local, 3), dtype=torch.float32).pin_memory()
+    v_keep = torch.empty((n_local, 3), dtype=torch.float32).pin_memory()
+    b.download_state_async(x_keep.data_ptr(), v_keep.data_ptr())  # the state the timed region starts from
+    b.synchronize()
     barrier(world)
     clocks.mark_start()
     step_launches = []
-    ms = time_steps(sim, sc.dt, args.steps, flush, ext, step_launches)
+    ms = time_steps(b, dt, args.steps, flush, ext, step_launches)
     clocks.mark_end()
-    status = sim.status()
-    # keep the GPU on the workload (untimed) while the samples after the
-    # timed region arrive, then put back the state the timed region left (the
-    # thousands of extra steps would carry the scene far from it)
-    keep_x = torch.empty((sc.n, 3), dtype=torch.float32).pin_memory()
-    keep_v = torch.empty((sc.n, 3), dtype=torch.float32).pin_memory()
-    sim.download_state_async(keep_x.data_ptr(), keep_v.data_ptr())
-    sim.synchronize()
+    status = b.status()
+    # keep the GPU on the workload (untimed) while the samples after the timed
+    # region arrive
     t_busy = time.time() + 0.5
     while time.time() < t_busy:
-        sim.step(sc.dt, 20)
-        sim.synchronize()
+        b.step(dt, 5)
+        b.synchronize()
     clk = clocks.stop(local, margin=0.5)
-    sim.upload_state_async(keep_x.data_ptr(), keep_v.data_ptr())
-    sim.synchronize()
     barrier(world)
     ms_step = dist_max(sum(ms) / len(ms), world)
-    iters = params.iterations
-    value = world * sc.n * iters / (ms_step * 1e-3)
+    value = n_total * ITERS / (ms_step * 1e-3)
     launches = int(sum(step_launches))  # the library's kernels in the timed region (no L2 flush)
 
     # live per-stage profile (CUDA events on the library stream)
-    prof = profile_stages(sim, sc.dt)
+    b.upload_state_async(x_keep.data_ptr(), v_keep.data_ptr())
+    prof = profile_stages(b, dt)
     peak, peak_kind = measured_peaks()
     cand = {k: v for k, v in prof.items() if k in STAGE_BYTES}
     dom = max(cand, key=lambda k: cand[k][0])
     ms_launch = cand[dom][0] / max(cand[dom][1], 1)
-    bytes_launch = STAGE_BYTES[dom] * sc.n
+    bytes_launch = STAGE_BYTES[dom] * n_local
     achieved = bytes_launch / (ms_launch * 1e-3) / 1e9
     traffic = read_traffic(dom)
     # whole-step algorithmic bytes per particle-iteration (state traffic model)
-    cells = (sc.domain[0] + 1) * (sc.domain[1] + 1) * (sc.domain[2] + 1)
-    bpi = 44 + (192 + 8 * cells / sc.n + 12 * sc.ns / sc.n) / iters
-    step_achieved = value / world * bpi / 1e9
+    cells = sum((sc.domain[0] + 1) * (sc.domain[1] + 1) * (sc.domain[2] + 1) for sc in scs)
+    bpi = 44 + (192 + 8 * cells / n_local) / ITERS
+    step_achieved = n_local * ITERS / (ms_step * 1e-3) * bpi / 1e9
+
+    # the plain step on the same scenes: one fp32 context per scene, each on
+    # its own stream; both arms timed by wall clock from the same state
+    b.upload_state_async(x_keep.data_ptr(), v_keep.data_ptr())
+    b.step(dt, 2)
+    b.synchronize()
+    k_wall = max(3, min(args.steps, 10))
+    t_batched = wall_per_step(lambda: b.step(dt), k_wall, flush)
+    sims = []
+    off = np.concatenate([[0], np.cumsum([sc.n for sc in scs])]).astype(int)
+    xs0 = x_keep.numpy()
+    vs0 = v_keep.numpy()
+    for k, sc in enumerate(scs):
+        s = PbfSim(pbf_params(*sc.domain, iterations=ITERS), sc.n)
+        s.upload(xs0[off[k]:off[k + 1]], vs0[off[k]:off[k + 1]])
+        s.step(dt, 2)
+        sims.append(s)
+    torch.cuda.synchronize()
+
+    def step_each():
+        for s in sims:
+            s.step(dt)
+
+    t_plain = wall_per_step(step_each, k_wall, flush)
+    b_fp32 = batch_context(scs, 0, dt, 2)
+    t_b32 = wall_per_step(lambda: b_fp32.step(dt), k_wall, flush)
+    b_fp32.close()
+    plain = {
+        "value": n_local * ITERS / t_plain, "ms_per_step": t_plain * 1e3,
+        "contexts": len(sims), "launches_per_step": sum(s.launches_per_step() for s in sims),
+        "status": max(s.status() for s in sims), "precision": "fp32",
+        "overlap": "one context per scene, each on its own stream: the scenes' steps overlap",
+        "batched_mixed_wall_ms_per_step": t_batched * 1e3,
+        "batched_fp32_wall_ms_per_step": t_b32 * 1e3,
+        "batched_mixed_over_plain": t_plain / t_batched,
+        "batched_fp32_over_plain": t_plain / t_b32,
+        "timing": "wall clock per step of all scenes, device synchronised on both sides, L2 flushed before",
+    }
+
+    # one step of both arms from the same state, for the FP64 check below:
+    # the smallest, median and largest scenes
+    order = np.argsort([sc.n for sc in scs])
+    check_ids = [int(order[0]), int(order[len(order) // 2]), int(order[-1])]
+    b.upload(xs0, vs0)
+    b.step(dt)
+    bx, _, _, brho = b.download(x=True, v=False, density=True)
+    checks = []
+    for k in check_ids:
+        sims[k].upload(xs0[off[k]:off[k + 1]], vs0[off[k]:off[k + 1]])
+        sims[k].step(dt)
+        px, _, _, prho = sims[k].download(x=True, v=False, density=True)
+        checks.append((scs[k], xs0[off[k]:off[k + 1]].copy(), vs0[off[k]:off[k + 1]].copy(),
+                       {"batched_mixed": (bx[off[k]:off[k + 1]], brho[off[k]:off[k + 1]]),
+                        "plain_fp32": (px, prho)}))
+    for s in sims:
+        s.close()
 
     # end to end through the C ABI with page-locked host buffers
-    e2e = run_e2e(sim, sc, args, ext)
+    e2e = run_e2e_batch(b, x_keep, v_keep, dt, args, world, n_total)
+    b.close()
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "impl": "ours",
-        "data": "synthetic (seeded jittered lattice + seeded heightmap solids)",
-        "config": {"workload": WORKLOAD, "fluid_particles": sc.n, "solid_particles": sc.ns,
-                   "box": list(sc.domain), "h": 1.0, "solver_iterations": iters, "dt": sc.dt,
-                   "precision": "fp32", "l2": "flushed (256 MiB write) before every timed step",
-                   "parallelism": f"replicas x{world}", "launch_shape": sim.tuned["tuning"]},
+        "data": "synthetic (seeded jittered dam-break blocks, log-uniform scene sizes)",
+        "config": {"workload": WORKLOAD, "scenes": len(allsc), "fluid_particles": n_total,
+                   "scene_particles": [int(min(counts)), int(max(counts))], "h": 1.0,
+                   "solver_iterations": ITERS, "dt": dt, "precision": "mixed (int cell + fp32 offset, "
+                   "Kahan density sums)", "arm": "batched: one context for all scenes, one CUDA graph per step",
+                   "l2": "flushed (256 MiB write) before every timed step; working set ~1 GB > L2",
+                   "parallelism": f"scenes sharded over {world} GPU(s)" if world > 1 else "1 GPU",
+                   "launch_shape": b.tuned["tuning"]},
         "gpu_launches": launches,
         "status": status,
+        "plain": plain,
         "e2e": e2e,
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
@@ -369,20 +593,52 @@ def run_ours(args, world, rank, local):
     }
     if clk:
         line["clocks"] = clk
-    if rank == 0:
-        rate, nsteps, t = cpu_reference_rate(sc, args.cpu_budget)
-        line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": 1, "kind": "port",
-                                "sample": f"median of {nsteps} single reference-semantics steps "
-                                          f"(1 solver iteration) of the full scene from one "
-                                          f"snapshot, {t * 1e3:.1f} ms each",
+    if rank == 0 and world == 1:
+        # the CPU leg: the reference step over the same scenes on every host
+        # core, and the FP64 check of both arms
+        cpu = CpuScenes(len(allsc))
+        walls, parts = [], 0
+        for _ in range(2):
+            w, parts = cpu.step(mine, counts)
+            walls.append(w)
+        cpu.close()
+        rate = parts / min(walls)
+        line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": cpu.workers, "kind": "port",
+                                "sample": f"all {len(mine)} scenes stepped once with the reference step "
+                                          f"(1 solver iteration), scenes spread over {cpu.workers} host "
+                                          f"processes, best of 2 passes ({min(walls):.2f} s)",
                                 "nproc": os.cpu_count()}
+        line["fp64_error"] = fp64_errors(b.params, checks)
     if not args.no_extras and rank == 0:
         line["variants"] = run_variants(args, flush)
     if rank == 0:
         print(json.dumps(line), flush=True)
 
 
-def run_e2e(sim, sc, args, ext):
+def run_e2e_batch(b, x_keep, v_keep, dt, args, world, n_total):
+    """The batched step through the C ABI with host buffers: every step
+    uploads x and v from page-locked memory, steps all scenes and downloads
+    x and v into the same buffers (lustrine_pbf_step_host)."""
+    x = x_keep.clone().pin_memory()
+    v = v_keep.clone().pin_memory()
+    n = x.shape[0]
+    steps = max(3, args.steps // 2)
+    for _ in range(2):
+        b.step_host(dt, x.data_ptr(), v.data_ptr())
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        b.step_host(dt, x.data_ptr(), v.data_ptr())
+    wall = dist_max((time.perf_counter() - t0) / steps, world)
+    return {"value": n_total * ITERS / wall, "unit": UNIT,
+            "h2d_bytes_per_step": 2 * 12 * n, "d2h_bytes_per_step": 2 * 12 * n,
+            "ms_per_step": wall * 1e3,
+            "path": "lustrine_pbf_step_host on the batched context (page-locked host buffers)"}
+
+
+def run_e2e_scene(sim, sc, args):
+    """config 1 through the C ABI with host buffers, and the reference
+    wrapper's frame (state on the device, positions to the host every step)."""
     import torch
     n = sc.n
     x = torch.from_numpy(sim.positions()).pin_memory()
@@ -392,32 +648,79 @@ def run_e2e(sim, sc, args, ext):
         sim.step_host(sc.dt, x.data_ptr(), v.data_ptr())
     t0 = time.perf_counter()
     for _ in range(steps):
-        # uploads x, v, steps, downloads x, v into the same page-locked
-        # buffers and waits: the host holds the step's result
         sim.step_host(sc.dt, x.data_ptr(), v.data_ptr())
     dt_wall = (time.perf_counter() - t0) / steps
-    # the reference wrapper's frame (simulate, then simulation_bind_positions_copy):
-    # the state stays on the device, the positions come to the host every step
-    sim.synchronize()
-    for _ in range(2):
-        sim.step(sc.dt)
-        sim.download_state_async(x.data_ptr(), None)
-        sim.synchronize()
-    t1 = time.perf_counter()
-    for _ in range(steps):
-        sim.step(sc.dt)
-        sim.download_state_async(x.data_ptr(), None)
-        sim.synchronize()
-    frame = (time.perf_counter() - t1) / steps
     return {"value": n * sim.params.iterations / dt_wall, "unit": UNIT,
             "h2d_bytes_per_step": 2 * 12 * n, "d2h_bytes_per_step": 2 * 12 * n,
             "ms_per_step": dt_wall * 1e3,
-            "path": "lustrine_pbf_step_host (page-locked host buffers, read and written by the kernels)",
-            "positions_out_frame": {"value": n * sim.params.iterations / frame, "ms_per_step": frame * 1e3,
-                                    "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 12 * n,
-                                    "path": "state resident on the device, positions to page-locked host "
-                                            "memory every step (the reference wrapper's simulate + "
-                                            "simulation_bind_positions_copy frame)"}}
+            "path": "lustrine_pbf_step_host (page-locked host buffers, read and written by the kernels)"}
+
+
+def run_wrapper_frames(frames):
+    """The reference's own C entry points on the global simulation, as a game
+    binding calls them: init_grid_box + init_simulation_extra_parameters (a
+    64^3 block), set_simulate_function(3) (the PBF step), then per frame
+    simulate(dt, false, false) and simulation_bind_positions_copy into
+    page-locked host memory.  Wall clock per frame."""
+    import torch
+    from lustrine_gb300 import wrapper as W
+    prm = W.SimulationParameters(128, 72, 128, 0.5, 1.0)
+    g = W.init_grid_box(prm, 64, 64, 64, (0.0, 0.0, 0.0))
+    W.init_simulation_extra_parameters(prm, [g], [], 1, 2.0, 0)
+    st_init = W.last_status()
+    W.set_simulate_function(3)
+    n = W.get_num_sand_particles()
+    buf = torch.empty((n, 3), dtype=torch.float32).pin_memory()
+    out = buf.numpy()
+    for _ in range(3):
+        W.simulate(1.0 / 60.0)
+        W.simulation_bind_positions_copy(out)
+    ts = []
+    for _ in range(frames):
+        t0 = time.perf_counter()
+        W.simulate(1.0 / 60.0)
+        W.simulation_bind_positions_copy(out)
+        ts.append(time.perf_counter() - t0)
+    st = W.last_status()
+    ctx = W.global_context()
+    iters = ctx.params.iterations if ctx else 1
+    W.cleanup_simulation()
+    W.free_grid(g)
+    t = statistics.median(ts)
+    return {"value": n * iters / t, "unit": UNIT, "ms_per_frame": t * 1e3, "particles": n,
+            "solver_iterations": iters, "status": [st_init, st], "d2h_bytes_per_step": 12 * n,
+            "path": "simulate + simulation_bind_positions_copy (the reference's wrapper entry points)"}
+
+
+def run_config1(args, flush):
+    """config 1 (262,144 fluid + ~50,000 static particles, PBF): fp32 and
+    mixed precision, e2e through the C ABI, the dominant kernel's roofline
+    fraction; and the reference semantics on the GPU against the reference
+    step on one host core on the same scene (the same work per
+    particle-iteration)."""
+    from lustrine_gb300 import PRECISION_MIXED, pbf_params, scenes
+    k = max(3, min(args.steps, 10))
+    sc = scenes.config1()
+    out = {}
+    for name, prec in (("fp32", 0), ("mixed", PRECISION_MIXED)):
+        p = pbf_params(*sc.domain, iterations=sc.iterations, c_xsph=sc.c_xsph, precision=prec)
+        sim, _, ms, st = run_scene(sc, p, k, 3, flush)
+        prof = profile_stages(sim, sc.dt, reps=2)
+        d = prof["delta"]
+        ms_l = d[0] / max(d[1], 1)
+        out[name] = {"value": sc.n * p.iterations / (np.mean(ms) * 1e-3), "ms_per_step": float(np.mean(ms)),
+                     "status": st, "launch_shape": sim.tuned["tuning"],
+                     "stage_ms": {a: round(b[0], 4) for a, b in prof.items()},
+                     "delta_frac": STAGE_BYTES["delta"] * sc.n / (ms_l * 1e-3) / 1e9 / measured_peaks()[0]}
+        if name == "fp32":
+            out["e2e"] = run_e2e_scene(sim, sc, args)
+        sim.close()
+    sem = run_reference_semantics(k, flush)
+    rate, nsteps, t = cpu_reference_rate(sc, min(args.cpu_budget, 10.0))
+    sem["cpu_port_1_core"] = {"value": rate, "ms_per_step": t * 1e3, "steps": nsteps}
+    sem["gpu_over_cpu"] = sem["value"] / rate
+    out["reference_semantics"] = sem
+    return out
 
 
 def run_variants(args, flush):
@@ -425,21 +728,7 @@ def run_variants(args, flush):
     from lustrine_gb300 import PRECISION_MIXED, pbf_params, scenes
     out = {}
     k = max(3, min(args.steps, 10))
-    sc = scenes.config1()
-    p = pbf_params(*sc.domain, iterations=sc.iterations, c_xsph=sc.c_xsph, precision=PRECISION_MIXED)
-    sim, _, ms, st = run_scene(sc, p, k, 3, flush)
-    out["config1_mixed"] = {"value": sc.n * p.iterations / (np.mean(ms) * 1e-3),
-                            "ms_per_step": float(np.mean(ms)), "status": st,
-                            "launch_shape": sim.tuned["tuning"]}
-    sim.close()
-    # the same step without programmatic dependent launch between kernels
-    os.environ["LUSTRINE_NO_PDL"] = "1"
-    p = pbf_params(*sc.domain, iterations=sc.iterations, c_xsph=sc.c_xsph)
-    sim, _, ms, st = run_scene(sc, p, k, 3, flush)
-    del os.environ["LUSTRINE_NO_PDL"]
-    out["config1_no_pdl"] = {"value": sc.n * p.iterations / (np.mean(ms) * 1e-3),
-                             "ms_per_step": float(np.mean(ms)), "status": st}
-    sim.close()
+    out["config1_voxel_solids_262k"] = run_config1(args, flush)
     sc = scenes.config2()
     p = pbf_params(*sc.domain, iterations=sc.iterations, c_xsph=sc.c_xsph)
     sim, _, ms, st = run_scene(sc, p, k, 3, flush)
@@ -449,10 +738,9 @@ def run_variants(args, flush):
                                "launch_shape": sim.tuned["tuning"],
                                "stage_ms": {a: round(b[0], 4) for a, b in prof.items()}}
     sim.close()
-    out["reference_semantics_config1"] = run_reference_semantics(k, flush)
     out["sand_config1_262k"] = run_sand(k, flush)
     out["sources_sinks_config1"] = run_sources_sinks(max(k, 10))
-    out["config3_batched_vs_plain"] = run_config3(max(3, min(args.steps, 10)), flush)
+    out["wrapper_frames_64cube"] = run_wrapper_frames(max(k, 10))
     # 4,194,304 particles in a 4096 x 256 x 4096 box: 4.3e9 cells, so the
     # grid is hashed (2^23 buckets); mixed precision is the mode the box needs
     sc = scenes.config4()
@@ -463,7 +751,7 @@ def run_variants(args, flush):
         out[name] = {"value": sc.n * p.iterations / (np.mean(ms) * 1e-3),
                      "ms_per_step": float(np.mean(ms)), "status": st,
                      "launch_shape": sim.tuned["tuning"],
-                     "max_density_error": sim.reduce()["max_density_error"],
+                     "constraint_residual_max_abs_rho_over_rho0_minus_1": sim.reduce()["max_density_error"],
                      "stage_ms": {a: round(b[0], 4) for a, b in prof.items()}}
         sim.close()
     return out
@@ -570,77 +858,6 @@ def run_sources_sinks(frames):
                     q.append(time.perf_counter() - t0)
                 out[label] = float(np.median(q) * 1e6)
         sim.close()
-    return out
-
-
-def run_config3(steps, flush):
-    """512 independent scenes (log-uniform 1,024-65,536 particles): the batched
-    step (one launch per stage for all scenes, fp32 and mixed precision)
-    against the plain step applied scene by scene (one context and stream per
-    scene), both with the scenes' steps overlapping on the GPU and one after
-    another.  Wall-clock time per step of all scenes, device synchronised,
-    L2 flushed before each step; the equal-error condition (batched mixed
-    density within 1e-4 of FP64) is asserted by tests/test_gpu_batch.py."""
-    import torch
-    from lustrine_gb300 import PRECISION_MIXED, PbfSim, pbf_params, scenes, tuning
-    scs = scenes.config3()
-    total = sum(sc.n for sc in scs)
-    dt = scs[0].dt
-    x_all = np.concatenate([sc.x for sc in scs])
-    out = {"scenes": len(scs), "fluid_particles": total, "iterations": 4}
-
-    def wall(step_all):
-        ts = []
-        for _ in range(steps):
-            flush.zero_()
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            step_all()
-            torch.cuda.synchronize()
-            ts.append(time.perf_counter() - t0)
-        return statistics.median(ts)
-
-    for name, prec in (("batched_fp32", 0), ("batched_mixed", PRECISION_MIXED)):
-        b = PbfSim.batch(pbf_params(8, 8, 8, iterations=4, precision=prec), [sc.domain for sc in scs],
-                         [sc.n for sc in scs])
-        b.upload(x_all)
-        b.step(dt, 3)
-        tuned = tuning.tune(b, dt, steps=2, cache=None)
-        b.step(dt, 2)
-        t = wall(lambda: b.step(dt))
-        out[name] = {"value": total * 4 / t, "ms_per_step": t * 1e3, "status": b.status(),
-                     "launch_shape": tuned["tuning"], "launches_per_step": b.launches_per_step()}
-        b.close()
-    sims = []
-    for sc in scs:
-        s = PbfSim(pbf_params(*sc.domain, iterations=4), sc.n)
-        s.upload(sc.x)
-        s.step(dt, 2)
-        sims.append(s)
-
-    def step_each():
-        for s in sims:
-            s.step(dt)
-
-    t = wall(step_each)
-    out["plain_per_scene"] = {"value": total * 4 / t, "ms_per_step": t * 1e3,
-                              "status": max(s.status() for s in sims),
-                              "launches_per_step": sum(s.launches_per_step() for s in sims),
-                              "overlap": "each scene's context on its own stream: the scenes' steps overlap"}
-
-    def step_each_serial():
-        for s in sims:
-            s.step(dt)
-            s.synchronize()
-
-    t = wall(step_each_serial)
-    out["plain_serial"] = {"value": total * 4 / t, "ms_per_step": t * 1e3,
-                           "status": max(s.status() for s in sims),
-                           "overlap": "none: each scene's step completes before the next is issued"}
-    for s in sims:
-        s.close()
-    out["batched_mixed_over_plain"] = out["batched_mixed"]["value"] / out["plain_per_scene"]["value"]
-    out["batched_mixed_over_plain_serial"] = out["batched_mixed"]["value"] / out["plain_serial"]["value"]
     return out
 
 
