@@ -121,6 +121,41 @@ __device__ __forceinline__ void walk_row(const StepParams& p, const float4& self
     }
 }
 
+// The candidates [t_begin, t_end) of one row, gathered 4 at a time (the
+// loads of a chunk are in flight together; the tests run in slot order, so
+// the list is the one walk_row builds).  b1, b2: the row's cell bounds, read
+// in mixed precision only (the entry's dz code and the cell shift; fp32
+// entries carry dz = 0, which no fp32 pass reads).
+template <bool MIXED, bool SOLID>
+__device__ __forceinline__ void walk_range(const StepParams& p, const float4& self, int s,
+                                           const float4* __restrict__ pos, int t_begin, int t_end, int b1, int b2,
+                                           int dz0, int dx, int dy, LambdaAcc& a, int& c_n, int* __restrict__ nbr) {
+    const float sx = -(float)dx * p.cell, sy = -(float)dy * p.cell;
+    for (int t0 = t_begin; t0 < t_end; t0 += 4) {
+        float4 q[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+            if (t0 + u < t_end) q[u] = SOLID ? __ldg(&pos[t0 + u]) : pos[t0 + u];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const int t = t0 + u;
+            if (t >= t_end || (!SOLID && t == s)) continue;
+            const int dz = MIXED ? dz0 + (t >= b1) + (t >= b2) : 0;
+            float3 d = make_float3(__fsub_rn(self.x, q[u].x), __fsub_rn(self.y, q[u].y), __fsub_rn(self.z, q[u].z));
+            if (MIXED) {
+                d.x = __fadd_rn(d.x, sx);
+                d.y = __fadd_rn(d.y, sy);
+                d.z = __fadd_rn(d.z, -(float)dz * p.cell);
+            }
+            if (dot3e(d.x, d.y, d.z) <= p.h2) {
+                if (c_n < p.max_nbrs) nbr[(size_t)c_n * p.n + s] = entry(t, dx, dy, dz, SOLID);
+                c_n++;
+                lambda_accumulate<MIXED>(p, a, d, SOLID);
+            }
+        }
+    }
+}
+
 // One cell of the stencil on a hashed grid: the particles of its bucket,
 // kept only if they belong to that cell.
 template <bool MIXED, bool SOLID>
@@ -171,13 +206,46 @@ __global__ void __launch_bounds__(B) k_lists_lambda(StepParams p, CellPack cp, f
     const int slab = g.gx * g.gz;
     // static particles only where the cell's neighbourhood holds some
     const bool solids = p.ns > 0 && p.solid_near && __ldg(&p.solid_near[__ldg(&key_sorted[s])]);
-    for (int dy = -1; dy <= 1; dy++) {
+    if (!HASHED) {
+        const int z0 = max(c.z - 1, 0), z1 = min(c.z + 1, g.gz - 1);
+        for (int dy = -1; dy <= 1; dy++) {
+            const int y = c.y + dy;
+            if (y < 0 || y >= g.gy) continue;
+            // the fluid slot ranges of the layer's three rows, loaded together
+            int b0[3], b1[3], b2[3], b3[3];
+#pragma unroll
+            for (int r = 0; r < 3; r++) {
+                const int xx = c.x + r - 1;
+                b0[r] = b1[r] = b2[r] = b3[r] = 0;
+                if (xx >= 0 && xx < g.gx) {
+                    const int row = g.off + y * slab + xx * g.gz;
+                    b0[r] = fstart[row + z0];
+                    b3[r] = fstart[row + z1 + 1];
+                    if (MIXED) {
+                        b1[r] = fstart[row + z0 + 1];
+                        b2[r] = (z0 + 1 <= z1) ? fstart[row + z0 + 2] : b1[r];
+                    }
+                }
+            }
+#pragma unroll
+            for (int r = 0; r < 3; r++) {
+                const int xx = c.x + r - 1;
+                if (xx < 0 || xx >= g.gx) continue;
+                walk_range<MIXED, false>(p, self, s, xs, b0[r], b3[r], b1[r], b2[r], z0 - c.z, r - 1, dy, a, c_n,
+                                         nbr);
+                if (solids)
+                    walk_row<MIXED, true>(p, self, s, solid, sstart, g.off + y * slab + xx * g.gz, c.z, g.gz, r - 1,
+                                          dy, a, c_n, nbr);
+            }
+        }
+    }
+    for (int dy = -1; dy <= 1 && HASHED; dy++) {
         const int y = c.y + dy;
         if (y < 0 || y >= g.gy) continue;
         for (int dx = -1; dx <= 1; dx++) {
             const int xx = c.x + dx;
             if (xx < 0 || xx >= g.gx) continue;
-            if (HASHED) {
+            {
                 // cells past the packed field widths hold no particle
                 if (xx > (int)cp.mx || y > (int)cp.my) continue;
                 // the dense walk's entry order: the row's fluid cells, then its solid cells
@@ -195,12 +263,7 @@ __global__ void __launch_bounds__(B) k_lists_lambda(StepParams p, CellPack cp, f
                                                       cell_bucket(cn, p.hash_bits), (int)pack_bits(cp, cn),
                                                       dx, dy, z - c.z, a, c_n, nbr);
                     }
-                continue;
             }
-            const int row = g.off + y * slab + xx * g.gz;
-            walk_row<MIXED, false>(p, self, s, xs, fstart, row, c.z, g.gz, dx, dy, a, c_n, nbr);
-            if (solids)
-                walk_row<MIXED, true>(p, self, s, solid, sstart, row, c.z, g.gz, dx, dy, a, c_n, nbr);
         }
     }
     if (c_n > p.max_nbrs) {
