@@ -307,6 +307,28 @@ LUSTRINE_API int lustrine_pbf_destroy(lustrine_pbf* s);
  * scenes with one launch per stage. */
 LUSTRINE_API int lustrine_batch_create(const lustrine_pbf_params* p, int num_scenes, const int* domains,
                                        const int* n_fluid, const int* n_solid, lustrine_pbf** out);
+/* How a batch runs the part of its step after the cell sort (no counterpart
+ * in the reference, which has no batches).
+ * LUSTRINE_SOLVER_STAGES (the default): one launch per stage and pass for all
+ * scenes.
+ * LUSTRINE_SOLVER_ONCHIP: one persistent launch of thread-block clusters of
+ * 16 CTAs that take bins of scenes from a work queue; a scene's lists,
+ * iterations, XSPH and commit run out of its cluster's distributed shared
+ * memory (4,096 particles per CTA, scenes of up to 65,536).  It applies to
+ * PBF batches on a dense grid without static particles and with
+ * max_neighbors <= 255 (in mixed precision, boxes of at most 256 cells a
+ * side), on a GPU that runs such clusters; elsewhere set_solver(ONCHIP)
+ * returns LUSTRINE_ERR_UNSUPPORTED.  In fp32 both give the same bits; in
+ * mixed precision the on-chip solve iterates on positions relative to the
+ * scene's box corner and commits cell + offset.  The autotuner times both. */
+enum { LUSTRINE_SOLVER_STAGES = 0, LUSTRINE_SOLVER_ONCHIP = 1 };
+LUSTRINE_API int lustrine_batch_set_solver(lustrine_pbf* s, int solver);
+LUSTRINE_API int lustrine_batch_get_solver(const lustrine_pbf* s, int* solver);
+/* The on-chip solve's launch: clusters of the persistent grid (0: the solve
+ * does not apply to this batch), bins of scenes in its work queue, threads
+ * per CTA (512 or 1024; the 4,096 particles of a CTA are dealt to them). */
+LUSTRINE_API int lustrine_batch_onchip_layout(const lustrine_pbf* s, int* clusters, int* bins, int* threads);
+LUSTRINE_API int lustrine_batch_set_onchip_threads(lustrine_pbf* s, int threads);
 /* Change parameters (same precision, domain, cell size, grid mode and
  * max_neighbors as at create; the mode may change -- entering sand mode
  * from another mode clears the attract flags). */
@@ -399,7 +421,8 @@ enum {
     LUSTRINE_STAGE_LAMBDA = 4,  /* density constraint pass(es) */
     LUSTRINE_STAGE_DELTA = 5,   /* position correction pass(es) */
     LUSTRINE_STAGE_XSPH = 6,    /* XSPH + commit */
-    LUSTRINE_NUM_STAGES = 7
+    LUSTRINE_STAGE_SOLVE = 7,   /* a batch's on-chip solve: lists, iterations, XSPH, commit */
+    LUSTRINE_NUM_STAGES = 8
 };
 LUSTRINE_API int lustrine_pbf_profile_step(lustrine_pbf* s, float dt, double* stage_ms,
                                            int* stage_launches, int num_stages);

@@ -25,6 +25,7 @@ ERRORS = {
     10: "LUSTRINE_ERR_TOO_LARGE",
 }
 MODE_REFERENCE, MODE_PBF, MODE_SAND = 0, 1, 2
+SOLVER_STAGES, SOLVER_ONCHIP = 0, 1
 PRECISION_FP32, PRECISION_MIXED = 0, 1
 
 
@@ -169,6 +170,10 @@ SIGNATURES = {
     "lustrine_pbf_create": (C.c_int, [C.POINTER(PbfParams), C.c_int, C.c_int, C.POINTER(_P)]),
     "lustrine_pbf_destroy": (C.c_int, [_P]),
     "lustrine_batch_create": (C.c_int, [C.POINTER(PbfParams), C.c_int, _P, _P, _P, C.POINTER(_P)]),
+    "lustrine_batch_set_solver": (C.c_int, [_P, C.c_int]),
+    "lustrine_batch_get_solver": (C.c_int, [_P, _IP]),
+    "lustrine_batch_onchip_layout": (C.c_int, [_P, _IP, _IP, _IP]),
+    "lustrine_batch_set_onchip_threads": (C.c_int, [_P, C.c_int]),
     "lustrine_pbf_set_params": (C.c_int, [_P, C.POINTER(PbfParams)]),
     "lustrine_pbf_get_params": (C.c_int, [_P, C.POINTER(PbfParams)]),
     "lustrine_pbf_counts": (C.c_int, [_P, _IP, _IP]),

@@ -201,7 +201,8 @@ void lustrine_pbf::free_buffers() {
     void* ptrs[] = {x[0], x[1], xs[0], xs[1], v[0], v[1], id[0], id[1], xs_alt, xs_pred, vtmp, key, key_sorted,
                     rank, tmp, perm, count, start, block_sums, tile_sum, solid_near, solid, solid_raw, sstart, nbr, cnt, lam,
                     lam_by_id, rho, status, red, qcount, out3, out3d, iota, slot_of, solid_id, d_scenes, d_scene_of,
-                    d_solid_scene_of, cellk, cell_sorted, solid_cell, att[0], att[1]};
+                    d_solid_scene_of, cellk, cell_sorted, solid_cell, att[0], att[1], d_bins, d_scene_slot0,
+                    d_queue};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     x[0] = x[1] = xs[0] = xs[1] = v[0] = v[1] = nullptr;
@@ -215,6 +216,10 @@ void lustrine_pbf::free_buffers() {
     lam = lam_by_id = rho = out3 = nullptr;
     red = out3d = nullptr;
     d_scenes = nullptr;
+    d_bins = nullptr;
+    d_scene_slot0 = d_queue = nullptr;
+    num_bins = onchip_clusters = onchip_clusters512 = 0;
+    onchip = false;
 }
 
 int lgb_write_sentinel(lustrine_pbf* s) {
@@ -391,6 +396,64 @@ static int derive_batch(const lustrine_pbf_params& q0, const std::vector<int>& d
     return LUSTRINE_OK;
 }
 
+// The on-chip scene solve for a batch, where it applies: PBF mode on a dense
+// grid, no static particles, every scene of at most SOLVE_MAX_SCENE particles,
+// lists of at most 255 entries, in mixed precision boxes of at most
+// SOLVE_MIXED_MAX_CELLS cells a side (the solve iterates on positions relative
+// to the scene's box corner), and a GPU that runs clusters of SOLVE_CLUSTER
+// CTAs with the solve's shared memory.  Scenes are packed into bins of
+// SOLVE_CLUSTER CTAs (ceil(n / SOLVE_M) CTAs each, first fit by decreasing
+// size).  The step keeps the per-stage kernels until lustrine_batch_set_solver
+// (or the autotuner) selects the on-chip solve.
+static int setup_onchip(lustrine_pbf* s) {
+    s->onchip = false;
+    s->onchip_clusters = s->onchip_clusters512 = 0;
+    if (s->prm.mode != LUSTRINE_MODE_PBF || s->sp.hash_bits || s->ns > 0 || s->sp.max_nbrs > 255) return LUSTRINE_OK;
+    const int S = (int)s->b_nfluid.size();
+    for (int k = 0; k < S; k++)
+        if (s->b_nfluid[(size_t)k] > SOLVE_MAX_SCENE) return LUSTRINE_OK;
+    if (s->mixed())
+        for (size_t k = 0; k < s->b_domains.size(); k++)
+            if ((float)s->b_domains[k] > SOLVE_MIXED_MAX_CELLS * s->sp.cell) return LUSTRINE_OK;
+    int clusters = 0, clusters512 = 0;
+    scene_solve_prepare(s->mixed(), 512, &clusters512);
+    if (!scene_solve_prepare(s->mixed(), 1024, &clusters) || clusters < 1) return LUSTRINE_OK;
+    std::vector<int> order;
+    for (int k = 0; k < S; k++)
+        if (s->b_nfluid[(size_t)k] > 0) order.push_back(k);
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int a, int b) { return s->b_nfluid[(size_t)a] > s->b_nfluid[(size_t)b]; });
+    std::vector<int> room;        // free CTAs of every bin
+    std::vector<SolveSlot> bins;  // SOLVE_CLUSTER per bin
+    for (int k : order) {
+        const int ctas = (s->b_nfluid[(size_t)k] + SOLVE_M - 1) / SOLVE_M;
+        size_t b = 0;
+        while (b < room.size() && room[b] < ctas) b++;
+        if (b == room.size()) {
+            room.push_back(SOLVE_CLUSTER);
+            bins.resize(bins.size() + SOLVE_CLUSTER, SolveSlot{-1, 0, 0});
+        }
+        const int first = SOLVE_CLUSTER - room[b];
+        for (int r = 0; r < ctas; r++) bins[b * SOLVE_CLUSTER + (size_t)(first + r)] = SolveSlot{k, r, ctas};
+        room[b] -= ctas;
+    }
+    std::vector<int> slot0((size_t)S + 1, 0);
+    for (int k = 0; k < S; k++) slot0[(size_t)k + 1] = slot0[(size_t)k] + s->b_nfluid[(size_t)k];
+    s->num_bins = (int)room.size();
+    int rc = dalloc(&s->d_bins, bins.size() ? bins.size() : 1);
+    if (!rc) rc = dalloc(&s->d_scene_slot0, slot0.size());
+    if (!rc) rc = dalloc(&s->d_queue, 2);
+    if (rc) return rc;
+    if (!bins.empty())
+        CK(cudaMemcpy(s->d_bins, bins.data(), bins.size() * sizeof(SolveSlot), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(s->d_scene_slot0, slot0.data(), slot0.size() * sizeof(int), cudaMemcpyHostToDevice));
+    CK(cudaMemset(s->d_queue, 0, 2 * sizeof(int)));
+    s->onchip_clusters = std::max(1, std::min(clusters, s->num_bins));
+    s->onchip_clusters512 = clusters512 > 0 ? std::max(1, std::min(clusters512, s->num_bins)) : 0;
+    s->onchip_threads = 1024;
+    return LUSTRINE_OK;
+}
+
 extern "C" int lustrine_batch_create(const lustrine_pbf_params* p, int num_scenes, const int* domains,
                                      const int* n_fluid, const int* n_solid, lustrine_pbf** out) {
     if (!p || !out || num_scenes < 1 || !domains || !n_fluid) return LUSTRINE_ERR_ARGS;
@@ -446,7 +509,47 @@ extern "C" int lustrine_batch_create(const lustrine_pbf_params* p, int num_scene
     s->sp.scenes = s->d_scenes;
     s->sp.scene_of = s->d_scene_of;
     s->sp.solid_scene_of = s->d_solid_scene_of;
+    rc = setup_onchip(s);
+    if (rc) {
+        delete s;
+        return rc;
+    }
     *out = s;
+    return LUSTRINE_OK;
+}
+
+extern "C" int lustrine_batch_set_solver(lustrine_pbf* s, int solver) {
+    if (!s || !s->is_batch() || (solver != LUSTRINE_SOLVER_STAGES && solver != LUSTRINE_SOLVER_ONCHIP))
+        return LUSTRINE_ERR_ARGS;
+    if (solver == LUSTRINE_SOLVER_ONCHIP && !s->onchip_clusters) return LUSTRINE_ERR_UNSUPPORTED;
+    if (s->onchip != (solver == LUSTRINE_SOLVER_ONCHIP)) {
+        s->onchip = solver == LUSTRINE_SOLVER_ONCHIP;
+        s->invalidate_graphs();
+    }
+    return LUSTRINE_OK;
+}
+
+extern "C" int lustrine_batch_get_solver(const lustrine_pbf* s, int* solver) {
+    if (!s || !solver || !s->is_batch()) return LUSTRINE_ERR_ARGS;
+    *solver = s->onchip ? LUSTRINE_SOLVER_ONCHIP : LUSTRINE_SOLVER_STAGES;
+    return LUSTRINE_OK;
+}
+
+extern "C" int lustrine_batch_onchip_layout(const lustrine_pbf* s, int* clusters, int* bins, int* threads) {
+    if (!s || !s->is_batch()) return LUSTRINE_ERR_ARGS;
+    if (clusters) *clusters = s->onchip_threads == 512 ? s->onchip_clusters512 : s->onchip_clusters;
+    if (bins) *bins = s->num_bins;
+    if (threads) *threads = s->onchip_threads;
+    return LUSTRINE_OK;
+}
+
+extern "C" int lustrine_batch_set_onchip_threads(lustrine_pbf* s, int threads) {
+    if (!s || !s->is_batch() || (threads != 512 && threads != 1024)) return LUSTRINE_ERR_ARGS;
+    if (!s->onchip_clusters || (threads == 512 && !s->onchip_clusters512)) return LUSTRINE_ERR_UNSUPPORTED;
+    if (s->onchip_threads != threads) {
+        s->onchip_threads = threads;
+        s->invalidate_graphs();
+    }
     return LUSTRINE_OK;
 }
 
@@ -805,6 +908,36 @@ static int enqueue_step(lustrine_pbf* s, cudaStream_t st, StageMarks* mk = nullp
                          s->lam_by_id, st);
         if (mk) mk->mark(LUSTRINE_STAGE_DELTA, st);
         k += 3;
+    } else if (s->onchip && s->num_bins > 0) {
+        // the batch's lists, iterations, XSPH and commit in one persistent
+        // launch of clusters (the lambdas end where the per-stage path leaves them)
+        SolveArgs sa;
+        sa.bins = s->d_bins;
+        sa.num_bins = s->num_bins;
+        sa.iters = s->prm.iterations;
+        sa.queue = s->d_queue;
+        sa.scene_slot0 = s->d_scene_slot0;
+        sa.xs = s->xs[o];
+        sa.x = s->x[o];
+        sa.key_sorted = s->key_sorted;
+        sa.start = s->start;
+        sa.nbr = s->nbr;
+        sa.cnt = s->cnt;
+        sa.rho = s->rho;
+        sa.lam_out = (s->prm.iterations % 2 == 1) ? s->xs[o] : s->xs_alt;
+        sa.x_out = s->x[o];
+        sa.v_out = s->v[o];
+        sa.status = s->status;
+        sa.xs_next = tail ? s->xs_pred : nullptr;
+        sa.key = s->key;
+        sa.rank = s->rank;
+        sa.count = s->count;
+        sa.cellk = s->cellk;
+        sa.tile_count = tail ? tiles_of(s, o) : nullptr;
+        launch_scene_solve(mixed, s->onchip_threads, p, s->cp, sa,
+                           s->onchip_threads == 512 ? s->onchip_clusters512 : s->onchip_clusters, st);
+        k += 1;
+        if (mk) mk->mark(LUSTRINE_STAGE_SOLVE, st);
     } else {
         // iteration 0's lambda pass builds the neighbour lists as it goes
         float4* a = s->xs[o];

@@ -7,6 +7,7 @@
 
 #include "lustrine_gb300.h"
 #include "pbf_common.cuh"
+#include "pbf_kernels.h"
 
 int lgb_cuda_status(cudaError_t e, const char* what);
 
@@ -92,6 +93,16 @@ struct lustrine_pbf {
     int* d_scene_of = nullptr;
     int* d_solid_scene_of = nullptr;
     bool is_batch() const { return !b_nfluid.empty(); }
+    // on-chip scene solve of a batch (pbf_scene_solve.cu): bins of scenes,
+    // the scenes' first slots, the work queue, the clusters launched
+    lgb::SolveSlot* d_bins = nullptr;
+    int num_bins = 0;
+    int* d_scene_slot0 = nullptr;
+    int* d_queue = nullptr;
+    int onchip_clusters = 0;     // 0: the batch cannot take the on-chip solve (CTAs of 1024 threads)
+    int onchip_clusters512 = 0;  // the same with CTAs of 512 threads
+    int onchip_threads = 1024;
+    bool onchip = false;         // the step uses it
 
     // captured steps: parity + 2 * (own prediction) + 4 * (predicts the next step)
     cudaGraphExec_t graph_exec[8] = {};

@@ -150,4 +150,50 @@ void launch_pack_predict(bool mixed, const StepParams& p, const CellPack& cp, co
 void launch_reduce(bool mixed, const StepParams& p, const CellPack& cp, const float4* x,
                    const float4* v, const float* rho, double* out, cudaStream_t st);
 
+// pbf_scene_solve.cu: a batch's lists, iterations, XSPH and commit out of the
+// distributed shared memory of thread-block clusters (PBF, dense grid, no
+// static particles, scenes of at most SOLVE_MAX_SCENE particles)
+constexpr int SOLVE_M = 4096;         // particles per CTA (threads per CTA: 512 or 1024)
+constexpr int SOLVE_M_SHIFT = 12;
+constexpr int SOLVE_CAP = 10;         // list entries per particle kept in shared memory
+constexpr int SOLVE_CLUSTER = 16;     // CTAs per cluster
+constexpr int SOLVE_MAX_SCENE = SOLVE_M * SOLVE_CLUSTER;
+constexpr float SOLVE_MIXED_MAX_CELLS = 256.0f;  // mixed precision: largest box side, in cells
+// One CTA of a bin: its scene (-1: none), its rank among the scene's CTAs and
+// the scene's CTA count.
+struct SolveSlot {
+    int scene, rank, ctas;
+};
+struct SolveArgs {
+    const SolveSlot* bins;   // num_bins x SOLVE_CLUSTER
+    int num_bins;
+    int iters;               // solver iterations
+    int* queue;              // [0] next bin, [1] clusters done (both zero at launch)
+    const int* scene_slot0;  // S + 1 first slots
+    const float4* xs;        // the step's predicted positions in cell order
+    const float4* x;         // committed positions in cell order
+    const int* key_sorted;
+    const int* start;
+    int* nbr;                // the lists (slots), also written to global memory (neighbour queries)
+    int* cnt;
+    float* rho;              // densities of the last lambda pass (may be null)
+    float4* lam_out;         // w: lambdas of the last lambda pass
+    float4* x_out;           // committed state
+    float4* v_out;
+    int* status;
+    float4* xs_next;         // the next step's prediction (null: none), as predict_one
+    int* key;
+    int* rank;
+    int* count;
+    int* cellk;
+    int* tile_count;
+};
+size_t scene_solve_smem_bytes();
+// Sets the kernel's attributes for CTAs of `threads` (512 or 1024) threads;
+// returns the clusters that fit the GPU at once (0: the on-chip solve cannot
+// run here).
+int scene_solve_prepare(bool mixed, int threads, int* max_clusters);
+void launch_scene_solve(bool mixed, int threads, const StepParams& p, const CellPack& cp, const SolveArgs& a,
+                        int clusters, cudaStream_t st);
+
 }  // namespace lgb

@@ -138,6 +138,29 @@ class PbfSim:
         self.h = h
         return self
 
+    # batches: the on-chip scene solve ----------------------------------------
+    def set_solver(self, onchip: bool):
+        """The on-chip scene solve (clusters, distributed shared memory) or
+        one launch per stage; raises LustrineError (unsupported) where the
+        on-chip solve does not apply."""
+        check(self.lib.lustrine_batch_set_solver(self.h, 1 if onchip else 0), "batch_set_solver")
+
+    def solver(self) -> str:
+        v = C.c_int()
+        check(self.lib.lustrine_batch_get_solver(self.h, C.byref(v)), "batch_get_solver")
+        return "onchip" if v.value == 1 else "stages"
+
+    def onchip_layout(self) -> dict:
+        """Clusters of the on-chip solve's persistent grid, bins of scenes,
+        threads per CTA."""
+        c, b, t = C.c_int(), C.c_int(), C.c_int()
+        check(self.lib.lustrine_batch_onchip_layout(self.h, C.byref(c), C.byref(b), C.byref(t)),
+              "batch_onchip_layout")
+        return {"clusters": c.value, "bins": b.value, "threads": t.value}
+
+    def set_onchip_threads(self, threads: int):
+        check(self.lib.lustrine_batch_set_onchip_threads(self.h, int(threads)), "batch_set_onchip_threads")
+
     # lifecycle -------------------------------------------------------------
     def close(self):
         if getattr(self, "h", None) and self.h.value:
@@ -302,7 +325,7 @@ class PbfSim:
         return ({"block": t.block, "unroll": t.unroll, "list_block": t.list_block, "xsph_unroll": t.xsph_unroll},
                 float(ms.value))
 
-    STAGES = ("predict", "scan", "sort", "lists", "lambda", "delta", "xsph")
+    STAGES = ("predict", "scan", "sort", "lists", "lambda", "delta", "xsph", "solve")
 
     def profile_step(self, dt: float) -> dict:
         """One step with a CUDA event after each stage (direct launches):
