@@ -430,19 +430,30 @@ LUSTRINE_API int lustrine_pbf_profile_step(lustrine_pbf* s, float dt, double* st
  * the neighbour-list build.  block and list_block: 64, 128 or 256 threads;
  * unroll: neighbour gathers in flight per thread of the lambda and delta-p
  * passes, 1, 2, 4 or 8; xsph_unroll: the same for the XSPH pass (0 in
- * lustrine_pbf_set_tuning: as unroll). */
+ * lustrine_pbf_set_tuning: as unroll); particles_per_thread: 1 or 2 particles
+ * per thread of the lambda and delta-p passes, whose lists are walked
+ * together (0: 1; with 2, unroll is at most 2); solver and solver_threads:
+ * batches only, LUSTRINE_SOLVER_* and the on-chip solve's threads per CTA
+ * (512 or 1024; 0: unchanged). */
 typedef struct lustrine_pbf_tuning {
     int block;
     int unroll;
     int list_block;
     int xsph_unroll;
+    int particles_per_thread;
+    int solver;
+    int solver_threads;
 } lustrine_pbf_tuning;
 LUSTRINE_API int lustrine_pbf_set_tuning(lustrine_pbf* s, const lustrine_pbf_tuning* t);
 LUSTRINE_API int lustrine_pbf_get_tuning(const lustrine_pbf* s, lustrine_pbf_tuning* t);
 /* Autotuner: times `steps` graph-replayed steps of every launch shape from
  * the current state (restored before each candidate and at the end), keeps
- * the fastest and returns it with its milliseconds per step.  The state is
- * unchanged on return.  Reference mode has a single shape (returned as is). */
+ * the fastest and returns it with its milliseconds per step: block size x
+ * gathers in flight x particles per thread of the iteration passes, the list
+ * build's block size, the XSPH pass's gathers in flight and, for a batch, the
+ * solver (per-stage kernels, or the on-chip solve with 512 or 1024 threads
+ * per CTA).  The state is unchanged on return.  Reference mode has a single
+ * shape (returned as is). */
 LUSTRINE_API int lustrine_pbf_autotune(lustrine_pbf* s, float dt, int steps, lustrine_pbf_tuning* best,
                                        float* best_ms);
 /* Sand mode (LUSTRINE_MODE_SAND) inputs that lustrine_pbf_params does not

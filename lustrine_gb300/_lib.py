@@ -83,7 +83,8 @@ GRID_AUTO, GRID_DENSE, GRID_HASHED = 0, 1, 2
 
 
 class PbfTuning(C.Structure):
-    _fields_ = [("block", C.c_int), ("unroll", C.c_int), ("list_block", C.c_int), ("xsph_unroll", C.c_int)]
+    _fields_ = [("block", C.c_int), ("unroll", C.c_int), ("list_block", C.c_int), ("xsph_unroll", C.c_int),
+                ("particles_per_thread", C.c_int), ("solver", C.c_int), ("solver_threads", C.c_int)]
 
 
 class SandControls(C.Structure):

@@ -92,6 +92,7 @@ struct Tuning {
     int unroll;       // neighbour gathers in flight per thread of the lambda and delta passes (1, 2, 4, 8)
     int list_block;   // threads per block of the list build (64, 128, 256)
     int xsph_unroll;  // neighbour gathers in flight per thread of the XSPH pass (1, 2, 4, 8)
+    int ppt;          // particles per thread of the lambda and delta passes (1, 2)
 };
 
 // Mixed precision: a cell's integer coordinates packed into 32 bits,

@@ -1124,8 +1124,22 @@ extern "C" int lustrine_pbf_set_tuning(lustrine_pbf* s, const lustrine_pbf_tunin
     auto ok = [](int b) { return b == 64 || b == 128 || b == 256; };
     auto ok_u = [](int u) { return u == 1 || u == 2 || u == 4 || u == 8; };
     const int xu = t->xsph_unroll ? t->xsph_unroll : t->unroll;  // 0: as the other passes
-    if (!ok(t->block) || !ok(t->list_block) || !ok_u(t->unroll) || !ok_u(xu)) return LUSTRINE_ERR_ARGS;
-    s->tune = Tuning{t->block, t->unroll, t->list_block, xu};
+    const int ppt = t->particles_per_thread ? t->particles_per_thread : 1;
+    if (!ok(t->block) || !ok(t->list_block) || !ok_u(t->unroll) || !ok_u(xu) || (ppt != 1 && ppt != 2) ||
+        (ppt == 2 && t->unroll > 2))
+        return LUSTRINE_ERR_ARGS;
+    if (t->solver != LUSTRINE_SOLVER_STAGES && t->solver != LUSTRINE_SOLVER_ONCHIP) return LUSTRINE_ERR_ARGS;
+    if (s->is_batch()) {
+        int rc = lustrine_batch_set_solver(s, t->solver);
+        if (rc) return rc;
+        if (t->solver == LUSTRINE_SOLVER_ONCHIP && t->solver_threads) {
+            rc = lustrine_batch_set_onchip_threads(s, t->solver_threads);
+            if (rc) return rc;
+        }
+    } else if (t->solver != LUSTRINE_SOLVER_STAGES) {
+        return LUSTRINE_ERR_ARGS;
+    }
+    s->tune = Tuning{t->block, t->unroll, t->list_block, xu, ppt};
     s->invalidate_graphs();
     return LUSTRINE_OK;
 }
@@ -1136,6 +1150,9 @@ extern "C" int lustrine_pbf_get_tuning(const lustrine_pbf* s, lustrine_pbf_tunin
     t->unroll = s->tune.unroll;
     t->list_block = s->tune.list_block;
     t->xsph_unroll = s->tune.xsph_unroll;
+    t->particles_per_thread = s->tune.ppt;
+    t->solver = s->onchip ? LUSTRINE_SOLVER_ONCHIP : LUSTRINE_SOLVER_STAGES;
+    t->solver_threads = s->onchip_threads;
     return LUSTRINE_OK;
 }
 
@@ -1222,23 +1239,29 @@ extern "C" int lustrine_pbf_autotune(lustrine_pbf* s, float dt, int steps, lustr
     int rc = snapshot_take(s, sn);
     const int side = s->cur;
     Tuning keep = s->tune, top = s->tune;
+    const bool keep_onchip = s->onchip;
+    const int keep_threads = s->onchip_threads;
+    s->onchip = false;  // the per-stage kernels' shapes first
     float top_ms = 3.4e38f;
     static const int blocks[3] = {64, 128, 256};
     static const int unrolls[4] = {1, 2, 4, 8};
-    // the iteration kernels' shape first, then the list build's block size
+    // the iteration kernels' shape first (block x gathers in flight x
+    // particles per thread), then the list build's block size
     for (int bi = 0; bi < 3 && !rc; bi++)
-        for (int ui = 0; ui < 4 && !rc; ui++) {
-            s->tune = Tuning{blocks[bi], unrolls[ui], keep.list_block, unrolls[ui]};
-            s->invalidate_graphs();
-            float ms = 0.0f;
-            rc = time_candidate(s, sn, side, dt, steps, &ms);
-            if (!rc && ms < top_ms) {
-                top_ms = ms;
-                top = s->tune;
+        for (int ui = 0; ui < 4 && !rc; ui++)
+            for (int pi = 1; pi <= 2 && !rc; pi++) {
+                if (pi == 2 && unrolls[ui] > 2) continue;
+                s->tune = Tuning{blocks[bi], unrolls[ui], keep.list_block, unrolls[ui], pi};
+                s->invalidate_graphs();
+                float ms = 0.0f;
+                rc = time_candidate(s, sn, side, dt, steps, &ms);
+                if (!rc && ms < top_ms) {
+                    top_ms = ms;
+                    top = s->tune;
+                }
             }
-        }
     for (int bi = 0; bi < 3 && !rc; bi++) {
-        s->tune = Tuning{top.block, top.unroll, blocks[bi], top.xsph_unroll};
+        s->tune = Tuning{top.block, top.unroll, blocks[bi], top.xsph_unroll, top.ppt};
         s->invalidate_graphs();
         float ms = 0.0f;
         rc = time_candidate(s, sn, side, dt, steps, &ms);
@@ -1250,7 +1273,7 @@ extern "C" int lustrine_pbf_autotune(lustrine_pbf* s, float dt, int steps, lustr
     // then the XSPH pass's gathers in flight (it gains from more than the others)
     for (int ui = 0; ui < 4 && !rc; ui++) {
         if (unrolls[ui] == top.xsph_unroll) continue;
-        s->tune = Tuning{top.block, top.unroll, top.list_block, unrolls[ui]};
+        s->tune = Tuning{top.block, top.unroll, top.list_block, unrolls[ui], top.ppt};
         s->invalidate_graphs();
         float ms = 0.0f;
         rc = time_candidate(s, sn, side, dt, steps, &ms);
@@ -1259,7 +1282,29 @@ extern "C" int lustrine_pbf_autotune(lustrine_pbf* s, float dt, int steps, lustr
             top = s->tune;
         }
     }
+    // a batch: the on-chip solve (both CTA widths) against the best per-stage shape
+    bool top_onchip = false;
+    int top_threads = keep_threads;
+    if (!rc && s->onchip_clusters > 0) {
+        s->tune = top;
+        for (int threads : {512, 1024}) {
+            if (threads == 512 && !s->onchip_clusters512) continue;
+            s->onchip = true;
+            s->onchip_threads = threads;
+            s->invalidate_graphs();
+            float ms = 0.0f;
+            rc = time_candidate(s, sn, side, dt, steps, &ms);
+            if (rc) break;
+            if (ms < top_ms) {
+                top_ms = ms;
+                top_onchip = true;
+                top_threads = threads;
+            }
+        }
+    }
     s->tune = rc ? keep : top;
+    s->onchip = rc ? keep_onchip : top_onchip;
+    s->onchip_threads = rc ? keep_threads : top_threads;
     s->invalidate_graphs();
     s->prm.use_graph = use_graph;
     int rc2 = snapshot_restore(s, sn, side);

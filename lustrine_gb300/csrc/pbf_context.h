@@ -22,7 +22,7 @@ struct lustrine_pbf {
     lustrine_pbf_params prm{};
     lgb::StepParams sp{};
     lgb::CellPack cp{};
-    lgb::Tuning tune{128, 2, 128, 8};
+    lgb::Tuning tune{128, 2, 128, 8, 1};
     int n = 0, ns = 0;
     int cap = 0;  // fluid particles the buffers hold (n <= cap; sources append up to it)
     cudaStream_t stream = nullptr;

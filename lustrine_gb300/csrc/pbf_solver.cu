@@ -310,11 +310,43 @@ __device__ __forceinline__ void for_each_entry(const StepParams& p, const int* _
     }
 }
 
+// P particles per thread: the lists of slots s[0..P) walked together, U
+// entries of each per round, so the loads of all P lists and their gathers
+// are in flight at once; f(r, entry, position) per entry of particle r in
+// list order.  Past its own count a particle reads the sentinel entry (every
+// pair term with it is exactly zero), so the lists may differ in length.
+template <int U, int P, bool SOL, class F>
+__device__ __forceinline__ void for_each_entry_p(const StepParams& p, const int* __restrict__ nbr,
+                                                 const int (&s)[P], const int (&c)[P],
+                                                 const float4* __restrict__ xs, const float4* __restrict__ solid,
+                                                 F&& f) {
+    int cmax = 0;
+#pragma unroll
+    for (int r = 0; r < P; r++) cmax = max(cmax, c[r]);
+    const int sent = sentinel_entry(p);
+    for (int k = 0; k < cmax; k += U) {
+        int e[P][U];
+        float4 q[P][U];
+#pragma unroll
+        for (int r = 0; r < P; r++)
+#pragma unroll
+            for (int u = 0; u < U; u++) e[r][u] = k + u < c[r] ? __ldg(&nbr[(size_t)(k + u) * p.n + s[r]]) : sent;
+#pragma unroll
+        for (int r = 0; r < P; r++)
+#pragma unroll
+            for (int u = 0; u < U; u++) q[r][u] = SOL ? load_entry(e[r][u], xs, solid) : xs[entry_slot(e[r][u])];
+#pragma unroll
+        for (int u = 0; u < U; u++)
+#pragma unroll
+            for (int r = 0; r < P; r++) f(r, e[r][u], q[r][u]);
+    }
+}
+
 // Lambda pass over the lists (iterations after the first); U neighbour
 // gathers in flight per thread.
 // F: bit 0 mixed precision, bit 1 the scene has static particles (the
 // solid-free kernels skip the per-entry solid tests).
-template <int F, int U, int B>
+template <int F, int U, int B, int P = 1>
 __global__ void __launch_bounds__(B) k_lambda(StepParams p, float4* __restrict__ xs,
                                               const int* __restrict__ nbr, const int* __restrict__ cnt,
                                               const float4* __restrict__ solid,
@@ -323,68 +355,87 @@ __global__ void __launch_bounds__(B) k_lambda(StepParams p, float4* __restrict__
     pdl_wait();
     __shared__ float4 shift_tab[MIXED ? 64 : 1];
     if (MIXED) fill_shift_table(p, shift_tab);
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= p.n) return;
-    const float4 self = xs[s];
-    LambdaAcc a = lambda_init(p);
-    for_each_entry<U, SOL>(p, nbr + s, cnt, s, xs, solid, [&](int e, float4 q) {
-        float3 d = rel_t<MIXED>(self, q, e, shift_tab);
-        lambda_accumulate<MIXED>(p, a, d, SOL && entry_solid(e));
+    if (P == 1) {
+        const int s = blockIdx.x * blockDim.x + threadIdx.x;
+        if (s >= p.n) return;
+        const float4 self = xs[s];
+        LambdaAcc a = lambda_init(p);
+        for_each_entry<U, SOL>(p, nbr + s, cnt, s, xs, solid, [&](int e, float4 q) {
+            float3 d = rel_t<MIXED>(self, q, e, shift_tab);
+            lambda_accumulate<MIXED>(p, a, d, SOL && entry_solid(e));
+        });
+        reinterpret_cast<float*>(xs)[4 * (size_t)s + 3] = lambda_of(p, a);
+        if (rho) rho[s] = density_of(p, a);
+        return;
+    }
+    // P slots per thread, B apart (each load of the block coalesced)
+    int s[P], c[P];
+    float4 self[P];
+    LambdaAcc a[P];
+#pragma unroll
+    for (int r = 0; r < P; r++) {
+        s[r] = (blockIdx.x * P + r) * B + threadIdx.x;
+        const bool ok = s[r] < p.n;
+        c[r] = ok ? __ldg(&cnt[s[r]]) : 0;
+        self[r] = ok ? xs[s[r]] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        a[r] = lambda_init(p);
+    }
+    for_each_entry_p<U, P, SOL>(p, nbr, s, c, xs, solid, [&](int r, int e, float4 q) {
+        float3 d = rel_t<MIXED>(self[r], q, e, shift_tab);
+        lambda_accumulate<MIXED>(p, a[r], d, SOL && entry_solid(e));
     });
-    reinterpret_cast<float*>(xs)[4 * (size_t)s + 3] = lambda_of(p, a);
-    if (rho) rho[s] = density_of(p, a);
+#pragma unroll
+    for (int r = 0; r < P; r++) {
+        if (s[r] >= p.n) continue;
+        reinterpret_cast<float*>(xs)[4 * (size_t)s[r] + 3] = lambda_of(p, a[r]);
+        if (rho) rho[s[r]] = density_of(p, a[r]);
+    }
 }
 
 // Position correction with s_corr, solid push-out and box clamp (Jacobi).
-// The last iteration also writes v = (x* - x) / dt.  With up to 2 gathers in
-// flight the kernel fits 40 registers without spilling: 6 blocks of 256
-// threads per SM instead of 5 (a 262,144-particle pass then takes 1.12
-// waves of the GPU instead of 1.35).
-template <int F, int U, int B>
-__global__ void __launch_bounds__(B, U <= 2 ? 1536 / B : 1) k_delta(StepParams p, CellPack cp, const float4* __restrict__ xs,
-                                               float4* __restrict__ xs_out, const int* __restrict__ nbr,
-                                               const int* __restrict__ cnt,
-                                               const float4* __restrict__ solid,
-                                               const int* __restrict__ key_sorted,
-                                               const float4* __restrict__ x, float4* __restrict__ v_out) {
-    constexpr bool MIXED = (F & 1) != 0, SOL = (F & 2) != 0;
-    pdl_wait();
-    __shared__ float4 shift_tab[MIXED ? 64 : 1];
-    if (MIXED) fill_shift_table(p, shift_tab);
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= p.n) return;
-    const float4 self = xs[s];
+// The last iteration also writes v = (x* - x) / dt.
+struct DeltaAcc {
+    float px, py, pz, cx, cy, cz;
+    int nct;
+};
+
+template <bool MIXED, bool SOL>
+__device__ __forceinline__ void delta_pair(const StepParams& p, DeltaAcc& a, const float4& self, int e, float4 q,
+                                           const float4* tab) {
     const float li = self.w;
-    float px = 0.0f, py = 0.0f, pz = 0.0f;
-    float cx = 0.0f, cy = 0.0f, cz = 0.0f;
-    int nct = 0;
-    for_each_entry<U, SOL>(p, nbr + s, cnt, s, xs, solid, [&](int e, float4 q) {
-        const bool sol = SOL && entry_solid(e);
-        float3 d = rel_t<MIXED>(self, q, e, shift_tab);
-        const float r2 = dot3e(d.x, d.y, d.z);
-        const float inv_r = inv_r_of(r2);
-        const float r = __fmul_rn(r2, inv_r);
-        const float lj = sol ? li : q.w;
-        const float w = __fmul_rn(__fadd_rn(__fadd_rn(li, lj), scorr_hd(p, hdiff(p, r2))), spiky_g(p, r, inv_r));
-        px = __fmaf_rn(w, d.x, px);
-        py = __fmaf_rn(w, d.y, py);
-        pz = __fmaf_rn(w, d.z, pz);
-        if (sol && r < p.contact && r2 > 0.0f) {
-            const float t = __fmul_rn(__fsub_rn(p.contact, r), inv_r);
-            cx = __fmaf_rn(t, d.x, cx);
-            cy = __fmaf_rn(t, d.y, cy);
-            cz = __fmaf_rn(t, d.z, cz);
-            nct++;
-        }
-    });
-    // dp = (m / rho0) sum (lambda_i + lambda_j + s_corr) dW, dW = -Ks g d
+    const bool sol = SOL && entry_solid(e);
+    float3 d = rel_t<MIXED>(self, q, e, tab);
+    const float r2 = dot3e(d.x, d.y, d.z);
+    const float inv_r = inv_r_of(r2);
+    const float r = __fmul_rn(r2, inv_r);
+    const float lj = sol ? li : q.w;
+    const float w = __fmul_rn(__fadd_rn(__fadd_rn(li, lj), scorr_hd(p, hdiff(p, r2))), spiky_g(p, r, inv_r));
+    a.px = __fmaf_rn(w, d.x, a.px);
+    a.py = __fmaf_rn(w, d.y, a.py);
+    a.pz = __fmaf_rn(w, d.z, a.pz);
+    if (sol && r < p.contact && r2 > 0.0f) {
+        const float t = __fmul_rn(__fsub_rn(p.contact, r), inv_r);
+        a.cx = __fmaf_rn(t, d.x, a.cx);
+        a.cy = __fmaf_rn(t, d.y, a.cy);
+        a.cz = __fmaf_rn(t, d.z, a.cz);
+        a.nct++;
+    }
+}
+
+// dp = (m / rho0) sum (lambda_i + lambda_j + s_corr) dW, dW = -Ks g d; the
+// solid push-out averaged; the box clamp; x* and (last pass) v written.
+template <bool MIXED>
+__device__ __forceinline__ void delta_finish(const StepParams& p, const CellPack& cp, int s, const float4& self,
+                                             const DeltaAcc& a, float4* __restrict__ xs_out,
+                                             const int* __restrict__ key_sorted, const float4* __restrict__ x,
+                                             float4* __restrict__ v_out) {
     const float kd = __fmul_rn(-p.ks, p.mr);
-    float dx = __fmul_rn(px, kd), dy = __fmul_rn(py, kd), dz = __fmul_rn(pz, kd);
-    if (nct) {
-        const float inv = __frcp_rn((float)nct);
-        dx = __fmaf_rn(cx, inv, dx);
-        dy = __fmaf_rn(cy, inv, dy);
-        dz = __fmaf_rn(cz, inv, dz);
+    float dx = __fmul_rn(a.px, kd), dy = __fmul_rn(a.py, kd), dz = __fmul_rn(a.pz, kd);
+    if (a.nct) {
+        const float inv = __frcp_rn((float)a.nct);
+        dx = __fmaf_rn(a.cx, inv, dx);
+        dy = __fmaf_rn(a.cy, inv, dy);
+        dz = __fmaf_rn(a.cz, inv, dz);
     }
     float4 out;
     int3 cs = make_int3(0, 0, 0);
@@ -410,6 +461,49 @@ __global__ void __launch_bounds__(B, U <= 2 ? 1536 / B : 1) k_delta(StepParams p
         }
         v_out[s] = make_float4(__fmul_rn(d.x, p.inv_dt), __fmul_rn(d.y, p.inv_dt), __fmul_rn(d.z, p.inv_dt), 0.0f);
     }
+}
+
+// With one particle per thread and up to 2 gathers in flight the kernel
+// fits 40 registers without spilling: 6 blocks of 256 threads per SM instead
+// of 5 (a 262,144-particle pass then takes 1.12 waves of the GPU instead of
+// 1.35).  P = 2: two particles per thread (B apart), their lists walked
+// together.
+template <int F, int U, int B, int P = 1>
+__global__ void __launch_bounds__(B, (U <= 2 && P == 1) ? 1536 / B : 1)
+    k_delta(StepParams p, CellPack cp, const float4* __restrict__ xs, float4* __restrict__ xs_out,
+            const int* __restrict__ nbr, const int* __restrict__ cnt, const float4* __restrict__ solid,
+            const int* __restrict__ key_sorted, const float4* __restrict__ x, float4* __restrict__ v_out) {
+    constexpr bool MIXED = (F & 1) != 0, SOL = (F & 2) != 0;
+    pdl_wait();
+    __shared__ float4 shift_tab[MIXED ? 64 : 1];
+    if (MIXED) fill_shift_table(p, shift_tab);
+    if (P == 1) {
+        const int s = blockIdx.x * blockDim.x + threadIdx.x;
+        if (s >= p.n) return;
+        const float4 self = xs[s];
+        DeltaAcc a{0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0};
+        for_each_entry<U, SOL>(p, nbr + s, cnt, s, xs, solid,
+                               [&](int e, float4 q) { delta_pair<MIXED, SOL>(p, a, self, e, q, shift_tab); });
+        delta_finish<MIXED>(p, cp, s, self, a, xs_out, key_sorted, x, v_out);
+        return;
+    }
+    int s[P], c[P];
+    float4 self[P];
+    DeltaAcc a[P];
+#pragma unroll
+    for (int r = 0; r < P; r++) {
+        s[r] = (blockIdx.x * P + r) * B + threadIdx.x;
+        const bool ok = s[r] < p.n;
+        c[r] = ok ? __ldg(&cnt[s[r]]) : 0;
+        self[r] = ok ? xs[s[r]] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        a[r] = DeltaAcc{0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0};
+    }
+    for_each_entry_p<U, P, SOL>(p, nbr, s, c, xs, solid, [&](int r, int e, float4 q) {
+        delta_pair<MIXED, SOL>(p, a[r], self[r], e, q, shift_tab);
+    });
+#pragma unroll
+    for (int r = 0; r < P; r++)
+        if (s[r] < p.n) delta_finish<MIXED>(p, cp, s[r], self[r], a[r], xs_out, key_sorted, x, v_out);
 }
 
 // XSPH viscosity (Macklin & Mueller eq. 17) and commit x = x*.
@@ -821,6 +915,38 @@ void launch_key(bool mixed, const StepParams& p, const CellPack& cp, const float
 // scene pick one (TUNE_DISPATCH expands the switch).
 #define TUNE_LAUNCH(KERNEL, MIX, U_, B_, N, ST, ...)                                            \
     launch_k(KERNEL<MIX, U_, B_>, blocks_for(N, B_), B_, ST, pdl_enabled(), __VA_ARGS__)
+// two particles per thread (the lambda and delta-p passes), U in {1, 2}
+#define TUNE_LAUNCH_P2(KERNEL, MIX, U_, B_, N, ST, ...)                                         \
+    launch_k(KERNEL<MIX, U_, B_, 2>, blocks_for(N, 2 * B_), B_, ST, pdl_enabled(), __VA_ARGS__)
+#define TUNE_BLOCKS_P2(KERNEL, MIX, U_, tu, N, ST, ...)                                         \
+    do {                                                                                        \
+        if (tu.block <= 64)                                                                     \
+            TUNE_LAUNCH_P2(KERNEL, MIX, U_, 64, N, ST, __VA_ARGS__);                            \
+        else if (tu.block <= 128)                                                               \
+            TUNE_LAUNCH_P2(KERNEL, MIX, U_, 128, N, ST, __VA_ARGS__);                           \
+        else                                                                                    \
+            TUNE_LAUNCH_P2(KERNEL, MIX, U_, 256, N, ST, __VA_ARGS__);                           \
+    } while (0)
+#define TUNE_CASE_P2(KERNEL, MIX, tu, N, ST, ...)                                               \
+    do {                                                                                        \
+        if (tu.unroll <= 1)                                                                     \
+            TUNE_BLOCKS_P2(KERNEL, MIX, 1, tu, N, ST, __VA_ARGS__);                             \
+        else                                                                                    \
+            TUNE_BLOCKS_P2(KERNEL, MIX, 2, tu, N, ST, __VA_ARGS__);                             \
+    } while (0)
+#define TUNE_DISPATCH_PPT(KERNEL, mixed, tu, N, ST, ...)                                        \
+    do {                                                                                        \
+        if (tu.ppt != 2) {                                                                      \
+            TUNE_DISPATCH(KERNEL, mixed, tu, N, ST, __VA_ARGS__);                               \
+            break;                                                                              \
+        }                                                                                       \
+        switch ((mixed ? 1 : 0) | (p.ns > 0 ? 2 : 0)) {                                         \
+            case 0: TUNE_CASE_P2(KERNEL, 0, tu, N, ST, __VA_ARGS__); break;                     \
+            case 1: TUNE_CASE_P2(KERNEL, 1, tu, N, ST, __VA_ARGS__); break;                     \
+            case 2: TUNE_CASE_P2(KERNEL, 2, tu, N, ST, __VA_ARGS__); break;                     \
+            default: TUNE_CASE_P2(KERNEL, 3, tu, N, ST, __VA_ARGS__); break;                    \
+        }                                                                                       \
+    } while (0)
 #define TUNE_BLOCKS(KERNEL, MIX, U_, tu, N, ST, ...)                                            \
     do {                                                                                        \
         if (tu.block <= 64)                                                                     \
@@ -885,7 +1011,7 @@ void launch_lists_lambda(bool mixed, const Tuning& tu, const StepParams& p, cons
 void launch_lambda(bool mixed, const Tuning& tu, const StepParams& p, float4* xs, const int* nbr,
                    const int* cnt, const float4* solid, float* rho, cudaStream_t st) {
     if (p.n <= 0) return;
-    TUNE_DISPATCH(k_lambda, mixed, tu, p.n, st, p, xs, nbr, cnt, solid, rho);
+    TUNE_DISPATCH_PPT(k_lambda, mixed, tu, p.n, st, p, xs, nbr, cnt, solid, rho);
 }
 
 void launch_delta(bool mixed, const Tuning& tu, const StepParams& p, const CellPack& cp,
@@ -893,7 +1019,7 @@ void launch_delta(bool mixed, const Tuning& tu, const StepParams& p, const CellP
                   const float4* solid, const int* key_sorted, const float4* x, float4* v_out,
                   cudaStream_t st) {
     if (p.n <= 0) return;
-    TUNE_DISPATCH(k_delta, mixed, tu, p.n, st, p, cp, xs, xs_out, nbr, cnt, solid, key_sorted, x, v_out);
+    TUNE_DISPATCH_PPT(k_delta, mixed, tu, p.n, st, p, cp, xs, xs_out, nbr, cnt, solid, key_sorted, x, v_out);
 }
 
 void launch_xsph(bool mixed, const Tuning& tu, const StepParams& p, const CellPack& cp,

@@ -94,6 +94,12 @@ def sand_params(X, Y, Z, *, radius=0.5, kernel_radius_scale=2.0, mass=1.0, gravi
     return p
 
 
+def _tuning_dict(t) -> dict:
+    return {"block": t.block, "unroll": t.unroll, "list_block": t.list_block, "xsph_unroll": t.xsph_unroll,
+            "particles_per_thread": t.particles_per_thread, "solver": t.solver,
+            "solver_threads": t.solver_threads}
+
+
 def _f32(a, n):
     a = np.ascontiguousarray(a, dtype=np.float32).reshape(-1)
     if a.size != 3 * n:
@@ -276,7 +282,7 @@ class PbfSim:
     def get_tuning(self) -> dict:
         t = _lib.PbfTuning()
         check(self.lib.lustrine_pbf_get_tuning(self.h, C.byref(t)), "get_tuning")
-        return {"block": t.block, "unroll": t.unroll, "list_block": t.list_block, "xsph_unroll": t.xsph_unroll}
+        return _tuning_dict(t)
 
     # sand mode -------------------------------------------------------------
     def set_sand_controls(self, player=None, attract=None, blow=None, attract_radius=None,
@@ -311,8 +317,9 @@ class PbfSim:
             raise ValueError(f"expected {self.n} flags, got {a.size}")
         check(self.lib.lustrine_pbf_set_attracted(self.h, a.ctypes.data), "set_attracted")
 
-    def set_tuning(self, block: int, unroll: int, list_block: int, xsph_unroll: int = 0):
-        t = _lib.PbfTuning(block, unroll, list_block, xsph_unroll)
+    def set_tuning(self, block: int, unroll: int, list_block: int, xsph_unroll: int = 0,
+                   particles_per_thread: int = 1, solver: int = 0, solver_threads: int = 0):
+        t = _lib.PbfTuning(block, unroll, list_block, xsph_unroll, particles_per_thread, solver, solver_threads)
         check(self.lib.lustrine_pbf_set_tuning(self.h, C.byref(t)), "set_tuning")
 
     def autotune(self, dt: float, steps: int = 3) -> tuple[dict, float]:
@@ -322,8 +329,7 @@ class PbfSim:
         ms = C.c_float()
         check(self.lib.lustrine_pbf_autotune(self.h, float(dt), int(steps), C.byref(t), C.byref(ms)),
               "autotune")
-        return ({"block": t.block, "unroll": t.unroll, "list_block": t.list_block, "xsph_unroll": t.xsph_unroll},
-                float(ms.value))
+        return _tuning_dict(t), float(ms.value)
 
     STAGES = ("predict", "scan", "sort", "lists", "lambda", "delta", "xsph", "solve")
 

@@ -50,7 +50,8 @@ def tune(sim: PbfSim, dt: float, steps: int = 3, cache: str | None = CACHE, refr
     db = _load(cache) if cache else {}
     if not refresh and key in db:
         t = db[key]["tuning"]
-        sim.set_tuning(t["block"], t["unroll"], t["list_block"], t.get("xsph_unroll", 0))
+        sim.set_tuning(t["block"], t["unroll"], t["list_block"], t.get("xsph_unroll", 0),
+                       t.get("particles_per_thread", 1), t.get("solver", 0), t.get("solver_threads", 0))
         return {"tuning": t, "ms": db[key]["ms"], "cached": True}
     t, ms = sim.autotune(dt, steps)
     if cache:

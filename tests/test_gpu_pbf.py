@@ -174,6 +174,34 @@ def test_autotune_keeps_state_and_all_shapes_agree():
     sim.close()
 
 
+@pytest.mark.parametrize("with_solids", [False, True])
+def test_two_particles_per_thread_give_the_same_bits(with_solids):
+    """The lambda and delta-p passes with two particles per thread (their
+    lists walked together, the shorter one padded with the sentinel, whose
+    terms are exact zeros) compute the same fp32 bits as one per thread."""
+    from lustrine_gb300 import PbfSim, scenes
+    rng = np.random.default_rng(8)
+    if with_solids:
+        solid, _ = scenes.heightmap_solids(16, 600, origin=(0, 0, 0), rng=rng, max_height=3)
+        x = scenes.jitter(scenes.lattice((8, 8, 8), (4, 3, 4)), 0.05, rng)
+        sc = scenes.Scene("solids", (16, 14, 16), x, solid)
+    else:
+        sc = scenes.config0(seed=31)
+    res = []
+    for unroll, ppt in ((1, 1), (2, 1), (1, 2), (2, 2)):
+        sim = PbfSim(_params(sc), sc.n, sc.ns)
+        sim.upload(sc.x, None, sc.solid if sc.ns else None)
+        sim.set_tuning(128, unroll, 128, 2, ppt)
+        assert sim.get_tuning()["particles_per_thread"] == ppt
+        sim.step(sc.dt, 4)
+        assert sim.status() == 0
+        res.append(sim.download(lambdas=True, density=True))
+        sim.close()
+    for r in res[1:]:
+        for a, b in zip(res[0], r):
+            np.testing.assert_array_equal(a, b)
+
+
 def test_graph_and_direct_launches_are_identical():
     from lustrine_gb300 import PbfSim, scenes
     sc = scenes.config0(seed=24)
