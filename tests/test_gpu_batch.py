@@ -102,3 +102,35 @@ def test_batch_config3_shapes_run():
         assert (xs >= 0.5 - 1e-4).all() and (xs <= np.array(sc.domain) - 0.5 + 1e-4).all()
         off += sc.n
     b.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_sharded_batches_equal_the_full_batch(precision):
+    """The multi-GPU split of a batch (sharding.shard_scenes: every rank
+    steps one batch of its own scenes, no collective on the data path) on one
+    GPU: the batches built from shard 0 and shard 1 of 24 scenes of the
+    512-scene distribution give every scene exactly what the full batch
+    gives."""
+    from lustrine_gb300 import PbfSim, pbf_params, scenes, sharding
+    scs = scenes.config3(num=24)
+    counts = [sc.n for sc in scs]
+    parts = sharding.shard_scenes(counts, 2)
+    assert sorted(parts[0] + parts[1]) == list(range(24)) and parts[0] and parts[1]
+
+    def run(ids):
+        sub = [scs[i] for i in ids]
+        b = PbfSim.batch(pbf_params(8, 8, 8, iterations=4, precision=precision), [sc.domain for sc in sub],
+                         [sc.n for sc in sub])
+        b.upload(np.concatenate([sc.x for sc in sub]))
+        b.step(1 / 60, 3)
+        assert b.status() == 0
+        x, v, _, _ = b.download()
+        b.close()
+        off = np.concatenate([[0], np.cumsum([sc.n for sc in sub])])
+        return {i: (x[off[k]:off[k + 1]], v[off[k]:off[k + 1]]) for k, i in enumerate(ids)}
+
+    full = run(list(range(24)))
+    for ids in parts:
+        for i, (x, v) in run(ids).items():
+            np.testing.assert_array_equal(x, full[i][0])
+            np.testing.assert_array_equal(v, full[i][1])
