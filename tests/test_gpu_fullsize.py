@@ -11,9 +11,11 @@ box, FP64 mass):
   and z to its neighbourhood (y and the floor kept).
 
 Tolerances: per particle, positions within 1e-5 of max(h, its FP64
-displacement) plus two units in the last place of an fp32 number of the
-coordinate's size (the representation's own rounding; velocities the same
-over dt); densities within 1e-5 relative in fp32 and 1e-4 in mixed precision
+displacement) plus half a unit in the last place of an fp32 number of the
+coordinate's size per rounding of the stored position (fp32 rounds it at the
+prediction, at every Jacobi update and at the commit; mixed precision keeps
+cell-relative offsets and rounds the absolute position once, at the download,
+counted twice); velocities the same over dt; densities within 1e-5 relative in fp32 and 1e-4 in mixed precision
 (its contract, also 3,900+ cells from the origin), lambdas within that
 density tolerance carried through lambda = -(rho / rho0 - 1) / (S + eps) plus
 1e-4 of max |lambda| (near the rest density lambda is a small difference);
@@ -25,16 +27,21 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def position_bound(x64, x0, h=1.0):
+def position_bound(x64, x0, roundings, h=1.0):
     """Per-particle bound on |x - x64|: 1e-5 of max(h, the FP64 displacement)
-    plus two fp32 units in the last place of the coordinates' size."""
+    plus half an fp32 unit in the last place of the coordinates' size per
+    rounding of the stored position (normwise over the three axes)."""
     disp = np.linalg.norm(np.asarray(x64, np.float64) - np.asarray(x0, np.float64), axis=1)
     ulp = np.spacing(np.abs(np.asarray(x64, np.float32)).max(axis=1)).astype(np.float64)
-    return 1e-5 * np.maximum(h, disp) + 2.0 * np.sqrt(3.0) * ulp
+    return 1e-5 * np.maximum(h, disp) + np.sqrt(3.0) * 0.5 * roundings * ulp
 
 
-def check_positions(x, x64, x0, v, v64, dt, h=1.0):
-    bound = position_bound(x64, x0, h)
+def roundings_of(precision, iterations):
+    return 2 if precision else iterations + 2
+
+
+def check_positions(x, x64, x0, v, v64, dt, roundings, h=1.0):
+    bound = position_bound(x64, x0, roundings, h)
     err = np.linalg.norm(np.asarray(x, np.float64) - x64, axis=1)
     assert np.all(err <= bound), (err.max(), int(np.argmax(err / bound)))
     verr = np.linalg.norm(np.asarray(v, np.float64) - v64, axis=1)
@@ -63,7 +70,8 @@ def check_sets(cnt, idx, xs64, h, solid=None):
     allowed = np.sort(src * N + dst)
     rows = np.repeat(np.arange(n, dtype=np.int64), cnt)
     cols = idx[np.arange(idx.shape[1])[None, :] < cnt[:, None]].astype(np.int64)
-    got = np.sort(rows * N + cols)
+    keep = cols != rows  # PBF lists report the particle itself first
+    got = np.sort(rows[keep] * N + cols[keep])
     assert len(got) == len(np.unique(got))
     assert np.all(np.isin(sure, got)), int((~np.isin(sure, got)).sum())
     assert np.all(np.isin(got, allowed)), int((~np.isin(got, allowed)).sum())
@@ -101,10 +109,12 @@ def _step_and_check(orc, sc, precision):
     assert cnt.max() <= 16
     q = _oracle_params(orc, p, sc.domain)
     o = orc.pbf_step(q, sc.dt, sc.x, np.zeros_like(sc.x), solid=sc.solid if sc.ns else None)
-    check_positions(x, o["x"], sc.x, v, o["v"], sc.dt)
+    check_positions(x, o["x"], sc.x, v, o["v"], sc.dt, roundings_of(precision, sc.iterations))
     xs64 = predicted64(sc.x, np.zeros_like(sc.x), p, sc.dt, sc.domain)
     edge = check_sets(cnt, idx, xs64, p.kernel_radius, sc.solid if sc.ns else None)
-    assert edge <= 1e-3 * sc.n, edge
+    # the lattice puts six neighbours of every particle at r = h +- 0.07 (jitter
+    # +-0.05 per axis): about 1.2e-3 pairs per particle fall within 1e-5 h of h
+    assert edge <= 3e-3 * sc.n, edge
     tol = 1e-4 if precision else 1e-5  # the mixed representation's density contract: 1e-4
     rmax = np.abs(o["density"]).max()
     assert np.abs(rho - o["density"]).max() <= tol * rmax
@@ -185,7 +195,8 @@ def test_config3_full_batch_step_vs_fp64_oracle(orc, mixed):
         sc = scs[k]
         q = _oracle_params(orc, p, sc.domain)
         o = orc.pbf_step(q, sc.dt, sc.x, np.zeros_like(sc.x))
-        check_positions(x[off[k]:off[k + 1]], o["x"], sc.x, v[off[k]:off[k + 1]], o["v"], sc.dt)
+        check_positions(x[off[k]:off[k + 1]], o["x"], sc.x, v[off[k]:off[k + 1]], o["v"], sc.dt,
+                        roundings_of(mixed, 4))
 
 
 def test_config1_reference_semantics_full_step_vs_oracle(orc):
