@@ -78,6 +78,15 @@ __device__ __forceinline__ Geo geo_slot(const StepParams& p, int s) {
     return p.scenes ? geo_scene(p, __ldg(&p.scene_of[s])) : geo_single(p);
 }
 
+// The scene of fluid slot s (0 for one scene), loaded ahead of its use, and
+// the geometry from it.
+__device__ __forceinline__ int scene_index(const StepParams& p, int s) {
+    return p.scenes ? __ldg(&p.scene_of[s]) : 0;
+}
+__device__ __forceinline__ Geo geo_of(const StepParams& p, int scene) {
+    return p.scenes ? geo_scene(p, scene) : geo_single(p);
+}
+
 __device__ __forceinline__ int linear_cell(const Geo& g, int3 c) {
     return g.off + c.y * g.gx * g.gz + c.x * g.gz + c.z;
 }

@@ -280,21 +280,45 @@ __global__ void __launch_bounds__(B) k_lists_lambda(StepParams p, CellPack cp, f
 }
 
 // Walk a particle's list U entries at a time, calling f(entry, position)
-// for each (SOL: the scene has static particles, whose entries read solid).  The first U entries are loaded together with the count and
-// every next chunk's entries while the current chunk's positions are
-// gathered.  The list is padded with sentinel entries to a multiple of U
-// (the list build's pad), and the buffer holds at least 8 rows, so every
-// entry of a chunk below the count is valid and every load in bounds.
-template <int U, bool SOL, class F>
+// for each (SOL: the scene has static particles, whose entries read solid).
+// E entries (U or LIST_PAD_MAX) are loaded together with the count, the
+// rest a chunk ahead of their gathers: with E = LIST_PAD_MAX a list of up to
+// 8 neighbours waits for one round trip to DRAM for its entries and then one
+// to L2 per chunk of gathers, at the price of loading 8 entries for shorter
+// lists (the position pass gains, measured; the lambda pass, with fewer
+// instructions per pair to hide the latency behind, loses and keeps E = U).
+// The list is padded with sentinel entries to a multiple of U (the list
+// build's pad) and the buffer holds at least LIST_PAD_MAX rows (2
+// LIST_PAD_MAX when a count exceeds LIST_PAD_MAX), so every entry a chunk
+// below the count reads is valid and every load in bounds.
+template <int U, bool SOL, int E = U, class F>
 __device__ __forceinline__ void for_each_entry(const StepParams& p, const int* __restrict__ col,
                                                const int* __restrict__ cnt, int s,
                                                const float4* __restrict__ xs,
                                                const float4* __restrict__ solid, F&& f) {
+    static_assert(E % U == 0 && E <= LIST_PAD_MAX, "prefetch depth");
+    int e0[E];
+#pragma unroll
+    for (int u = 0; u < E; u++) e0[u] = __ldg(&col[(size_t)u * p.n]);
+    const int c = __ldg(&cnt[s]);
+    if (E > U) {
+#pragma unroll
+        for (int k = 0; k < E; k += U) {
+            if (k >= c) return;
+            float4 q[U];
+#pragma unroll
+            for (int u = 0; u < U; u++) q[u] = SOL ? load_entry(e0[k + u], xs, solid) : xs[entry_slot(e0[k + u])];
+#pragma unroll
+            for (int u = 0; u < U; u++) f(e0[k + u], q[u]);
+        }
+        if (c <= E) return;
+    }
+    // the chunks from E on (E = U: from the first), each chunk's entries
+    // loaded while the one before is gathered
     int nx[U];
 #pragma unroll
-    for (int u = 0; u < U; u++) nx[u] = __ldg(&col[(size_t)u * p.n]);
-    const int c = __ldg(&cnt[s]);
-    for (int k = 0; k < c; k += U) {
+    for (int u = 0; u < U; u++) nx[u] = E > U ? __ldg(&col[(size_t)(E + u) * p.n]) : e0[u];
+    for (int k = E > U ? E : 0; k < c; k += U) {
         int e[U];
         float4 q[U];
 #pragma unroll
@@ -424,11 +448,14 @@ __device__ __forceinline__ void delta_pair(const StepParams& p, DeltaAcc& a, con
 
 // dp = (m / rho0) sum (lambda_i + lambda_j + s_corr) dW, dW = -Ks g d; the
 // solid push-out averaged; the box clamp; x* and (last pass) v written.
+// scene: the slot's scene index (scene_index); packed: its packed cell in
+// mixed precision on a sorted packed-cell array (else unused), both loaded
+// before the neighbour walk.
 template <bool MIXED>
 __device__ __forceinline__ void delta_finish(const StepParams& p, const CellPack& cp, int s, const float4& self,
                                              const DeltaAcc& a, float4* __restrict__ xs_out,
                                              const int* __restrict__ key_sorted, const float4* __restrict__ x,
-                                             float4* __restrict__ v_out) {
+                                             float4* __restrict__ v_out, int scene, int packed) {
     const float kd = __fmul_rn(-p.ks, p.mr);
     float dx = __fmul_rn(a.px, kd), dy = __fmul_rn(a.py, kd), dz = __fmul_rn(a.pz, kd);
     if (a.nct) {
@@ -439,12 +466,17 @@ __device__ __forceinline__ void delta_finish(const StepParams& p, const CellPack
     }
     float4 out;
     int3 cs = make_int3(0, 0, 0);
-    const Geo g = geo_slot(p, s);
+    const Geo g = geo_of(p, scene);
     if (!MIXED) {
         out = make_float4(clampf(__fadd_rn(self.x, dx), g.lox, g.hix), clampf(__fadd_rn(self.y, dy), g.loy, g.hiy),
                           clampf(__fadd_rn(self.z, dz), g.loz, g.hiz), 0.0f);
     } else {
-        cs = slot_cell(p, cp, g, key_sorted, p.cell_sorted, s);
+        if (p.cell_sorted) {
+            const unsigned u = (unsigned)packed;
+            cs = make_int3((int)(u & cp.mx), (int)((u >> cp.by_shift) & cp.my), (int)((u >> cp.bz_shift) & cp.mz));
+        } else {
+            cs = slot_cell(p, cp, g, key_sorted, nullptr, s);
+        }
         out = make_float4(clamp_offset(p, __fadd_rn(self.x, dx), cs.x, g.lox, g.hix),
                           clamp_offset(p, __fadd_rn(self.y, dy), cs.y, g.loy, g.hiy),
                           clamp_offset(p, __fadd_rn(self.z, dz), cs.z, g.loz, g.hiz), 0.0f);
@@ -481,10 +513,13 @@ __global__ void __launch_bounds__(B, (U <= 2 && P == 1) ? 1536 / B : 1)
         const int s = blockIdx.x * blockDim.x + threadIdx.x;
         if (s >= p.n) return;
         const float4 self = xs[s];
+        const int scene = scene_index(p, s);
+        const int packed = (MIXED && p.cell_sorted) ? __ldg(&p.cell_sorted[s]) : 0;
         DeltaAcc a{0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0};
-        for_each_entry<U, SOL>(p, nbr + s, cnt, s, xs, solid,
-                               [&](int e, float4 q) { delta_pair<MIXED, SOL>(p, a, self, e, q, shift_tab); });
-        delta_finish<MIXED>(p, cp, s, self, a, xs_out, key_sorted, x, v_out);
+        for_each_entry<U, SOL, LIST_PAD_MAX>(p, nbr + s, cnt, s, xs, solid, [&](int e, float4 q) {
+            delta_pair<MIXED, SOL>(p, a, self, e, q, shift_tab);
+        });
+        delta_finish<MIXED>(p, cp, s, self, a, xs_out, key_sorted, x, v_out, scene, packed);
         return;
     }
     int s[P], c[P];
@@ -503,7 +538,9 @@ __global__ void __launch_bounds__(B, (U <= 2 && P == 1) ? 1536 / B : 1)
     });
 #pragma unroll
     for (int r = 0; r < P; r++)
-        if (s[r] < p.n) delta_finish<MIXED>(p, cp, s[r], self[r], a[r], xs_out, key_sorted, x, v_out);
+        if (s[r] < p.n)
+            delta_finish<MIXED>(p, cp, s[r], self[r], a[r], xs_out, key_sorted, x, v_out, scene_index(p, s[r]),
+                                (MIXED && p.cell_sorted) ? __ldg(&p.cell_sorted[s[r]]) : 0);
 }
 
 // XSPH viscosity (Macklin & Mueller eq. 17) and commit x = x*.
