@@ -60,7 +60,13 @@ enum {
 
 enum {
     LUSTRINE_PRECISION_FP32 = 0,  /* absolute fp32 positions */
-    LUSTRINE_PRECISION_MIXED = 1  /* int cell index + fp32 offset, Kahan density (PBF mode) */
+    LUSTRINE_PRECISION_MIXED = 1, /* int cell index + fp32 offset, Kahan density (PBF mode): the
+                                     iterations work on offsets from each particle's cell, every
+                                     pair adding its cell difference */
+    LUSTRINE_PRECISION_MIXED_SCENE = 2 /* the same stored state (cell index + fp32 offset), Kahan
+                                     density; the iterations work in fp32 on positions relative to
+                                     the scene's box corner (PBF mode, dense grid, boxes of at most
+                                     256 cells a side: a resolution of at most 2^-15 cell) */
 };
 
 /* ------------------------------------------------- layer 1: reference ABI */

@@ -26,7 +26,7 @@ ERRORS = {
 }
 MODE_REFERENCE, MODE_PBF, MODE_SAND = 0, 1, 2
 SOLVER_STAGES, SOLVER_ONCHIP = 0, 1
-PRECISION_FP32, PRECISION_MIXED = 0, 1
+PRECISION_FP32, PRECISION_MIXED, PRECISION_MIXED_SCENE = 0, 1, 2
 
 
 class LustrineError(RuntimeError):

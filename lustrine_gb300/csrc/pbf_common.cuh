@@ -74,6 +74,7 @@ struct StepParams {
     float gxv, gyv, gzv;  // gravity
     float lox, loy, loz, hix, hiy, hiz;  // box bounds for the position clamp
     float dt;
+    int frame;            // mixed storage, iterations in the scene frame (LUSTRINE_PRECISION_MIXED_SCENE)
 };
 
 // Sand mode: simulate_sand's per-call inputs (Simulate.cpp:156-209).

@@ -81,8 +81,10 @@ static int derive(const lustrine_pbf_params& q, int n, int ns, StepParams* sp, C
     if (!(q.s_corr_n >= 0.0f)) return LUSTRINE_ERR_ARGS;  // (W / W(dq))^n with W = 0 at r = h
     if (q.mode != LUSTRINE_MODE_REFERENCE && q.mode != LUSTRINE_MODE_PBF && q.mode != LUSTRINE_MODE_SAND)
         return LUSTRINE_ERR_ARGS;
-    if (q.precision == LUSTRINE_PRECISION_MIXED && q.mode != LUSTRINE_MODE_PBF)
-        return LUSTRINE_ERR_UNSUPPORTED;
+    if (q.precision != LUSTRINE_PRECISION_FP32 && q.precision != LUSTRINE_PRECISION_MIXED &&
+        q.precision != LUSTRINE_PRECISION_MIXED_SCENE)
+        return LUSTRINE_ERR_ARGS;
+    if (q.precision != LUSTRINE_PRECISION_FP32 && q.mode != LUSTRINE_MODE_PBF) return LUSTRINE_ERR_UNSUPPORTED;
     StepParams p;
     std::memset(&p, 0, sizeof(p));
     p.n = n;
@@ -100,6 +102,11 @@ static int derive(const lustrine_pbf_params& q, int n, int ns, StepParams* sp, C
                          (q.grid_mode == LUSTRINE_GRID_AUTO && (C > (1LL << 31) - 2 || C > 32 * parts + (1LL << 24))));
     if (q.grid_mode == LUSTRINE_GRID_HASHED && q.mode != LUSTRINE_MODE_PBF) return LUSTRINE_ERR_UNSUPPORTED;
     if (!hashed && C > (1LL << 31) - 2) return LUSTRINE_ERR_UNSUPPORTED;
+    // the scene frame: a dense grid and boxes of at most 256 cells a side
+    if (q.precision == LUSTRINE_PRECISION_MIXED_SCENE &&
+        (hashed || std::max(dX, std::max(dY, dZ)) > 256.0f * q.cell_size))
+        return LUSTRINE_ERR_UNSUPPORTED;
+    p.frame = q.precision == LUSTRINE_PRECISION_MIXED_SCENE ? 1 : 0;
     // PBF neighbour entries hold a 25-bit slot
     if (q.mode == LUSTRINE_MODE_PBF && (n >= (1 << 25) || ns >= (1 << 25))) return LUSTRINE_ERR_UNSUPPORTED;
     if (hashed) {
@@ -164,7 +171,7 @@ static int derive(const lustrine_pbf_params& q, int n, int ns, StepParams* sp, C
     }
     CellPack c;
     std::memset(&c, 0, sizeof(c));
-    if (q.precision == LUSTRINE_PRECISION_MIXED || hashed) {
+    if (q.precision != LUSTRINE_PRECISION_FP32 || hashed) {
         // cells a clamped position can occupy: 0 .. floor(hi / cell)
         int vx = (int)std::floor(p.hix / p.cell) + 1, vy = (int)std::floor(p.hiy / p.cell) + 1,
             vz = (int)std::floor(p.hiz / p.cell) + 1;
@@ -281,7 +288,7 @@ static int ctx_alloc(lustrine_pbf* s) {
     // packed cells, unsorted and sorted: the hashed grid tells cells sharing a
     // bucket apart by them; mixed precision reads a slot's cell from them
     // (shifts and masks, where the dense key would need two integer divisions)
-    if (s->sp.hash_bits || s->prm.precision == LUSTRINE_PRECISION_MIXED) {
+    if (s->sp.hash_bits || s->mixed()) {
         rc = rc ? rc : dalloc(&s->cellk, m);
         rc = rc ? rc : dalloc(&s->cell_sorted, n);
         s->sp.cell_sorted = s->cell_sorted;
@@ -641,7 +648,7 @@ static int clear_tiles(lustrine_pbf* s) {
     return LUSTRINE_OK;
 }
 
-bool lustrine_pbf::mixed() const { return prm.precision == LUSTRINE_PRECISION_MIXED; }
+bool lustrine_pbf::mixed() const { return prm.precision != LUSTRINE_PRECISION_FP32; }
 
 // Sort the static solids by cell once (ascending id within a cell).
 static int setup_solids(lustrine_pbf* s) {
@@ -694,6 +701,8 @@ static int pack_solids(lustrine_pbf* s, const float* dsolid) {
     if (rc) return rc;
     if (s->ns > 0)
         CK(cudaMemcpyAsync(s->solid_id, s->perm, (size_t)s->ns * sizeof(int), cudaMemcpyDeviceToDevice, s->stream));
+    // the passes of a scene-frame context read the static particles in that frame
+    if (s->ns > 0 && s->sp.frame) launch_to_scene_frame(s->sp, s->cp, s->solid, s->ns, s->stream);
     return LUSTRINE_OK;
 }
 

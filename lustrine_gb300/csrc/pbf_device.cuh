@@ -265,7 +265,10 @@ __device__ __forceinline__ void predict_one(const StepParams& p, const CellPack&
         renorm_axis(p, ox, c.x, g.lox, g.hix);
         renorm_axis(p, oy, c.y, g.loy, g.hiy);
         renorm_axis(p, oz, c.z, g.loz, g.hiz);
-        s = make_float4(ox, oy, oz, 0.0f);
+        // the scene frame: the position relative to the box corner
+        s = p.frame ? make_float4(__fmaf_rn((float)c.x, p.cell, ox), __fmaf_rn((float)c.y, p.cell, oy),
+                                  __fmaf_rn((float)c.z, p.cell, oz), 0.0f)
+                    : make_float4(ox, oy, oz, 0.0f);
     }
     xs[i] = s;
     const int k = cell_key(p, cp, g, c, cellk, i);
@@ -290,13 +293,14 @@ __device__ __forceinline__ LambdaAcc lambda_init(const StepParams&) {
     return LambdaAcc{0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
 }
 
-template <bool MIXED>
+// KAHAN: compensated density sum (both mixed representations)
+template <bool KAHAN>
 __device__ __forceinline__ void lambda_accumulate(const StepParams& p, LambdaAcc& a, float3 d,
                                                   bool solid) {
     const float r2 = dot3e(d.x, d.y, d.z);
     const float hd = hdiff(p, r2);
     const float w = __fmul_rn(__fmul_rn(hd, hd), hd);
-    if (MIXED) {
+    if (KAHAN) {
         const float y = __fsub_rn(w, a.comp);
         const float t = __fadd_rn(a.wsum, y);
         a.comp = __fsub_rn(__fsub_rn(t, a.wsum), y);

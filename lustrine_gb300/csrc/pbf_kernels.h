@@ -125,6 +125,8 @@ void launch_unpermute_pos(bool mixed, const StepParams& p, const CellPack& cp, c
                           const int* id, int n, float* out, cudaStream_t st);
 void launch_unpermute_pos_d(bool mixed, const StepParams& p, const CellPack& cp, const float4* a,
                             const int* id, int n, double* out, cudaStream_t st);
+// cell + offset positions (w: packed cell) into the scene frame, w kept
+void launch_to_scene_frame(const StepParams& p, const CellPack& cp, float4* a, int m, cudaStream_t st);
 void launch_pack_pos(bool mixed, const StepParams& p, const CellPack& cp, const float* in, int n,
                      const int* scene_of,
                      float4* out, cudaStream_t st);

@@ -176,7 +176,8 @@ __global__ void __launch_bounds__(T, 1) k_scene_solve(StepParams p, CellPack cp,
             const int s = sv.slot0 + l0 + lc;
             const float4 q = a.xs[s];
             const int3 c = solve_cell<MIXED>(p, cp, sv.g, a.key_sorted, q, s);
-            const float3 f = scene_frame<MIXED>(p, q, c);
+            // (a scene-frame context's prediction wrote the frame already)
+            const float3 f = p.frame ? make_float3(q.x, q.y, q.z) : scene_frame<MIXED>(p, q, c);
             sm.pos[lc] = make_float4(f.x, f.y, f.z, 0.0f);
         }
         cluster.sync();

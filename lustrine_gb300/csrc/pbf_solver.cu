@@ -91,7 +91,7 @@ __global__ void k_mark_solid_near(StepParams p, CellPack cp, const float4* __res
 // then runs as many rounds as its fullest row, not the sum over the three
 // cells of its fullest cell); a candidate's dz follows from the cell bounds,
 // loaded once per row.  The candidates come in the same order as cell by cell.
-template <bool MIXED, bool SOLID>
+template <bool MIXED, bool SOLID, bool KAHAN = MIXED>
 __device__ __forceinline__ void walk_row(const StepParams& p, const float4& self, int s,
                                          const float4* __restrict__ pos, const int* __restrict__ start,
                                          int row, int zc, int gz, int dx, int dy, LambdaAcc& a, int& c_n,
@@ -116,7 +116,7 @@ __device__ __forceinline__ void walk_row(const StepParams& p, const float4& self
         if (dot3e(d.x, d.y, d.z) <= p.h2) {
             if (c_n < p.max_nbrs) nbr[(size_t)c_n * p.n + s] = entry(t, dx, dy, dz, SOLID);
             c_n++;
-            lambda_accumulate<MIXED>(p, a, d, SOLID);
+            lambda_accumulate<KAHAN>(p, a, d, SOLID);
         }
     }
 }
@@ -126,7 +126,7 @@ __device__ __forceinline__ void walk_row(const StepParams& p, const float4& self
 // the list is the one walk_row builds).  b1, b2: the row's cell bounds, read
 // in mixed precision only (the entry's dz code and the cell shift; fp32
 // entries carry dz = 0, which no fp32 pass reads).
-template <bool MIXED, bool SOLID>
+template <bool MIXED, bool SOLID, bool KAHAN = MIXED>
 __device__ __forceinline__ void walk_range(const StepParams& p, const float4& self, int s,
                                            const float4* __restrict__ pos, int t_begin, int t_end, int b1, int b2,
                                            int dz0, int dx, int dy, LambdaAcc& a, int& c_n, int* __restrict__ nbr) {
@@ -150,7 +150,7 @@ __device__ __forceinline__ void walk_range(const StepParams& p, const float4& se
             if (dot3e(d.x, d.y, d.z) <= p.h2) {
                 if (c_n < p.max_nbrs) nbr[(size_t)c_n * p.n + s] = entry(t, dx, dy, dz, SOLID);
                 c_n++;
-                lambda_accumulate<MIXED>(p, a, d, SOLID);
+                lambda_accumulate<KAHAN>(p, a, d, SOLID);
             }
         }
     }
@@ -158,7 +158,7 @@ __device__ __forceinline__ void walk_range(const StepParams& p, const float4& se
 
 // One cell of the stencil on a hashed grid: the particles of its bucket,
 // kept only if they belong to that cell.
-template <bool MIXED, bool SOLID>
+template <bool MIXED, bool SOLID, bool KAHAN = MIXED>
 __device__ __forceinline__ void walk_hashed_cell(const StepParams& p, const float4& self, int s,
                                                  const float4* __restrict__ pos,
                                                  const int* __restrict__ start,
@@ -178,12 +178,15 @@ __device__ __forceinline__ void walk_hashed_cell(const StepParams& p, const floa
         if (dot3e(d.x, d.y, d.z) <= p.h2) {
             if (c_n < p.max_nbrs) nbr[(size_t)c_n * p.n + s] = entry(t, dx, dy, dz, SOLID);
             c_n++;
-            lambda_accumulate<MIXED>(p, a, d, SOLID);
+            lambda_accumulate<KAHAN>(p, a, d, SOLID);
         }
     }
 }
 
-template <bool MIXED, bool HASHED, int B>
+// FRAME: mixed storage with the iterations in the scene frame (positions
+// relative to the box corner, compensated density sums; the walk's cell is
+// the step's key, which rounding of the frame position could move)
+template <bool MIXED, bool HASHED, int B, bool FRAME = false>
 __global__ void __launch_bounds__(B) k_lists_lambda(StepParams p, CellPack cp, float4* __restrict__ xs,
                                                     const int* __restrict__ key_sorted,
                                                     const int* __restrict__ cell_sorted,
@@ -199,8 +202,9 @@ __global__ void __launch_bounds__(B) k_lists_lambda(StepParams p, CellPack cp, f
     const float4 self = xs[s];
     const Geo g = geo_slot(p, s);
     // fp32 on a dense grid: the cell the prediction keyed this position by
-    const int3 c = (MIXED || HASHED) ? slot_cell(p, cp, g, key_sorted, cell_sorted, s)
-                                     : plain_cell(p, g, self.x, self.y, self.z);
+    constexpr bool KAHAN = MIXED || FRAME;
+    const int3 c = (MIXED || HASHED || FRAME) ? slot_cell(p, cp, g, key_sorted, cell_sorted, s)
+                                              : plain_cell(p, g, self.x, self.y, self.z);
     LambdaAcc a = lambda_init(p);
     int c_n = 0;
     const int slab = g.gx * g.gz;
@@ -231,11 +235,11 @@ __global__ void __launch_bounds__(B) k_lists_lambda(StepParams p, CellPack cp, f
             for (int r = 0; r < 3; r++) {
                 const int xx = c.x + r - 1;
                 if (xx < 0 || xx >= g.gx) continue;
-                walk_range<MIXED, false>(p, self, s, xs, b0[r], b3[r], b1[r], b2[r], z0 - c.z, r - 1, dy, a, c_n,
-                                         nbr);
+                walk_range<MIXED, false, KAHAN>(p, self, s, xs, b0[r], b3[r], b1[r], b2[r], z0 - c.z, r - 1, dy,
+                                                a, c_n, nbr);
                 if (solids)
-                    walk_row<MIXED, true>(p, self, s, solid, sstart, g.off + y * slab + xx * g.gz, c.z, g.gz, r - 1,
-                                          dy, a, c_n, nbr);
+                    walk_row<MIXED, true, KAHAN>(p, self, s, solid, sstart, g.off + y * slab + xx * g.gz, c.z, g.gz,
+                                                 r - 1, dy, a, c_n, nbr);
             }
         }
     }
@@ -252,14 +256,14 @@ __global__ void __launch_bounds__(B) k_lists_lambda(StepParams p, CellPack cp, f
                 const int z0 = max(c.z - 1, 0), z1 = min(min(c.z + 1, g.gz - 1), (int)cp.mz);
                 for (int z = z0; z <= z1; z++) {
                     const int3 cn = make_int3(xx, y, z);
-                    walk_hashed_cell<MIXED, false>(p, self, s, xs, fstart, cell_sorted,
+                    walk_hashed_cell<MIXED, false, KAHAN>(p, self, s, xs, fstart, cell_sorted,
                                                    cell_bucket(cn, p.hash_bits), (int)pack_bits(cp, cn),
                                                    dx, dy, z - c.z, a, c_n, nbr);
                 }
                 if (solids)
                     for (int z = z0; z <= z1; z++) {
                         const int3 cn = make_int3(xx, y, z);
-                        walk_hashed_cell<MIXED, true>(p, self, s, solid, sstart, solid_cell,
+                        walk_hashed_cell<MIXED, true, KAHAN>(p, self, s, solid, sstart, solid_cell,
                                                       cell_bucket(cn, p.hash_bits), (int)pack_bits(cp, cn),
                                                       dx, dy, z - c.z, a, c_n, nbr);
                     }
@@ -375,7 +379,8 @@ __global__ void __launch_bounds__(B) k_lambda(StepParams p, float4* __restrict__
                                               const int* __restrict__ nbr, const int* __restrict__ cnt,
                                               const float4* __restrict__ solid,
                                               float* __restrict__ rho) {
-    constexpr bool MIXED = (F & 1) != 0, SOL = (F & 2) != 0;
+    // F bit 2: the scene frame (fp32 pair offsets, compensated density sums)
+    constexpr bool MIXED = (F & 1) != 0, SOL = (F & 2) != 0, KAHAN = MIXED || (F & 4) != 0;
     pdl_wait();
     __shared__ float4 shift_tab[MIXED ? 64 : 1];
     if (MIXED) fill_shift_table(p, shift_tab);
@@ -386,7 +391,7 @@ __global__ void __launch_bounds__(B) k_lambda(StepParams p, float4* __restrict__
         LambdaAcc a = lambda_init(p);
         for_each_entry<U, SOL>(p, nbr + s, cnt, s, xs, solid, [&](int e, float4 q) {
             float3 d = rel_t<MIXED>(self, q, e, shift_tab);
-            lambda_accumulate<MIXED>(p, a, d, SOL && entry_solid(e));
+            lambda_accumulate<KAHAN>(p, a, d, SOL && entry_solid(e));
         });
         reinterpret_cast<float*>(xs)[4 * (size_t)s + 3] = lambda_of(p, a);
         if (rho) rho[s] = density_of(p, a);
@@ -406,7 +411,7 @@ __global__ void __launch_bounds__(B) k_lambda(StepParams p, float4* __restrict__
     }
     for_each_entry_p<U, P, SOL>(p, nbr, s, c, xs, solid, [&](int r, int e, float4 q) {
         float3 d = rel_t<MIXED>(self[r], q, e, shift_tab);
-        lambda_accumulate<MIXED>(p, a[r], d, SOL && entry_solid(e));
+        lambda_accumulate<KAHAN>(p, a[r], d, SOL && entry_solid(e));
     });
 #pragma unroll
     for (int r = 0; r < P; r++) {
@@ -483,7 +488,12 @@ __device__ __forceinline__ void delta_finish(const StepParams& p, const CellPack
     }
     xs_out[s] = out;
     if (v_out) {
-        const float4 xo = x[s];
+        float4 xo = x[s];
+        if (!MIXED && p.frame) {  // the committed state is cell + offset: into the scene frame
+            const int3 co = unpack_cell(cp, xo.w);
+            xo = make_float4(__fmaf_rn((float)co.x, p.cell, xo.x), __fmaf_rn((float)co.y, p.cell, xo.y),
+                             __fmaf_rn((float)co.z, p.cell, xo.z), 0.0f);
+        }
         float3 d = make_float3(__fsub_rn(out.x, xo.x), __fsub_rn(out.y, xo.y), __fsub_rn(out.z, xo.z));
         if (MIXED) {
             int3 co = unpack_cell(cp, xo.w);
@@ -599,14 +609,24 @@ __global__ void __launch_bounds__(B) k_xsph(StepParams p, CellPack cp, const flo
     v_out[s] = vc;
     const Geo g = geo_slot(p, s);
     float4 xc;
-    if (!MIXED) {
+    if (!MIXED && !p.frame) {
         xc = make_float4(self.x, self.y, self.z, 0.0f);
     } else {
-        int3 cs = slot_cell(p, cp, g, key_sorted, p.cell_sorted, s);
-        xc = make_float4(self.x, self.y, self.z, pack_cell(cp, cs.x, cs.y, cs.z));
+        const int3 cs = slot_cell(p, cp, g, key_sorted, p.cell_sorted, s);
+        if (MIXED)
+            xc = make_float4(self.x, self.y, self.z, pack_cell(cp, cs.x, cs.y, cs.z));
+        else  // scene frame: back to the offset from the step's cell
+            xc = make_float4(__fsub_rn(self.x, __fmul_rn((float)cs.x, p.cell)),
+                             __fsub_rn(self.y, __fmul_rn((float)cs.y, p.cell)),
+                             __fsub_rn(self.z, __fmul_rn((float)cs.z, p.cell)), pack_cell(cp, cs.x, cs.y, cs.z));
     }
     x_out[s] = xc;
-    if (xs_next) predict_one<MIXED>(p, cp, g, xc, vc, s, xs_next, key, rank, count, cellk, tile_count);
+    if (xs_next) {
+        if (MIXED || p.frame)
+            predict_one<true>(p, cp, g, xc, vc, s, xs_next, key, rank, count, cellk, tile_count);
+        else
+            predict_one<false>(p, cp, g, xc, vc, s, xs_next, key, rank, count, cellk, tile_count);
+    }
 }
 
 // Absolute positions (float3 triples) in the caller's id order.
@@ -663,6 +683,18 @@ __device__ __forceinline__ float4 pack_position(const StepParams& p, const CellP
     int cz = min(max((int)floorf(z * p.inv_cell), 0), (int)floorf(g.hiz * p.inv_cell));
     return make_float4(x - (float)cx * p.cell, y - (float)cy * p.cell, z - (float)cz * p.cell,
                        pack_cell(cp, cx, cy, cz));
+}
+
+// Positions stored as cell + offset (w: the packed cell) into the scene
+// frame, w kept: the static particles of a context that iterates in the
+// scene frame (their cells stay in w for the cell keys).
+__global__ void k_to_scene_frame(StepParams p, CellPack cp, float4* __restrict__ a, int m) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    const float4 q = a[i];
+    const int3 c = unpack_cell(cp, q.w);
+    a[i] = make_float4(__fmaf_rn((float)c.x, p.cell, q.x), __fmaf_rn((float)c.y, p.cell, q.y),
+                       __fmaf_rn((float)c.z, p.cell, q.z), q.w);
 }
 
 // Caller positions (float3, id order) into the state representation, slot = id.
@@ -971,13 +1003,13 @@ void launch_key(bool mixed, const StepParams& p, const CellPack& cp, const float
         else                                                                                    \
             TUNE_BLOCKS_P2(KERNEL, MIX, 2, tu, N, ST, __VA_ARGS__);                             \
     } while (0)
-#define TUNE_DISPATCH_PPT(KERNEL, mixed, tu, N, ST, ...)                                        \
+#define TUNE_DISPATCH_PPT(KERNEL, fcode, tu, N, ST, ...)                                        \
     do {                                                                                        \
         if (tu.ppt != 2) {                                                                      \
-            TUNE_DISPATCH(KERNEL, mixed, tu, N, ST, __VA_ARGS__);                               \
+            TUNE_DISPATCH(KERNEL, fcode, tu, N, ST, __VA_ARGS__);                               \
             break;                                                                              \
         }                                                                                       \
-        switch ((mixed ? 1 : 0) | (p.ns > 0 ? 2 : 0)) {                                         \
+        switch (fcode) {                                                                        \
             case 0: TUNE_CASE_P2(KERNEL, 0, tu, N, ST, __VA_ARGS__); break;                     \
             case 1: TUNE_CASE_P2(KERNEL, 1, tu, N, ST, __VA_ARGS__); break;                     \
             case 2: TUNE_CASE_P2(KERNEL, 2, tu, N, ST, __VA_ARGS__); break;                     \
@@ -1004,14 +1036,22 @@ void launch_key(bool mixed, const StepParams& p, const CellPack& cp, const float
         else                                                                                    \
             TUNE_BLOCKS(KERNEL, MIX, 8, tu, N, ST, __VA_ARGS__);                                \
     } while (0)
-#define TUNE_DISPATCH(KERNEL, mixed, tu, N, ST, ...)                                            \
+// fcode: bit 0 mixed (cell-relative pair offsets), bit 1 static particles,
+// bit 2 (the lambda pass only) the scene frame's compensated sums
+#define TUNE_DISPATCH(KERNEL, fcode, tu, N, ST, ...)                                            \
     do {                                                                                        \
-        switch ((mixed ? 1 : 0) | (p.ns > 0 ? 2 : 0)) {                                         \
+        switch (fcode) {                                                                        \
             case 0: TUNE_CASE(KERNEL, 0, tu, N, ST, __VA_ARGS__); break;                        \
             case 1: TUNE_CASE(KERNEL, 1, tu, N, ST, __VA_ARGS__); break;                        \
             case 2: TUNE_CASE(KERNEL, 2, tu, N, ST, __VA_ARGS__); break;                        \
             default: TUNE_CASE(KERNEL, 3, tu, N, ST, __VA_ARGS__); break;                       \
         }                                                                                       \
+    } while (0)
+#define TUNE_DISPATCH_FRAME(KERNEL, fcode, tu, N, ST, ...)                                      \
+    do {                                                                                        \
+        if (fcode == 4) TUNE_CASE(KERNEL, 4, tu, N, ST, __VA_ARGS__);                           \
+        else if (fcode == 6) TUNE_CASE(KERNEL, 6, tu, N, ST, __VA_ARGS__);                      \
+        else TUNE_DISPATCH(KERNEL, fcode, tu, N, ST, __VA_ARGS__);                              \
     } while (0)
 
 void launch_lists_lambda(bool mixed, const Tuning& tu, const StepParams& p, const CellPack& cp,
@@ -1032,7 +1072,15 @@ void launch_lists_lambda(bool mixed, const Tuning& tu, const StepParams& p, cons
         if (p.hash_bits) LGB_LISTS_H(MIX, true, BB); \
         else LGB_LISTS_H(MIX, false, BB);        \
     } while (0)
-    if (mixed) {
+    if (mixed && p.frame) {  // the scene frame: fp32 pair offsets, compensated sums
+        if (B == 64) launch_k(k_lists_lambda<false, false, 64, true>, blocks_for(p.n, 64), 64, st, pdl, pp, cp, xs,
+                              key_sorted, cell_sorted, fstart, solid, solid_cell, sstart, nbr, cnt, rho, status);
+        else if (B == 128) launch_k(k_lists_lambda<false, false, 128, true>, blocks_for(p.n, 128), 128, st, pdl, pp, cp,
+                                    xs, key_sorted, cell_sorted, fstart, solid, solid_cell, sstart, nbr, cnt, rho,
+                                    status);
+        else launch_k(k_lists_lambda<false, false, 256, true>, blocks_for(p.n, 256), 256, st, pdl, pp, cp, xs,
+                      key_sorted, cell_sorted, fstart, solid, solid_cell, sstart, nbr, cnt, rho, status);
+    } else if (mixed) {
         if (B == 64) LGB_LISTS(true, 64);
         else if (B == 128) LGB_LISTS(true, 128);
         else LGB_LISTS(true, 256);
@@ -1048,7 +1096,11 @@ void launch_lists_lambda(bool mixed, const Tuning& tu, const StepParams& p, cons
 void launch_lambda(bool mixed, const Tuning& tu, const StepParams& p, float4* xs, const int* nbr,
                    const int* cnt, const float4* solid, float* rho, cudaStream_t st) {
     if (p.n <= 0) return;
-    TUNE_DISPATCH_PPT(k_lambda, mixed, tu, p.n, st, p, xs, nbr, cnt, solid, rho);
+    const int f = ((mixed && !p.frame) ? 1 : 0) | (p.ns > 0 ? 2 : 0);
+    if (mixed && p.frame)  // the scene frame: one particle per thread
+        TUNE_DISPATCH_FRAME(k_lambda, f | 4, tu, p.n, st, p, xs, nbr, cnt, solid, rho);
+    else
+        TUNE_DISPATCH_PPT(k_lambda, f, tu, p.n, st, p, xs, nbr, cnt, solid, rho);
 }
 
 void launch_delta(bool mixed, const Tuning& tu, const StepParams& p, const CellPack& cp,
@@ -1056,7 +1108,8 @@ void launch_delta(bool mixed, const Tuning& tu, const StepParams& p, const CellP
                   const float4* solid, const int* key_sorted, const float4* x, float4* v_out,
                   cudaStream_t st) {
     if (p.n <= 0) return;
-    TUNE_DISPATCH_PPT(k_delta, mixed, tu, p.n, st, p, cp, xs, xs_out, nbr, cnt, solid, key_sorted, x, v_out);
+    const int f = ((mixed && !p.frame) ? 1 : 0) | (p.ns > 0 ? 2 : 0);
+    TUNE_DISPATCH_PPT(k_delta, f, tu, p.n, st, p, cp, xs, xs_out, nbr, cnt, solid, key_sorted, x, v_out);
 }
 
 void launch_xsph(bool mixed, const Tuning& tu, const StepParams& p, const CellPack& cp,
@@ -1066,7 +1119,8 @@ void launch_xsph(bool mixed, const Tuning& tu, const StepParams& p, const CellPa
     if (p.n <= 0) return;
     Tuning tx = tu;  // the XSPH pass has its own gathers in flight
     tx.unroll = tu.xsph_unroll;
-    TUNE_DISPATCH(k_xsph, mixed, tx, p.n, st, p, cp, xs, v_in, nbr, cnt, key_sorted, x_out, v_out, xs_next, key,
+    const int f = ((mixed && !p.frame) ? 1 : 0) | (p.ns > 0 ? 2 : 0);
+    TUNE_DISPATCH(k_xsph, f, tx, p.n, st, p, cp, xs, v_in, nbr, cnt, key_sorted, x_out, v_out, xs_next, key,
                   rank, count, cellk, tile_count);
 }
 
@@ -1080,6 +1134,11 @@ void launch_unpermute_pos_d(bool mixed, const StepParams& p, const CellPack& cp,
                             const int* id, int n, double* out, cudaStream_t st) {
     if (n <= 0) return;
     LGB_DISPATCH(mixed, k_unpermute_pos_d, blocks_for(n, 256), 256, st, p, cp, a, id, n, out);
+}
+
+void launch_to_scene_frame(const StepParams& p, const CellPack& cp, float4* a, int m, cudaStream_t st) {
+    if (m <= 0) return;
+    k_to_scene_frame<<<blocks_for(m, 256), 256, 0, st>>>(p, cp, a, m);
 }
 
 void launch_pack_pos(bool mixed, const StepParams& p, const CellPack& cp, const float* in, int n,

@@ -17,12 +17,13 @@ import math
 import numpy as np
 
 from . import _lib
-from ._lib import (MODE_PBF, MODE_REFERENCE, MODE_SAND, PRECISION_FP32, PRECISION_MIXED, LustrineError,
+from ._lib import (MODE_PBF, MODE_REFERENCE, MODE_SAND, PRECISION_FP32, PRECISION_MIXED, PRECISION_MIXED_SCENE,
+                   LustrineError,
                    PbfParams, check)
 
 __all__ = ["PbfSim", "PbfParams", "reference_params", "pbf_params", "sand_params", "MODE_PBF",
            "MODE_REFERENCE", "MODE_SAND",
-           "PRECISION_FP32", "PRECISION_MIXED", "LustrineError"]
+           "PRECISION_FP32", "PRECISION_MIXED", "PRECISION_MIXED_SCENE", "LustrineError"]
 
 
 def reference_params(X, Y, Z, radius=0.5, kernel_radius_scale=2.0) -> PbfParams:

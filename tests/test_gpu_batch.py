@@ -25,7 +25,7 @@ def _params(precision, domain=(8, 8, 8)):
     return pbf_params(*domain, iterations=4, precision=precision)
 
 
-@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("precision", [0, 1, 2])
 def test_batch_equals_scenes_stepped_alone(precision):
     from lustrine_gb300 import PbfSim
     scs = _scenes()
@@ -104,7 +104,7 @@ def test_batch_config3_shapes_run():
     b.close()
 
 
-@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("precision", [0, 1, 2])
 def test_sharded_batches_equal_the_full_batch(precision):
     """The multi-GPU split of a batch (sharding.shard_scenes: every rank
     steps one batch of its own scenes, no collective on the data path) on one

@@ -296,7 +296,7 @@ def test_edge_cases_empty_single_and_no_solids():
         PbfSim(bad, 10, 0)
 
 
-@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("precision", [0, 1, 2])
 def test_state_transfers_page_locked_and_pageable_agree(precision):
     """upload/download_state_async read and write page-locked host buffers
     directly from the kernels and stage pageable ones through copies: both
@@ -357,7 +357,7 @@ def test_state_transfers_page_locked_and_pageable_agree(precision):
     b.close()
 
 
-@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("precision", [0, 1, 2])
 def test_next_step_prediction_in_commit_kernel_is_exact(precision):
     """The commit kernel predicts the next step when nothing changes in
     between; a context made to predict every step itself (re-setting its
