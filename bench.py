@@ -500,7 +500,8 @@ def run_ours(args, world, rank, local):
     dom = max(cand, key=lambda k: cand[k][0])
     ms_launch = cand[dom][0] / max(cand[dom][1], 1)
     bytes_launch = STAGE_BYTES[dom] * n_local
-    achieved = bytes_launch / (ms_launch * 1e-3) / 1e9
+    # (under a profiler that serialises the launches the events can read 0)
+    achieved = bytes_launch / (ms_launch * 1e-3) / 1e9 if ms_launch > 0 else 0.0
     traffic = read_traffic(dom)
     # whole-step algorithmic bytes per particle-iteration (state traffic model)
     cells = sum((sc.domain[0] + 1) * (sc.domain[1] + 1) * (sc.domain[2] + 1) for sc in scs)
