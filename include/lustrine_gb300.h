@@ -376,6 +376,10 @@ LUSTRINE_API int lustrine_pbf_download_positions_f64(lustrine_pbf* s, double* x)
 /* Neighbour lists of the last step in the caller's ids (solids n_fluid + k):
  * count[n_fluid], idx[n_fluid * cap] row-major.  Synchronises. */
 LUSTRINE_API int lustrine_pbf_neighbors(lustrine_pbf* s, int* count, int* idx, int cap);
+/* The form the last step's lists took: LUSTRINE_LISTS_COMPACT or
+ * LUSTRINE_LISTS_COLUMN (also before the first step and for the on-chip
+ * solve, whose lists are column lists). */
+LUSTRINE_API int lustrine_pbf_list_format(const lustrine_pbf* s, int* format);
 /* FP64 reductions on the device: [0] mass, [1..3] momentum, [4] kinetic
  * energy, [5..7] centre of mass, [8] max |rho / rho0 - 1| of the last lambda
  * pass (0 in sand mode, which computes no density).  Synchronises. */
@@ -440,7 +444,15 @@ LUSTRINE_API int lustrine_pbf_profile_step(lustrine_pbf* s, float dt, double* st
  * per thread of the lambda and delta-p passes, whose lists are walked
  * together (0: 1; with 2, unroll is at most 2); solver and solver_threads:
  * batches only, LUSTRINE_SOLVER_* and the on-chip solve's threads per CTA
- * (512 or 1024; 0: unchanged). */
+ * (512 or 1024; 0: unchanged); list_format: LUSTRINE_LISTS_* (compact lists
+ * apply in PBF mode, fp32 or LUSTRINE_PRECISION_MIXED_SCENE, with
+ * max_neighbors <= 255, no static particles, scenes of at most 65,535 and
+ * contexts of fewer than 2^24 fluid particles, and one particle per thread;
+ * elsewhere the step keeps column lists whatever list_format says). */
+enum {
+    LUSTRINE_LISTS_COLUMN = 0,  /* count + column-major 32-bit entries */
+    LUSTRINE_LISTS_COMPACT = 1  /* one 16-byte record per particle: count, 6 entries as 16-bit scene offsets */
+};
 typedef struct lustrine_pbf_tuning {
     int block;
     int unroll;
@@ -449,6 +461,7 @@ typedef struct lustrine_pbf_tuning {
     int particles_per_thread;
     int solver;
     int solver_threads;
+    int list_format;
 } lustrine_pbf_tuning;
 LUSTRINE_API int lustrine_pbf_set_tuning(lustrine_pbf* s, const lustrine_pbf_tuning* t);
 LUSTRINE_API int lustrine_pbf_get_tuning(const lustrine_pbf* s, lustrine_pbf_tuning* t);

@@ -80,11 +80,13 @@ class PbfParams(C.Structure):
 
 
 GRID_AUTO, GRID_DENSE, GRID_HASHED = 0, 1, 2
+LISTS_COLUMN, LISTS_COMPACT = 0, 1
 
 
 class PbfTuning(C.Structure):
     _fields_ = [("block", C.c_int), ("unroll", C.c_int), ("list_block", C.c_int), ("xsph_unroll", C.c_int),
-                ("particles_per_thread", C.c_int), ("solver", C.c_int), ("solver_threads", C.c_int)]
+                ("particles_per_thread", C.c_int), ("solver", C.c_int), ("solver_threads", C.c_int),
+                ("list_format", C.c_int)]
 
 
 class SandControls(C.Structure):
@@ -189,6 +191,7 @@ SIGNATURES = {
     "lustrine_pbf_step_host": (C.c_int, [_P, C.c_float, _P, _P]),
     "lustrine_pbf_download_positions_f64": (C.c_int, [_P, _P]),
     "lustrine_pbf_neighbors": (C.c_int, [_P, _P, _P, C.c_int]),
+    "lustrine_pbf_list_format": (C.c_int, [_P, _IP]),
     "lustrine_pbf_reduce": (C.c_int, [_P, _DP]),
     "lustrine_pbf_query_cell_count": (C.c_int, [_P, _FP, _FP, C.c_int, _IP]),
     "lustrine_pbf_reserve": (C.c_int, [_P, C.c_int]),

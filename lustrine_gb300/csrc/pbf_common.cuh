@@ -11,6 +11,11 @@
 //   neighbour lists: nbr[max_nbrs * n], column-major (entry k of slot i at
 //     k * n + i) so a warp's loads of entry k are one coalesced line;
 //     fluid neighbours are slot numbers >= 0, solids are -1 - solid slot.
+//   compact lists (PBF mode, scenes of at most COMPACT_MAX_SCENE particles,
+//     no static particles, no cell codes): rec uint4[n], one 16-byte record
+//     per slot with the count, the scene's first slot and the first
+//     COMPACT_INLINE neighbours as 16-bit scene-local slots; entries from
+//     COMPACT_INLINE on in the column-major rows of nbr as plain slots.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -35,7 +40,18 @@ enum : int {
 struct SceneInfo {
     int gx, gy, gz, cell_off;
     float lox, loy, loz, hix, hiy, hiz;
+    int slot0, spare;  // the scene's first fluid slot
 };
+
+// Compact neighbour lists (StepParams::rec): record.x = count | first slot
+// of the particle's scene << 8; .y, .z, .w = entries 0-5 as 16-bit offsets
+// from that slot, entry 2k in the low half, COMPACT_SENTINEL past the count
+// (the sentinel slot n).
+constexpr int COMPACT_INLINE = 6;
+constexpr unsigned COMPACT_SENTINEL = 0xFFFFu;
+constexpr int COMPACT_MAX_SCENE = 65535;   // scene-local offsets 0..65534
+constexpr int COMPACT_MAX_N = 1 << 24;     // first slot in 24 bits
+constexpr int COMPACT_MAX_NBRS = 255;      // count in 8 bits
 
 // Everything a step kernel reads, passed by value (constant bank).
 struct StepParams {
@@ -75,6 +91,7 @@ struct StepParams {
     float lox, loy, loz, hix, hiy, hiz;  // box bounds for the position clamp
     float dt;
     int frame;            // mixed storage, iterations in the scene frame (LUSTRINE_PRECISION_MIXED_SCENE)
+    uint4* rec;           // compact neighbour lists of this step (nullptr: column lists with counts)
 };
 
 // Sand mode: simulate_sand's per-call inputs (Simulate.cpp:156-209).
@@ -94,6 +111,7 @@ struct Tuning {
     int list_block;   // threads per block of the list build (64, 128, 256)
     int xsph_unroll;  // neighbour gathers in flight per thread of the XSPH pass (1, 2, 4, 8)
     int ppt;          // particles per thread of the lambda and delta passes (1, 2)
+    int lists;        // 1: compact lists where the step allows them, 0: column lists
 };
 
 // Mixed precision: a cell's integer coordinates packed into 32 bits,

@@ -209,7 +209,7 @@ void lustrine_pbf::free_buffers() {
                     rank, tmp, perm, count, start, block_sums, tile_sum, solid_near, solid, solid_raw, sstart, nbr, cnt, lam,
                     lam_by_id, rho, status, red, qcount, out3, out3d, iota, slot_of, solid_id, d_scenes, d_scene_of,
                     d_solid_scene_of, cellk, cell_sorted, solid_cell, att[0], att[1], d_bins, d_scene_slot0,
-                    d_queue};
+                    d_queue, rec};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     x[0] = x[1] = xs[0] = xs[1] = v[0] = v[1] = nullptr;
@@ -218,6 +218,8 @@ void lustrine_pbf::free_buffers() {
     key = key_sorted = rank = tmp = perm = count = start = block_sums = tile_sum = sstart = nullptr;
     nbr = cnt = status = qcount = iota = slot_of = solid_id = d_scene_of = d_solid_scene_of = nullptr;
     cellk = cell_sorted = solid_cell = nullptr;
+    rec = nullptr;
+    lists_compact = false;
     att[0] = att[1] = nullptr;
     solid_near = nullptr;
     lam = lam_by_id = rho = out3 = nullptr;
@@ -238,6 +240,23 @@ int lgb_write_sentinel(lustrine_pbf* s) {
     CK(cudaMemsetAsync(s->vtmp + n, 0, sizeof(float4), s->stream));
     CK(cudaStreamSynchronize(s->stream));
     return LUSTRINE_OK;
+}
+
+// Whether the context's steps can use compact neighbour lists: PBF mode in
+// fp32 or the scene frame (no cell codes in the entries), lists of at most
+// COMPACT_MAX_NBRS entries, fewer than COMPACT_MAX_N fluid slots and scenes
+// of at most COMPACT_MAX_SCENE (one scene: the capacity).  A step uses them
+// when the tuning asks for them and the context holds no static particles.
+static bool compact_capable(const lustrine_pbf* s) {
+    if (s->prm.mode != LUSTRINE_MODE_PBF || (s->mixed() && !s->sp.frame)) return false;
+    if (s->sp.max_nbrs > COMPACT_MAX_NBRS || s->cap >= COMPACT_MAX_N) return false;
+    int largest = s->cap;
+    if (s->is_batch()) largest = *std::max_element(s->b_nfluid.begin(), s->b_nfluid.end());
+    return largest <= COMPACT_MAX_SCENE;
+}
+
+static bool compact_now(const lustrine_pbf* s) {
+    return s->rec && s->tune.lists && s->tune.ppt == 1 && s->ns == 0 && compact_capable(s);
 }
 
 // Device buffers for s->cap fluid particles (s->n of them active).
@@ -269,6 +288,7 @@ static int ctx_alloc(lustrine_pbf* s) {
     const size_t list_rows = (size_t)((s->sp.max_nbrs + LIST_PAD_MAX - 1) / LIST_PAD_MAX * LIST_PAD_MAX);
     rc = rc ? rc : dalloc(&s->nbr, list_rows * (size_t)n);
     rc = rc ? rc : dalloc(&s->cnt, n);
+    if (compact_capable(s)) rc = rc ? rc : dalloc(&s->rec, n);
     rc = rc ? rc : dalloc(&s->lam, n);
     s->lam_by_id_len = (size_t)(n + ns > s->sp.max_nbrs ? n + ns : s->sp.max_nbrs) + 1;
     rc = rc ? rc : dalloc(&s->lam_by_id, s->lam_by_id_len);
@@ -382,10 +402,13 @@ static int derive_batch(const lustrine_pbf_params& q0, const std::vector<int>& d
     int rc = derive(q, (int)n, (int)ns, sp, cp);
     if (rc) return rc;
     table->clear();
-    long long off = 0;
+    long long off = 0, slot = 0;
     const float r = q.particle_radius;
     for (int k = 0; k < S; k++) {
         SceneInfo si;
+        si.slot0 = (int)slot;
+        si.spare = 0;
+        slot += nf[k];
         const float dX = (float)dom[3 * k], dY = (float)dom[3 * k + 1], dZ = (float)dom[3 * k + 2];
         si.gx = (int)(dX / q.cell_size) + 1;
         si.gy = (int)(dY / q.cell_size) + 1;
@@ -878,6 +901,7 @@ static int enqueue_step(lustrine_pbf* s, cudaStream_t st, StageMarks* mk = nullp
     set_pdl(s->use_pdl);
     if (s->sand_mode()) {
         k = enqueue_sand_step(s, st, mk);
+        s->lists_compact = false;
         set_pdl(false);
         return k;
     }
@@ -917,6 +941,7 @@ static int enqueue_step(lustrine_pbf* s, cudaStream_t st, StageMarks* mk = nullp
                          s->lam_by_id, st);
         if (mk) mk->mark(LUSTRINE_STAGE_DELTA, st);
         k += 3;
+        s->lists_compact = false;
     } else if (s->onchip && s->num_bins > 0) {
         // the batch's lists, iterations, XSPH and commit in one persistent
         // launch of clusters (the lambdas end where the per-stage path leaves them)
@@ -946,9 +971,14 @@ static int enqueue_step(lustrine_pbf* s, cudaStream_t st, StageMarks* mk = nullp
         launch_scene_solve(mixed, s->onchip_threads, p, s->cp, sa,
                            s->onchip_threads == 512 ? s->onchip_clusters512 : s->onchip_clusters, st);
         k += 1;
+        s->lists_compact = false;
         if (mk) mk->mark(LUSTRINE_STAGE_SOLVE, st);
     } else {
         // iteration 0's lambda pass builds the neighbour lists as it goes
+        // (compact records where the step allows them)
+        StepParams pl = p;
+        pl.rec = compact_now(s) ? s->rec : nullptr;
+        s->lists_compact = pl.rec != nullptr;
         float4* a = s->xs[o];
         float4* b = s->xs_alt;
         const int iters = s->prm.iterations;
@@ -956,14 +986,14 @@ static int enqueue_step(lustrine_pbf* s, cudaStream_t st, StageMarks* mk = nullp
         for (int it = 0; it < iters; it++) {
             float* rho = it == iters - 1 ? s->rho : nullptr;  // densities of the last pass only
             if (it == 0) {
-                launch_lists_lambda(mixed, tu, p, s->cp, a, s->key_sorted, s->cell_sorted, s->start,
+                launch_lists_lambda(mixed, tu, pl, s->cp, a, s->key_sorted, s->cell_sorted, s->start,
                                     s->solid, s->solid_cell, s->sstart, s->nbr, s->cnt, rho, s->status, st);
                 if (mk) mk->mark(LUSTRINE_STAGE_LISTS, st);
             } else {
-                launch_lambda(mixed, tu, p, a, s->nbr, s->cnt, s->solid, rho, st);
+                launch_lambda(mixed, tu, pl, a, s->nbr, s->cnt, s->solid, rho, st);
                 if (mk) mk->mark(LUSTRINE_STAGE_LAMBDA, st);
             }
-            launch_delta(mixed, tu, p, s->cp, a, b, s->nbr, s->cnt, s->solid, s->key_sorted, s->x[o],
+            launch_delta(mixed, tu, pl, s->cp, a, b, s->nbr, s->cnt, s->solid, s->key_sorted, s->x[o],
                          it == iters - 1 ? s->vtmp : nullptr, st);
             if (mk) mk->mark(LUSTRINE_STAGE_DELTA, st);
             float4* t = a;
@@ -978,7 +1008,7 @@ static int enqueue_step(lustrine_pbf* s, cudaStream_t st, StageMarks* mk = nullp
                                 s->side);
             k += 1;
         }
-        launch_xsph(mixed, tu, p, s->cp, a, s->vtmp, s->nbr, s->cnt, s->key_sorted, s->x[o], s->v[o],
+        launch_xsph(mixed, tu, pl, s->cp, a, s->vtmp, s->nbr, s->cnt, s->key_sorted, s->x[o], s->v[o],
                     tail ? s->xs_pred : nullptr, s->key, s->rank, s->count, s->cellk,
                     tail ? tiles_of(s, o) : nullptr, st);
         k += 1;
@@ -1135,7 +1165,7 @@ extern "C" int lustrine_pbf_set_tuning(lustrine_pbf* s, const lustrine_pbf_tunin
     const int xu = t->xsph_unroll ? t->xsph_unroll : t->unroll;  // 0: as the other passes
     const int ppt = t->particles_per_thread ? t->particles_per_thread : 1;
     if (!ok(t->block) || !ok(t->list_block) || !ok_u(t->unroll) || !ok_u(xu) || (ppt != 1 && ppt != 2) ||
-        (ppt == 2 && t->unroll > 2))
+        (ppt == 2 && t->unroll > 2) || (t->list_format != LUSTRINE_LISTS_COLUMN && t->list_format != LUSTRINE_LISTS_COMPACT))
         return LUSTRINE_ERR_ARGS;
     if (t->solver != LUSTRINE_SOLVER_STAGES && t->solver != LUSTRINE_SOLVER_ONCHIP) return LUSTRINE_ERR_ARGS;
     if (s->is_batch()) {
@@ -1148,7 +1178,7 @@ extern "C" int lustrine_pbf_set_tuning(lustrine_pbf* s, const lustrine_pbf_tunin
     } else if (t->solver != LUSTRINE_SOLVER_STAGES) {
         return LUSTRINE_ERR_ARGS;
     }
-    s->tune = Tuning{t->block, t->unroll, t->list_block, xu, ppt};
+    s->tune = Tuning{t->block, t->unroll, t->list_block, xu, ppt, t->list_format};
     s->invalidate_graphs();
     return LUSTRINE_OK;
 }
@@ -1162,6 +1192,7 @@ extern "C" int lustrine_pbf_get_tuning(const lustrine_pbf* s, lustrine_pbf_tunin
     t->particles_per_thread = s->tune.ppt;
     t->solver = s->onchip ? LUSTRINE_SOLVER_ONCHIP : LUSTRINE_SOLVER_STAGES;
     t->solver_threads = s->onchip_threads;
+    t->list_format = s->tune.lists;
     return LUSTRINE_OK;
 }
 
@@ -1255,22 +1286,26 @@ extern "C" int lustrine_pbf_autotune(lustrine_pbf* s, float dt, int steps, lustr
     static const int blocks[3] = {64, 128, 256};
     static const int unrolls[4] = {1, 2, 4, 8};
     // the iteration kernels' shape first (block x gathers in flight x
-    // particles per thread), then the list build's block size
-    for (int bi = 0; bi < 3 && !rc; bi++)
-        for (int ui = 0; ui < 4 && !rc; ui++)
-            for (int pi = 1; pi <= 2 && !rc; pi++) {
-                if (pi == 2 && unrolls[ui] > 2) continue;
-                s->tune = Tuning{blocks[bi], unrolls[ui], keep.list_block, unrolls[ui], pi};
-                s->invalidate_graphs();
-                float ms = 0.0f;
-                rc = time_candidate(s, sn, side, dt, steps, &ms);
-                if (!rc && ms < top_ms) {
-                    top_ms = ms;
-                    top = s->tune;
+    // particles per thread x list format, compact first where it can
+    // apply), then the list build's block size
+    const int formats = s->rec && s->ns == 0 ? 2 : 1;
+    for (int lf = 0; lf < formats && !rc; lf++)
+        for (int bi = 0; bi < 3 && !rc; bi++)
+            for (int ui = 0; ui < 4 && !rc; ui++)
+                for (int pi = 1; pi <= 2 && !rc; pi++) {
+                    const int lists = formats == 2 ? 1 - lf : keep.lists;
+                    if (pi == 2 && (unrolls[ui] > 2 || (formats == 2 && lists == 1))) continue;
+                    s->tune = Tuning{blocks[bi], unrolls[ui], keep.list_block, unrolls[ui], pi, lists};
+                    s->invalidate_graphs();
+                    float ms = 0.0f;
+                    rc = time_candidate(s, sn, side, dt, steps, &ms);
+                    if (!rc && ms < top_ms) {
+                        top_ms = ms;
+                        top = s->tune;
+                    }
                 }
-            }
     for (int bi = 0; bi < 3 && !rc; bi++) {
-        s->tune = Tuning{top.block, top.unroll, blocks[bi], top.xsph_unroll, top.ppt};
+        s->tune = Tuning{top.block, top.unroll, blocks[bi], top.xsph_unroll, top.ppt, top.lists};
         s->invalidate_graphs();
         float ms = 0.0f;
         rc = time_candidate(s, sn, side, dt, steps, &ms);
@@ -1282,7 +1317,7 @@ extern "C" int lustrine_pbf_autotune(lustrine_pbf* s, float dt, int steps, lustr
     // then the XSPH pass's gathers in flight (it gains from more than the others)
     for (int ui = 0; ui < 4 && !rc; ui++) {
         if (unrolls[ui] == top.xsph_unroll) continue;
-        s->tune = Tuning{top.block, top.unroll, top.list_block, unrolls[ui], top.ppt};
+        s->tune = Tuning{top.block, top.unroll, top.list_block, unrolls[ui], top.ppt, top.lists};
         s->invalidate_graphs();
         float ms = 0.0f;
         rc = time_candidate(s, sn, side, dt, steps, &ms);
@@ -1489,11 +1524,31 @@ extern "C" int lustrine_pbf_neighbors(lustrine_pbf* s, int* count, int* idx, int
     // Lists refer to the sorted slots of the state the step started from:
     // the committed side's id array maps fluid slots; solid slots map back
     // through the solid sort permutation.
-    CK(cudaMemcpyAsync(cnt.data(), s->cnt, (size_t)n * sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+    std::vector<uint4> rec(s->lists_compact ? (size_t)n : 0);
+    if (s->lists_compact)
+        CK(cudaMemcpyAsync(rec.data(), s->rec, (size_t)n * sizeof(uint4), cudaMemcpyDeviceToHost, s->stream));
+    else
+        CK(cudaMemcpyAsync(cnt.data(), s->cnt, (size_t)n * sizeof(int), cudaMemcpyDeviceToHost, s->stream));
     CK(cudaMemcpyAsync(ids.data(), s->id[s->cur], (size_t)n * sizeof(int), cudaMemcpyDeviceToHost, s->stream));
     CK(cudaMemcpyAsync(nbr.data(), s->nbr, (size_t)maxn * n * sizeof(int), cudaMemcpyDeviceToHost, s->stream));
     if (s->ns) CK(cudaMemcpyAsync(sid.data(), s->solid_id, (size_t)s->ns * sizeof(int), cudaMemcpyDeviceToHost, s->stream));
     CK(cudaStreamSynchronize(s->stream));
+    if (s->lists_compact) {
+        // compact records into the column form: count, inline entries as
+        // the scene's first slot + offset, the rest from the overflow rows
+        std::vector<int> col((size_t)maxn * n);
+        for (int k = 0; k < n; k++) {
+            const uint4 r = rec[(size_t)k];
+            const int c = (int)(r.x & 0xFFu), base = (int)(r.x >> 8);
+            const unsigned w[3] = {r.y, r.z, r.w};
+            cnt[(size_t)k] = c;
+            for (int e = 0; e < c; e++)
+                col[(size_t)e * n + k] = e < COMPACT_INLINE
+                                             ? base + (int)((w[e >> 1] >> ((e & 1) * 16)) & 0xFFFFu)
+                                             : nbr[(size_t)(e - COMPACT_INLINE) * n + k];
+        }
+        nbr.swap(col);
+    }
     int rc = LUSTRINE_OK;
     // reference-semantics lists: slot t >= 0 or static slot -1 - u; the sand
     // lists leave the particle itself out (the reference lists it twice)
@@ -1516,6 +1571,12 @@ extern "C" int lustrine_pbf_neighbors(lustrine_pbf* s, int* count, int* idx, int
         }
     }
     return rc;
+}
+
+extern "C" int lustrine_pbf_list_format(const lustrine_pbf* s, int* format) {
+    if (!s || !format) return LUSTRINE_ERR_ARGS;
+    *format = s->lists_compact ? LUSTRINE_LISTS_COMPACT : LUSTRINE_LISTS_COLUMN;
+    return LUSTRINE_OK;
 }
 
 extern "C" int lustrine_pbf_reduce(lustrine_pbf* s, double out[9]) {

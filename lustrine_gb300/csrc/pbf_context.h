@@ -22,7 +22,7 @@ struct lustrine_pbf {
     lustrine_pbf_params prm{};
     lgb::StepParams sp{};
     lgb::CellPack cp{};
-    lgb::Tuning tune{128, 2, 128, 8, 1};
+    lgb::Tuning tune{128, 2, 128, 8, 1, 1};
     int n = 0, ns = 0;
     int cap = 0;  // fluid particles the buffers hold (n <= cap; sources append up to it)
     cudaStream_t stream = nullptr;
@@ -67,6 +67,8 @@ struct lustrine_pbf {
     // neighbour lists and per-particle outputs
     int* nbr = nullptr;
     int* cnt = nullptr;
+    uint4* rec = nullptr;        // compact list records (allocated where compact lists can apply)
+    bool lists_compact = false;  // the last list build wrote compact lists
     float* lam = nullptr;
     float4* lam_src = nullptr;  // PBF: the buffer whose w holds the last lambdas
     float* lam_by_id = nullptr;

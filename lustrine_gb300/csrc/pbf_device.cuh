@@ -62,15 +62,21 @@ __device__ __forceinline__ float pack_cell(const CellPack& cp, int cx, int cy, i
 struct Geo {
     int gx, gy, gz, off;
     float lox, loy, loz, hix, hiy, hiz;
+    int slot0;  // first fluid slot of the scene
 };
 
 __device__ __forceinline__ Geo geo_single(const StepParams& p) {
-    return Geo{p.gx, p.gy, p.gz, 0, p.lox, p.loy, p.loz, p.hix, p.hiy, p.hiz};
+    return Geo{p.gx, p.gy, p.gz, 0, p.lox, p.loy, p.loz, p.hix, p.hiy, p.hiz, 0};
 }
 
 __device__ __forceinline__ Geo geo_scene(const StepParams& p, int scene) {
     const SceneInfo si = p.scenes[scene];
-    return Geo{si.gx, si.gy, si.gz, si.cell_off, si.lox, si.loy, si.loz, si.hix, si.hiy, si.hiz};
+    return Geo{si.gx, si.gy, si.gz, si.cell_off, si.lox, si.loy, si.loz, si.hix, si.hiy, si.hiz, si.slot0};
+}
+
+// Slot of a compact list's 16-bit entry v (record base: the scene's first slot).
+__device__ __forceinline__ int compact_slot(const StepParams& p, int base, unsigned v) {
+    return v == COMPACT_SENTINEL ? p.n : base + (int)v;
 }
 
 // geometry of fluid slot s (slots of a scene are a fixed range)

@@ -86,16 +86,73 @@ __global__ void k_mark_solid_near(StepParams p, CellPack cp, const float4* __res
             }
 }
 
+// Where the list build puts a particle's entries.  Column lists: entry k of
+// slot s at nbr[k * n + s] with its cell codes and solid flag.
+struct ColumnLists {
+    int* nbr;
+    int n, s;
+    __device__ __forceinline__ void put(int k, int t, int dx, int dy, int dz, bool solid) {
+        nbr[(size_t)k * n + s] = entry(t, dx, dy, dz, solid);
+    }
+};
+
+// Compact lists: the first COMPACT_INLINE entries as 16-bit offsets from the
+// scene's first slot, held in registers until the record is written (fields
+// start at COMPACT_SENTINEL, an entry XORs its offset in); the rest as plain
+// slots in the column rows of nbr from row 0.  No cell codes and no solids
+// (the step uses compact lists only without either).
+struct CompactLists {
+    int* ovf;
+    int n, s, base;
+    unsigned w0, w1, w2;
+    __device__ __forceinline__ void put(int k, int t, int, int, int, bool) {
+        if (k >= COMPACT_INLINE) {
+            ovf[(size_t)(k - COMPACT_INLINE) * n + s] = t;
+            return;
+        }
+        const unsigned v = ((unsigned)(t - base) ^ COMPACT_SENTINEL) << ((k & 1) << 4);
+        if (k < 2) w0 ^= v;
+        else if (k < 4) w1 ^= v;
+        else w2 ^= v;
+    }
+};
+
+template <bool COMPACT>
+struct ListsOf {
+    using T = ColumnLists;
+};
+template <>
+struct ListsOf<true> {
+    using T = CompactLists;
+};
+__device__ __forceinline__ ColumnLists open_lists(ColumnLists*, int* nbr, int n, int s, int) {
+    return ColumnLists{nbr, n, s};
+}
+__device__ __forceinline__ CompactLists open_lists(CompactLists*, int* nbr, int n, int s, int base) {
+    return CompactLists{nbr, n, s, base, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu};
+}
+// The count and the sentinel entries up to a multiple of the passes' chunk
+// (pad divides the buffer's rows: max_nbrs rounded up to LIST_PAD_MAX).
+__device__ __forceinline__ void close_lists(const StepParams& p, const ColumnLists& l, int* __restrict__ cnt,
+                                            int c_n) {
+    cnt[l.s] = c_n;
+    for (int k = c_n; k % p.pad != 0; k++) l.nbr[(size_t)k * p.n + l.s] = sentinel_entry(p);
+}
+__device__ __forceinline__ void close_lists(const StepParams& p, const CompactLists& l, int*, int c_n) {
+    p.rec[l.s] = make_uint4((unsigned)c_n | ((unsigned)l.base << 8), l.w0, l.w1, l.w2);
+    for (int k = c_n - COMPACT_INLINE; k > 0 && k % p.pad != 0; k++) l.ovf[(size_t)k * p.n + l.s] = p.n;
+}
+
 // One row (dy, dx) of the stencil: the cells z0..z1 of a row are consecutive
 // ids, so their particles form one slot range, walked in one loop (a warp
 // then runs as many rounds as its fullest row, not the sum over the three
 // cells of its fullest cell); a candidate's dz follows from the cell bounds,
 // loaded once per row.  The candidates come in the same order as cell by cell.
-template <bool MIXED, bool SOLID, bool KAHAN = MIXED>
+template <bool MIXED, bool SOLID, bool KAHAN, class L>
 __device__ __forceinline__ void walk_row(const StepParams& p, const float4& self, int s,
                                          const float4* __restrict__ pos, const int* __restrict__ start,
                                          int row, int zc, int gz, int dx, int dy, LambdaAcc& a, int& c_n,
-                                         int* __restrict__ nbr) {
+                                         L& out) {
     const int z0 = max(zc - 1, 0), z1 = min(zc + 1, gz - 1);
     const int b0 = start[row + z0];
     const int b1 = start[row + z0 + 1];
@@ -114,7 +171,7 @@ __device__ __forceinline__ void walk_row(const StepParams& p, const float4& self
             d.z = __fadd_rn(d.z, -(float)dz * p.cell);
         }
         if (dot3e(d.x, d.y, d.z) <= p.h2) {
-            if (c_n < p.max_nbrs) nbr[(size_t)c_n * p.n + s] = entry(t, dx, dy, dz, SOLID);
+            if (c_n < p.max_nbrs) out.put(c_n, t, dx, dy, dz, SOLID);
             c_n++;
             lambda_accumulate<KAHAN>(p, a, d, SOLID);
         }
@@ -126,10 +183,10 @@ __device__ __forceinline__ void walk_row(const StepParams& p, const float4& self
 // the list is the one walk_row builds).  b1, b2: the row's cell bounds, read
 // in mixed precision only (the entry's dz code and the cell shift; fp32
 // entries carry dz = 0, which no fp32 pass reads).
-template <bool MIXED, bool SOLID, bool KAHAN = MIXED>
+template <bool MIXED, bool SOLID, bool KAHAN, class L>
 __device__ __forceinline__ void walk_range(const StepParams& p, const float4& self, int s,
                                            const float4* __restrict__ pos, int t_begin, int t_end, int b1, int b2,
-                                           int dz0, int dx, int dy, LambdaAcc& a, int& c_n, int* __restrict__ nbr) {
+                                           int dz0, int dx, int dy, LambdaAcc& a, int& c_n, L& out) {
     const float sx = -(float)dx * p.cell, sy = -(float)dy * p.cell;
     for (int t0 = t_begin; t0 < t_end; t0 += 4) {
         float4 q[4];
@@ -148,7 +205,7 @@ __device__ __forceinline__ void walk_range(const StepParams& p, const float4& se
                 d.z = __fadd_rn(d.z, -(float)dz * p.cell);
             }
             if (dot3e(d.x, d.y, d.z) <= p.h2) {
-                if (c_n < p.max_nbrs) nbr[(size_t)c_n * p.n + s] = entry(t, dx, dy, dz, SOLID);
+                if (c_n < p.max_nbrs) out.put(c_n, t, dx, dy, dz, SOLID);
                 c_n++;
                 lambda_accumulate<KAHAN>(p, a, d, SOLID);
             }
@@ -158,13 +215,12 @@ __device__ __forceinline__ void walk_range(const StepParams& p, const float4& se
 
 // One cell of the stencil on a hashed grid: the particles of its bucket,
 // kept only if they belong to that cell.
-template <bool MIXED, bool SOLID, bool KAHAN = MIXED>
+template <bool MIXED, bool SOLID, bool KAHAN, class L>
 __device__ __forceinline__ void walk_hashed_cell(const StepParams& p, const float4& self, int s,
                                                  const float4* __restrict__ pos,
                                                  const int* __restrict__ start,
                                                  const int* __restrict__ cells, int b, int packed,
-                                                 int dx, int dy, int dz, LambdaAcc& a, int& c_n,
-                                                 int* __restrict__ nbr) {
+                                                 int dx, int dy, int dz, LambdaAcc& a, int& c_n, L& out) {
     const float sx = -(float)dx * p.cell, sy = -(float)dy * p.cell, sz = -(float)dz * p.cell;
     for (int t = start[b], e = start[b + 1]; t < e; t++) {
         if ((!SOLID && t == s) || __ldg(&cells[t]) != packed) continue;
@@ -176,7 +232,7 @@ __device__ __forceinline__ void walk_hashed_cell(const StepParams& p, const floa
             d.z = __fadd_rn(d.z, sz);
         }
         if (dot3e(d.x, d.y, d.z) <= p.h2) {
-            if (c_n < p.max_nbrs) nbr[(size_t)c_n * p.n + s] = entry(t, dx, dy, dz, SOLID);
+            if (c_n < p.max_nbrs) out.put(c_n, t, dx, dy, dz, SOLID);
             c_n++;
             lambda_accumulate<KAHAN>(p, a, d, SOLID);
         }
@@ -185,8 +241,9 @@ __device__ __forceinline__ void walk_hashed_cell(const StepParams& p, const floa
 
 // FRAME: mixed storage with the iterations in the scene frame (positions
 // relative to the box corner, compensated density sums; the walk's cell is
-// the step's key, which rounding of the frame position could move)
-template <bool MIXED, bool HASHED, int B, bool FRAME = false>
+// the step's key, which rounding of the frame position could move).
+// COMPACT: the lists go to p.rec (no cell codes, no static particles).
+template <bool MIXED, bool HASHED, int B, bool FRAME = false, bool COMPACT = false>
 __global__ void __launch_bounds__(B) k_lists_lambda(StepParams p, CellPack cp, float4* __restrict__ xs,
                                                     const int* __restrict__ key_sorted,
                                                     const int* __restrict__ cell_sorted,
@@ -207,6 +264,8 @@ __global__ void __launch_bounds__(B) k_lists_lambda(StepParams p, CellPack cp, f
                                               : plain_cell(p, g, self.x, self.y, self.z);
     LambdaAcc a = lambda_init(p);
     int c_n = 0;
+    using Lists = typename ListsOf<COMPACT>::T;
+    Lists out = open_lists((Lists*)nullptr, nbr, p.n, s, g.slot0);
     const int slab = g.gx * g.gz;
     // static particles only where the cell's neighbourhood holds some
     const bool solids = p.ns > 0 && p.solid_near && __ldg(&p.solid_near[__ldg(&key_sorted[s])]);
@@ -236,10 +295,10 @@ __global__ void __launch_bounds__(B) k_lists_lambda(StepParams p, CellPack cp, f
                 const int xx = c.x + r - 1;
                 if (xx < 0 || xx >= g.gx) continue;
                 walk_range<MIXED, false, KAHAN>(p, self, s, xs, b0[r], b3[r], b1[r], b2[r], z0 - c.z, r - 1, dy,
-                                                a, c_n, nbr);
+                                                a, c_n, out);
                 if (solids)
                     walk_row<MIXED, true, KAHAN>(p, self, s, solid, sstart, g.off + y * slab + xx * g.gz, c.z, g.gz,
-                                                 r - 1, dy, a, c_n, nbr);
+                                                 r - 1, dy, a, c_n, out);
             }
         }
     }
@@ -258,14 +317,14 @@ __global__ void __launch_bounds__(B) k_lists_lambda(StepParams p, CellPack cp, f
                     const int3 cn = make_int3(xx, y, z);
                     walk_hashed_cell<MIXED, false, KAHAN>(p, self, s, xs, fstart, cell_sorted,
                                                    cell_bucket(cn, p.hash_bits), (int)pack_bits(cp, cn),
-                                                   dx, dy, z - c.z, a, c_n, nbr);
+                                                   dx, dy, z - c.z, a, c_n, out);
                 }
                 if (solids)
                     for (int z = z0; z <= z1; z++) {
                         const int3 cn = make_int3(xx, y, z);
                         walk_hashed_cell<MIXED, true, KAHAN>(p, self, s, solid, sstart, solid_cell,
                                                       cell_bucket(cn, p.hash_bits), (int)pack_bits(cp, cn),
-                                                      dx, dy, z - c.z, a, c_n, nbr);
+                                                      dx, dy, z - c.z, a, c_n, out);
                     }
             }
         }
@@ -274,10 +333,7 @@ __global__ void __launch_bounds__(B) k_lists_lambda(StepParams p, CellPack cp, f
         set_status(status, ST_NBR_OVERFLOW);
         c_n = p.max_nbrs;
     }
-    cnt[s] = c_n;
-    // sentinel entries up to a multiple of the passes' chunk (pad divides the
-    // buffer's rows: max_nbrs rounded up to LIST_PAD_MAX)
-    for (int k = c_n; k % p.pad != 0; k++) nbr[(size_t)k * p.n + s] = sentinel_entry(p);
+    close_lists(p, out, cnt, c_n);
     // lambda into w in place: neighbours read only xyz of this element here
     reinterpret_cast<float*>(xs)[4 * (size_t)s + 3] = lambda_of(p, a);
     if (rho) rho[s] = density_of(p, a);
@@ -370,6 +426,54 @@ __device__ __forceinline__ void for_each_entry_p(const StepParams& p, const int*
     }
 }
 
+// Walk a compact list (record r of slot s; col = nbr + s, its overflow
+// rows): gather(slot) loads what f(slot, value) needs of each neighbour.
+// The inline entries go min(U, 6) at a time, all gathers of a chunk in
+// flight together, so with U >= 4 a list of up to 4 neighbours waits for
+// one round trip to DRAM (the record, with the particle's own loads) and
+// one to L2 for the neighbours.  Past the count an inline entry reads the
+// sentinel slot, whose terms are exactly zero; the overflow rows are padded
+// with it to a multiple of U (the list build's pad).
+template <int U, class T, class G, class F>
+__device__ __forceinline__ void walk_compact(const StepParams& p, const uint4& r, const int* __restrict__ col,
+                                             G&& gather, F&& f) {
+    constexpr int V = U < COMPACT_INLINE ? U : COMPACT_INLINE;
+    const int c = (int)(r.x & 0xFFu);
+    const int base = (int)(r.x >> 8);
+    const int sl[COMPACT_INLINE] = {compact_slot(p, base, r.y & 0xFFFFu), compact_slot(p, base, r.y >> 16),
+                                    compact_slot(p, base, r.z & 0xFFFFu), compact_slot(p, base, r.z >> 16),
+                                    compact_slot(p, base, r.w & 0xFFFFu), compact_slot(p, base, r.w >> 16)};
+#pragma unroll
+    for (int k = 0; k < COMPACT_INLINE; k += V) {
+        if (k >= c) return;
+        T q[V];
+#pragma unroll
+        for (int u = 0; u < V; u++)
+            if (k + u < COMPACT_INLINE) q[u] = gather(sl[k + u]);
+#pragma unroll
+        for (int u = 0; u < V; u++)
+            if (k + u < COMPACT_INLINE) f(sl[k + u], q[u]);
+    }
+    if (c <= COMPACT_INLINE) return;
+    int nx[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) nx[u] = __ldg(&col[(size_t)u * p.n]);
+    for (int k = COMPACT_INLINE; k < c; k += U) {
+        int e[U];
+        T q[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) e[u] = nx[u];
+        if (k + U < c) {
+#pragma unroll
+            for (int u = 0; u < U; u++) nx[u] = __ldg(&col[(size_t)(k - COMPACT_INLINE + U + u) * p.n]);
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) q[u] = gather(e[u]);
+#pragma unroll
+        for (int u = 0; u < U; u++) f(e[u], q[u]);
+    }
+}
+
 // Lambda pass over the lists (iterations after the first); U neighbour
 // gathers in flight per thread.
 // F: bit 0 mixed precision, bit 1 the scene has static particles (the
@@ -380,7 +484,10 @@ __global__ void __launch_bounds__(B) k_lambda(StepParams p, float4* __restrict__
                                               const float4* __restrict__ solid,
                                               float* __restrict__ rho) {
     // F bit 2: the scene frame (fp32 pair offsets, compensated density sums)
+    // F bit 3: compact lists (fp32 pair offsets, no static particles)
     constexpr bool MIXED = (F & 1) != 0, SOL = (F & 2) != 0, KAHAN = MIXED || (F & 4) != 0;
+    constexpr bool COMPACT = (F & 8) != 0;
+    static_assert(!COMPACT || (!MIXED && !SOL && P == 1), "compact lists");
     pdl_wait();
     __shared__ float4 shift_tab[MIXED ? 64 : 1];
     if (MIXED) fill_shift_table(p, shift_tab);
@@ -389,10 +496,16 @@ __global__ void __launch_bounds__(B) k_lambda(StepParams p, float4* __restrict__
         if (s >= p.n) return;
         const float4 self = xs[s];
         LambdaAcc a = lambda_init(p);
-        for_each_entry<U, SOL>(p, nbr + s, cnt, s, xs, solid, [&](int e, float4 q) {
-            float3 d = rel_t<MIXED>(self, q, e, shift_tab);
-            lambda_accumulate<KAHAN>(p, a, d, SOL && entry_solid(e));
-        });
+        if (COMPACT) {
+            walk_compact<U, float4>(
+                p, __ldg(&p.rec[s]), nbr + s, [&](int t) { return xs[t]; },
+                [&](int, float4 q) { lambda_accumulate<KAHAN>(p, a, rel_t<false>(self, q, 0, shift_tab), false); });
+        } else {
+            for_each_entry<U, SOL>(p, nbr + s, cnt, s, xs, solid, [&](int e, float4 q) {
+                float3 d = rel_t<MIXED>(self, q, e, shift_tab);
+                lambda_accumulate<KAHAN>(p, a, d, SOL && entry_solid(e));
+            });
+        }
         reinterpret_cast<float*>(xs)[4 * (size_t)s + 3] = lambda_of(p, a);
         if (rho) rho[s] = density_of(p, a);
         return;
@@ -515,7 +628,8 @@ __global__ void __launch_bounds__(B, (U <= 2 && P == 1) ? 1536 / B : 1)
     k_delta(StepParams p, CellPack cp, const float4* __restrict__ xs, float4* __restrict__ xs_out,
             const int* __restrict__ nbr, const int* __restrict__ cnt, const float4* __restrict__ solid,
             const int* __restrict__ key_sorted, const float4* __restrict__ x, float4* __restrict__ v_out) {
-    constexpr bool MIXED = (F & 1) != 0, SOL = (F & 2) != 0;
+    constexpr bool MIXED = (F & 1) != 0, SOL = (F & 2) != 0, COMPACT = (F & 8) != 0;
+    static_assert(!COMPACT || (!MIXED && !SOL && P == 1), "compact lists");
     pdl_wait();
     __shared__ float4 shift_tab[MIXED ? 64 : 1];
     if (MIXED) fill_shift_table(p, shift_tab);
@@ -526,9 +640,15 @@ __global__ void __launch_bounds__(B, (U <= 2 && P == 1) ? 1536 / B : 1)
         const int scene = scene_index(p, s);
         const int packed = (MIXED && p.cell_sorted) ? __ldg(&p.cell_sorted[s]) : 0;
         DeltaAcc a{0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0};
-        for_each_entry<U, SOL, LIST_PAD_MAX>(p, nbr + s, cnt, s, xs, solid, [&](int e, float4 q) {
-            delta_pair<MIXED, SOL>(p, a, self, e, q, shift_tab);
-        });
+        if (COMPACT) {
+            walk_compact<U, float4>(
+                p, __ldg(&p.rec[s]), nbr + s, [&](int t) { return xs[t]; },
+                [&](int t, float4 q) { delta_pair<false, false>(p, a, self, t, q, shift_tab); });
+        } else {
+            for_each_entry<U, SOL, LIST_PAD_MAX>(p, nbr + s, cnt, s, xs, solid, [&](int e, float4 q) {
+                delta_pair<MIXED, SOL>(p, a, self, e, q, shift_tab);
+            });
+        }
         delta_finish<MIXED>(p, cp, s, self, a, xs_out, key_sorted, x, v_out, scene, packed);
         return;
     }
@@ -553,6 +673,24 @@ __global__ void __launch_bounds__(B, (U <= 2 && P == 1) ? 1536 / B : 1)
                                 (MIXED && p.cell_sorted) ? __ldg(&p.cell_sorted[s[r]]) : 0);
 }
 
+// A neighbour's predicted position and velocity (the XSPH gathers).
+struct PosVel {
+    float4 x, v;
+};
+
+// One XSPH pair: a += (v_j - v_i) hd^3 (the sum is scaled by c K6 once).
+template <bool MIXED>
+__device__ __forceinline__ void xsph_pair(const StepParams& p, const float4& self, const float4& vi,
+                                          const float4& q, const float4& vj, int e, const float4* tab, float& ax,
+                                          float& ay, float& az) {
+    float3 d = rel_t<MIXED>(self, q, e, tab);
+    const float hd = hdiff(p, dot3e(d.x, d.y, d.z));
+    const float w = __fmul_rn(__fmul_rn(hd, hd), hd);
+    ax = __fmaf_rn(__fsub_rn(vj.x, vi.x), w, ax);
+    ay = __fmaf_rn(__fsub_rn(vj.y, vi.y), w, ay);
+    az = __fmaf_rn(__fsub_rn(vj.z, vi.z), w, az);
+}
+
 // XSPH viscosity (Macklin & Mueller eq. 17) and commit x = x*.
 // With xs_next, also the next step's prediction from the state it commits
 // (into xs_next, key, rank, count, cellk; count is zero here, the step's
@@ -566,7 +704,8 @@ __global__ void __launch_bounds__(B) k_xsph(StepParams p, CellPack cp, const flo
                                             float4* __restrict__ xs_next, int* __restrict__ key,
                                             int* __restrict__ rank, int* __restrict__ count,
                                             int* __restrict__ cellk, int* __restrict__ tile_count) {
-    constexpr bool MIXED = (F & 1) != 0, SOL = (F & 2) != 0;
+    constexpr bool MIXED = (F & 1) != 0, SOL = (F & 2) != 0, COMPACT = (F & 8) != 0;
+    static_assert(!COMPACT || (!MIXED && !SOL), "compact lists");
     pdl_wait();
     __shared__ float4 shift_tab[MIXED ? 64 : 1];
     if (MIXED) fill_shift_table(p, shift_tab);
@@ -574,10 +713,14 @@ __global__ void __launch_bounds__(B) k_xsph(StepParams p, CellPack cp, const flo
     if (s >= p.n) return;
     const float4 self = xs[s];
     const float4 vi = v_in[s];
-    const int c = cnt[s];
     const int* __restrict__ col = nbr + s;
     float ax = 0.0f, ay = 0.0f, az = 0.0f;
-    if (p.c_xsph != 0.0f) {
+    if (COMPACT && p.c_xsph != 0.0f) {
+        walk_compact<U, PosVel>(
+            p, __ldg(&p.rec[s]), col, [&](int t) { return PosVel{xs[t], v_in[t]}; },
+            [&](int t, const PosVel& q) { xsph_pair<false>(p, self, vi, q.x, q.v, t, shift_tab, ax, ay, az); });
+    } else if (p.c_xsph != 0.0f) {
+        const int c = cnt[s];
         const int sent = sentinel_entry(p);
         for (int k = 0; k < c; k += U) {
             int e[U];
@@ -593,14 +736,7 @@ __global__ void __launch_bounds__(B) k_xsph(StepParams p, CellPack cp, const flo
                 vj[u] = v_in[entry_slot(e[u])];
             }
 #pragma unroll
-            for (int u = 0; u < U; u++) {
-                float3 d = rel_t<MIXED>(self, q[u], e[u], shift_tab);
-                const float hd = hdiff(p, dot3e(d.x, d.y, d.z));
-                const float w = __fmul_rn(__fmul_rn(hd, hd), hd);
-                ax = __fmaf_rn(__fsub_rn(vj[u].x, vi.x), w, ax);
-                ay = __fmaf_rn(__fsub_rn(vj[u].y, vi.y), w, ay);
-                az = __fmaf_rn(__fsub_rn(vj[u].z, vi.z), w, az);
-            }
+            for (int u = 0; u < U; u++) xsph_pair<MIXED>(p, self, vi, q[u], vj[u], e[u], shift_tab, ax, ay, az);
         }
     }
     // v += c sum (v_j - v_i) W, W = K6 hd^3
@@ -1037,7 +1173,8 @@ void launch_key(bool mixed, const StepParams& p, const CellPack& cp, const float
             TUNE_BLOCKS(KERNEL, MIX, 8, tu, N, ST, __VA_ARGS__);                                \
     } while (0)
 // fcode: bit 0 mixed (cell-relative pair offsets), bit 1 static particles,
-// bit 2 (the lambda pass only) the scene frame's compensated sums
+// bit 2 (the lambda pass only) the scene frame's compensated sums, bit 3
+// compact lists (with bit 2 at most)
 #define TUNE_DISPATCH(KERNEL, fcode, tu, N, ST, ...)                                            \
     do {                                                                                        \
         switch (fcode) {                                                                        \
@@ -1072,7 +1209,22 @@ void launch_lists_lambda(bool mixed, const Tuning& tu, const StepParams& p, cons
         if (p.hash_bits) LGB_LISTS_H(MIX, true, BB); \
         else LGB_LISTS_H(MIX, false, BB);        \
     } while (0)
-    if (mixed && p.frame) {  // the scene frame: fp32 pair offsets, compensated sums
+    if (p.rec) {  // compact lists: fp32 pair offsets (the scene frame: compensated sums)
+#define LGB_LISTS_C(H, FR, BB)                                                                    \
+    launch_k(k_lists_lambda<false, H, BB, FR, true>, blocks_for(p.n, BB), BB, st, pdl, pp, cp, xs, key_sorted, \
+             cell_sorted, fstart, solid, solid_cell, sstart, nbr, cnt, rho, status)
+#define LGB_LISTS_CB(H, FR)                        \
+    do {                                           \
+        if (B == 64) LGB_LISTS_C(H, FR, 64);       \
+        else if (B == 128) LGB_LISTS_C(H, FR, 128); \
+        else LGB_LISTS_C(H, FR, 256);              \
+    } while (0)
+        if (p.frame) LGB_LISTS_CB(false, true);
+        else if (p.hash_bits) LGB_LISTS_CB(true, false);
+        else LGB_LISTS_CB(false, false);
+#undef LGB_LISTS_CB
+#undef LGB_LISTS_C
+    } else if (mixed && p.frame) {  // the scene frame: fp32 pair offsets, compensated sums
         if (B == 64) launch_k(k_lists_lambda<false, false, 64, true>, blocks_for(p.n, 64), 64, st, pdl, pp, cp, xs,
                               key_sorted, cell_sorted, fstart, solid, solid_cell, sstart, nbr, cnt, rho, status);
         else if (B == 128) launch_k(k_lists_lambda<false, false, 128, true>, blocks_for(p.n, 128), 128, st, pdl, pp, cp,
@@ -1097,7 +1249,10 @@ void launch_lambda(bool mixed, const Tuning& tu, const StepParams& p, float4* xs
                    const int* cnt, const float4* solid, float* rho, cudaStream_t st) {
     if (p.n <= 0) return;
     const int f = ((mixed && !p.frame) ? 1 : 0) | (p.ns > 0 ? 2 : 0);
-    if (mixed && p.frame)  // the scene frame: one particle per thread
+    if (p.rec) {  // compact lists: one particle per thread
+        if (p.frame) TUNE_CASE(k_lambda, 12, tu, p.n, st, p, xs, nbr, cnt, solid, rho);
+        else TUNE_CASE(k_lambda, 8, tu, p.n, st, p, xs, nbr, cnt, solid, rho);
+    } else if (mixed && p.frame)  // the scene frame: one particle per thread
         TUNE_DISPATCH_FRAME(k_lambda, f | 4, tu, p.n, st, p, xs, nbr, cnt, solid, rho);
     else
         TUNE_DISPATCH_PPT(k_lambda, f, tu, p.n, st, p, xs, nbr, cnt, solid, rho);
@@ -1109,7 +1264,10 @@ void launch_delta(bool mixed, const Tuning& tu, const StepParams& p, const CellP
                   cudaStream_t st) {
     if (p.n <= 0) return;
     const int f = ((mixed && !p.frame) ? 1 : 0) | (p.ns > 0 ? 2 : 0);
-    TUNE_DISPATCH_PPT(k_delta, f, tu, p.n, st, p, cp, xs, xs_out, nbr, cnt, solid, key_sorted, x, v_out);
+    if (p.rec)  // compact lists: one particle per thread
+        TUNE_CASE(k_delta, 8, tu, p.n, st, p, cp, xs, xs_out, nbr, cnt, solid, key_sorted, x, v_out);
+    else
+        TUNE_DISPATCH_PPT(k_delta, f, tu, p.n, st, p, cp, xs, xs_out, nbr, cnt, solid, key_sorted, x, v_out);
 }
 
 void launch_xsph(bool mixed, const Tuning& tu, const StepParams& p, const CellPack& cp,
@@ -1120,8 +1278,12 @@ void launch_xsph(bool mixed, const Tuning& tu, const StepParams& p, const CellPa
     Tuning tx = tu;  // the XSPH pass has its own gathers in flight
     tx.unroll = tu.xsph_unroll;
     const int f = ((mixed && !p.frame) ? 1 : 0) | (p.ns > 0 ? 2 : 0);
-    TUNE_DISPATCH(k_xsph, f, tx, p.n, st, p, cp, xs, v_in, nbr, cnt, key_sorted, x_out, v_out, xs_next, key,
-                  rank, count, cellk, tile_count);
+    if (p.rec)
+        TUNE_CASE(k_xsph, 8, tx, p.n, st, p, cp, xs, v_in, nbr, cnt, key_sorted, x_out, v_out, xs_next, key, rank,
+                  count, cellk, tile_count);
+    else
+        TUNE_DISPATCH(k_xsph, f, tx, p.n, st, p, cp, xs, v_in, nbr, cnt, key_sorted, x_out, v_out, xs_next, key,
+                      rank, count, cellk, tile_count);
 }
 
 void launch_unpermute_pos(bool mixed, const StepParams& p, const CellPack& cp, const float4* a,

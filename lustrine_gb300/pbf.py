@@ -98,7 +98,7 @@ def sand_params(X, Y, Z, *, radius=0.5, kernel_radius_scale=2.0, mass=1.0, gravi
 def _tuning_dict(t) -> dict:
     return {"block": t.block, "unroll": t.unroll, "list_block": t.list_block, "xsph_unroll": t.xsph_unroll,
             "particles_per_thread": t.particles_per_thread, "solver": t.solver,
-            "solver_threads": t.solver_threads}
+            "solver_threads": t.solver_threads, "list_format": t.list_format}
 
 
 def _f32(a, n):
@@ -271,6 +271,12 @@ class PbfSim:
         check(self.lib.lustrine_pbf_neighbors(self.h, _ptr(cnt), _ptr(idx), cap), "neighbors")
         return cnt, idx
 
+    def list_format(self) -> str:
+        """"compact" or "column": the form of the last step's neighbour lists."""
+        v = C.c_int()
+        check(self.lib.lustrine_pbf_list_format(self.h, C.byref(v)), "list_format")
+        return "compact" if v.value == _lib.LISTS_COMPACT else "column"
+
     def reduce(self):
         """FP64 device reductions: mass, momentum[3], kinetic energy,
         centre of mass[3], max |rho/rho0 - 1|."""
@@ -319,8 +325,12 @@ class PbfSim:
         check(self.lib.lustrine_pbf_set_attracted(self.h, a.ctypes.data), "set_attracted")
 
     def set_tuning(self, block: int, unroll: int, list_block: int, xsph_unroll: int = 0,
-                   particles_per_thread: int = 1, solver: int = 0, solver_threads: int = 0):
-        t = _lib.PbfTuning(block, unroll, list_block, xsph_unroll, particles_per_thread, solver, solver_threads)
+                   particles_per_thread: int = 1, solver: int = 0, solver_threads: int = 0,
+                   list_format: int = _lib.LISTS_COMPACT):
+        """Launch shape (lustrine_pbf_set_tuning); list_format LISTS_COMPACT
+        applies where the step allows compact lists, else column lists."""
+        t = _lib.PbfTuning(block, unroll, list_block, xsph_unroll, particles_per_thread, solver, solver_threads,
+                           list_format)
         check(self.lib.lustrine_pbf_set_tuning(self.h, C.byref(t)), "set_tuning")
 
     def autotune(self, dt: float, steps: int = 3) -> tuple[dict, float]:

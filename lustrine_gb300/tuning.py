@@ -51,7 +51,8 @@ def tune(sim: PbfSim, dt: float, steps: int = 3, cache: str | None = CACHE, refr
     if not refresh and key in db:
         t = db[key]["tuning"]
         sim.set_tuning(t["block"], t["unroll"], t["list_block"], t.get("xsph_unroll", 0),
-                       t.get("particles_per_thread", 1), t.get("solver", 0), t.get("solver_threads", 0))
+                       t.get("particles_per_thread", 1), t.get("solver", 0), t.get("solver_threads", 0),
+                       t.get("list_format", 1))
         return {"tuning": t, "ms": db[key]["ms"], "cached": True}
     t, ms = sim.autotune(dt, steps)
     if cache:

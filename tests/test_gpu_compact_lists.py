@@ -1,0 +1,133 @@
+"""Compact neighbour lists (one 16-byte record per particle: the count, the
+scene's first slot and six entries as 16-bit scene offsets; longer lists go
+on in the column rows) against the column lists: the same entries in the
+same order, so every pass sums the same terms in the same order and the
+step's fp32 results are bitwise equal; and the cases where the step must
+keep column lists."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _run(sc, p, list_format, unroll=2, xsph_unroll=8, steps=3, solids=None):
+    from lustrine_gb300 import PbfSim
+    sim = PbfSim(p, sc.n, 0 if solids is None else len(solids))
+    sim.upload(sc.x, None, solids)
+    sim.set_tuning(128, unroll, 128, xsph_unroll, 1, list_format=list_format)
+    sim.step(sc.dt, steps)
+    assert sim.status() == 0
+    out = sim.download(lambdas=True, density=True)
+    fmt = sim.list_format()
+    cnt, idx = sim.neighbors()
+    sim.close()
+    return out, fmt, cnt, idx
+
+
+def _params(sc, precision, **kw):
+    from lustrine_gb300 import pbf_params
+    p = pbf_params(*sc.domain, iterations=sc.iterations, c_xsph=sc.c_xsph, precision=precision)
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+def _assert_same(a, b):
+    for u, w in zip(a, b):
+        np.testing.assert_array_equal(u, w)
+
+
+@pytest.mark.parametrize("precision", [0, 2])
+def test_compact_lists_give_the_column_bits(precision):
+    """Config-0 dam break (10,000 particles): compact lists with 1, 2, 4 and 8
+    gathers in flight against column lists, positions, velocities, lambdas,
+    densities and the neighbour lists all equal."""
+    from lustrine_gb300 import LISTS_COLUMN, LISTS_COMPACT, scenes
+    sc = scenes.config0(seed=41)
+    ref, fmt, cnt0, idx0 = _run(sc, _params(sc, precision), LISTS_COLUMN)
+    assert fmt == "column"
+    for unroll in (1, 2, 4, 8):
+        got, fmt, cnt, idx = _run(sc, _params(sc, precision), LISTS_COMPACT, unroll, unroll)
+        assert fmt == "compact"
+        _assert_same(ref, got)
+        np.testing.assert_array_equal(cnt0, cnt)
+        np.testing.assert_array_equal(idx0, idx)
+
+
+@pytest.mark.parametrize("unroll", [1, 2, 4, 8])
+def test_compact_overflow_rows(unroll):
+    """A block at spacing 0.6 h: about 18 neighbours a particle, so every list
+    runs past the six inline entries into the overflow rows (padded with the
+    sentinel to the chunk); results and lists equal the column lists'."""
+    from lustrine_gb300 import LISTS_COLUMN, LISTS_COMPACT, scenes
+    rng = np.random.default_rng(42)
+    x = scenes.jitter(scenes.lattice((14, 12, 14), (4, 1, 4)) * 0.6, 0.05, rng)
+    sc = scenes.Scene("dense", (16, 16, 16), x.astype(np.float32), dt=1 / 60, iterations=4)
+    p = _params(sc, 0)
+    ref, _, cnt0, idx0 = _run(sc, p, LISTS_COLUMN, unroll, unroll, steps=2)
+    got, fmt, cnt, idx = _run(sc, p, LISTS_COMPACT, unroll, unroll, steps=2)
+    assert fmt == "compact"
+    assert (cnt0 > 7).mean() > 0.5  # count includes the particle itself
+    _assert_same(ref, got)
+    np.testing.assert_array_equal(cnt0, cnt)
+    np.testing.assert_array_equal(idx0, idx)
+
+
+@pytest.mark.parametrize("precision", [0, 2])
+def test_compact_batch_equals_column_batch(precision):
+    """48 scenes of the batched distribution (the smaller ones, 1,029 to about
+    6,000 particles): compact records carry each scene's first slot; the
+    batch's results and lists equal the column lists'."""
+    from lustrine_gb300 import LISTS_COLUMN, LISTS_COMPACT, PbfSim, pbf_params, scenes
+    scs = sorted(scenes.config3(), key=lambda s: s.n)[:48]
+    x = np.concatenate([s.x for s in scs])
+    res = []
+    for lf in (LISTS_COLUMN, LISTS_COMPACT):
+        b = PbfSim.batch(pbf_params(8, 8, 8, iterations=4, precision=precision), [s.domain for s in scs],
+                         [s.n for s in scs])
+        b.upload(x)
+        b.set_tuning(128, 4, 128, 4, 1, list_format=lf)
+        b.step(scs[0].dt, 3)
+        assert b.status() == 0
+        res.append((b.download(lambdas=True, density=True), b.list_format(), b.neighbors()))
+        b.close()
+    assert res[0][1] == "column" and res[1][1] == "compact"
+    _assert_same(res[0][0], res[1][0])
+    _assert_same(res[0][2], res[1][2])
+
+
+def test_compact_lists_only_where_they_apply():
+    """Scenes of 65,535 particles take compact lists, 65,536 do not (16-bit
+    offsets, one value kept for the sentinel); nor do static particles, the
+    cell-relative mixed form (cell codes in the entries), two particles per
+    thread or the reference's step."""
+    from lustrine_gb300 import (LISTS_COMPACT, MODE_REFERENCE, PRECISION_MIXED, PbfSim, pbf_params,
+                                reference_params, scenes)
+    rng = np.random.default_rng(43)
+    big = scenes.jitter(scenes.lattice((64, 17, 64)), 0.05, rng)[:65536]
+
+    def fmt_of(p, x, solids=None, ppt=1):
+        sim = PbfSim(p, len(x), 0 if solids is None else len(solids))
+        sim.upload(x, None, solids)
+        sim.set_tuning(128, 2, 128, 2, ppt, list_format=LISTS_COMPACT)
+        sim.step(1 / 60)
+        assert sim.status() == 0
+        f = sim.list_format()
+        sim.close()
+        return f
+
+    assert fmt_of(pbf_params(130, 40, 130), big[:65535]) == "compact"
+    assert fmt_of(pbf_params(130, 40, 130), big) == "column"
+    small = big[:4000]
+    assert fmt_of(pbf_params(130, 40, 130, precision=PRECISION_MIXED), small) == "column"
+    assert fmt_of(pbf_params(130, 40, 130), small, ppt=2) == "column"
+    solid, _ = scenes.heightmap_solids(16, 300, origin=(0, 0, 0), rng=rng, max_height=2)
+    assert fmt_of(pbf_params(130, 40, 130), small, solids=solid) == "column"
+    rp = reference_params(130, 40, 130, 0.5, 2.0)
+    assert fmt_of(rp, small) == "column"
+    # a batch with one scene past the limit keeps column lists for all
+    b = PbfSim.batch(pbf_params(8, 8, 8, iterations=2), [(130, 40, 130), (40, 40, 40)], [65536, 1000])
+    b.upload(np.concatenate([big, scenes.jitter(scenes.lattice((10, 10, 10), (5, 0, 5)), 0.05, rng)]))
+    b.step(1 / 60)
+    assert b.status() == 0 and b.list_format() == "column"
+    b.close()

@@ -139,4 +139,4 @@ def test_ctypes_structs_follow_the_header():
     from lustrine_gb300._lib import PbfTuning, SandControls
     for cls, name in ((PbfTuning, "lustrine_pbf_tuning"), (SandControls, "lustrine_sand_controls")):
         assert [f[0] for f in cls._fields_] == _header_struct_fields(name), name
-    assert C.sizeof(PbfTuning) == 28
+    assert C.sizeof(PbfTuning) == 32
