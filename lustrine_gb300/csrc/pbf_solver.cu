@@ -243,16 +243,13 @@ __device__ __forceinline__ void walk_hashed_cell(const StepParams& p, const floa
 // relative to the box corner, compensated density sums; the walk's cell is
 // the step's key, which rounding of the frame position could move).
 // COMPACT: the lists go to p.rec (no cell codes, no static particles).
-template <bool MIXED, bool HASHED, int B, bool FRAME = false, bool COMPACT = false>
-__global__ void __launch_bounds__(B) k_lists_lambda(StepParams p, CellPack cp, float4* __restrict__ xs,
-                                                    const int* __restrict__ key_sorted,
-                                                    const int* __restrict__ cell_sorted,
-                                                    const int* __restrict__ fstart,
-                                                    const float4* __restrict__ solid,
-                                                    const int* __restrict__ solid_cell,
-                                                    const int* __restrict__ sstart,
-                                                    int* __restrict__ nbr, int* __restrict__ cnt,
-                                                    float* __restrict__ rho, int* status) {
+template <bool MIXED, bool HASHED, bool FRAME, bool COMPACT>
+__device__ __forceinline__ void lists_lambda(const StepParams& p, const CellPack& cp, float4* __restrict__ xs,
+                                             const int* __restrict__ key_sorted, const int* __restrict__ cell_sorted,
+                                             const int* __restrict__ fstart, const float4* __restrict__ solid,
+                                             const int* __restrict__ solid_cell, const int* __restrict__ sstart,
+                                             int* __restrict__ nbr, int* __restrict__ cnt, float* __restrict__ rho,
+                                             int* status) {
     pdl_wait();
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= p.n) return;
@@ -337,6 +334,35 @@ __global__ void __launch_bounds__(B) k_lists_lambda(StepParams p, CellPack cp, f
     // lambda into w in place: neighbours read only xyz of this element here
     reinterpret_cast<float*>(xs)[4 * (size_t)s + 3] = lambda_of(p, a);
     if (rho) rho[s] = density_of(p, a);
+}
+
+template <bool MIXED, bool HASHED, int B, bool FRAME = false>
+__global__ void __launch_bounds__(B) k_lists_lambda(StepParams p, CellPack cp, float4* __restrict__ xs,
+                                                    const int* __restrict__ key_sorted,
+                                                    const int* __restrict__ cell_sorted,
+                                                    const int* __restrict__ fstart,
+                                                    const float4* __restrict__ solid,
+                                                    const int* __restrict__ solid_cell,
+                                                    const int* __restrict__ sstart,
+                                                    int* __restrict__ nbr, int* __restrict__ cnt,
+                                                    float* __restrict__ rho, int* status) {
+    lists_lambda<MIXED, HASHED, FRAME, false>(p, cp, xs, key_sorted, cell_sorted, fstart, solid, solid_cell, sstart,
+                                              nbr, cnt, rho, status);
+}
+
+// Compact lists (no static particles, fp32 pair offsets).
+template <bool HASHED, int B, bool FRAME>
+__global__ void __launch_bounds__(B) k_lists_compact(StepParams p, CellPack cp, float4* __restrict__ xs,
+                                                             const int* __restrict__ key_sorted,
+                                                             const int* __restrict__ cell_sorted,
+                                                             const int* __restrict__ fstart,
+                                                             const float4* __restrict__ solid,
+                                                             const int* __restrict__ solid_cell,
+                                                             const int* __restrict__ sstart,
+                                                             int* __restrict__ nbr, int* __restrict__ cnt,
+                                                             float* __restrict__ rho, int* status) {
+    lists_lambda<false, HASHED, FRAME, true>(p, cp, xs, key_sorted, cell_sorted, fstart, solid, solid_cell, sstart,
+                                             nbr, cnt, rho, status);
 }
 
 // Walk a particle's list U entries at a time, calling f(entry, position)
@@ -440,19 +466,22 @@ __device__ __forceinline__ void walk_compact(const StepParams& p, const uint4& r
     constexpr int V = U < COMPACT_INLINE ? U : COMPACT_INLINE;
     const int c = (int)(r.x & 0xFFu);
     const int base = (int)(r.x >> 8);
-    const int sl[COMPACT_INLINE] = {compact_slot(p, base, r.y & 0xFFFFu), compact_slot(p, base, r.y >> 16),
-                                    compact_slot(p, base, r.z & 0xFFFFu), compact_slot(p, base, r.z >> 16),
-                                    compact_slot(p, base, r.w & 0xFFFFu), compact_slot(p, base, r.w >> 16)};
+    // each chunk decodes its own entries (a short list decodes only those it uses)
 #pragma unroll
     for (int k = 0; k < COMPACT_INLINE; k += V) {
         if (k >= c) return;
+        int sl[V];
         T q[V];
 #pragma unroll
         for (int u = 0; u < V; u++)
-            if (k + u < COMPACT_INLINE) q[u] = gather(sl[k + u]);
+            if (k + u < COMPACT_INLINE) {
+                const unsigned w = (k + u) < 2 ? r.y : ((k + u) < 4 ? r.z : r.w);
+                sl[u] = compact_slot(p, base, ((k + u) & 1) ? (w >> 16) : (w & 0xFFFFu));
+                q[u] = gather(sl[u]);
+            }
 #pragma unroll
         for (int u = 0; u < V; u++)
-            if (k + u < COMPACT_INLINE) f(sl[k + u], q[u]);
+            if (k + u < COMPACT_INLINE) f(sl[u], q[u]);
     }
     if (c <= COMPACT_INLINE) return;
     int nx[U];
@@ -621,10 +650,11 @@ __device__ __forceinline__ void delta_finish(const StepParams& p, const CellPack
 // With one particle per thread and up to 2 gathers in flight the kernel
 // fits 40 registers without spilling: 6 blocks of 256 threads per SM instead
 // of 5 (a 262,144-particle pass then takes 1.12 waves of the GPU instead of
-// 1.35).  P = 2: two particles per thread (B apart), their lists walked
-// together.
+// 1.35).  Compact lists with one gather in flight fit 32 registers (8 bytes
+// spilled): 16 blocks of 128 threads per SM, the whole SM's warps.  P = 2:
+// two particles per thread (B apart), their lists walked together.
 template <int F, int U, int B, int P = 1>
-__global__ void __launch_bounds__(B, (U <= 2 && P == 1) ? 1536 / B : 1)
+__global__ void __launch_bounds__(B, ((F & 8) && U == 1) ? 2048 / B : ((U <= 2 && P == 1) ? 1536 / B : 1))
     k_delta(StepParams p, CellPack cp, const float4* __restrict__ xs, float4* __restrict__ xs_out,
             const int* __restrict__ nbr, const int* __restrict__ cnt, const float4* __restrict__ solid,
             const int* __restrict__ key_sorted, const float4* __restrict__ x, float4* __restrict__ v_out) {
@@ -1211,7 +1241,7 @@ void launch_lists_lambda(bool mixed, const Tuning& tu, const StepParams& p, cons
     } while (0)
     if (p.rec) {  // compact lists: fp32 pair offsets (the scene frame: compensated sums)
 #define LGB_LISTS_C(H, FR, BB)                                                                    \
-    launch_k(k_lists_lambda<false, H, BB, FR, true>, blocks_for(p.n, BB), BB, st, pdl, pp, cp, xs, key_sorted, \
+    launch_k(k_lists_compact<H, BB, FR>, blocks_for(p.n, BB), BB, st, pdl, pp, cp, xs, key_sorted, \
              cell_sorted, fstart, solid, solid_cell, sstart, nbr, cnt, rho, status)
 #define LGB_LISTS_CB(H, FR)                        \
     do {                                           \
