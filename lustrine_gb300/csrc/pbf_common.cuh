@@ -14,8 +14,10 @@
 //   compact lists (PBF mode, scenes of at most COMPACT_MAX_SCENE particles,
 //     no static particles, no cell codes): rec uint4[n], one 16-byte record
 //     per slot with the count, the scene's first slot and the first
-//     COMPACT_INLINE neighbours as 16-bit scene-local slots; entries from
-//     COMPACT_INLINE on in the column-major rows of nbr as plain slots.
+//     COMPACT_INLINE neighbours as 16-bit scene-local slots; rec2 uint4[n],
+//     the next COMPACT_EXT (written for lists longer than COMPACT_INLINE);
+//     entries from COMPACT_RECORDS on in the column-major rows of nbr as
+//     plain slots.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -43,11 +45,13 @@ struct SceneInfo {
     int slot0, spare;  // the scene's first fluid slot
 };
 
-// Compact neighbour lists (StepParams::rec): record.x = count | first slot
-// of the particle's scene << 8; .y, .z, .w = entries 0-5 as 16-bit offsets
-// from that slot, entry 2k in the low half, COMPACT_SENTINEL past the count
-// (the sentinel slot n).
+// Compact neighbour lists (StepParams::rec, rec2): record.x = count | first
+// slot of the particle's scene << 8; .y, .z, .w = entries 0-5 as 16-bit
+// offsets from that slot, entry 2k in the low half, COMPACT_SENTINEL past the
+// count (the sentinel slot n); the second record, entries 6-13 the same way.
 constexpr int COMPACT_INLINE = 6;
+constexpr int COMPACT_EXT = 8;
+constexpr int COMPACT_RECORDS = COMPACT_INLINE + COMPACT_EXT;
 constexpr unsigned COMPACT_SENTINEL = 0xFFFFu;
 constexpr int COMPACT_MAX_SCENE = 65535;   // scene-local offsets 0..65534
 constexpr int COMPACT_MAX_N = 1 << 24;     // first slot in 24 bits
@@ -92,6 +96,7 @@ struct StepParams {
     float dt;
     int frame;            // mixed storage, iterations in the scene frame (LUSTRINE_PRECISION_MIXED_SCENE)
     uint4* rec;           // compact neighbour lists of this step (nullptr: column lists with counts)
+    uint4* rec2;          // their second records
 };
 
 // Sand mode: simulate_sand's per-call inputs (Simulate.cpp:156-209).

@@ -209,7 +209,7 @@ void lustrine_pbf::free_buffers() {
                     rank, tmp, perm, count, start, block_sums, tile_sum, solid_near, solid, solid_raw, sstart, nbr, cnt, lam,
                     lam_by_id, rho, status, red, qcount, out3, out3d, iota, slot_of, solid_id, d_scenes, d_scene_of,
                     d_solid_scene_of, cellk, cell_sorted, solid_cell, att[0], att[1], d_bins, d_scene_slot0,
-                    d_queue, rec};
+                    d_queue, rec, rec2};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     x[0] = x[1] = xs[0] = xs[1] = v[0] = v[1] = nullptr;
@@ -218,7 +218,7 @@ void lustrine_pbf::free_buffers() {
     key = key_sorted = rank = tmp = perm = count = start = block_sums = tile_sum = sstart = nullptr;
     nbr = cnt = status = qcount = iota = slot_of = solid_id = d_scene_of = d_solid_scene_of = nullptr;
     cellk = cell_sorted = solid_cell = nullptr;
-    rec = nullptr;
+    rec = rec2 = nullptr;
     lists_compact = false;
     att[0] = att[1] = nullptr;
     solid_near = nullptr;
@@ -288,7 +288,10 @@ static int ctx_alloc(lustrine_pbf* s) {
     const size_t list_rows = (size_t)((s->sp.max_nbrs + LIST_PAD_MAX - 1) / LIST_PAD_MAX * LIST_PAD_MAX);
     rc = rc ? rc : dalloc(&s->nbr, list_rows * (size_t)n);
     rc = rc ? rc : dalloc(&s->cnt, n);
-    if (compact_capable(s)) rc = rc ? rc : dalloc(&s->rec, n);
+    if (compact_capable(s)) {
+        rc = rc ? rc : dalloc(&s->rec, n);
+        rc = rc ? rc : dalloc(&s->rec2, n);
+    }
     rc = rc ? rc : dalloc(&s->lam, n);
     s->lam_by_id_len = (size_t)(n + ns > s->sp.max_nbrs ? n + ns : s->sp.max_nbrs) + 1;
     rc = rc ? rc : dalloc(&s->lam_by_id, s->lam_by_id_len);
@@ -978,6 +981,7 @@ static int enqueue_step(lustrine_pbf* s, cudaStream_t st, StageMarks* mk = nullp
         // (compact records where the step allows them)
         StepParams pl = p;
         pl.rec = compact_now(s) ? s->rec : nullptr;
+        pl.rec2 = pl.rec ? s->rec2 : nullptr;
         s->lists_compact = pl.rec != nullptr;
         float4* a = s->xs[o];
         float4* b = s->xs_alt;
@@ -1524,28 +1528,31 @@ extern "C" int lustrine_pbf_neighbors(lustrine_pbf* s, int* count, int* idx, int
     // Lists refer to the sorted slots of the state the step started from:
     // the committed side's id array maps fluid slots; solid slots map back
     // through the solid sort permutation.
-    std::vector<uint4> rec(s->lists_compact ? (size_t)n : 0);
-    if (s->lists_compact)
+    std::vector<uint4> rec(s->lists_compact ? (size_t)n : 0), rec2(rec.size());
+    if (s->lists_compact) {
         CK(cudaMemcpyAsync(rec.data(), s->rec, (size_t)n * sizeof(uint4), cudaMemcpyDeviceToHost, s->stream));
-    else
+        CK(cudaMemcpyAsync(rec2.data(), s->rec2, (size_t)n * sizeof(uint4), cudaMemcpyDeviceToHost, s->stream));
+    } else
         CK(cudaMemcpyAsync(cnt.data(), s->cnt, (size_t)n * sizeof(int), cudaMemcpyDeviceToHost, s->stream));
     CK(cudaMemcpyAsync(ids.data(), s->id[s->cur], (size_t)n * sizeof(int), cudaMemcpyDeviceToHost, s->stream));
     CK(cudaMemcpyAsync(nbr.data(), s->nbr, (size_t)maxn * n * sizeof(int), cudaMemcpyDeviceToHost, s->stream));
     if (s->ns) CK(cudaMemcpyAsync(sid.data(), s->solid_id, (size_t)s->ns * sizeof(int), cudaMemcpyDeviceToHost, s->stream));
     CK(cudaStreamSynchronize(s->stream));
     if (s->lists_compact) {
-        // compact records into the column form: count, inline entries as
-        // the scene's first slot + offset, the rest from the overflow rows
+        // compact records into the column form: count, the records'
+        // entries as the scene's first slot + offset (the second record is
+        // written only for lists longer than its first), the rest from the
+        // overflow rows
         std::vector<int> col((size_t)maxn * n);
         for (int k = 0; k < n; k++) {
-            const uint4 r = rec[(size_t)k];
+            const uint4 r = rec[(size_t)k], x = rec2[(size_t)k];
             const int c = (int)(r.x & 0xFFu), base = (int)(r.x >> 8);
-            const unsigned w[3] = {r.y, r.z, r.w};
+            const unsigned w[COMPACT_RECORDS / 2] = {r.y, r.z, r.w, x.x, x.y, x.z, x.w};
             cnt[(size_t)k] = c;
             for (int e = 0; e < c; e++)
-                col[(size_t)e * n + k] = e < COMPACT_INLINE
+                col[(size_t)e * n + k] = e < COMPACT_RECORDS
                                              ? base + (int)((w[e >> 1] >> ((e & 1) * 16)) & 0xFFFFu)
-                                             : nbr[(size_t)(e - COMPACT_INLINE) * n + k];
+                                             : nbr[(size_t)(e - COMPACT_RECORDS) * n + k];
         }
         nbr.swap(col);
     }

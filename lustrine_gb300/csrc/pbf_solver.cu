@@ -96,24 +96,23 @@ struct ColumnLists {
     }
 };
 
-// Compact lists: the first COMPACT_INLINE entries as 16-bit offsets from the
-// scene's first slot, held in registers until the record is written (fields
-// start at COMPACT_SENTINEL, an entry XORs its offset in); the rest as plain
-// slots in the column rows of nbr from row 0.  No cell codes and no solids
-// (the step uses compact lists only without either).
+// Compact lists: the first COMPACT_RECORDS entries as 16-bit offsets from
+// the scene's first slot, staged in the thread's COMPACT_STRIDE words of
+// shared memory (filled with COMPACT_SENTINEL first; a stride of 9 words
+// keeps a warp's stores and loads free of bank conflicts) until the records
+// are written; the rest as plain slots in the column rows of nbr from row 0.
+// No cell codes and no solids (the step uses compact lists only without
+// either).
+constexpr int COMPACT_STRIDE = 9;
 struct CompactLists {
     int* ovf;
     int n, s, base;
-    unsigned w0, w1, w2;
+    unsigned* stage;  // this thread's words
     __device__ __forceinline__ void put(int k, int t, int, int, int, bool) {
-        if (k >= COMPACT_INLINE) {
-            ovf[(size_t)(k - COMPACT_INLINE) * n + s] = t;
-            return;
-        }
-        const unsigned v = ((unsigned)(t - base) ^ COMPACT_SENTINEL) << ((k & 1) << 4);
-        if (k < 2) w0 ^= v;
-        else if (k < 4) w1 ^= v;
-        else w2 ^= v;
+        if (k < COMPACT_RECORDS)
+            reinterpret_cast<unsigned short*>(stage)[k] = (unsigned short)(t - base);
+        else
+            ovf[(size_t)(k - COMPACT_RECORDS) * n + s] = t;
     }
 };
 
@@ -125,11 +124,15 @@ template <>
 struct ListsOf<true> {
     using T = CompactLists;
 };
-__device__ __forceinline__ ColumnLists open_lists(ColumnLists*, int* nbr, int n, int s, int) {
+__device__ __forceinline__ ColumnLists open_lists(ColumnLists*, int* nbr, int n, int s, int, unsigned*) {
     return ColumnLists{nbr, n, s};
 }
-__device__ __forceinline__ CompactLists open_lists(CompactLists*, int* nbr, int n, int s, int base) {
-    return CompactLists{nbr, n, s, base, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu};
+__device__ __forceinline__ CompactLists open_lists(CompactLists*, int* nbr, int n, int s, int base,
+                                                   unsigned* stage) {
+    unsigned* mine = stage + COMPACT_STRIDE * threadIdx.x;
+#pragma unroll
+    for (int q = 0; q < COMPACT_RECORDS / 2; q++) mine[q] = 0xFFFFFFFFu;
+    return CompactLists{nbr, n, s, base, mine};
 }
 // The count and the sentinel entries up to a multiple of the passes' chunk
 // (pad divides the buffer's rows: max_nbrs rounded up to LIST_PAD_MAX).
@@ -139,8 +142,10 @@ __device__ __forceinline__ void close_lists(const StepParams& p, const ColumnLis
     for (int k = c_n; k % p.pad != 0; k++) l.nbr[(size_t)k * p.n + l.s] = sentinel_entry(p);
 }
 __device__ __forceinline__ void close_lists(const StepParams& p, const CompactLists& l, int*, int c_n) {
-    p.rec[l.s] = make_uint4((unsigned)c_n | ((unsigned)l.base << 8), l.w0, l.w1, l.w2);
-    for (int k = c_n - COMPACT_INLINE; k > 0 && k % p.pad != 0; k++) l.ovf[(size_t)k * p.n + l.s] = p.n;
+    const unsigned* w = l.stage;
+    p.rec[l.s] = make_uint4((unsigned)c_n | ((unsigned)l.base << 8), w[0], w[1], w[2]);
+    if (c_n > COMPACT_INLINE) p.rec2[l.s] = make_uint4(w[3], w[4], w[5], w[6]);
+    for (int k = c_n - COMPACT_RECORDS; k > 0 && k % p.pad != 0; k++) l.ovf[(size_t)k * p.n + l.s] = p.n;
 }
 
 // One row (dy, dx) of the stencil: the cells z0..z1 of a row are consecutive
@@ -249,7 +254,7 @@ __device__ __forceinline__ void lists_lambda(const StepParams& p, const CellPack
                                              const int* __restrict__ fstart, const float4* __restrict__ solid,
                                              const int* __restrict__ solid_cell, const int* __restrict__ sstart,
                                              int* __restrict__ nbr, int* __restrict__ cnt, float* __restrict__ rho,
-                                             int* status) {
+                                             int* status, unsigned* stage = nullptr) {
     pdl_wait();
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= p.n) return;
@@ -262,7 +267,7 @@ __device__ __forceinline__ void lists_lambda(const StepParams& p, const CellPack
     LambdaAcc a = lambda_init(p);
     int c_n = 0;
     using Lists = typename ListsOf<COMPACT>::T;
-    Lists out = open_lists((Lists*)nullptr, nbr, p.n, s, g.slot0);
+    Lists out = open_lists((Lists*)nullptr, nbr, p.n, s, g.slot0, stage);
     const int slab = g.gx * g.gz;
     // static particles only where the cell's neighbourhood holds some
     const bool solids = p.ns > 0 && p.solid_near && __ldg(&p.solid_near[__ldg(&key_sorted[s])]);
@@ -361,8 +366,9 @@ __global__ void __launch_bounds__(B) k_lists_compact(StepParams p, CellPack cp, 
                                                              const int* __restrict__ sstart,
                                                              int* __restrict__ nbr, int* __restrict__ cnt,
                                                              float* __restrict__ rho, int* status) {
+    __shared__ unsigned stage[COMPACT_STRIDE * B];
     lists_lambda<false, HASHED, FRAME, true>(p, cp, xs, key_sorted, cell_sorted, fstart, solid, solid_cell, sstart,
-                                             nbr, cnt, rho, status);
+                                             nbr, cnt, rho, status, stage);
 }
 
 // Walk a particle's list U entries at a time, calling f(entry, position)
@@ -452,49 +458,66 @@ __device__ __forceinline__ void for_each_entry_p(const StepParams& p, const int*
     }
 }
 
-// Walk a compact list (record r of slot s; col = nbr + s, its overflow
-// rows): gather(slot) loads what f(slot, value) needs of each neighbour.
-// The inline entries go min(U, 6) at a time, all gathers of a chunk in
-// flight together, so with U >= 4 a list of up to 4 neighbours waits for
-// one round trip to DRAM (the record, with the particle's own loads) and
-// one to L2 for the neighbours.  Past the count an inline entry reads the
-// sentinel slot, whose terms are exactly zero; the overflow rows are padded
-// with it to a multiple of U (the list build's pad).
-template <int U, class T, class G, class F>
-__device__ __forceinline__ void walk_compact(const StepParams& p, const uint4& r, const int* __restrict__ col,
-                                             G&& gather, F&& f) {
-    constexpr int V = U < COMPACT_INLINE ? U : COMPACT_INLINE;
-    const int c = (int)(r.x & 0xFFu);
-    const int base = (int)(r.x >> 8);
+// Field j of a record: .y .z .w of the first (M = 6), .x .y .z .w of the second.
+template <int M>
+__device__ __forceinline__ unsigned record_field(const uint4& r, int j) {
+    const int f = j + (M == COMPACT_INLINE ? 1 : 0);
+    return f == 0 ? r.x : (f == 1 ? r.y : (f == 2 ? r.z : r.w));
+}
+
+// The entries [K0, K0 + M) of a compact list from record r, min(U, M)
+// gathers at a time; false once the count is reached.
+template <int U, int M, int K0, class T, class G, class F>
+__device__ __forceinline__ bool walk_record(const StepParams& p, const uint4& r, int c, int base, G&& gather,
+                                            F&& f) {
+    constexpr int V = U < M ? U : M;
     // each chunk decodes its own entries (a short list decodes only those it uses)
 #pragma unroll
-    for (int k = 0; k < COMPACT_INLINE; k += V) {
-        if (k >= c) return;
+    for (int k = 0; k < M; k += V) {
+        if (K0 + k >= c) return false;
         int sl[V];
         T q[V];
 #pragma unroll
         for (int u = 0; u < V; u++)
-            if (k + u < COMPACT_INLINE) {
-                const unsigned w = (k + u) < 2 ? r.y : ((k + u) < 4 ? r.z : r.w);
-                sl[u] = compact_slot(p, base, ((k + u) & 1) ? (w >> 16) : (w & 0xFFFFu));
+            if (k + u < M) {
+                const unsigned x = record_field<M>(r, (k + u) >> 1);
+                sl[u] = compact_slot(p, base, ((k + u) & 1) ? (x >> 16) : (x & 0xFFFFu));
                 q[u] = gather(sl[u]);
             }
 #pragma unroll
         for (int u = 0; u < V; u++)
-            if (k + u < COMPACT_INLINE) f(sl[u], q[u]);
+            if (k + u < M) f(sl[u], q[u]);
     }
-    if (c <= COMPACT_INLINE) return;
+    return K0 + M < c;
+}
+
+// Walk a compact list (record r of slot s, r2 its second record; col =
+// nbr + s, its overflow rows): gather(slot) loads what f(slot, value) needs
+// of each neighbour.  A record's entries go min(U, 6 or 8) at a time, all
+// gathers of a chunk in flight together, so with U >= 4 a list of up to 4
+// neighbours waits for one round trip to DRAM (the record, with the
+// particle's own loads) and one to L2 for the neighbours; the second record
+// is loaded only for a list longer than 6.  Past the count an entry reads the
+// sentinel slot, whose terms are exactly zero; the overflow rows are padded
+// with it to a multiple of U (the list build's pad).
+template <int U, class T, class G, class F>
+__device__ __forceinline__ void walk_compact(const StepParams& p, const uint4& r, const uint4* __restrict__ r2,
+                                             const int* __restrict__ col, G&& gather, F&& f) {
+    const int c = (int)(r.x & 0xFFu);
+    const int base = (int)(r.x >> 8);
+    if (!walk_record<U, COMPACT_INLINE, 0, T>(p, r, c, base, gather, f)) return;
+    if (!walk_record<U, COMPACT_EXT, COMPACT_INLINE, T>(p, __ldg(r2), c, base, gather, f)) return;
     int nx[U];
 #pragma unroll
     for (int u = 0; u < U; u++) nx[u] = __ldg(&col[(size_t)u * p.n]);
-    for (int k = COMPACT_INLINE; k < c; k += U) {
+    for (int k = COMPACT_RECORDS; k < c; k += U) {
         int e[U];
         T q[U];
 #pragma unroll
         for (int u = 0; u < U; u++) e[u] = nx[u];
         if (k + U < c) {
 #pragma unroll
-            for (int u = 0; u < U; u++) nx[u] = __ldg(&col[(size_t)(k - COMPACT_INLINE + U + u) * p.n]);
+            for (int u = 0; u < U; u++) nx[u] = __ldg(&col[(size_t)(k - COMPACT_RECORDS + U + u) * p.n]);
         }
 #pragma unroll
         for (int u = 0; u < U; u++) q[u] = gather(e[u]);
@@ -527,7 +550,7 @@ __global__ void __launch_bounds__(B) k_lambda(StepParams p, float4* __restrict__
         LambdaAcc a = lambda_init(p);
         if (COMPACT) {
             walk_compact<U, float4>(
-                p, __ldg(&p.rec[s]), nbr + s, [&](int t) { return xs[t]; },
+                p, __ldg(&p.rec[s]), p.rec2 + s, nbr + s, [&](int t) { return xs[t]; },
                 [&](int, float4 q) { lambda_accumulate<KAHAN>(p, a, rel_t<false>(self, q, 0, shift_tab), false); });
         } else {
             for_each_entry<U, SOL>(p, nbr + s, cnt, s, xs, solid, [&](int e, float4 q) {
@@ -672,7 +695,7 @@ __global__ void __launch_bounds__(B, ((F & 8) && U == 1) ? 2048 / B : ((U <= 2 &
         DeltaAcc a{0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0};
         if (COMPACT) {
             walk_compact<U, float4>(
-                p, __ldg(&p.rec[s]), nbr + s, [&](int t) { return xs[t]; },
+                p, __ldg(&p.rec[s]), p.rec2 + s, nbr + s, [&](int t) { return xs[t]; },
                 [&](int t, float4 q) { delta_pair<false, false>(p, a, self, t, q, shift_tab); });
         } else {
             for_each_entry<U, SOL, LIST_PAD_MAX>(p, nbr + s, cnt, s, xs, solid, [&](int e, float4 q) {
@@ -747,7 +770,7 @@ __global__ void __launch_bounds__(B) k_xsph(StepParams p, CellPack cp, const flo
     float ax = 0.0f, ay = 0.0f, az = 0.0f;
     if (COMPACT && p.c_xsph != 0.0f) {
         walk_compact<U, PosVel>(
-            p, __ldg(&p.rec[s]), col, [&](int t) { return PosVel{xs[t], v_in[t]}; },
+            p, __ldg(&p.rec[s]), p.rec2 + s, col, [&](int t) { return PosVel{xs[t], v_in[t]}; },
             [&](int t, const PosVel& q) { xsph_pair<false>(p, self, vi, q.x, q.v, t, shift_tab, ax, ay, az); });
     } else if (p.c_xsph != 0.0f) {
         const int c = cnt[s];
