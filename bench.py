@@ -382,11 +382,14 @@ def run_reference(args, world, rank):
 
 def time_steps(sim, dt, steps, flush, ext, launches=None):
     """CUDA-event milliseconds of each of `steps` steps (L2 flushed before
-    each); `launches`, a list, receives the library's kernel launches per step."""
+    each); `launches`, a list, receives the library's kernel launches per step.
+    The steps run inside the NVTX range "timed" (a profiler can capture them
+    alone: ncu --nvtx --nvtx-include timed/)."""
     import torch
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
     torch.cuda.synchronize()
+    torch.cuda.nvtx.range_push("timed")
     for k in range(steps):
         with torch.cuda.stream(ext):
             flush.zero_()
@@ -396,6 +399,7 @@ def time_steps(sim, dt, steps, flush, ext, launches=None):
             launches.append(sim.launches_per_step())
         with torch.cuda.stream(ext):
             ends[k].record(ext)
+    torch.cuda.nvtx.range_pop()
     torch.cuda.synchronize()
     return [s.elapsed_time(e) for s, e in zip(starts, ends)]
 
@@ -531,19 +535,25 @@ def run_ours(args, world, rank, local):
             s.step(dt)
 
     t_plain = wall_per_step(step_each, k_wall, flush)
-    # the other batched arms: fp32; mixed with cell-relative iterations; the
-    # headline's representation with the on-chip solve
+    # the other batched arms, from the same state: fp32; mixed with
+    # cell-relative iterations; the headline's representation with the
+    # on-chip solve
     arms = {}
     b_fp32 = batch_context(scs, 0, dt, 2)
+    b_fp32.upload(xs0, vs0)
+    b_fp32.step(dt, 2)
     arms["batched_fp32"] = {"wall_ms_per_step": wall_per_step(lambda: b_fp32.step(dt), k_wall, flush) * 1e3,
                             "tuning": b_fp32.tuned["tuning"]}
     b_fp32.close()
     b_rel = batch_context(scs, PRECISION_MIXED, dt, 2)
+    b_rel.upload(xs0, vs0)
+    b_rel.step(dt, 2)
     arms["batched_mixed_cell_relative"] = {
         "wall_ms_per_step": wall_per_step(lambda: b_rel.step(dt), k_wall, flush) * 1e3,
         "tuning": b_rel.tuned["tuning"]}
     try:
         b.set_solver(True)
+        b.upload(xs0, vs0)
         b.step(dt, 2)
         arms["batched_mixed_scene_onchip"] = {"wall_ms_per_step": wall_per_step(lambda: b.step(dt), k_wall,
                                                                                 flush) * 1e3,
@@ -554,6 +564,29 @@ def run_ours(args, world, rank, local):
     for a in arms.values():
         if "wall_ms_per_step" in a:
             a["over_plain"] = t_plain * 1e3 / a["wall_ms_per_step"]
+    # the same two arms along the scenes' 100-step run: the dam breaks
+    # compress, the neighbour lists grow (about 4 entries a particle at the
+    # start, 9 by step 100) and both arms slow down
+    rollout = []
+    if not args.no_extras:
+        x_init = np.concatenate([sc.x for sc in scs])
+        b.upload(x_init, np.zeros_like(x_init))
+        done = 0
+        for target in (5, 50, 100):
+            b.step(dt, target - done)
+            done = target
+            xt, vt = b.download(x=True, v=True)[:2]
+            for k, s in enumerate(sims):
+                s.upload(xt[off[k]:off[k + 1]], vt[off[k]:off[k + 1]])
+                s.step(dt, 2)
+            b.upload(xt, vt)
+            b.step(dt, 2)
+            torch.cuda.synchronize()
+            tb = wall_per_step(lambda: b.step(dt), k_wall, flush)
+            tp = wall_per_step(step_each, k_wall, flush)
+            b.upload(xt, vt)
+            rollout.append({"step": target, "batched_ms_per_step": tb * 1e3, "plain_ms_per_step": tp * 1e3,
+                            "batched_over_plain": tp / tb})
     plain = {
         "value": n_local * ITERS / t_plain, "ms_per_step": t_plain * 1e3,
         "contexts": len(sims), "launches_per_step": sum(s.launches_per_step() for s in sims),
@@ -562,6 +595,7 @@ def run_ours(args, world, rank, local):
         "batched_mixed_wall_ms_per_step": t_batched * 1e3,
         "batched_mixed_over_plain": t_plain / t_batched,
         "other_batched_arms": arms,
+        "rollout": rollout,
         "timing": "wall clock per step of all scenes, device synchronised on both sides, L2 flushed before",
     }
 

@@ -748,15 +748,14 @@ __device__ __forceinline__ void xsph_pair(const StepParams& p, const float4& sel
 // With xs_next, also the next step's prediction from the state it commits
 // (into xs_next, key, rank, count, cellk; count is zero here, the step's
 // scan having consumed it).
-template <int F, int U, int B>
-__global__ void __launch_bounds__(B) k_xsph(StepParams p, CellPack cp, const float4* __restrict__ xs,
-                                            const float4* __restrict__ v_in,
-                                            const int* __restrict__ nbr, const int* __restrict__ cnt,
-                                            const int* __restrict__ key_sorted,
+template <int F, int U>
+__device__ __forceinline__ void xsph_commit(const StepParams& p, const CellPack& cp, const float4* __restrict__ xs,
+                                            const float4* __restrict__ v_in, const int* __restrict__ nbr,
+                                            const int* __restrict__ cnt, const int* __restrict__ key_sorted,
                                             float4* __restrict__ x_out, float4* __restrict__ v_out,
                                             float4* __restrict__ xs_next, int* __restrict__ key,
-                                            int* __restrict__ rank, int* __restrict__ count,
-                                            int* __restrict__ cellk, int* __restrict__ tile_count) {
+                                            int* __restrict__ rank, int* __restrict__ count, int* __restrict__ cellk,
+                                            int* __restrict__ tile_count) {
     constexpr bool MIXED = (F & 1) != 0, SOL = (F & 2) != 0, COMPACT = (F & 8) != 0;
     static_assert(!COMPACT || (!MIXED && !SOL), "compact lists");
     pdl_wait();
@@ -816,6 +815,33 @@ __global__ void __launch_bounds__(B) k_xsph(StepParams p, CellPack cp, const flo
         else
             predict_one<false>(p, cp, g, xc, vc, s, xs_next, key, rank, count, cellk, tile_count);
     }
+}
+
+template <int F, int U, int B>
+__global__ void __launch_bounds__(B) k_xsph(StepParams p, CellPack cp, const float4* __restrict__ xs,
+                                            const float4* __restrict__ v_in,
+                                            const int* __restrict__ nbr, const int* __restrict__ cnt,
+                                            const int* __restrict__ key_sorted,
+                                            float4* __restrict__ x_out, float4* __restrict__ v_out,
+                                            float4* __restrict__ xs_next, int* __restrict__ key,
+                                            int* __restrict__ rank, int* __restrict__ count,
+                                            int* __restrict__ cellk, int* __restrict__ tile_count) {
+    xsph_commit<F, U>(p, cp, xs, v_in, nbr, cnt, key_sorted, x_out, v_out, xs_next, key, rank, count, cellk,
+                      tile_count);
+}
+
+// Compact lists (F = 8) with one gather in flight: registers capped at 32
+// for every warp slot of the SM (64 bytes spilled; config 3 XSPH 0.175 ->
+// 0.141 ms at step 5, 0.239 -> 0.219 ms at step 100 against the best
+// uncapped shape).  More gathers in flight keep k_xsph.
+template <int F, int U, int B>
+__global__ void __launch_bounds__(B, 2048 / B) k_xsph_compact(
+    StepParams p, CellPack cp, const float4* __restrict__ xs, const float4* __restrict__ v_in,
+    const int* __restrict__ nbr, const int* __restrict__ cnt, const int* __restrict__ key_sorted,
+    float4* __restrict__ x_out, float4* __restrict__ v_out, float4* __restrict__ xs_next, int* __restrict__ key,
+    int* __restrict__ rank, int* __restrict__ count, int* __restrict__ cellk, int* __restrict__ tile_count) {
+    xsph_commit<F, U>(p, cp, xs, v_in, nbr, cnt, key_sorted, x_out, v_out, xs_next, key, rank, count, cellk,
+                      tile_count);
 }
 
 // Absolute positions (float3 triples) in the caller's id order.
@@ -1331,7 +1357,16 @@ void launch_xsph(bool mixed, const Tuning& tu, const StepParams& p, const CellPa
     Tuning tx = tu;  // the XSPH pass has its own gathers in flight
     tx.unroll = tu.xsph_unroll;
     const int f = ((mixed && !p.frame) ? 1 : 0) | (p.ns > 0 ? 2 : 0);
-    if (p.rec)
+    if (p.rec && tx.unroll <= 1) {
+        const int B = tx.block <= 64 ? 64 : (tx.block <= 128 ? 128 : 256);
+#define LGB_XC(BB)                                                                                     \
+    launch_k(k_xsph_compact<8, 1, BB>, blocks_for(p.n, BB), BB, st, pdl_enabled(), p, cp, xs, v_in, nbr, cnt, \
+             key_sorted, x_out, v_out, xs_next, key, rank, count, cellk, tile_count)
+        if (B == 64) LGB_XC(64);
+        else if (B == 128) LGB_XC(128);
+        else LGB_XC(256);
+#undef LGB_XC
+    } else if (p.rec)
         TUNE_CASE(k_xsph, 8, tx, p.n, st, p, cp, xs, v_in, nbr, cnt, key_sorted, x_out, v_out, xs_next, key, rank,
                   count, cellk, tile_count);
     else
