@@ -183,23 +183,25 @@ __device__ __forceinline__ void walk_row(const StepParams& p, const float4& self
     }
 }
 
-// The candidates [t_begin, t_end) of one row, gathered 4 at a time (the
+// The candidates [t_begin, t_end) of one row, gathered W at a time (the
 // loads of a chunk are in flight together; the tests run in slot order, so
-// the list is the one walk_row builds).  b1, b2: the row's cell bounds, read
+// the list is the one walk_row builds).  W = 4; the compact list build takes
+// 2, which fits it in 55-56 registers (9 blocks of 128 per SM; config 3
+// lists 0.522 -> 0.504 ms at step 50 of the run).  b1, b2: the row's cell bounds, read
 // in mixed precision only (the entry's dz code and the cell shift; fp32
 // entries carry dz = 0, which no fp32 pass reads).
-template <bool MIXED, bool SOLID, bool KAHAN, class L>
+template <bool MIXED, bool SOLID, bool KAHAN, class L, int W = 4>
 __device__ __forceinline__ void walk_range(const StepParams& p, const float4& self, int s,
                                            const float4* __restrict__ pos, int t_begin, int t_end, int b1, int b2,
                                            int dz0, int dx, int dy, LambdaAcc& a, int& c_n, L& out) {
     const float sx = -(float)dx * p.cell, sy = -(float)dy * p.cell;
-    for (int t0 = t_begin; t0 < t_end; t0 += 4) {
-        float4 q[4];
+    for (int t0 = t_begin; t0 < t_end; t0 += W) {
+        float4 q[W];
 #pragma unroll
-        for (int u = 0; u < 4; u++)
+        for (int u = 0; u < W; u++)
             if (t0 + u < t_end) q[u] = SOLID ? __ldg(&pos[t0 + u]) : pos[t0 + u];
 #pragma unroll
-        for (int u = 0; u < 4; u++) {
+        for (int u = 0; u < W; u++) {
             const int t = t0 + u;
             if (t >= t_end || (!SOLID && t == s)) continue;
             const int dz = MIXED ? dz0 + (t >= b1) + (t >= b2) : 0;
@@ -296,8 +298,8 @@ __device__ __forceinline__ void lists_lambda(const StepParams& p, const CellPack
             for (int r = 0; r < 3; r++) {
                 const int xx = c.x + r - 1;
                 if (xx < 0 || xx >= g.gx) continue;
-                walk_range<MIXED, false, KAHAN>(p, self, s, xs, b0[r], b3[r], b1[r], b2[r], z0 - c.z, r - 1, dy,
-                                                a, c_n, out);
+                walk_range<MIXED, false, KAHAN, Lists, COMPACT ? 2 : 4>(p, self, s, xs, b0[r], b3[r], b1[r], b2[r],
+                                                                     z0 - c.z, r - 1, dy, a, c_n, out);
                 if (solids)
                     walk_row<MIXED, true, KAHAN>(p, self, s, solid, sstart, g.off + y * slab + xx * g.gz, c.z, g.gz,
                                                  r - 1, dy, a, c_n, out);
