@@ -376,9 +376,9 @@ LUSTRINE_API int lustrine_pbf_download_positions_f64(lustrine_pbf* s, double* x)
 /* Neighbour lists of the last step in the caller's ids (solids n_fluid + k):
  * count[n_fluid], idx[n_fluid * cap] row-major.  Synchronises. */
 LUSTRINE_API int lustrine_pbf_neighbors(lustrine_pbf* s, int* count, int* idx, int cap);
-/* The form the last step's lists took: LUSTRINE_LISTS_COMPACT or
- * LUSTRINE_LISTS_COLUMN (also before the first step and for the on-chip
- * solve, whose lists are column lists). */
+/* The form the last step's lists took: LUSTRINE_LISTS_COMPACT,
+ * LUSTRINE_LISTS_COMPACT_WIDE or LUSTRINE_LISTS_COLUMN (also before the
+ * first step and for the on-chip solve, whose lists are column lists). */
 LUSTRINE_API int lustrine_pbf_list_format(const lustrine_pbf* s, int* format);
 /* FP64 reductions on the device: [0] mass, [1..3] momentum, [4] kinetic
  * energy, [5..7] centre of mass, [8] max |rho / rho0 - 1| of the last lambda
@@ -444,14 +444,17 @@ LUSTRINE_API int lustrine_pbf_profile_step(lustrine_pbf* s, float dt, double* st
  * per thread of the lambda and delta-p passes, whose lists are walked
  * together (0: 1; with 2, unroll is at most 2); solver and solver_threads:
  * batches only, LUSTRINE_SOLVER_* and the on-chip solve's threads per CTA
- * (512 or 1024; 0: unchanged); list_format: LUSTRINE_LISTS_* (compact lists
- * apply in PBF mode, fp32 or LUSTRINE_PRECISION_MIXED_SCENE, with
- * max_neighbors <= 255, no static particles, scenes of at most 65,535 and
- * contexts of fewer than 2^24 fluid particles, and one particle per thread;
- * elsewhere the step keeps column lists whatever list_format says). */
+ * (512 or 1024; 0: unchanged); list_format: LUSTRINE_LISTS_COLUMN or
+ * LUSTRINE_LISTS_COMPACT (compact lists apply in PBF mode, fp32 or
+ * LUSTRINE_PRECISION_MIXED_SCENE, with max_neighbors <= 255, no static
+ * particles and one particle per thread: 16-bit entries for scenes of at most
+ * 65,535 in contexts of fewer than 2^24 fluid particles, wide records
+ * otherwise; elsewhere the step keeps column lists whatever list_format
+ * says). */
 enum {
-    LUSTRINE_LISTS_COLUMN = 0,  /* count + column-major 32-bit entries */
-    LUSTRINE_LISTS_COMPACT = 1  /* one 16-byte record per particle: count, 6 entries as 16-bit scene offsets */
+    LUSTRINE_LISTS_COLUMN = 0,       /* count + column-major 32-bit entries */
+    LUSTRINE_LISTS_COMPACT = 1,      /* 16-byte records: count, scene's first slot, 6 (+8) 16-bit offsets */
+    LUSTRINE_LISTS_COMPACT_WIDE = 2  /* reported only: 16-byte records, count and 3 (+4) 32-bit slots */
 };
 typedef struct lustrine_pbf_tuning {
     int block;

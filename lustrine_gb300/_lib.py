@@ -80,7 +80,7 @@ class PbfParams(C.Structure):
 
 
 GRID_AUTO, GRID_DENSE, GRID_HASHED = 0, 1, 2
-LISTS_COLUMN, LISTS_COMPACT = 0, 1
+LISTS_COLUMN, LISTS_COMPACT, LISTS_COMPACT_WIDE = 0, 1, 2
 
 
 class PbfTuning(C.Structure):

@@ -11,13 +11,13 @@
 //   neighbour lists: nbr[max_nbrs * n], column-major (entry k of slot i at
 //     k * n + i) so a warp's loads of entry k are one coalesced line;
 //     fluid neighbours are slot numbers >= 0, solids are -1 - solid slot.
-//   compact lists (PBF mode, scenes of at most COMPACT_MAX_SCENE particles,
-//     no static particles, no cell codes): rec uint4[n], one 16-byte record
-//     per slot with the count, the scene's first slot and the first
-//     COMPACT_INLINE neighbours as 16-bit scene-local slots; rec2 uint4[n],
-//     the next COMPACT_EXT (written for lists longer than COMPACT_INLINE);
-//     entries from COMPACT_RECORDS on in the column-major rows of nbr as
-//     plain slots.
+//   compact lists (PBF mode, no static particles, no cell codes): rec
+//     uint4[n], one 16-byte record per slot; rec2 uint4[n], a second record
+//     for longer lists; the entries past both in the column-major rows of nbr
+//     as plain slots.  Scenes of at most COMPACT_MAX_SCENE particles: the
+//     count, the scene's first slot and 6 + 8 neighbours as 16-bit
+//     scene-local slots; larger scenes (wide records): the count and 3 + 4
+//     neighbours as 32-bit slots.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -52,6 +52,12 @@ struct SceneInfo {
 constexpr int COMPACT_INLINE = 6;
 constexpr int COMPACT_EXT = 8;
 constexpr int COMPACT_RECORDS = COMPACT_INLINE + COMPACT_EXT;
+// Wide records (StepParams::wide): record.x = count; .y, .z, .w = entries
+// 0-2 as slots (the sentinel slot n past the count); the second record,
+// entries 3-6.
+constexpr int WIDE_INLINE = 3;
+constexpr int WIDE_EXT = 4;
+constexpr int WIDE_RECORDS = WIDE_INLINE + WIDE_EXT;
 constexpr unsigned COMPACT_SENTINEL = 0xFFFFu;
 constexpr int COMPACT_MAX_SCENE = 65535;   // scene-local offsets 0..65534
 constexpr int COMPACT_MAX_N = 1 << 24;     // first slot in 24 bits
@@ -97,6 +103,7 @@ struct StepParams {
     int frame;            // mixed storage, iterations in the scene frame (LUSTRINE_PRECISION_MIXED_SCENE)
     uint4* rec;           // compact neighbour lists of this step (nullptr: column lists with counts)
     uint4* rec2;          // their second records
+    int wide;             // compact lists in wide records (32-bit slots)
 };
 
 // Sand mode: simulate_sand's per-call inputs (Simulate.cpp:156-209).

@@ -219,7 +219,7 @@ void lustrine_pbf::free_buffers() {
     nbr = cnt = status = qcount = iota = slot_of = solid_id = d_scene_of = d_solid_scene_of = nullptr;
     cellk = cell_sorted = solid_cell = nullptr;
     rec = rec2 = nullptr;
-    lists_compact = false;
+    lists_format = LUSTRINE_LISTS_COLUMN;
     att[0] = att[1] = nullptr;
     solid_near = nullptr;
     lam = lam_by_id = rho = out3 = nullptr;
@@ -242,21 +242,26 @@ int lgb_write_sentinel(lustrine_pbf* s) {
     return LUSTRINE_OK;
 }
 
-// Whether the context's steps can use compact neighbour lists: PBF mode in
-// fp32 or the scene frame (no cell codes in the entries), lists of at most
-// COMPACT_MAX_NBRS entries, fewer than COMPACT_MAX_N fluid slots and scenes
-// of at most COMPACT_MAX_SCENE (one scene: the capacity).  A step uses them
-// when the tuning asks for them and the context holds no static particles.
-static bool compact_capable(const lustrine_pbf* s) {
-    if (s->prm.mode != LUSTRINE_MODE_PBF || (s->mixed() && !s->sp.frame)) return false;
-    if (s->sp.max_nbrs > COMPACT_MAX_NBRS || s->cap >= COMPACT_MAX_N) return false;
+// The compact neighbour lists the context's steps can use: PBF mode in fp32
+// or the scene frame (no cell codes in the entries) and lists of at most
+// COMPACT_MAX_NBRS entries; 16-bit entries (LUSTRINE_LISTS_COMPACT) for
+// fewer than COMPACT_MAX_N fluid slots in scenes of at most
+// COMPACT_MAX_SCENE (one scene: the capacity), wide records
+// (LUSTRINE_LISTS_COMPACT_WIDE) otherwise; LUSTRINE_LISTS_COLUMN when none.
+// A step uses them when the tuning asks for them, with one particle per
+// thread, and the context holds no static particles.
+static int compact_capable(const lustrine_pbf* s) {
+    if (s->prm.mode != LUSTRINE_MODE_PBF || (s->mixed() && !s->sp.frame)) return LUSTRINE_LISTS_COLUMN;
+    if (s->sp.max_nbrs > COMPACT_MAX_NBRS) return LUSTRINE_LISTS_COLUMN;
     int largest = s->cap;
     if (s->is_batch()) largest = *std::max_element(s->b_nfluid.begin(), s->b_nfluid.end());
-    return largest <= COMPACT_MAX_SCENE;
+    return (largest <= COMPACT_MAX_SCENE && s->cap < COMPACT_MAX_N) ? LUSTRINE_LISTS_COMPACT
+                                                                     : LUSTRINE_LISTS_COMPACT_WIDE;
 }
 
-static bool compact_now(const lustrine_pbf* s) {
-    return s->rec && s->tune.lists && s->tune.ppt == 1 && s->ns == 0 && compact_capable(s);
+static int compact_now(const lustrine_pbf* s) {
+    if (!s->rec || !s->tune.lists || s->tune.ppt != 1 || s->ns != 0) return LUSTRINE_LISTS_COLUMN;
+    return compact_capable(s);
 }
 
 // Device buffers for s->cap fluid particles (s->n of them active).
@@ -288,7 +293,7 @@ static int ctx_alloc(lustrine_pbf* s) {
     const size_t list_rows = (size_t)((s->sp.max_nbrs + LIST_PAD_MAX - 1) / LIST_PAD_MAX * LIST_PAD_MAX);
     rc = rc ? rc : dalloc(&s->nbr, list_rows * (size_t)n);
     rc = rc ? rc : dalloc(&s->cnt, n);
-    if (compact_capable(s)) {
+    if (compact_capable(s) != LUSTRINE_LISTS_COLUMN) {
         rc = rc ? rc : dalloc(&s->rec, n);
         rc = rc ? rc : dalloc(&s->rec2, n);
     }
@@ -904,7 +909,7 @@ static int enqueue_step(lustrine_pbf* s, cudaStream_t st, StageMarks* mk = nullp
     set_pdl(s->use_pdl);
     if (s->sand_mode()) {
         k = enqueue_sand_step(s, st, mk);
-        s->lists_compact = false;
+        s->lists_format = LUSTRINE_LISTS_COLUMN;
         set_pdl(false);
         return k;
     }
@@ -944,7 +949,7 @@ static int enqueue_step(lustrine_pbf* s, cudaStream_t st, StageMarks* mk = nullp
                          s->lam_by_id, st);
         if (mk) mk->mark(LUSTRINE_STAGE_DELTA, st);
         k += 3;
-        s->lists_compact = false;
+        s->lists_format = LUSTRINE_LISTS_COLUMN;
     } else if (s->onchip && s->num_bins > 0) {
         // the batch's lists, iterations, XSPH and commit in one persistent
         // launch of clusters (the lambdas end where the per-stage path leaves them)
@@ -974,15 +979,16 @@ static int enqueue_step(lustrine_pbf* s, cudaStream_t st, StageMarks* mk = nullp
         launch_scene_solve(mixed, s->onchip_threads, p, s->cp, sa,
                            s->onchip_threads == 512 ? s->onchip_clusters512 : s->onchip_clusters, st);
         k += 1;
-        s->lists_compact = false;
+        s->lists_format = LUSTRINE_LISTS_COLUMN;
         if (mk) mk->mark(LUSTRINE_STAGE_SOLVE, st);
     } else {
         // iteration 0's lambda pass builds the neighbour lists as it goes
         // (compact records where the step allows them)
         StepParams pl = p;
-        pl.rec = compact_now(s) ? s->rec : nullptr;
+        s->lists_format = compact_now(s);
+        pl.rec = s->lists_format != LUSTRINE_LISTS_COLUMN ? s->rec : nullptr;
         pl.rec2 = pl.rec ? s->rec2 : nullptr;
-        s->lists_compact = pl.rec != nullptr;
+        pl.wide = s->lists_format == LUSTRINE_LISTS_COMPACT_WIDE;
         float4* a = s->xs[o];
         float4* b = s->xs_alt;
         const int iters = s->prm.iterations;
@@ -1292,7 +1298,7 @@ extern "C" int lustrine_pbf_autotune(lustrine_pbf* s, float dt, int steps, lustr
     // the iteration kernels' shape first (block x gathers in flight x
     // particles per thread x list format, compact first where it can
     // apply), then the list build's block size
-    const int formats = s->rec && s->ns == 0 ? 2 : 1;
+    const int formats = s->rec && s->ns == 0 && compact_capable(s) != LUSTRINE_LISTS_COLUMN ? 2 : 1;
     for (int lf = 0; lf < formats && !rc; lf++)
         for (int bi = 0; bi < 3 && !rc; bi++)
             for (int ui = 0; ui < 4 && !rc; ui++)
@@ -1528,8 +1534,9 @@ extern "C" int lustrine_pbf_neighbors(lustrine_pbf* s, int* count, int* idx, int
     // Lists refer to the sorted slots of the state the step started from:
     // the committed side's id array maps fluid slots; solid slots map back
     // through the solid sort permutation.
-    std::vector<uint4> rec(s->lists_compact ? (size_t)n : 0), rec2(rec.size());
-    if (s->lists_compact) {
+    const bool compact = s->lists_format != LUSTRINE_LISTS_COLUMN;
+    std::vector<uint4> rec(compact ? (size_t)n : 0), rec2(rec.size());
+    if (compact) {
         CK(cudaMemcpyAsync(rec.data(), s->rec, (size_t)n * sizeof(uint4), cudaMemcpyDeviceToHost, s->stream));
         CK(cudaMemcpyAsync(rec2.data(), s->rec2, (size_t)n * sizeof(uint4), cudaMemcpyDeviceToHost, s->stream));
     } else
@@ -1538,21 +1545,23 @@ extern "C" int lustrine_pbf_neighbors(lustrine_pbf* s, int* count, int* idx, int
     CK(cudaMemcpyAsync(nbr.data(), s->nbr, (size_t)maxn * n * sizeof(int), cudaMemcpyDeviceToHost, s->stream));
     if (s->ns) CK(cudaMemcpyAsync(sid.data(), s->solid_id, (size_t)s->ns * sizeof(int), cudaMemcpyDeviceToHost, s->stream));
     CK(cudaStreamSynchronize(s->stream));
-    if (s->lists_compact) {
-        // compact records into the column form: count, the records'
-        // entries as the scene's first slot + offset (the second record is
-        // written only for lists longer than its first), the rest from the
-        // overflow rows
+    if (compact) {
+        // compact records into the column form: count, the records' entries
+        // (16-bit: the scene's first slot + offset; wide: the slot; the
+        // second record is written only for lists longer than its first),
+        // the rest from the overflow rows
+        const bool wide = s->lists_format == LUSTRINE_LISTS_COMPACT_WIDE;
+        const int R = wide ? WIDE_RECORDS : COMPACT_RECORDS;
         std::vector<int> col((size_t)maxn * n);
         for (int k = 0; k < n; k++) {
             const uint4 r = rec[(size_t)k], x = rec2[(size_t)k];
-            const int c = (int)(r.x & 0xFFu), base = (int)(r.x >> 8);
-            const unsigned w[COMPACT_RECORDS / 2] = {r.y, r.z, r.w, x.x, x.y, x.z, x.w};
+            const unsigned w[7] = {r.y, r.z, r.w, x.x, x.y, x.z, x.w};
+            const int c = wide ? (int)r.x : (int)(r.x & 0xFFu), base = wide ? 0 : (int)(r.x >> 8);
             cnt[(size_t)k] = c;
             for (int e = 0; e < c; e++)
-                col[(size_t)e * n + k] = e < COMPACT_RECORDS
-                                             ? base + (int)((w[e >> 1] >> ((e & 1) * 16)) & 0xFFFFu)
-                                             : nbr[(size_t)(e - COMPACT_RECORDS) * n + k];
+                col[(size_t)e * n + k] = e >= R ? nbr[(size_t)(e - R) * n + k]
+                                         : wide ? (int)w[e]
+                                                : base + (int)((w[e >> 1] >> ((e & 1) * 16)) & 0xFFFFu);
         }
         nbr.swap(col);
     }
@@ -1582,7 +1591,7 @@ extern "C" int lustrine_pbf_neighbors(lustrine_pbf* s, int* count, int* idx, int
 
 extern "C" int lustrine_pbf_list_format(const lustrine_pbf* s, int* format) {
     if (!s || !format) return LUSTRINE_ERR_ARGS;
-    *format = s->lists_compact ? LUSTRINE_LISTS_COMPACT : LUSTRINE_LISTS_COLUMN;
+    *format = s->lists_format;
     return LUSTRINE_OK;
 }
 

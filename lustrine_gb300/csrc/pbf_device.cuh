@@ -299,7 +299,11 @@ __device__ __forceinline__ LambdaAcc lambda_init(const StepParams&) {
     return LambdaAcc{0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
 }
 
-// KAHAN: compensated density sum (both mixed representations)
+// KAHAN: compensated density sum (both mixed representations).  A term of
+// exactly zero (a pair at r >= h, the sentinel entry that pads a chunk)
+// leaves the compensated sum as it is: a compensation step with a zero
+// addend would fold the carried error into the sum, so the result would
+// depend on how many padding entries a walk visits.
 template <bool KAHAN>
 __device__ __forceinline__ void lambda_accumulate(const StepParams& p, LambdaAcc& a, float3 d,
                                                   bool solid) {
@@ -309,8 +313,10 @@ __device__ __forceinline__ void lambda_accumulate(const StepParams& p, LambdaAcc
     if (KAHAN) {
         const float y = __fsub_rn(w, a.comp);
         const float t = __fadd_rn(a.wsum, y);
-        a.comp = __fsub_rn(__fsub_rn(t, a.wsum), y);
-        a.wsum = t;
+        if (w != 0.0f) {
+            a.comp = __fsub_rn(__fsub_rn(t, a.wsum), y);
+            a.wsum = t;
+        }
     } else {
         a.wsum = __fadd_rn(a.wsum, w);
     }

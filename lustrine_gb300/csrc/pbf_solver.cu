@@ -96,43 +96,67 @@ struct ColumnLists {
     }
 };
 
-// Compact lists: the first COMPACT_RECORDS entries as 16-bit offsets from
-// the scene's first slot, staged in the thread's COMPACT_STRIDE words of
-// shared memory (filled with COMPACT_SENTINEL first; a stride of 9 words
-// keeps a warp's stores and loads free of bank conflicts) until the records
-// are written; the rest as plain slots in the column rows of nbr from row 0.
-// No cell codes and no solids (the step uses compact lists only without
-// either).
+// Entries a compact list keeps in its two records: inline (first record),
+// second record, both.
+template <bool WIDE>
+struct RecordFormat {
+    static constexpr int INLINE = WIDE ? WIDE_INLINE : COMPACT_INLINE;
+    static constexpr int EXT = WIDE ? WIDE_EXT : COMPACT_EXT;
+    static constexpr int RECORDS = INLINE + EXT;
+};
+
+// Compact lists: the records' entries (16-bit offsets from the scene's
+// first slot, or 32-bit slots in wide records) staged in the thread's
+// COMPACT_STRIDE words of shared memory (filled with the sentinel first; a
+// stride of 9 words keeps a warp's stores and loads free of bank conflicts)
+// until the records are written; the rest as plain slots in the column rows
+// of nbr from row 0.  No cell codes and no solids (the step uses compact
+// lists only without either).
 constexpr int COMPACT_STRIDE = 9;
+template <bool WIDE>
 struct CompactLists {
     int* ovf;
     int n, s, base;
     unsigned* stage;  // this thread's words
     __device__ __forceinline__ void put(int k, int t, int, int, int, bool) {
-        if (k < COMPACT_RECORDS)
-            reinterpret_cast<unsigned short*>(stage)[k] = (unsigned short)(t - base);
+        constexpr int R = RecordFormat<WIDE>::RECORDS;
+        if (k >= R)
+            ovf[(size_t)(k - R) * n + s] = t;
+        else if (WIDE)
+            stage[k] = (unsigned)t;
         else
-            ovf[(size_t)(k - COMPACT_RECORDS) * n + s] = t;
+            reinterpret_cast<unsigned short*>(stage)[k] = (unsigned short)(t - base);
     }
 };
 
-template <bool COMPACT>
+// 0: column lists; 1: compact; 2: compact in wide records
+template <int FORMAT>
 struct ListsOf {
     using T = ColumnLists;
 };
 template <>
-struct ListsOf<true> {
-    using T = CompactLists;
+struct ListsOf<1> {
+    using T = CompactLists<false>;
+};
+template <>
+struct ListsOf<2> {
+    using T = CompactLists<true>;
 };
 __device__ __forceinline__ ColumnLists open_lists(ColumnLists*, int* nbr, int n, int s, int, unsigned*) {
     return ColumnLists{nbr, n, s};
 }
-__device__ __forceinline__ CompactLists open_lists(CompactLists*, int* nbr, int n, int s, int base,
-                                                   unsigned* stage) {
+template <bool WIDE>
+__device__ __forceinline__ CompactLists<WIDE> open_lists(CompactLists<WIDE>*, int* nbr, int n, int s, int base,
+                                                         unsigned* stage) {
     unsigned* mine = stage + COMPACT_STRIDE * threadIdx.x;
+    if (WIDE) {
 #pragma unroll
-    for (int q = 0; q < COMPACT_RECORDS / 2; q++) mine[q] = 0xFFFFFFFFu;
-    return CompactLists{nbr, n, s, base, mine};
+        for (int q = 0; q < WIDE_RECORDS; q++) mine[q] = (unsigned)n;
+    } else {
+#pragma unroll
+        for (int q = 0; q < COMPACT_RECORDS / 2; q++) mine[q] = 0xFFFFFFFFu;
+    }
+    return CompactLists<WIDE>{nbr, n, s, base, mine};
 }
 // The count and the sentinel entries up to a multiple of the passes' chunk
 // (pad divides the buffer's rows: max_nbrs rounded up to LIST_PAD_MAX).
@@ -141,11 +165,18 @@ __device__ __forceinline__ void close_lists(const StepParams& p, const ColumnLis
     cnt[l.s] = c_n;
     for (int k = c_n; k % p.pad != 0; k++) l.nbr[(size_t)k * p.n + l.s] = sentinel_entry(p);
 }
-__device__ __forceinline__ void close_lists(const StepParams& p, const CompactLists& l, int*, int c_n) {
+template <bool WIDE>
+__device__ __forceinline__ void close_lists(const StepParams& p, const CompactLists<WIDE>& l, int*, int c_n) {
+    using RF = RecordFormat<WIDE>;
     const unsigned* w = l.stage;
-    p.rec[l.s] = make_uint4((unsigned)c_n | ((unsigned)l.base << 8), w[0], w[1], w[2]);
-    if (c_n > COMPACT_INLINE) p.rec2[l.s] = make_uint4(w[3], w[4], w[5], w[6]);
-    for (int k = c_n - COMPACT_RECORDS; k > 0 && k % p.pad != 0; k++) l.ovf[(size_t)k * p.n + l.s] = p.n;
+    if (WIDE) {
+        p.rec[l.s] = make_uint4((unsigned)c_n, w[0], w[1], w[2]);
+        if (c_n > RF::INLINE) p.rec2[l.s] = make_uint4(w[3], w[4], w[5], w[6]);
+    } else {
+        p.rec[l.s] = make_uint4((unsigned)c_n | ((unsigned)l.base << 8), w[0], w[1], w[2]);
+        if (c_n > RF::INLINE) p.rec2[l.s] = make_uint4(w[3], w[4], w[5], w[6]);
+    }
+    for (int k = c_n - RF::RECORDS; k > 0 && k % p.pad != 0; k++) l.ovf[(size_t)k * p.n + l.s] = p.n;
 }
 
 // One row (dy, dx) of the stencil: the cells z0..z1 of a row are consecutive
@@ -249,8 +280,9 @@ __device__ __forceinline__ void walk_hashed_cell(const StepParams& p, const floa
 // FRAME: mixed storage with the iterations in the scene frame (positions
 // relative to the box corner, compensated density sums; the walk's cell is
 // the step's key, which rounding of the frame position could move).
-// COMPACT: the lists go to p.rec (no cell codes, no static particles).
-template <bool MIXED, bool HASHED, bool FRAME, bool COMPACT>
+// FORMAT 1 or 2: compact lists (in wide records with 2) to p.rec (no cell
+// codes, no static particles).
+template <bool MIXED, bool HASHED, bool FRAME, int FORMAT>
 __device__ __forceinline__ void lists_lambda(const StepParams& p, const CellPack& cp, float4* __restrict__ xs,
                                              const int* __restrict__ key_sorted, const int* __restrict__ cell_sorted,
                                              const int* __restrict__ fstart, const float4* __restrict__ solid,
@@ -268,7 +300,8 @@ __device__ __forceinline__ void lists_lambda(const StepParams& p, const CellPack
                                               : plain_cell(p, g, self.x, self.y, self.z);
     LambdaAcc a = lambda_init(p);
     int c_n = 0;
-    using Lists = typename ListsOf<COMPACT>::T;
+    constexpr bool COMPACT = FORMAT != 0;
+    using Lists = typename ListsOf<FORMAT>::T;
     Lists out = open_lists((Lists*)nullptr, nbr, p.n, s, g.slot0, stage);
     const int slab = g.gx * g.gz;
     // static particles only where the cell's neighbourhood holds some
@@ -353,12 +386,12 @@ __global__ void __launch_bounds__(B) k_lists_lambda(StepParams p, CellPack cp, f
                                                     const int* __restrict__ sstart,
                                                     int* __restrict__ nbr, int* __restrict__ cnt,
                                                     float* __restrict__ rho, int* status) {
-    lists_lambda<MIXED, HASHED, FRAME, false>(p, cp, xs, key_sorted, cell_sorted, fstart, solid, solid_cell, sstart,
-                                              nbr, cnt, rho, status);
+    lists_lambda<MIXED, HASHED, FRAME, 0>(p, cp, xs, key_sorted, cell_sorted, fstart, solid, solid_cell, sstart, nbr,
+                                          cnt, rho, status);
 }
 
-// Compact lists (no static particles, fp32 pair offsets).
-template <bool HASHED, int B, bool FRAME>
+// Compact lists (no static particles, fp32 pair offsets; WIDE: wide records).
+template <bool HASHED, int B, bool FRAME, bool WIDE>
 __global__ void __launch_bounds__(B) k_lists_compact(StepParams p, CellPack cp, float4* __restrict__ xs,
                                                              const int* __restrict__ key_sorted,
                                                              const int* __restrict__ cell_sorted,
@@ -369,8 +402,8 @@ __global__ void __launch_bounds__(B) k_lists_compact(StepParams p, CellPack cp, 
                                                              int* __restrict__ nbr, int* __restrict__ cnt,
                                                              float* __restrict__ rho, int* status) {
     __shared__ unsigned stage[COMPACT_STRIDE * B];
-    lists_lambda<false, HASHED, FRAME, true>(p, cp, xs, key_sorted, cell_sorted, fstart, solid, solid_cell, sstart,
-                                             nbr, cnt, rho, status, stage);
+    lists_lambda<false, HASHED, FRAME, WIDE ? 2 : 1>(p, cp, xs, key_sorted, cell_sorted, fstart, solid, solid_cell,
+                                                     sstart, nbr, cnt, rho, status, stage);
 }
 
 // Walk a particle's list U entries at a time, calling f(entry, position)
@@ -460,16 +493,17 @@ __device__ __forceinline__ void for_each_entry_p(const StepParams& p, const int*
     }
 }
 
-// Field j of a record: .y .z .w of the first (M = 6), .x .y .z .w of the second.
-template <int M>
+// Field j of a record: .y .z .w of the first, .x .y .z .w of the second.
+template <bool FIRST>
 __device__ __forceinline__ unsigned record_field(const uint4& r, int j) {
-    const int f = j + (M == COMPACT_INLINE ? 1 : 0);
+    const int f = j + (FIRST ? 1 : 0);
     return f == 0 ? r.x : (f == 1 ? r.y : (f == 2 ? r.z : r.w));
 }
 
-// The entries [K0, K0 + M) of a compact list from record r, min(U, M)
-// gathers at a time; false once the count is reached.
-template <int U, int M, int K0, class T, class G, class F>
+// The entries [K0, K0 + M) of a compact list from record r (K0 = 0: the
+// first record), min(U, M) gathers at a time; false once the count is
+// reached.
+template <int U, int M, int K0, bool WIDE, class T, class G, class F>
 __device__ __forceinline__ bool walk_record(const StepParams& p, const uint4& r, int c, int base, G&& gather,
                                             F&& f) {
     constexpr int V = U < M ? U : M;
@@ -482,8 +516,12 @@ __device__ __forceinline__ bool walk_record(const StepParams& p, const uint4& r,
 #pragma unroll
         for (int u = 0; u < V; u++)
             if (k + u < M) {
-                const unsigned x = record_field<M>(r, (k + u) >> 1);
-                sl[u] = compact_slot(p, base, ((k + u) & 1) ? (x >> 16) : (x & 0xFFFFu));
+                if (WIDE) {
+                    sl[u] = (int)record_field<K0 == 0>(r, k + u);
+                } else {
+                    const unsigned x = record_field<K0 == 0>(r, (k + u) >> 1);
+                    sl[u] = compact_slot(p, base, ((k + u) & 1) ? (x >> 16) : (x & 0xFFFFu));
+                }
                 q[u] = gather(sl[u]);
             }
 #pragma unroll
@@ -495,31 +533,33 @@ __device__ __forceinline__ bool walk_record(const StepParams& p, const uint4& r,
 
 // Walk a compact list (record r of slot s, r2 its second record; col =
 // nbr + s, its overflow rows): gather(slot) loads what f(slot, value) needs
-// of each neighbour.  A record's entries go min(U, 6 or 8) at a time, all
-// gathers of a chunk in flight together, so with U >= 4 a list of up to 4
-// neighbours waits for one round trip to DRAM (the record, with the
-// particle's own loads) and one to L2 for the neighbours; the second record
-// is loaded only for a list longer than 6.  Past the count an entry reads the
-// sentinel slot, whose terms are exactly zero; the overflow rows are padded
-// with it to a multiple of U (the list build's pad).
-template <int U, class T, class G, class F>
+// of each neighbour.  A record's entries go min(U, its entries) at a time,
+// all gathers of a chunk in flight together, so with U >= 4 a list of up to
+// 4 neighbours (3 in wide records) waits for one round trip to DRAM (the
+// record, with the particle's own loads) and one to L2 for the neighbours;
+// the second record is loaded only for a longer list.  Past the count an
+// entry reads the sentinel slot, whose terms are exactly zero; the overflow
+// rows are padded with it to a multiple of U (the list build's pad).
+template <int U, bool WIDE, class T, class G, class F>
 __device__ __forceinline__ void walk_compact(const StepParams& p, const uint4& r, const uint4* __restrict__ r2,
                                              const int* __restrict__ col, G&& gather, F&& f) {
-    const int c = (int)(r.x & 0xFFu);
-    const int base = (int)(r.x >> 8);
-    if (!walk_record<U, COMPACT_INLINE, 0, T>(p, r, c, base, gather, f)) return;
-    if (!walk_record<U, COMPACT_EXT, COMPACT_INLINE, T>(p, __ldg(r2), c, base, gather, f)) return;
+    using RF = RecordFormat<WIDE>;
+    const int c = WIDE ? (int)r.x : (int)(r.x & 0xFFu);
+    const int base = WIDE ? 0 : (int)(r.x >> 8);
+    if (!walk_record<U, RF::INLINE, 0, WIDE, T>(p, r, c, base, gather, f)) return;
+    if (!walk_record<U, RF::EXT, RF::INLINE, WIDE, T>(p, __ldg(r2), c, base, gather, f)) return;
+    constexpr int R = RF::RECORDS;
     int nx[U];
 #pragma unroll
     for (int u = 0; u < U; u++) nx[u] = __ldg(&col[(size_t)u * p.n]);
-    for (int k = COMPACT_RECORDS; k < c; k += U) {
+    for (int k = R; k < c; k += U) {
         int e[U];
         T q[U];
 #pragma unroll
         for (int u = 0; u < U; u++) e[u] = nx[u];
         if (k + U < c) {
 #pragma unroll
-            for (int u = 0; u < U; u++) nx[u] = __ldg(&col[(size_t)(k - COMPACT_RECORDS + U + u) * p.n]);
+            for (int u = 0; u < U; u++) nx[u] = __ldg(&col[(size_t)(k - R + U + u) * p.n]);
         }
 #pragma unroll
         for (int u = 0; u < U; u++) q[u] = gather(e[u]);
@@ -538,9 +578,9 @@ __global__ void __launch_bounds__(B) k_lambda(StepParams p, float4* __restrict__
                                               const float4* __restrict__ solid,
                                               float* __restrict__ rho) {
     // F bit 2: the scene frame (fp32 pair offsets, compensated density sums)
-    // F bit 3: compact lists (fp32 pair offsets, no static particles)
+    // F bit 3: compact lists (fp32 pair offsets, no static particles); bit 4: in wide records
     constexpr bool MIXED = (F & 1) != 0, SOL = (F & 2) != 0, KAHAN = MIXED || (F & 4) != 0;
-    constexpr bool COMPACT = (F & 8) != 0;
+    constexpr bool COMPACT = (F & 8) != 0, WIDE = (F & 16) != 0;
     static_assert(!COMPACT || (!MIXED && !SOL && P == 1), "compact lists");
     pdl_wait();
     __shared__ float4 shift_tab[MIXED ? 64 : 1];
@@ -551,7 +591,7 @@ __global__ void __launch_bounds__(B) k_lambda(StepParams p, float4* __restrict__
         const float4 self = xs[s];
         LambdaAcc a = lambda_init(p);
         if (COMPACT) {
-            walk_compact<U, float4>(
+            walk_compact<U, WIDE, float4>(
                 p, __ldg(&p.rec[s]), p.rec2 + s, nbr + s, [&](int t) { return xs[t]; },
                 [&](int, float4 q) { lambda_accumulate<KAHAN>(p, a, rel_t<false>(self, q, 0, shift_tab), false); });
         } else {
@@ -683,7 +723,7 @@ __global__ void __launch_bounds__(B, ((F & 8) && U == 1) ? 2048 / B : ((U <= 2 &
     k_delta(StepParams p, CellPack cp, const float4* __restrict__ xs, float4* __restrict__ xs_out,
             const int* __restrict__ nbr, const int* __restrict__ cnt, const float4* __restrict__ solid,
             const int* __restrict__ key_sorted, const float4* __restrict__ x, float4* __restrict__ v_out) {
-    constexpr bool MIXED = (F & 1) != 0, SOL = (F & 2) != 0, COMPACT = (F & 8) != 0;
+    constexpr bool MIXED = (F & 1) != 0, SOL = (F & 2) != 0, COMPACT = (F & 8) != 0, WIDE = (F & 16) != 0;
     static_assert(!COMPACT || (!MIXED && !SOL && P == 1), "compact lists");
     pdl_wait();
     __shared__ float4 shift_tab[MIXED ? 64 : 1];
@@ -696,7 +736,7 @@ __global__ void __launch_bounds__(B, ((F & 8) && U == 1) ? 2048 / B : ((U <= 2 &
         const int packed = (MIXED && p.cell_sorted) ? __ldg(&p.cell_sorted[s]) : 0;
         DeltaAcc a{0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0};
         if (COMPACT) {
-            walk_compact<U, float4>(
+            walk_compact<U, WIDE, float4>(
                 p, __ldg(&p.rec[s]), p.rec2 + s, nbr + s, [&](int t) { return xs[t]; },
                 [&](int t, float4 q) { delta_pair<false, false>(p, a, self, t, q, shift_tab); });
         } else {
@@ -758,7 +798,7 @@ __device__ __forceinline__ void xsph_commit(const StepParams& p, const CellPack&
                                             float4* __restrict__ xs_next, int* __restrict__ key,
                                             int* __restrict__ rank, int* __restrict__ count, int* __restrict__ cellk,
                                             int* __restrict__ tile_count) {
-    constexpr bool MIXED = (F & 1) != 0, SOL = (F & 2) != 0, COMPACT = (F & 8) != 0;
+    constexpr bool MIXED = (F & 1) != 0, SOL = (F & 2) != 0, COMPACT = (F & 8) != 0, WIDE = (F & 16) != 0;
     static_assert(!COMPACT || (!MIXED && !SOL), "compact lists");
     pdl_wait();
     __shared__ float4 shift_tab[MIXED ? 64 : 1];
@@ -770,7 +810,7 @@ __device__ __forceinline__ void xsph_commit(const StepParams& p, const CellPack&
     const int* __restrict__ col = nbr + s;
     float ax = 0.0f, ay = 0.0f, az = 0.0f;
     if (COMPACT && p.c_xsph != 0.0f) {
-        walk_compact<U, PosVel>(
+        walk_compact<U, WIDE, PosVel>(
             p, __ldg(&p.rec[s]), p.rec2 + s, col, [&](int t) { return PosVel{xs[t], v_in[t]}; },
             [&](int t, const PosVel& q) { xsph_pair<false>(p, self, vi, q.x, q.v, t, shift_tab, ax, ay, az); });
     } else if (p.c_xsph != 0.0f) {
@@ -832,7 +872,7 @@ __global__ void __launch_bounds__(B) k_xsph(StepParams p, CellPack cp, const flo
                       tile_count);
 }
 
-// Compact lists (F = 8) with one gather in flight: registers capped at 32
+// Compact lists (F = 8, 24) with one gather in flight: registers capped at 32
 // for every warp slot of the SM (64 bytes spilled; config 3 XSPH 0.175 ->
 // 0.141 ms at step 5, 0.239 -> 0.219 ms at step 100 against the best
 // uncapped shape).  More gathers in flight keep k_xsph.
@@ -1255,7 +1295,7 @@ void launch_key(bool mixed, const StepParams& p, const CellPack& cp, const float
     } while (0)
 // fcode: bit 0 mixed (cell-relative pair offsets), bit 1 static particles,
 // bit 2 (the lambda pass only) the scene frame's compensated sums, bit 3
-// compact lists (with bit 2 at most)
+// compact lists (with bit 2 at most), bit 4 their wide records
 #define TUNE_DISPATCH(KERNEL, fcode, tu, N, ST, ...)                                            \
     do {                                                                                        \
         switch (fcode) {                                                                        \
@@ -1291,18 +1331,21 @@ void launch_lists_lambda(bool mixed, const Tuning& tu, const StepParams& p, cons
         else LGB_LISTS_H(MIX, false, BB);        \
     } while (0)
     if (p.rec) {  // compact lists: fp32 pair offsets (the scene frame: compensated sums)
-#define LGB_LISTS_C(H, FR, BB)                                                                    \
-    launch_k(k_lists_compact<H, BB, FR>, blocks_for(p.n, BB), BB, st, pdl, pp, cp, xs, key_sorted, \
+#define LGB_LISTS_C(H, FR, W, BB)                                                                    \
+    launch_k(k_lists_compact<H, BB, FR, W>, blocks_for(p.n, BB), BB, st, pdl, pp, cp, xs, key_sorted, \
              cell_sorted, fstart, solid, solid_cell, sstart, nbr, cnt, rho, status)
-#define LGB_LISTS_CB(H, FR)                        \
-    do {                                           \
-        if (B == 64) LGB_LISTS_C(H, FR, 64);       \
-        else if (B == 128) LGB_LISTS_C(H, FR, 128); \
-        else LGB_LISTS_C(H, FR, 256);              \
+#define LGB_LISTS_CB(H, FR, W)                        \
+    do {                                              \
+        if (B == 64) LGB_LISTS_C(H, FR, W, 64);       \
+        else if (B == 128) LGB_LISTS_C(H, FR, W, 128); \
+        else LGB_LISTS_C(H, FR, W, 256);              \
     } while (0)
-        if (p.frame) LGB_LISTS_CB(false, true);
-        else if (p.hash_bits) LGB_LISTS_CB(true, false);
-        else LGB_LISTS_CB(false, false);
+        if (p.frame && p.wide) LGB_LISTS_CB(false, true, true);
+        else if (p.frame) LGB_LISTS_CB(false, true, false);
+        else if (p.hash_bits && p.wide) LGB_LISTS_CB(true, false, true);
+        else if (p.hash_bits) LGB_LISTS_CB(true, false, false);
+        else if (p.wide) LGB_LISTS_CB(false, false, true);
+        else LGB_LISTS_CB(false, false, false);
 #undef LGB_LISTS_CB
 #undef LGB_LISTS_C
     } else if (mixed && p.frame) {  // the scene frame: fp32 pair offsets, compensated sums
@@ -1331,7 +1374,9 @@ void launch_lambda(bool mixed, const Tuning& tu, const StepParams& p, float4* xs
     if (p.n <= 0) return;
     const int f = ((mixed && !p.frame) ? 1 : 0) | (p.ns > 0 ? 2 : 0);
     if (p.rec) {  // compact lists: one particle per thread
-        if (p.frame) TUNE_CASE(k_lambda, 12, tu, p.n, st, p, xs, nbr, cnt, solid, rho);
+        if (p.frame && p.wide) TUNE_CASE(k_lambda, 28, tu, p.n, st, p, xs, nbr, cnt, solid, rho);
+        else if (p.frame) TUNE_CASE(k_lambda, 12, tu, p.n, st, p, xs, nbr, cnt, solid, rho);
+        else if (p.wide) TUNE_CASE(k_lambda, 24, tu, p.n, st, p, xs, nbr, cnt, solid, rho);
         else TUNE_CASE(k_lambda, 8, tu, p.n, st, p, xs, nbr, cnt, solid, rho);
     } else if (mixed && p.frame)  // the scene frame: one particle per thread
         TUNE_DISPATCH_FRAME(k_lambda, f | 4, tu, p.n, st, p, xs, nbr, cnt, solid, rho);
@@ -1345,7 +1390,9 @@ void launch_delta(bool mixed, const Tuning& tu, const StepParams& p, const CellP
                   cudaStream_t st) {
     if (p.n <= 0) return;
     const int f = ((mixed && !p.frame) ? 1 : 0) | (p.ns > 0 ? 2 : 0);
-    if (p.rec)  // compact lists: one particle per thread
+    if (p.rec && p.wide)  // compact lists: one particle per thread
+        TUNE_CASE(k_delta, 24, tu, p.n, st, p, cp, xs, xs_out, nbr, cnt, solid, key_sorted, x, v_out);
+    else if (p.rec)
         TUNE_CASE(k_delta, 8, tu, p.n, st, p, cp, xs, xs_out, nbr, cnt, solid, key_sorted, x, v_out);
     else
         TUNE_DISPATCH_PPT(k_delta, f, tu, p.n, st, p, cp, xs, xs_out, nbr, cnt, solid, key_sorted, x, v_out);
@@ -1361,14 +1408,23 @@ void launch_xsph(bool mixed, const Tuning& tu, const StepParams& p, const CellPa
     const int f = ((mixed && !p.frame) ? 1 : 0) | (p.ns > 0 ? 2 : 0);
     if (p.rec && tx.unroll <= 1) {
         const int B = tx.block <= 64 ? 64 : (tx.block <= 128 ? 128 : 256);
-#define LGB_XC(BB)                                                                                     \
-    launch_k(k_xsph_compact<8, 1, BB>, blocks_for(p.n, BB), BB, st, pdl_enabled(), p, cp, xs, v_in, nbr, cnt, \
+#define LGB_XC(FF, BB)                                                                                  \
+    launch_k(k_xsph_compact<FF, 1, BB>, blocks_for(p.n, BB), BB, st, pdl_enabled(), p, cp, xs, v_in, nbr, cnt, \
              key_sorted, x_out, v_out, xs_next, key, rank, count, cellk, tile_count)
-        if (B == 64) LGB_XC(64);
-        else if (B == 128) LGB_XC(128);
-        else LGB_XC(256);
+        if (p.wide) {
+            if (B == 64) LGB_XC(24, 64);
+            else if (B == 128) LGB_XC(24, 128);
+            else LGB_XC(24, 256);
+        } else {
+            if (B == 64) LGB_XC(8, 64);
+            else if (B == 128) LGB_XC(8, 128);
+            else LGB_XC(8, 256);
+        }
 #undef LGB_XC
-    } else if (p.rec)
+    } else if (p.rec && p.wide)
+        TUNE_CASE(k_xsph, 24, tx, p.n, st, p, cp, xs, v_in, nbr, cnt, key_sorted, x_out, v_out, xs_next, key, rank,
+                  count, cellk, tile_count);
+    else if (p.rec)
         TUNE_CASE(k_xsph, 8, tx, p.n, st, p, cp, xs, v_in, nbr, cnt, key_sorted, x_out, v_out, xs_next, key, rank,
                   count, cellk, tile_count);
     else

@@ -272,10 +272,11 @@ class PbfSim:
         return cnt, idx
 
     def list_format(self) -> str:
-        """"compact" or "column": the form of the last step's neighbour lists."""
+        """"compact", "compact_wide" or "column": the form of the last step's
+        neighbour lists."""
         v = C.c_int()
         check(self.lib.lustrine_pbf_list_format(self.h, C.byref(v)), "list_format")
-        return "compact" if v.value == _lib.LISTS_COMPACT else "column"
+        return {_lib.LISTS_COMPACT: "compact", _lib.LISTS_COMPACT_WIDE: "compact_wide"}.get(v.value, "column")
 
     def reduce(self):
         """FP64 device reductions: mass, momentum[3], kinetic energy,

@@ -1,5 +1,6 @@
-"""Compact neighbour lists (one 16-byte record per particle: the count, the
-scene's first slot and six entries as 16-bit scene offsets; longer lists go
+"""Compact neighbour lists (16-byte records: the count, the scene's first
+slot and 6 + 8 entries as 16-bit scene offsets; for larger scenes wide
+records with the count and 3 + 4 entries as 32-bit slots; longer lists go
 on in the column rows) against the column lists: the same entries in the
 same order, so every pass sums the same terms in the same order and the
 step's fp32 results are bitwise equal; and the cases where the step must
@@ -55,22 +56,43 @@ def test_compact_lists_give_the_column_bits(precision):
 
 
 @pytest.mark.parametrize("unroll", [1, 2, 4, 8])
-def test_compact_overflow_rows(unroll):
+@pytest.mark.parametrize("dims,fmt_expected", [((14, 12, 14), "compact"), ((42, 40, 42), "compact_wide")])
+def test_compact_overflow_rows(unroll, dims, fmt_expected):
     """A block at spacing 0.6 h: about 18 neighbours a particle, so every list
-    runs past the six inline entries into the overflow rows (padded with the
-    sentinel to the chunk); results and lists equal the column lists'."""
+    fills both records and runs on into the overflow rows (padded with the
+    sentinel to the chunk); 2,352 particles take 16-bit entries, 70,560 wide
+    records.  Results and lists equal the column lists'."""
     from lustrine_gb300 import LISTS_COLUMN, LISTS_COMPACT, scenes
     rng = np.random.default_rng(42)
-    x = scenes.jitter(scenes.lattice((14, 12, 14), (4, 1, 4)) * 0.6, 0.05, rng)
-    sc = scenes.Scene("dense", (16, 16, 16), x.astype(np.float32), dt=1 / 60, iterations=4)
+    x = scenes.jitter(scenes.lattice(dims, (4, 1, 4)) * 0.6, 0.05, rng)
+    box = int(np.ceil(0.6 * max(dims))) + 6
+    sc = scenes.Scene("dense", (box, box, box), x.astype(np.float32), dt=1 / 60, iterations=4)
     p = _params(sc, 0)
     ref, _, cnt0, idx0 = _run(sc, p, LISTS_COLUMN, unroll, unroll, steps=2)
     got, fmt, cnt, idx = _run(sc, p, LISTS_COMPACT, unroll, unroll, steps=2)
-    assert fmt == "compact"
+    assert fmt == fmt_expected
     assert (cnt0 > 7).mean() > 0.5  # count includes the particle itself
     _assert_same(ref, got)
     np.testing.assert_array_equal(cnt0, cnt)
     np.testing.assert_array_equal(idx0, idx)
+
+
+@pytest.mark.parametrize("precision", [0, 2])
+def test_wide_records_give_the_column_bits(precision):
+    """A dam break of 70,560 particles (past the 16-bit entries' 65,535): wide
+    records at 1, 2 and 4 gathers in flight against column lists."""
+    from lustrine_gb300 import LISTS_COLUMN, LISTS_COMPACT, scenes
+    rng = np.random.default_rng(44)
+    x = scenes.jitter(scenes.lattice((42, 40, 42)), 0.05, rng)
+    sc = scenes.Scene("wide", (84, 44, 84), x, dt=1 / 60, iterations=4)
+    ref, fmt, cnt0, idx0 = _run(sc, _params(sc, precision), LISTS_COLUMN)
+    assert fmt == "column"
+    for unroll in (1, 2, 4):
+        got, fmt, cnt, idx = _run(sc, _params(sc, precision), LISTS_COMPACT, unroll, unroll)
+        assert fmt == "compact_wide"
+        _assert_same(ref, got)
+        np.testing.assert_array_equal(cnt0, cnt)
+        np.testing.assert_array_equal(idx0, idx)
 
 
 @pytest.mark.parametrize("precision", [0, 2])
@@ -97,10 +119,10 @@ def test_compact_batch_equals_column_batch(precision):
 
 
 def test_compact_lists_only_where_they_apply():
-    """Scenes of 65,535 particles take compact lists, 65,536 do not (16-bit
-    offsets, one value kept for the sentinel); nor do static particles, the
+    """Scenes of 65,535 particles take 16-bit entries, 65,536 wide records
+    (one 16-bit value is kept for the sentinel); static particles, the
     cell-relative mixed form (cell codes in the entries), two particles per
-    thread or the reference's step."""
+    thread and the reference's step keep column lists."""
     from lustrine_gb300 import (LISTS_COMPACT, MODE_REFERENCE, PRECISION_MIXED, PbfSim, pbf_params,
                                 reference_params, scenes)
     rng = np.random.default_rng(43)
@@ -117,7 +139,7 @@ def test_compact_lists_only_where_they_apply():
         return f
 
     assert fmt_of(pbf_params(130, 40, 130), big[:65535]) == "compact"
-    assert fmt_of(pbf_params(130, 40, 130), big) == "column"
+    assert fmt_of(pbf_params(130, 40, 130), big) == "compact_wide"
     small = big[:4000]
     assert fmt_of(pbf_params(130, 40, 130, precision=PRECISION_MIXED), small) == "column"
     assert fmt_of(pbf_params(130, 40, 130), small, ppt=2) == "column"
@@ -125,9 +147,9 @@ def test_compact_lists_only_where_they_apply():
     assert fmt_of(pbf_params(130, 40, 130), small, solids=solid) == "column"
     rp = reference_params(130, 40, 130, 0.5, 2.0)
     assert fmt_of(rp, small) == "column"
-    # a batch with one scene past the limit keeps column lists for all
+    # a batch with one scene past the 16-bit limit takes wide records for all
     b = PbfSim.batch(pbf_params(8, 8, 8, iterations=2), [(130, 40, 130), (40, 40, 40)], [65536, 1000])
     b.upload(np.concatenate([big, scenes.jitter(scenes.lattice((10, 10, 10), (5, 0, 5)), 0.05, rng)]))
     b.step(1 / 60)
-    assert b.status() == 0 and b.list_format() == "column"
+    assert b.status() == 0 and b.list_format() == "compact_wide"
     b.close()

@@ -202,6 +202,28 @@ def test_two_particles_per_thread_give_the_same_bits(with_solids):
             np.testing.assert_array_equal(a, b)
 
 
+@pytest.mark.parametrize("precision", [1, 2])
+def test_gathers_in_flight_give_the_same_bits_with_compensated_sums(precision):
+    """The mixed representations sum densities with Kahan compensation; a walk
+    with more gathers in flight visits more sentinel entries (exact zero
+    terms), which leave the compensated sum untouched, so 1, 2, 4 and 8
+    gathers in flight give the same bits (column lists)."""
+    from lustrine_gb300 import LISTS_COLUMN, PbfSim, scenes
+    sc = scenes.config0(seed=33)
+    res = []
+    for unroll in (1, 2, 4, 8):
+        sim = PbfSim(_params(sc, precision=precision), sc.n)
+        sim.upload(sc.x)
+        sim.set_tuning(128, unroll, 128, unroll, 1, list_format=LISTS_COLUMN)
+        sim.step(sc.dt, 4)
+        assert sim.status() == 0
+        res.append(sim.download(lambdas=True, density=True))
+        sim.close()
+    for r in res[1:]:
+        for a, b in zip(res[0], r):
+            np.testing.assert_array_equal(a, b)
+
+
 def test_graph_and_direct_launches_are_identical():
     from lustrine_gb300 import PbfSim, scenes
     sc = scenes.config0(seed=24)
