@@ -77,6 +77,43 @@ def test_compact_overflow_rows(unroll, dims, fmt_expected):
     np.testing.assert_array_equal(idx0, idx)
 
 
+@pytest.mark.parametrize("max_nbrs", [5, 8, 16])
+def test_compact_lists_at_their_capacity(max_nbrs):
+    """Lists cut at max_neighbors (5: inside the first record; 8: into the
+    second; 16: past both into the overflow rows) on the dense block: the
+    overflow status is raised, and results and the truncated lists equal the
+    column lists'."""
+    from lustrine_gb300 import LISTS_COLUMN, LISTS_COMPACT, PbfSim, scenes
+    rng = np.random.default_rng(45)
+    x = scenes.jitter(scenes.lattice((14, 12, 14), (4, 1, 4)) * 0.6, 0.05, rng).astype(np.float32)
+    sc = scenes.Scene("dense", (16, 16, 16), x, dt=1 / 60, iterations=4)
+    res = []
+    for lf in (LISTS_COLUMN, LISTS_COMPACT):
+        sim = PbfSim(_params(sc, 0, max_neighbors=max_nbrs), sc.n)
+        sim.upload(sc.x)
+        sim.set_tuning(128, 2, 128, 2, 1, list_format=lf)
+        sim.step(sc.dt)
+        assert sim.status() == 4  # LUSTRINE_ERR_NBR_OVERFLOW: lists truncated
+        res.append((sim.download(lambdas=True, density=True), sim.list_format(), sim.neighbors(cap=max_nbrs + 1)))
+        sim.close()
+    assert res[1][1] == "compact"
+    _assert_same(res[0][0], res[1][0])
+    _assert_same(res[0][2], res[1][2])
+
+
+def test_compact_lists_need_counts_below_256():
+    """The compact count field holds 8 bits: max_neighbors 256 keeps column lists."""
+    from lustrine_gb300 import LISTS_COMPACT, PbfSim, scenes
+    sc = scenes.config0(seed=46)
+    for cap, want in ((255, "compact"), (256, "column")):
+        sim = PbfSim(_params(sc, 0, max_neighbors=cap), sc.n)
+        sim.upload(sc.x)
+        sim.set_tuning(128, 2, 128, 2, 1, list_format=LISTS_COMPACT)
+        sim.step(sc.dt)
+        assert sim.status() == 0 and sim.list_format() == want
+        sim.close()
+
+
 @pytest.mark.parametrize("precision", [0, 2])
 def test_wide_records_give_the_column_bits(precision):
     """A dam break of 70,560 particles (past the 16-bit entries' 65,535): wide
