@@ -28,6 +28,7 @@ UNITS = {
     "pbf_compat.cu": ["--fmad=false"],
     "sand.cu": ["--fmad=false"],
     "pbf_solver.cu": [],
+    "pbf_compact.cu": [],
     "pbf_scene_solve.cu": [],
     "pbf_context.cu": [],
     "pbf_dynamic.cu": [],

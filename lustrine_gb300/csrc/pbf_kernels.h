@@ -121,6 +121,21 @@ void launch_xsph(bool mixed, const Tuning& tu, const StepParams& p, const CellPa
                  const float4* xs, const float4* v_in, const int* nbr, const int* cnt,
                  const int* key_sorted, float4* x_out, float4* v_out, float4* xs_next, int* key,
                  int* rank, int* count, int* cellk, int* tile_count, cudaStream_t st);
+// The same passes over compact lists (p.rec set; pbf_compact.cu).  B: the
+// list build's block size; p.pad: the passes' largest chunk.
+void launch_lists_compact(int B, const StepParams& p, const CellPack& cp, float4* xs, const int* key_sorted,
+                          const int* cell_sorted, const int* fstart, const float4* solid, const int* solid_cell,
+                          const int* sstart, int* nbr, int* cnt, float* rho, int* status, cudaStream_t st);
+void launch_lambda_compact(const Tuning& tu, const StepParams& p, float4* xs, const int* nbr, const int* cnt,
+                           const float4* solid, float* rho, cudaStream_t st);
+void launch_delta_compact(const Tuning& tu, const StepParams& p, const CellPack& cp, const float4* xs,
+                          float4* xs_out, const int* nbr, const int* cnt, const float4* solid,
+                          const int* key_sorted, const float4* x, float4* v_out, cudaStream_t st);
+// tx.unroll: the XSPH pass's gathers in flight
+void launch_xsph_compact(const Tuning& tx, const StepParams& p, const CellPack& cp, const float4* xs,
+                         const float4* v_in, const int* nbr, const int* cnt, const int* key_sorted, float4* x_out,
+                         float4* v_out, float4* xs_next, int* key, int* rank, int* count, int* cellk,
+                         int* tile_count, cudaStream_t st);
 void launch_unpermute_pos(bool mixed, const StepParams& p, const CellPack& cp, const float4* a,
                           const int* id, int n, float* out, cudaStream_t st);
 void launch_unpermute_pos_d(bool mixed, const StepParams& p, const CellPack& cp, const float4* a,
