@@ -1,8 +1,10 @@
-// pbf_passes.cuh -- the PBF step (mode P): the position-based-fluids solver the
-// reference's parameters describe (Simulation.hpp:157-171: rest density,
-// relaxation epsilon, s_corr, XSPH) on the poly6 / spiky kernels of
-// Kernels.cpp:43-67, with N Jacobi solver iterations over neighbour lists
-// built once per step.
+// pbf_passes.cuh -- the kernels of the PBF step (mode P): the
+// position-based-fluids solver the reference's parameters describe
+// (Simulation.hpp:157-171: rest density, relaxation epsilon, s_corr, XSPH) on
+// the poly6 / spiky kernels of Kernels.cpp:43-67, with N Jacobi solver
+// iterations over neighbour lists built once per step.  Templates only: the
+// launchers in pbf_solver.cu (column lists) and pbf_compact.cu (compact lists)
+// instantiate them.
 //
 // Position representations (template parameter MIXED):
 //   plain  float4 xyz = absolute position;
@@ -18,9 +20,10 @@
 // lambda, written in place by the lambda pass, so the position pass gathers
 // one float4 per neighbour.
 //
-// Neighbour list entry (int32): bits 0-24 slot, then the neighbour's cell
-// offset from the particle's cell, 2 bits per axis as d + 1 (x in 25-26, y in
-// 27-28, z in 29-30), bit 31 set for solids.
+// Neighbour list entry (int32, column lists): bits 0-24 slot, then the
+// neighbour's cell offset from the particle's cell, 2 bits per axis as d + 1
+// (x in 25-26, y in 27-28, z in 29-30), bit 31 set for solids.  Compact
+// lists (no cell codes, no solids): 16-byte records, see CompactLists.
 //
 // Grids: dense (cell id = offset + y gX gZ + x gZ + z; the three cells of a
 // stencil row are consecutive ids) or hashed (the counting sort runs over
