@@ -523,8 +523,15 @@ def run_ours(args, world, rank, local):
     off = np.concatenate([[0], np.cumsum([sc.n for sc in scs])]).astype(int)
     xs0 = x_keep.numpy()
     vs0 = v_keep.numpy()
+    # the per-scene contexts take the batched context's tuned launch shape
+    # (the per-stage kernels' shape and list format)
+    bt = b.tuned["tuning"]
+    plain_shape = dict(block=bt["block"], unroll=bt["unroll"], list_block=bt["list_block"],
+                       xsph_unroll=bt["xsph_unroll"], particles_per_thread=bt["particles_per_thread"],
+                       list_format=bt.get("list_format", 1))
     for k, sc in enumerate(scs):
         s = PbfSim(pbf_params(*sc.domain, iterations=ITERS), sc.n)
+        s.set_tuning(**plain_shape)
         s.upload(xs0[off[k]:off[k + 1]], vs0[off[k]:off[k + 1]])
         s.step(dt, 2)
         sims.append(s)
@@ -590,6 +597,7 @@ def run_ours(args, world, rank, local):
     plain = {
         "value": n_local * ITERS / t_plain, "ms_per_step": t_plain * 1e3,
         "contexts": len(sims), "launches_per_step": sum(s.launches_per_step() for s in sims),
+        "launch_shape": plain_shape,
         "status": max(s.status() for s in sims), "precision": "fp32",
         "overlap": "one context per scene, each on its own stream: the scenes' steps overlap",
         "batched_mixed_wall_ms_per_step": t_batched * 1e3,
