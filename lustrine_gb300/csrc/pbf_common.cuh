@@ -104,6 +104,8 @@ struct StepParams {
     uint4* rec;           // compact neighbour lists of this step (nullptr: column lists with counts)
     uint4* rec2;          // their second records
     int wide;             // compact lists in wide records (32-bit slots)
+    const int* src;       // the previous slot of each sorted slot, whose committed position the last
+                          // position pass reads from the unsorted state (nullptr: sorted with the step)
 };
 
 // Sand mode: simulate_sand's per-call inputs (Simulate.cpp:156-209).

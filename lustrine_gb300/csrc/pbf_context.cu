@@ -209,7 +209,7 @@ void lustrine_pbf::free_buffers() {
                     rank, tmp, perm, count, start, block_sums, tile_sum, solid_near, solid, solid_raw, sstart, nbr, cnt, lam,
                     lam_by_id, rho, status, red, qcount, out3, out3d, iota, slot_of, solid_id, d_scenes, d_scene_of,
                     d_solid_scene_of, cellk, cell_sorted, solid_cell, att[0], att[1], d_bins, d_scene_slot0,
-                    d_queue, rec, rec2};
+                    d_queue, rec, rec2, src};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     x[0] = x[1] = xs[0] = xs[1] = v[0] = v[1] = nullptr;
@@ -219,6 +219,7 @@ void lustrine_pbf::free_buffers() {
     nbr = cnt = status = qcount = iota = slot_of = solid_id = d_scene_of = d_solid_scene_of = nullptr;
     cellk = cell_sorted = solid_cell = nullptr;
     rec = rec2 = nullptr;
+    src = nullptr;
     lists_format = LUSTRINE_LISTS_COLUMN;
     att[0] = att[1] = nullptr;
     solid_near = nullptr;
@@ -293,6 +294,7 @@ static int ctx_alloc(lustrine_pbf* s) {
     const size_t list_rows = (size_t)((s->sp.max_nbrs + LIST_PAD_MAX - 1) / LIST_PAD_MAX * LIST_PAD_MAX);
     rc = rc ? rc : dalloc(&s->nbr, list_rows * (size_t)n);
     rc = rc ? rc : dalloc(&s->cnt, n);
+    rc = rc ? rc : dalloc(&s->src, n);
     if (compact_capable(s) != LUSTRINE_LISTS_COLUMN) {
         rc = rc ? rc : dalloc(&s->rec, n);
         rc = rc ? rc : dalloc(&s->rec2, n);
@@ -863,7 +865,8 @@ static int enqueue_sand_step(lustrine_pbf* s, cudaStream_t st, StageMarks* mk) {
     // index after sources or sinks changed the order), as the reference's
     // counting sort is (Sorting.cpp:29-32)
     launch_sort_state(s->key, s->rank, s->start, s->id[c], n, s->tmp, s->x[c], s->xs[c], nullptr, nullptr,
-                      s->key_sorted, s->x[o], s->xs[o], nullptr, nullptr, s->att[c], s->att[o], nullptr, st);
+                      s->key_sorted, s->x[o], s->xs[o], nullptr, nullptr, s->att[c], s->att[o], nullptr, nullptr,
+                      st);
     k += 2;
     if (mk) mk->mark(LUSTRINE_STAGE_SORT, st);
     launch_sand_lists(p, s->xs[o], s->key_sorted, s->start, s->solid, s->sstart, s->nbr, s->cnt, s->status, st);
@@ -933,10 +936,16 @@ static int enqueue_step(lustrine_pbf* s, cudaStream_t st, StageMarks* mk = nullp
     // reference's list order), by the previous slot otherwise
     const int* tie = s->prm.mode == LUSTRINE_MODE_REFERENCE ? s->id[c] : nullptr;
     // velocities are not carried: the last position pass recomputes them
-    // (v = (x* - x) / dt) before anything reads them
+    // (v = (x* - x) / dt) before anything reads them.  The per-stage PBF
+    // step leaves the committed positions in the previous order too: the
+    // sort records each new slot's previous slot and the last position pass
+    // reads x there (the commit then writes the new side whole)
+    const bool onchip = s->onchip && s->num_bins > 0;
+    const bool keep_x = ref || onchip;
     launch_sort_state(s->key, s->rank, s->start, tie, n, s->tmp, s->x[c], xs_in, nullptr, s->id[c],
-                      s->key_sorted, s->x[o], s->xs[o], s->v[o], s->id[o], s->cell_sorted ? s->cellk : nullptr,
-                      s->cell_sorted, s->slot_of, st);
+                      s->key_sorted, keep_x ? s->x[o] : nullptr, s->xs[o], s->v[o], s->id[o],
+                      s->cell_sorted ? s->cellk : nullptr, s->cell_sorted, s->slot_of, keep_x ? nullptr : s->src,
+                      st);
     k += 2;
     if (mk) mk->mark(LUSTRINE_STAGE_SORT, st);
     if (s->prm.mode == LUSTRINE_MODE_REFERENCE) {
@@ -950,7 +959,7 @@ static int enqueue_step(lustrine_pbf* s, cudaStream_t st, StageMarks* mk = nullp
         if (mk) mk->mark(LUSTRINE_STAGE_DELTA, st);
         k += 3;
         s->lists_format = LUSTRINE_LISTS_COLUMN;
-    } else if (s->onchip && s->num_bins > 0) {
+    } else if (onchip) {
         // the batch's lists, iterations, XSPH and commit in one persistent
         // launch of clusters (the lambdas end where the per-stage path leaves them)
         SolveArgs sa;
@@ -989,6 +998,7 @@ static int enqueue_step(lustrine_pbf* s, cudaStream_t st, StageMarks* mk = nullp
         pl.rec = s->lists_format != LUSTRINE_LISTS_COLUMN ? s->rec : nullptr;
         pl.rec2 = pl.rec ? s->rec2 : nullptr;
         pl.wide = s->lists_format == LUSTRINE_LISTS_COMPACT_WIDE;
+        pl.src = s->src;
         float4* a = s->xs[o];
         float4* b = s->xs_alt;
         const int iters = s->prm.iterations;
@@ -1003,7 +1013,7 @@ static int enqueue_step(lustrine_pbf* s, cudaStream_t st, StageMarks* mk = nullp
                 launch_lambda(mixed, tu, pl, a, s->nbr, s->cnt, s->solid, rho, st);
                 if (mk) mk->mark(LUSTRINE_STAGE_LAMBDA, st);
             }
-            launch_delta(mixed, tu, pl, s->cp, a, b, s->nbr, s->cnt, s->solid, s->key_sorted, s->x[o],
+            launch_delta(mixed, tu, pl, s->cp, a, b, s->nbr, s->cnt, s->solid, s->key_sorted, s->x[c],
                          it == iters - 1 ? s->vtmp : nullptr, st);
             if (mk) mk->mark(LUSTRINE_STAGE_DELTA, st);
             float4* t = a;

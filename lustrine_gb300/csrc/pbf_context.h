@@ -69,6 +69,7 @@ struct lustrine_pbf {
     int* cnt = nullptr;
     uint4* rec = nullptr;        // compact list records (allocated where compact lists can apply)
     uint4* rec2 = nullptr;       // their second records
+    int* src = nullptr;          // PBF step: previous slot of each sorted slot (its committed position)
     int lists_format = LUSTRINE_LISTS_COLUMN;  // the form the last list build wrote (LUSTRINE_LISTS_*)
     float* lam = nullptr;
     float4* lam_src = nullptr;  // PBF: the buffer whose w holds the last lambdas

@@ -57,11 +57,13 @@ void launch_counting_sort(const int* keys, int n, int num_cells, CountingSortScr
                           int* sorted, cudaStream_t st);
 // index scatter + stabilisation fused with the reorder of the particle state
 // (v may be nullptr: not carried; aux: an optional int per particle carried
-// into the new order, e.g. the packed cells of a hashed grid)
+// into the new order, e.g. the packed cells of a hashed grid; x_out nullptr:
+// x stays in the previous order and src_out receives each new slot's previous
+// slot instead)
 void launch_sort_state(const int* key, int* rank, const int* start, const int* tie, int n,
                        int* tmp, const float4* x, const float4* xs, const float4* v, const int* id,
                        int* key_out, float4* x_out, float4* xs_out, float4* v_out, int* id_out,
-                       const int* aux, int* aux_out, int* slot_of, cudaStream_t st);
+                       const int* aux, int* aux_out, int* slot_of, int* src_out, cudaStream_t st);
 void launch_gather_int(const int* perm, int n, const int* src, int* dst, cudaStream_t st);
 
 // pbf_compat.cu (reference semantics, no FMA contraction)

@@ -700,7 +700,7 @@ __device__ __forceinline__ void delta_finish(const StepParams& p, const CellPack
     }
     xs_out[s] = out;
     if (v_out) {
-        float4 xo = x[s];
+        float4 xo = x[p.src ? __ldg(&p.src[s]) : s];  // the committed position, unsorted when src is set
         if (!MIXED && p.frame) {  // the committed state is cell + offset: into the scene frame
             const int3 co = unpack_cell(cp, xo.w);
             xo = make_float4(__fmaf_rn((float)co.x, p.cell, xo.x), __fmaf_rn((float)co.y, p.cell, xo.y),

@@ -395,11 +395,13 @@ __global__ void __launch_bounds__(STAB_THREADS) k_stabilize_gather(
     const int* __restrict__ tie, int n, const float4* __restrict__ x, const float4* __restrict__ xs,
     const float4* __restrict__ v, const int* __restrict__ id, int* __restrict__ key_out,
     float4* __restrict__ x_out, float4* __restrict__ xs_out, float4* __restrict__ v_out, int* __restrict__ id_out,
-    const int* __restrict__ aux_in, int* __restrict__ aux_out, int* __restrict__ slot_of) {
+    const int* __restrict__ aux_in, int* __restrict__ aux_out, int* __restrict__ slot_of,
+    int* __restrict__ src_out) {
     pdl_wait();
     stabilize_block(tmp, aux, key, start, tie, n, [&](int f, int i) {
         key_out[f] = key[i];
-        x_out[f] = x[i];
+        if (x_out) x_out[f] = x[i];
+        if (src_out) src_out[f] = i;  // the committed position stays at i
         xs_out[f] = xs[i];
         if (v) v_out[f] = v[i];
         if (id) id_out[f] = id[i];
@@ -481,13 +483,13 @@ void launch_sort_tail(const int* key, int* rank, const int* start, const int* ti
 void launch_sort_state(const int* key, int* rank, const int* start, const int* tie, int n,
                        int* tmp, const float4* x, const float4* xs, const float4* v, const int* id,
                        int* key_out, float4* x_out, float4* xs_out, float4* v_out, int* id_out,
-                       const int* aux, int* aux_out, int* slot_of, cudaStream_t st) {
+                       const int* aux, int* aux_out, int* slot_of, int* src_out, cudaStream_t st) {
     if (n <= 0) return;
     const bool pdl = pdl_enabled();
     launch_k(k_scatter_index, blocks_for(n, 256), 256, st, pdl, key, (const int*)rank, start, n, tmp);
     // the rank array, read by the scatter only, is the big cells' merge space
     launch_k(k_stabilize_gather, blocks_for(n, STAB_THREADS), STAB_THREADS, st, pdl, tmp, rank, key, start, tie,
-             n, x, xs, v, id, key_out, x_out, xs_out, v_out, id_out, aux, aux_out, slot_of);
+             n, x, xs, v, id, key_out, x_out, xs_out, v_out, id_out, aux, aux_out, slot_of, src_out);
 }
 
 void launch_gather_solid(const int* perm, int n, const float4* src, float4* dst, cudaStream_t st) {
