@@ -92,6 +92,8 @@ struct StepParams {
     float inv_hdq2;       // 1 / (h^2 - dq^2) (0 when dq >= h: no s_corr)
     float mass, rho0, eps;
     float mr;             // mass / rho0
+    float lam_c2;         // (Ks mass / rho0)^2, the lambda denominator's factor
+    float inv_rho0;       // 1 / rho0
     float self_density;   // m W(0) = m K6 h^6 (the particle's own density term)
     float inv_dt;
     float dq, sk, sn;     // s_corr distance, k and exponent

@@ -144,6 +144,11 @@ static int derive(const lustrine_pbf_params& q, int n, int ns, StepParams* sp, C
     p.mass = q.mass;
     p.rho0 = q.rest_density;
     p.mr = q.mass / q.rest_density;
+    {
+        const float c = p.ks * p.mr;  // float products, as the kernels formed them
+        p.lam_c2 = c * c;
+    }
+    p.inv_rho0 = 1.0f / q.rest_density;
     p.eps = q.relaxation_epsilon;
     p.dq = q.s_corr_dq;
     p.sk = q.s_corr_k;
