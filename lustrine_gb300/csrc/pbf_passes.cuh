@@ -311,7 +311,23 @@ __device__ __forceinline__ void lists_lambda(const StepParams& p, const CellPack
     const int slab = g.gx * g.gz;
     // static particles only where the cell's neighbourhood holds some
     const bool solids = p.ns > 0 && p.solid_near && __ldg(&p.solid_near[__ldg(&key_sorted[s])]);
-    if (!HASHED) {
+    if (!HASHED && COMPACT) {
+        // each row's two bounds loaded just before its walk (fewer live
+        // registers than a layer's six: more resident warps for this
+        // issue-bound kernel)
+        const int z0 = max(c.z - 1, 0), z1 = min(c.z + 1, g.gz - 1);
+        for (int dy = -1; dy <= 1; dy++) {
+            const int y = c.y + dy;
+            if (y < 0 || y >= g.gy) continue;
+            for (int dx = -1; dx <= 1; dx++) {
+                const int xx = c.x + dx;
+                if (xx < 0 || xx >= g.gx) continue;
+                const int row = g.off + y * slab + xx * g.gz;
+                walk_range<MIXED, false, KAHAN, Lists, 2>(p, self, s, xs, fstart[row + z0], fstart[row + z1 + 1], 0, 0,
+                                                          z0 - c.z, dx, dy, a, c_n, out);
+            }
+        }
+    } else if (!HASHED) {
         const int z0 = max(c.z - 1, 0), z1 = min(c.z + 1, g.gz - 1);
         for (int dy = -1; dy <= 1; dy++) {
             const int y = c.y + dy;
