@@ -222,8 +222,9 @@ __device__ __forceinline__ void walk_row(const StepParams& p, const float4& self
 // The candidates [t_begin, t_end) of one row, gathered W at a time (the
 // loads of a chunk are in flight together; the tests run in slot order, so
 // the list is the one walk_row builds).  W = 4; the compact list build takes
-// 2, which fits it in 55-56 registers (9 blocks of 128 per SM; config 3
-// lists 0.522 -> 0.504 ms at step 50 of the run).  b1, b2: the row's cell bounds, read
+// 2 and loads each row's bounds just before the row, which fits it in 48-50
+// registers (10 blocks of 128 per SM; config 3 lists 0.522 -> 0.493 ms at
+// step 50 of the run, both steps together).  b1, b2: the row's cell bounds, read
 // in mixed precision only (the entry's dz code and the cell shift; fp32
 // entries carry dz = 0, which no fp32 pass reads).
 template <bool MIXED, bool SOLID, bool KAHAN, class L, int W = 4>
