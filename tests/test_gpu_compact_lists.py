@@ -132,6 +132,35 @@ def test_wide_records_give_the_column_bits(precision):
         np.testing.assert_array_equal(idx0, idx)
 
 
+def test_compact_lists_follow_particles_in_and_out():
+    """Sources and sinks change the particle count between steps (the records
+    and the sentinel slot n move with it): spawning and despawning the same
+    particles in a compact and a column context gives the same bits."""
+    from lustrine_gb300 import LISTS_COLUMN, LISTS_COMPACT, PbfSim, scenes
+    sc = scenes.config0(seed=49)
+    rng = np.random.default_rng(50)
+    add = scenes.jitter(scenes.lattice((6, 4, 6), (2, 30, 2)), 0.05, rng)
+    res = []
+    for lf in (LISTS_COLUMN, LISTS_COMPACT):
+        sim = PbfSim(_params(sc, 0), sc.n)
+        sim.reserve(sc.n + 2 * len(add))
+        sim.upload(sc.x)
+        sim.set_tuning(128, 2, 128, 2, 1, list_format=lf)
+        sim.step(sc.dt, 2)
+        sim.spawn(add)
+        sim.step(sc.dt, 2)
+        removed = sim.despawn_cells(np.arange(0, 4000, 7, dtype=np.int32))
+        sim.step(sc.dt, 2)
+        sim.spawn(add + np.float32(1.5))
+        sim.step(sc.dt, 2)
+        assert sim.status() == 0
+        res.append((removed, sim.n, sim.list_format(), sim.download(lambdas=True, density=True)))
+        sim.close()
+    assert res[1][2] == "compact"
+    assert res[0][:2] == res[1][:2]
+    _assert_same(res[0][3], res[1][3])
+
+
 @pytest.mark.parametrize("precision", [0, 2])
 def test_compact_batch_equals_column_batch(precision):
     """48 scenes of the batched distribution (the smaller ones, 1,029 to about
