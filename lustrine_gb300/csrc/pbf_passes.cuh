@@ -174,13 +174,9 @@ template <bool WIDE>
 __device__ __forceinline__ void close_lists(const StepParams& p, const CompactLists<WIDE>& l, int*, int c_n) {
     using RF = RecordFormat<WIDE>;
     const unsigned* w = l.stage;
-    if (WIDE) {
-        p.rec[l.s] = make_uint4((unsigned)c_n, w[0], w[1], w[2]);
-        if (c_n > RF::INLINE) p.rec2[l.s] = make_uint4(w[3], w[4], w[5], w[6]);
-    } else {
-        p.rec[l.s] = make_uint4((unsigned)c_n | ((unsigned)l.base << 8), w[0], w[1], w[2]);
-        if (c_n > RF::INLINE) p.rec2[l.s] = make_uint4(w[3], w[4], w[5], w[6]);
-    }
+    const unsigned head = WIDE ? (unsigned)c_n : ((unsigned)c_n | ((unsigned)l.base << 8));
+    p.rec[l.s] = make_uint4(head, w[0], w[1], w[2]);
+    if (c_n > RF::INLINE) p.rec2[l.s] = make_uint4(w[3], w[4], w[5], w[6]);
     for (int k = c_n - RF::RECORDS; k > 0 && k % p.pad != 0; k++) l.ovf[(size_t)k * p.n + l.s] = p.n;
 }
 
