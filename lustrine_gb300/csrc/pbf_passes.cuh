@@ -132,6 +132,13 @@ struct CompactLists {
         else
             reinterpret_cast<unsigned short*>(stage)[k] = (unsigned short)(t - base);
     }
+    // entry k < count of the list put so far (the thread reads back its own stores)
+    __device__ __forceinline__ int get(int k) const {
+        constexpr int R = RecordFormat<WIDE>::RECORDS;
+        if (k >= R) return ovf[(size_t)(k - R) * n + s];
+        if (WIDE) return (int)stage[k];
+        return base + reinterpret_cast<const unsigned short*>(stage)[k];
+    }
 };
 
 // 0: column lists; 1: compact; 2: compact in wide records
@@ -180,12 +187,24 @@ __device__ __forceinline__ void close_lists(const StepParams& p, const CompactLi
     for (int k = c_n - RF::RECORDS; k > 0 && k % p.pad != 0; k++) l.ovf[(size_t)k * p.n + l.s] = p.n;
 }
 
+// A candidate within h, the c_n-th accepted.  PH 0: listed (below the
+// capacity) and summed into the first lambda; PH 1: listed only (the sums
+// run over the list afterwards); PH 2: summed only if past the capacity (the
+// entries the list dropped, after the listed ones' sums).
+template <int PH, bool KAHAN, bool SOLID, class L>
+__device__ __forceinline__ void accept(const StepParams& p, LambdaAcc& a, const float3& d, int& c_n, L& out, int t,
+                                       int dx, int dy, int dz) {
+    if (PH != 2 && c_n < p.max_nbrs) out.put(c_n, t, dx, dy, dz, SOLID);
+    if (PH == 0 || (PH == 2 && c_n >= p.max_nbrs)) lambda_accumulate<KAHAN>(p, a, d, SOLID);
+    c_n++;
+}
+
 // One row (dy, dx) of the stencil: the cells z0..z1 of a row are consecutive
 // ids, so their particles form one slot range, walked in one loop (a warp
 // then runs as many rounds as its fullest row, not the sum over the three
 // cells of its fullest cell); a candidate's dz follows from the cell bounds,
 // loaded once per row.  The candidates come in the same order as cell by cell.
-template <bool MIXED, bool SOLID, bool KAHAN, class L>
+template <bool MIXED, bool SOLID, bool KAHAN, class L, int PH = 0>
 __device__ __forceinline__ void walk_row(const StepParams& p, const float4& self, int s,
                                          const float4* __restrict__ pos, const int* __restrict__ start,
                                          int row, int zc, int gz, int dx, int dy, LambdaAcc& a, int& c_n,
@@ -207,23 +226,19 @@ __device__ __forceinline__ void walk_row(const StepParams& p, const float4& self
             d.y = __fadd_rn(d.y, sy);
             d.z = __fadd_rn(d.z, -(float)dz * p.cell);
         }
-        if (dot3e(d.x, d.y, d.z) <= p.h2) {
-            if (c_n < p.max_nbrs) out.put(c_n, t, dx, dy, dz, SOLID);
-            c_n++;
-            lambda_accumulate<KAHAN>(p, a, d, SOLID);
-        }
+        if (dot3e(d.x, d.y, d.z) <= p.h2) accept<PH, KAHAN, SOLID>(p, a, d, c_n, out, t, dx, dy, dz);
     }
 }
 
 // The candidates [t_begin, t_end) of one row, gathered W at a time (the
 // loads of a chunk are in flight together; the tests run in slot order, so
 // the list is the one walk_row builds).  W = 4; the compact list build takes
-// 2 and loads each row's bounds just before the row, which fits it in 48-50
-// registers (10 blocks of 128 per SM; config 3 lists 0.522 -> 0.493 ms at
-// step 50 of the run, both steps together).  b1, b2: the row's cell bounds, read
+// 2 and loads each row's bounds just before the row, for fewer live
+// registers (config 3 lists 0.522 -> 0.493 ms at step 50 of the run, both
+// steps together).  b1, b2: the row's cell bounds, read
 // in mixed precision only (the entry's dz code and the cell shift; fp32
 // entries carry dz = 0, which no fp32 pass reads).
-template <bool MIXED, bool SOLID, bool KAHAN, class L, int W = 4>
+template <bool MIXED, bool SOLID, bool KAHAN, class L, int W = 4, int PH = 0>
 __device__ __forceinline__ void walk_range(const StepParams& p, const float4& self, int s,
                                            const float4* __restrict__ pos, int t_begin, int t_end, int b1, int b2,
                                            int dz0, int dx, int dy, LambdaAcc& a, int& c_n, L& out) {
@@ -244,18 +259,14 @@ __device__ __forceinline__ void walk_range(const StepParams& p, const float4& se
                 d.y = __fadd_rn(d.y, sy);
                 d.z = __fadd_rn(d.z, -(float)dz * p.cell);
             }
-            if (dot3e(d.x, d.y, d.z) <= p.h2) {
-                if (c_n < p.max_nbrs) out.put(c_n, t, dx, dy, dz, SOLID);
-                c_n++;
-                lambda_accumulate<KAHAN>(p, a, d, SOLID);
-            }
+            if (dot3e(d.x, d.y, d.z) <= p.h2) accept<PH, KAHAN, SOLID>(p, a, d, c_n, out, t, dx, dy, dz);
         }
     }
 }
 
 // One cell of the stencil on a hashed grid: the particles of its bucket,
 // kept only if they belong to that cell.
-template <bool MIXED, bool SOLID, bool KAHAN, class L>
+template <bool MIXED, bool SOLID, bool KAHAN, class L, int PH = 0>
 __device__ __forceinline__ void walk_hashed_cell(const StepParams& p, const float4& self, int s,
                                                  const float4* __restrict__ pos,
                                                  const int* __restrict__ start,
@@ -271,43 +282,22 @@ __device__ __forceinline__ void walk_hashed_cell(const StepParams& p, const floa
             d.y = __fadd_rn(d.y, sy);
             d.z = __fadd_rn(d.z, sz);
         }
-        if (dot3e(d.x, d.y, d.z) <= p.h2) {
-            if (c_n < p.max_nbrs) out.put(c_n, t, dx, dy, dz, SOLID);
-            c_n++;
-            lambda_accumulate<KAHAN>(p, a, d, SOLID);
-        }
+        if (dot3e(d.x, d.y, d.z) <= p.h2) accept<PH, KAHAN, SOLID>(p, a, d, c_n, out, t, dx, dy, dz);
     }
 }
 
-// FRAME: mixed storage with the iterations in the scene frame (positions
-// relative to the box corner, compensated density sums; the walk's cell is
-// the step's key, which rounding of the frame position could move).
-// FORMAT 1 or 2: compact lists (in wide records with 2) to p.rec (no cell
-// codes, no static particles).
-template <bool MIXED, bool HASHED, bool FRAME, int FORMAT>
-__device__ __forceinline__ void lists_lambda(const StepParams& p, const CellPack& cp, float4* __restrict__ xs,
-                                             const int* __restrict__ key_sorted, const int* __restrict__ cell_sorted,
-                                             const int* __restrict__ fstart, const float4* __restrict__ solid,
-                                             const int* __restrict__ solid_cell, const int* __restrict__ sstart,
-                                             int* __restrict__ nbr, int* __restrict__ cnt, float* __restrict__ rho,
-                                             int* status, unsigned* stage = nullptr) {
-    pdl_wait();
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= p.n) return;
-    const float4 self = xs[s];
-    const Geo g = geo_slot(p, s);
-    // fp32 on a dense grid: the cell the prediction keyed this position by
-    constexpr bool KAHAN = MIXED || FRAME;
-    const int3 c = (MIXED || HASHED || FRAME) ? slot_cell(p, cp, g, key_sorted, cell_sorted, s)
-                                              : plain_cell(p, g, self.x, self.y, self.z);
-    LambdaAcc a = lambda_init(p);
-    int c_n = 0;
-    constexpr bool COMPACT = FORMAT != 0;
-    using Lists = typename ListsOf<FORMAT>::T;
-    Lists out = open_lists((Lists*)nullptr, nbr, p.n, s, g.slot0, stage);
+// The stencil's candidates of fluid slot s in cell c, in list order: on a
+// dense grid the nine rows (with the static particles of each row after its
+// fluid ones where the neighbourhood holds some); on a hashed grid the
+// cells' buckets.  PH: what each accepted candidate does (accept()).
+template <int PH, bool MIXED, bool HASHED, bool KAHAN, bool COMPACT, class Lists>
+__device__ __forceinline__ void walk_stencil(const StepParams& p, const CellPack& cp, const float4& self, int s,
+                                             const int3& c, const Geo& g, const float4* __restrict__ xs,
+                                             const int* __restrict__ cell_sorted, const int* __restrict__ fstart,
+                                             const float4* __restrict__ solid, const int* __restrict__ solid_cell,
+                                             const int* __restrict__ sstart, bool solids, LambdaAcc& a, int& c_n,
+                                             Lists& out) {
     const int slab = g.gx * g.gz;
-    // static particles only where the cell's neighbourhood holds some
-    const bool solids = p.ns > 0 && p.solid_near && __ldg(&p.solid_near[__ldg(&key_sorted[s])]);
     if (!HASHED && COMPACT) {
         // each row's two bounds loaded just before its walk (fewer live
         // registers than a layer's six: more resident warps for this
@@ -320,8 +310,8 @@ __device__ __forceinline__ void lists_lambda(const StepParams& p, const CellPack
                 const int xx = c.x + dx;
                 if (xx < 0 || xx >= g.gx) continue;
                 const int row = g.off + y * slab + xx * g.gz;
-                walk_range<MIXED, false, KAHAN, Lists, 2>(p, self, s, xs, fstart[row + z0], fstart[row + z1 + 1], 0, 0,
-                                                          z0 - c.z, dx, dy, a, c_n, out);
+                walk_range<MIXED, false, KAHAN, Lists, 2, PH>(p, self, s, xs, fstart[row + z0], fstart[row + z1 + 1],
+                                                              0, 0, z0 - c.z, dx, dy, a, c_n, out);
             }
         }
     } else if (!HASHED) {
@@ -349,11 +339,11 @@ __device__ __forceinline__ void lists_lambda(const StepParams& p, const CellPack
             for (int r = 0; r < 3; r++) {
                 const int xx = c.x + r - 1;
                 if (xx < 0 || xx >= g.gx) continue;
-                walk_range<MIXED, false, KAHAN, Lists, COMPACT ? 2 : 4>(p, self, s, xs, b0[r], b3[r], b1[r], b2[r],
-                                                                     z0 - c.z, r - 1, dy, a, c_n, out);
+                walk_range<MIXED, false, KAHAN, Lists, COMPACT ? 2 : 4, PH>(p, self, s, xs, b0[r], b3[r], b1[r], b2[r],
+                                                                         z0 - c.z, r - 1, dy, a, c_n, out);
                 if (solids)
-                    walk_row<MIXED, true, KAHAN>(p, self, s, solid, sstart, g.off + y * slab + xx * g.gz, c.z, g.gz,
-                                                 r - 1, dy, a, c_n, out);
+                    walk_row<MIXED, true, KAHAN, Lists, PH>(p, self, s, solid, sstart, g.off + y * slab + xx * g.gz,
+                                                            c.z, g.gz, r - 1, dy, a, c_n, out);
             }
         }
     }
@@ -370,18 +360,79 @@ __device__ __forceinline__ void lists_lambda(const StepParams& p, const CellPack
                 const int z0 = max(c.z - 1, 0), z1 = min(min(c.z + 1, g.gz - 1), (int)cp.mz);
                 for (int z = z0; z <= z1; z++) {
                     const int3 cn = make_int3(xx, y, z);
-                    walk_hashed_cell<MIXED, false, KAHAN>(p, self, s, xs, fstart, cell_sorted,
-                                                   cell_bucket(cn, p.hash_bits), (int)pack_bits(cp, cn),
-                                                   dx, dy, z - c.z, a, c_n, out);
+                    walk_hashed_cell<MIXED, false, KAHAN, Lists, PH>(p, self, s, xs, fstart, cell_sorted,
+                                                                     cell_bucket(cn, p.hash_bits),
+                                                                     (int)pack_bits(cp, cn), dx, dy, z - c.z, a, c_n,
+                                                                     out);
                 }
                 if (solids)
                     for (int z = z0; z <= z1; z++) {
                         const int3 cn = make_int3(xx, y, z);
-                        walk_hashed_cell<MIXED, true, KAHAN>(p, self, s, solid, sstart, solid_cell,
-                                                      cell_bucket(cn, p.hash_bits), (int)pack_bits(cp, cn),
-                                                      dx, dy, z - c.z, a, c_n, out);
+                        walk_hashed_cell<MIXED, true, KAHAN, Lists, PH>(p, self, s, solid, sstart, solid_cell,
+                                                                        cell_bucket(cn, p.hash_bits),
+                                                                        (int)pack_bits(cp, cn), dx, dy, z - c.z, a,
+                                                                        c_n, out);
                     }
             }
+        }
+    }
+}
+
+// FRAME: mixed storage with the iterations in the scene frame (positions
+// relative to the box corner, compensated density sums; the walk's cell is
+// the step's key, which rounding of the frame position could move).
+// FORMAT 1 or 2: compact lists (in wide records with 2) to p.rec (no cell
+// codes, no static particles).  Column lists sum the first lambda as the
+// walk accepts each candidate.  Compact lists walk first (the accepted
+// candidates only listed: fewer instructions in the walk's divergent rounds,
+// where the sums of any one lane's accepted candidate held the whole warp)
+// and then sum over the finished list, two entries' positions loaded
+// together (in the cache from the walk); a list cut at the capacity walks
+// once more to sum the dropped entries after the listed ones.  The terms
+// and their order are the walk's, so the sums equal the column lists'.
+template <bool MIXED, bool HASHED, bool FRAME, int FORMAT>
+__device__ __forceinline__ void lists_lambda(const StepParams& p, const CellPack& cp, float4* __restrict__ xs,
+                                             const int* __restrict__ key_sorted, const int* __restrict__ cell_sorted,
+                                             const int* __restrict__ fstart, const float4* __restrict__ solid,
+                                             const int* __restrict__ solid_cell, const int* __restrict__ sstart,
+                                             int* __restrict__ nbr, int* __restrict__ cnt, float* __restrict__ rho,
+                                             int* status, unsigned* stage = nullptr) {
+    pdl_wait();
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= p.n) return;
+    const float4 self = xs[s];
+    const Geo g = geo_slot(p, s);
+    // fp32 on a dense grid: the cell the prediction keyed this position by
+    constexpr bool KAHAN = MIXED || FRAME;
+    const int3 c = (MIXED || HASHED || FRAME) ? slot_cell(p, cp, g, key_sorted, cell_sorted, s)
+                                              : plain_cell(p, g, self.x, self.y, self.z);
+    LambdaAcc a = lambda_init(p);
+    int c_n = 0;
+    constexpr bool COMPACT = FORMAT != 0;
+    using Lists = typename ListsOf<FORMAT>::T;
+    Lists out = open_lists((Lists*)nullptr, nbr, p.n, s, g.slot0, stage);
+    // static particles only where the cell's neighbourhood holds some
+    const bool solids = p.ns > 0 && p.solid_near && __ldg(&p.solid_near[__ldg(&key_sorted[s])]);
+    walk_stencil<COMPACT ? 1 : 0, MIXED, HASHED, KAHAN, COMPACT>(p, cp, self, s, c, g, xs, cell_sorted, fstart, solid,
+                                                                 solid_cell, sstart, solids, a, c_n, out);
+    if constexpr (COMPACT) {
+        // compact lists hold fluid slots only, with fp32 offsets: d as the walk formed it
+        const int m = min(c_n, p.max_nbrs);
+        for (int k = 0; k < m; k += 2) {
+            const bool two = k + 1 < m;
+            const float4 q0 = xs[out.get(k)];
+            const float4 q1 = two ? xs[out.get(k + 1)] : q0;
+            lambda_accumulate<KAHAN>(
+                p, a, make_float3(__fsub_rn(self.x, q0.x), __fsub_rn(self.y, q0.y), __fsub_rn(self.z, q0.z)), false);
+            if (two)
+                lambda_accumulate<KAHAN>(
+                    p, a, make_float3(__fsub_rn(self.x, q1.x), __fsub_rn(self.y, q1.y), __fsub_rn(self.z, q1.z)),
+                    false);
+        }
+        if (c_n > p.max_nbrs) {
+            int c2 = 0;
+            walk_stencil<2, MIXED, HASHED, KAHAN, COMPACT>(p, cp, self, s, c, g, xs, cell_sorted, fstart, solid,
+                                                           solid_cell, sstart, solids, a, c2, out);
         }
     }
     if (c_n > p.max_nbrs) {
@@ -409,8 +460,12 @@ __global__ void __launch_bounds__(B) k_lists_lambda(StepParams p, CellPack cp, f
 }
 
 // Compact lists (no static particles, fp32 pair offsets; WIDE: wide records).
+// Held to 12 blocks of 128 threads per SM (40 registers, a few bytes
+// spilled): the walk waits on its gathers, not on issue slots, so the extra
+// resident warps pay (config 3: 0.382 -> 0.353 ms a step; a walk that
+// loads the next row's bounds ahead, or 4 gathers in flight, was slower).
 template <bool HASHED, int B, bool FRAME, bool WIDE>
-__global__ void __launch_bounds__(B) k_lists_compact(StepParams p, CellPack cp, float4* __restrict__ xs,
+__global__ void __launch_bounds__(B, 1536 / B) k_lists_compact(StepParams p, CellPack cp, float4* __restrict__ xs,
                                                              const int* __restrict__ key_sorted,
                                                              const int* __restrict__ cell_sorted,
                                                              const int* __restrict__ fstart,
