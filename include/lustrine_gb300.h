@@ -446,8 +446,9 @@ LUSTRINE_API int lustrine_pbf_profile_step(lustrine_pbf* s, float dt, double* st
  * batches only, LUSTRINE_SOLVER_* and the on-chip solve's threads per CTA
  * (512 or 1024; 0: unchanged); list_format: LUSTRINE_LISTS_COLUMN or
  * LUSTRINE_LISTS_COMPACT (compact lists apply in PBF mode, fp32 or
- * LUSTRINE_PRECISION_MIXED_SCENE, with max_neighbors <= 255, no static
- * particles and one particle per thread: 16-bit entries for scenes of at most
+ * LUSTRINE_PRECISION_MIXED_SCENE, with max_neighbors <= 255, an s_corr_n
+ * that is an integer in [0, 32], no static particles and one particle per
+ * thread: 16-bit entries for scenes of at most
  * 65,535 in contexts of fewer than 2^24 fluid particles, wide records
  * otherwise; elsewhere the step keeps column lists whatever list_format
  * says). */

@@ -249,8 +249,9 @@ int lgb_write_sentinel(lustrine_pbf* s) {
 }
 
 // The compact neighbour lists the context's steps can use: PBF mode in fp32
-// or the scene frame (no cell codes in the entries) and lists of at most
-// COMPACT_MAX_NBRS entries; 16-bit entries (LUSTRINE_LISTS_COMPACT) for
+// or the scene frame (no cell codes in the entries), lists of at most
+// COMPACT_MAX_NBRS entries and an s_corr exponent that is an integer in
+// [0, 32] (the compact position pass is built without powf); 16-bit entries (LUSTRINE_LISTS_COMPACT) for
 // fewer than COMPACT_MAX_N fluid slots in scenes of at most
 // COMPACT_MAX_SCENE (one scene: the capacity), wide records
 // (LUSTRINE_LISTS_COMPACT_WIDE) otherwise; LUSTRINE_LISTS_COLUMN when none.
@@ -258,7 +259,7 @@ int lgb_write_sentinel(lustrine_pbf* s) {
 // thread, and the context holds no static particles.
 static int compact_capable(const lustrine_pbf* s) {
     if (s->prm.mode != LUSTRINE_MODE_PBF || (s->mixed() && !s->sp.frame)) return LUSTRINE_LISTS_COLUMN;
-    if (s->sp.max_nbrs > COMPACT_MAX_NBRS) return LUSTRINE_LISTS_COLUMN;
+    if (s->sp.max_nbrs > COMPACT_MAX_NBRS || s->sp.sn_int < 0) return LUSTRINE_LISTS_COLUMN;
     int largest = s->cap;
     if (s->is_batch()) largest = *std::max_element(s->b_nfluid.begin(), s->b_nfluid.end());
     return (largest <= COMPACT_MAX_SCENE && s->cap < COMPACT_MAX_N) ? LUSTRINE_LISTS_COMPACT

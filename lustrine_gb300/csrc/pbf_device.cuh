@@ -169,6 +169,11 @@ __device__ __forceinline__ float spiky_g(const StepParams& p, float r, float inv
     return __fmul_rn(__fmul_rn(f, f), inv_r);
 }
 
+// POW false: the exponent is an integer in [0, 32] (sn_int >= 0), and the
+// powf branch is left out (inlined once per gather of an unrolled walk, its
+// registers made the position pass over compact lists spill 100 bytes at 32
+// registers although the default exponent, 4, never takes it).
+template <bool POW = true>
 __device__ __forceinline__ float scorr_hd(const StepParams& p, float hd) {
     const float x = __fmul_rn(hd, p.inv_hdq2);
     float pw;
@@ -177,7 +182,7 @@ __device__ __forceinline__ float scorr_hd(const StepParams& p, float hd) {
         pw = __fmul_rn(__fmul_rn(x4, x4), x4);
     } else {
         const float t = __fmul_rn(__fmul_rn(x, x), x);
-        if (p.sn_int >= 0) {
+        if (!POW || p.sn_int >= 0) {
             pw = 1.0f;
             for (int e = 0; e < p.sn_int; e++) pw = __fmul_rn(pw, t);
         } else {

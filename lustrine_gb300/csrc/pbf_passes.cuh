@@ -708,7 +708,7 @@ struct DeltaAcc {
     int nct;
 };
 
-template <bool MIXED, bool SOL>
+template <bool MIXED, bool SOL, bool POW = true>
 __device__ __forceinline__ void delta_pair(const StepParams& p, DeltaAcc& a, const float4& self, int e, float4 q,
                                            const float4* tab) {
     const float li = self.w;
@@ -718,7 +718,7 @@ __device__ __forceinline__ void delta_pair(const StepParams& p, DeltaAcc& a, con
     const float inv_r = inv_r_of(r2);
     const float r = __fmul_rn(r2, inv_r);
     const float lj = sol ? li : q.w;
-    const float w = __fmul_rn(__fadd_rn(__fadd_rn(li, lj), scorr_hd(p, hdiff(p, r2))), spiky_g(p, r, inv_r));
+    const float w = __fmul_rn(__fadd_rn(__fadd_rn(li, lj), scorr_hd<POW>(p, hdiff(p, r2))), spiky_g(p, r, inv_r));
     a.px = __fmaf_rn(w, d.x, a.px);
     a.py = __fmaf_rn(w, d.y, a.py);
     a.pz = __fmaf_rn(w, d.z, a.pz);
@@ -788,8 +788,9 @@ __device__ __forceinline__ void delta_finish(const StepParams& p, const CellPack
 // With one particle per thread and up to 2 gathers in flight the kernel
 // fits 40 registers without spilling: 6 blocks of 256 threads per SM instead
 // of 5 (a 262,144-particle pass then takes 1.12 waves of the GPU instead of
-// 1.35).  Compact lists with one gather in flight fit 32 registers (8 bytes
-// spilled): 16 blocks of 128 threads per SM, the whole SM's warps.  P = 2:
+// 1.35).  Compact lists with one gather in flight fit 32 registers without
+// spilling (their steps have an integer s_corr exponent: no powf): 16 blocks
+// of 128 threads per SM, the whole SM's warps.  P = 2:
 // two particles per thread (B apart), their lists walked together.
 template <int F, int U, int B, int P = 1>
 __global__ void __launch_bounds__(B, ((F & 8) && U == 1) ? 2048 / B : ((U <= 2 && P == 1) ? 1536 / B : 1))
@@ -811,7 +812,7 @@ __global__ void __launch_bounds__(B, ((F & 8) && U == 1) ? 2048 / B : ((U <= 2 &
         if (COMPACT) {
             walk_compact<U, WIDE, float4>(
                 p, __ldg(&p.rec[s]), p.rec2 + s, nbr + s, [&](int t) { return xs[t]; },
-                [&](int t, float4 q) { delta_pair<false, false>(p, a, self, t, q, shift_tab); });
+                [&](int t, float4 q) { delta_pair<false, false, false>(p, a, self, t, q, shift_tab); });
         } else {
             for_each_entry<U, SOL, LIST_PAD_MAX>(p, nbr + s, cnt, s, xs, solid, [&](int e, float4 q) {
                 delta_pair<MIXED, SOL>(p, a, self, e, q, shift_tab);

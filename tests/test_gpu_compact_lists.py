@@ -188,7 +188,8 @@ def test_compact_lists_only_where_they_apply():
     """Scenes of 65,535 particles take 16-bit entries, 65,536 wide records
     (one 16-bit value is kept for the sentinel); static particles, the
     cell-relative mixed form (cell codes in the entries), two particles per
-    thread and the reference's step keep column lists."""
+    thread, an s_corr exponent that is not an integer in [0, 32] and the
+    reference's step keep column lists."""
     from lustrine_gb300 import (LISTS_COMPACT, MODE_REFERENCE, PRECISION_MIXED, PbfSim, pbf_params,
                                 reference_params, scenes)
     rng = np.random.default_rng(43)
@@ -209,6 +210,8 @@ def test_compact_lists_only_where_they_apply():
     small = big[:4000]
     assert fmt_of(pbf_params(130, 40, 130, precision=PRECISION_MIXED), small) == "column"
     assert fmt_of(pbf_params(130, 40, 130), small, ppt=2) == "column"
+    assert fmt_of(pbf_params(130, 40, 130, s_corr_n=2.5), small) == "column"
+    assert fmt_of(pbf_params(130, 40, 130, s_corr_n=3.0), small) == "compact"
     solid, _ = scenes.heightmap_solids(16, 300, origin=(0, 0, 0), rng=rng, max_height=2)
     assert fmt_of(pbf_params(130, 40, 130), small, solids=solid) == "column"
     rp = reference_params(130, 40, 130, 0.5, 2.0)
