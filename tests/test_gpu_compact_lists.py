@@ -55,19 +55,23 @@ def test_compact_lists_give_the_column_bits(precision):
         np.testing.assert_array_equal(idx0, idx)
 
 
+@pytest.mark.parametrize("grid", ["dense", "hashed"])
 @pytest.mark.parametrize("unroll", [1, 2, 4, 8])
 @pytest.mark.parametrize("dims,fmt_expected", [((14, 12, 14), "compact"), ((42, 40, 42), "compact_wide")])
-def test_compact_overflow_rows(unroll, dims, fmt_expected):
+def test_compact_overflow_rows(grid, unroll, dims, fmt_expected):
     """A block at spacing 0.6 h: about 18 neighbours a particle, so every list
     fills both records and runs on into the overflow rows (padded with the
     sentinel to the chunk); 2,352 particles take 16-bit entries, 70,560 wide
-    records.  Results and lists equal the column lists'."""
+    records.  On the dense grid (a stencil row's cells walked as one slot
+    range) and the hashed grid (each cell's bucket walked on its own) the
+    results and lists equal the column lists'."""
     from lustrine_gb300 import LISTS_COLUMN, LISTS_COMPACT, scenes
+    from lustrine_gb300._lib import GRID_DENSE, GRID_HASHED
     rng = np.random.default_rng(42)
     x = scenes.jitter(scenes.lattice(dims, (4, 1, 4)) * 0.6, 0.05, rng)
     box = int(np.ceil(0.6 * max(dims))) + 6
     sc = scenes.Scene("dense", (box, box, box), x.astype(np.float32), dt=1 / 60, iterations=4)
-    p = _params(sc, 0)
+    p = _params(sc, 0, grid_mode=GRID_HASHED if grid == "hashed" else GRID_DENSE)
     ref, _, cnt0, idx0 = _run(sc, p, LISTS_COLUMN, unroll, unroll, steps=2)
     got, fmt, cnt, idx = _run(sc, p, LISTS_COMPACT, unroll, unroll, steps=2)
     assert fmt == fmt_expected
@@ -77,19 +81,23 @@ def test_compact_overflow_rows(unroll, dims, fmt_expected):
     np.testing.assert_array_equal(idx0, idx)
 
 
+@pytest.mark.parametrize("grid", ["dense", "hashed"])
 @pytest.mark.parametrize("max_nbrs", [5, 8, 16])
-def test_compact_lists_at_their_capacity(max_nbrs):
+def test_compact_lists_at_their_capacity(grid, max_nbrs):
     """Lists cut at max_neighbors (5: inside the first record; 8: into the
-    second; 16: past both into the overflow rows) on the dense block: the
-    overflow status is raised, and results and the truncated lists equal the
-    column lists'."""
+    second; 16: past both into the overflow rows) on the dense block, on the
+    dense and the hashed grid: the overflow status is raised, and results
+    (the first lambda sums the dropped entries after the listed ones) and
+    the truncated lists equal the column lists'."""
     from lustrine_gb300 import LISTS_COLUMN, LISTS_COMPACT, PbfSim, scenes
+    from lustrine_gb300._lib import GRID_DENSE, GRID_HASHED
     rng = np.random.default_rng(45)
     x = scenes.jitter(scenes.lattice((14, 12, 14), (4, 1, 4)) * 0.6, 0.05, rng).astype(np.float32)
     sc = scenes.Scene("dense", (16, 16, 16), x, dt=1 / 60, iterations=4)
+    gm = GRID_HASHED if grid == "hashed" else GRID_DENSE
     res = []
     for lf in (LISTS_COLUMN, LISTS_COMPACT):
-        sim = PbfSim(_params(sc, 0, max_neighbors=max_nbrs), sc.n)
+        sim = PbfSim(_params(sc, 0, max_neighbors=max_nbrs, grid_mode=gm), sc.n)
         sim.upload(sc.x)
         sim.set_tuning(128, 2, 128, 2, 1, list_format=lf)
         sim.step(sc.dt)
