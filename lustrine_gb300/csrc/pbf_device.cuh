@@ -89,6 +89,13 @@ __device__ __forceinline__ Geo geo_slot(const StepParams& p, int s) {
 __device__ __forceinline__ int scene_index(const StepParams& p, int s) {
     return p.scenes ? __ldg(&p.scene_of[s]) : 0;
 }
+// The scene of a slot whose 16-bit compact record starts with word rec_x
+// (count | the scene's first slot << 8): scene_of at the scene's first slot,
+// one address for all of a scene's particles (an L1 hit, where scene_of[s]
+// streams 4 bytes a particle from DRAM).
+__device__ __forceinline__ int scene_of_record(const StepParams& p, unsigned rec_x) {
+    return p.scenes ? __ldg(&p.scene_of[rec_x >> 8]) : 0;
+}
 __device__ __forceinline__ Geo geo_of(const StepParams& p, int scene) {
     return p.scenes ? geo_scene(p, scene) : geo_single(p);
 }

@@ -806,12 +806,13 @@ __global__ void __launch_bounds__(B, ((F & 8) && U == 1) ? 2048 / B : ((U <= 2 &
         const int s = blockIdx.x * blockDim.x + threadIdx.x;
         if (s >= p.n) return;
         const float4 self = xs[s];
-        const int scene = scene_index(p, s);
+        const uint4 rec = COMPACT ? __ldg(&p.rec[s]) : make_uint4(0u, 0u, 0u, 0u);
+        const int scene = (COMPACT && !WIDE) ? scene_of_record(p, rec.x) : scene_index(p, s);
         const int packed = (MIXED && p.cell_sorted) ? __ldg(&p.cell_sorted[s]) : 0;
         DeltaAcc a{0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0};
         if (COMPACT) {
             walk_compact<U, WIDE, float4>(
-                p, __ldg(&p.rec[s]), p.rec2 + s, nbr + s, [&](int t) { return xs[t]; },
+                p, rec, p.rec2 + s, nbr + s, [&](int t) { return xs[t]; },
                 [&](int t, float4 q) { delta_pair<false, false, false>(p, a, self, t, q, shift_tab); });
         } else {
             for_each_entry<U, SOL, LIST_PAD_MAX>(p, nbr + s, cnt, s, xs, solid, [&](int e, float4 q) {
@@ -911,7 +912,8 @@ __device__ __forceinline__ void xsph_commit(const StepParams& p, const CellPack&
     const float cx = __fmul_rn(p.c_xsph, p.k6);
     const float4 vc = make_float4(__fmaf_rn(cx, ax, vi.x), __fmaf_rn(cx, ay, vi.y), __fmaf_rn(cx, az, vi.z), 0.0f);
     v_out[s] = vc;
-    const Geo g = geo_slot(p, s);
+    const Geo g = (COMPACT && !WIDE) ? geo_of(p, scene_of_record(p, __ldg(reinterpret_cast<const unsigned*>(p.rec + s))))
+                                     : geo_slot(p, s);
     float4 xc;
     if (!MIXED && !p.frame) {
         xc = make_float4(self.x, self.y, self.z, 0.0f);
