@@ -383,13 +383,13 @@ __device__ __forceinline__ void walk_stencil(const StepParams& p, const CellPack
 // the step's key, which rounding of the frame position could move).
 // FORMAT 1 or 2: compact lists (in wide records with 2) to p.rec (no cell
 // codes, no static particles).  Column lists sum the first lambda as the
-// walk accepts each candidate.  Compact lists walk first (the accepted
-// candidates only listed: fewer instructions in the walk's divergent rounds,
-// where the sums of any one lane's accepted candidate held the whole warp)
-// and then sum over the finished list, two entries' positions loaded
-// together (in the cache from the walk); a list cut at the capacity walks
-// once more to sum the dropped entries after the listed ones.  The terms
-// and their order are the walk's, so the sums equal the column lists'.
+// walk accepts each candidate.  Compact lists walk first, only listing the
+// accepted candidates (no sums live across the walk: fewer registers, so
+// more resident warps), and then sum over the finished list, two entries'
+// positions loaded together (in the cache from the walk); a list cut at the
+// capacity walks once more to sum the dropped entries after the listed
+// ones.  The terms and their order are the walk's, so the sums equal the
+// column lists'.
 template <bool MIXED, bool HASHED, bool FRAME, int FORMAT>
 __device__ __forceinline__ void lists_lambda(const StepParams& p, const CellPack& cp, float4* __restrict__ xs,
                                              const int* __restrict__ key_sorted, const int* __restrict__ cell_sorted,
@@ -461,9 +461,9 @@ __global__ void __launch_bounds__(B) k_lists_lambda(StepParams p, CellPack cp, f
 
 // Compact lists (no static particles, fp32 pair offsets; WIDE: wide records).
 // Held to 12 blocks of 128 threads per SM (40 registers, a few bytes
-// spilled): the walk waits on its gathers, not on issue slots, so the extra
-// resident warps pay (config 3: 0.382 -> 0.353 ms a step; a walk that
-// loads the next row's bounds ahead, or 4 gathers in flight, was slower).
+// spilled): the extra resident warps hide more of the gathers' latency
+// (config 3: 0.382 -> 0.353 ms a step; a walk that loads the next row's
+// bounds ahead, or 4 gathers in flight, was slower).
 template <bool HASHED, int B, bool FRAME, bool WIDE>
 __global__ void __launch_bounds__(B, 1536 / B) k_lists_compact(StepParams p, CellPack cp, float4* __restrict__ xs,
                                                              const int* __restrict__ key_sorted,
