@@ -300,8 +300,7 @@ __device__ __forceinline__ void walk_stencil(const StepParams& p, const CellPack
     const int slab = g.gx * g.gz;
     if (!HASHED && COMPACT) {
         // each row's two bounds loaded just before its walk (fewer live
-        // registers than a layer's six: more resident warps for this
-        // issue-bound kernel)
+        // registers than a layer's six: more resident warps)
         const int z0 = max(c.z - 1, 0), z1 = min(c.z + 1, g.gz - 1);
         for (int dy = -1; dy <= 1; dy++) {
             const int y = c.y + dy;
@@ -949,7 +948,7 @@ __global__ void __launch_bounds__(B) k_xsph(StepParams p, CellPack cp, const flo
 }
 
 // Compact lists (F = 8, 24) with one gather in flight: registers capped at 32
-// for every warp slot of the SM (64 bytes spilled; config 3 XSPH 0.175 ->
+// for every warp slot of the SM (at most 16 bytes spilled; config 3 XSPH 0.175 ->
 // 0.141 ms at step 5, 0.239 -> 0.219 ms at step 100 against the best
 // uncapped shape).  More gathers in flight keep k_xsph.
 template <int F, int U, int B>
