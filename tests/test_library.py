@@ -109,6 +109,24 @@ def test_scenes_match_config_shapes():
     assert s.n == 1500 and (s.x.max(0) < np.array(s.domain)).all()
 
 
+def test_bench_workloads_have_their_quoted_sizes():
+    """The seeded workloads the bench measures: config 3's 512 scenes hold
+    7,546,040 particles, 1,029 to 65,482 a scene (every scene below 65,536,
+    so the batch takes 16-bit compact entries), each inside its box; config
+    2 holds 2,097,152 and config 4 4,194,304 particles inside their domains."""
+    from lustrine_gb300 import scenes
+    c3 = scenes.config3()
+    counts = np.array([s.n for s in c3])
+    assert len(c3) == 512 and counts.sum() == 7_546_040
+    assert counts.min() == 1_029 and counts.max() == 65_482 < 65_536
+    for s in c3[:64]:
+        assert (s.x.min(0) > 0).all() and (s.x.max(0) < np.array(s.domain)).all()
+    c2 = scenes.config2()
+    assert c2.n == 2_097_152 and (c2.x.max(0) < np.array(c2.domain)).all()
+    c4 = scenes.config4()
+    assert c4.n == 4_194_304 and (c4.x.min(0) > 0).all() and (c4.x.max(0) < np.array(c4.domain)).all()
+
+
 def test_rest_lattice_mass_puts_the_rest_lattice_at_rest_density():
     """The PBF scenes' default mass: the poly6 density of the rest lattice
     equals the rest density, for h at the spacing and beyond it."""
